@@ -1,0 +1,367 @@
+"""Benchmark of the GB300 grouped-aggregation path.
+
+Default workload (the filtered high-cardinality DECIMAL aggregate, 100M rows):
+    SELECT k, COUNT(*), SUM(amount), AVG(amount) FROM t
+    WHERE d BETWEEN 2026-04-11 AND 2026-05-16 GROUP BY k ORDER BY SUM(amount) DESC LIMIT 10
+k BIGINT Zipf(1.1) over 10M values, amount DECIMAL(18,2), d DATE over 365 days.
+
+One step = one execution of that query over the whole table.
+  value  rows/s with the table resident in HBM (CUDA events on the query's stream)
+  e2e    rows/s through the C ABI from pinned HOST buffers: table registration
+         (H2D copy of the three columns + zone maps) + plan + execute + next
+         (D2H of the result) inside the timed region
+Inputs (2.0 GB) are larger than L2 (129 MB), so no flush between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--workload filtered|plain|distinct]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+from thindb_gb300 import abi, datagen  # noqa: E402
+
+WORKLOADS = {
+    "filtered": {
+        "name": "filtered high-cardinality DECIMAL aggregate: 100M rows, k BIGINT Zipf(1.1) over 10M, "
+                "amount DECIMAL(18,2) log-normal, d DATE 365 days, WHERE d BETWEEN (36 days, ~9.9%), "
+                "COUNT/SUM(int128)/AVG, ORDER BY SUM DESC LIMIT 10",
+        "rows": datagen.FILTERED_ROWS, "bytes_per_row": 20, "dtype": "int64/int128",
+    },
+    "plain": {
+        "name": "plain GROUP BY: 16,777,216 rows, k BIGINT over 1,024 values, v INT, COUNT/SUM/MIN/MAX",
+        "rows": datagen.PLAIN_ROWS, "bytes_per_row": 12, "dtype": "int64",
+    },
+    "distinct": {
+        "name": "composite key + COUNT(DISTINCT): 200M rows, (region SMALLINT, url DICT32), user_id BIGINT "
+                "Zipf(0.9) over 5M, latency DOUBLE, COUNT/COUNT(DISTINCT)/SUM(f64)",
+        "rows": datagen.DISTINCT_ROWS, "bytes_per_row": 22, "dtype": "int64/f64",
+    },
+}
+
+
+def load_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_traffic(workload):
+    """dram bytes per scan launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"scan_{workload}_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f).get("dram_bytes_per_launch")
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- inputs --
+
+def make_inputs(workload: str, n: int, pinned: bool):
+    """Host columns of the workload (pinned torch tensors when asked)."""
+    import torch
+
+    def buf(count, dtype):
+        return torch.empty(count, dtype=dtype, pin_memory=pinned)
+
+    if workload == "filtered":
+        k, a, d = buf(n, torch.int64), buf(n, torch.int64), buf(n, torch.int32)
+        datagen.filtered_into(n, 2, datagen.FILTERED_KEYS, k.data_ptr(), a.data_ptr(), d.data_ptr())
+        return [("k", abi.BIGINT, k, 0), ("amount", abi.DECIMAL64, a, 2), ("d", abi.DATE, d, 0)]
+    if workload == "plain":
+        k, v = buf(n, torch.int64), buf(n, torch.int32)
+        datagen.lib().tdg_plain(n, 1, k.data_ptr(), v.data_ptr(), 0)
+        return [("k", abi.BIGINT, k, 0), ("v", abi.INT, v, 0)]
+    r, u, us, lat = buf(n, torch.int16), buf(n, torch.int32), buf(n, torch.int64), buf(n, torch.float64)
+    datagen.lib().tdg_distinct(n, 3, datagen.DISTINCT_USERS, r.data_ptr(), u.data_ptr(), us.data_ptr(),
+                               lat.data_ptr(), 0)
+    return [("region", abi.SMALLINT, r, 0), ("url", abi.DICT32, u, 0), ("user_id", abi.BIGINT, us, 0),
+            ("latency_ms", abi.DOUBLE, lat, 0)]
+
+
+def make_request(workload: str, flags: int = 0, stream: int = 0):
+    from thindb_gb300.engine import AggSpec, Pred, Request, SortSpec
+
+    if workload == "filtered":
+        return Request(["k"], [AggSpec("count", None, "c"), AggSpec("sum", "amount", "s"),
+                               AggSpec("avg", "amount", "a")], [SortSpec("s", True)], limit=10,
+                       where=[Pred("d", "between", datagen.FILTER_LO, datagen.FILTER_HI)], flags=flags, stream=stream)
+    if workload == "plain":
+        return Request(["k"], [AggSpec("count", None, "c"), AggSpec("sum", "v", "s"), AggSpec("min", "v", "mn"),
+                               AggSpec("max", "v", "mx")], flags=flags, stream=stream)
+    return Request(["region", "url"], [AggSpec("count", None, "c"), AggSpec("count_distinct", "user_id", "u"),
+                                       AggSpec("sum", "latency_ms", "lat")], flags=flags, stream=stream)
+
+
+def columns_of(inputs, ndv=None):
+    from thindb_gb300.engine import Column
+
+    return [Column(nm, ty, t, scale=sc, ndv_hint=(ndv or {}).get(nm, 0)) for nm, ty, t, sc in inputs]
+
+
+# ------------------------------------------------------------ CPU legs --
+
+def cpu_sample_rows(workload: str) -> int:
+    return {"filtered": 20_000_000, "plain": 16_777_216, "distinct": 10_000_000}[workload]
+
+
+def run_oracle_sample(workload: str, n_sample: int, threads: int):
+    """The oracle (C++ restatement of thinDB's silo executor) over a bounded
+    sample of the workload; returns (rows/s, seconds)."""
+    import oracle
+    from thindb_gb300.engine import Column
+
+    if workload == "filtered":
+        d = datagen.filtered(n_sample, seed=2)
+        cols = [Column("k", abi.BIGINT, d["k"]), Column("amount", abi.DECIMAL64, d["amount"], scale=2),
+                Column("d", abi.DATE, d["d"])]
+    elif workload == "plain":
+        d = datagen.plain(n_sample, seed=1)
+        cols = [Column("k", abi.BIGINT, d["k"]), Column("v", abi.INT, d["v"])]
+    else:
+        d = datagen.distinct(n_sample, seed=3)
+        cols = [Column("region", abi.SMALLINT, d["region"]), Column("url", abi.DICT32, d["url"]),
+                Column("user_id", abi.BIGINT, d["user_id"]), Column("latency_ms", abi.DOUBLE, d["latency_ms"])]
+    t = oracle.HostTable(cols)
+    req = make_request(workload)
+    t0 = time.perf_counter()
+    oracle.run(t, req, threads=threads)
+    dt = time.perf_counter() - t0
+    return n_sample / dt, dt
+
+
+def reference_arm(args, wl):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    n_sample = cpu_sample_rows(args.workload)
+    for _ in range(max(0, min(args.warmup, 1))):
+        run_oracle_sample(args.workload, min(n_sample, 2_000_000), threads)
+    vals = []
+    for _ in range(args.steps):
+        v, dt = run_oracle_sample(args.workload, n_sample, threads)
+        vals.append(v)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": "GROUP BY rows/s", "value": value, "unit": "rows/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": wl["rows"] / value * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": wl["dtype"],
+        "data": "synthetic (seeded generator)",
+        "config": {"workload": wl["name"], "rows": wl["rows"]},
+        "cpu_baseline": {"value": value, "unit": "rows/s", "cores": threads, "kind": "port",
+                         "sample": f"first {n_sample:,} rows of the workload per step, all host threads; "
+                                   "C++ restatement of thinDB's silo executor (Zig toolchain absent)"},
+        "e2e": {"value": value, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------- GPU arm --
+
+def gpu_arm(args, wl):
+    import torch
+
+    from thindb_gb300 import engine
+    from thindb_gb300.engine import Table, try_build_group_topn
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    n = wl["rows"]
+    inputs = make_inputs(args.workload, n, pinned=True)
+    h2d_bytes = sum(t.numel() * t.element_size() for _, _, t, _ in inputs)
+
+    stream = torch.cuda.Stream()
+    table = Table(columns_of(inputs), compute_ndv=True, stream=stream.cuda_stream)
+    ndv = {nm: table.ndv(nm) for nm, _, _, _ in inputs}
+    req = make_request(args.workload, flags=abi.FLAG_TIMING, stream=stream.cuda_stream)
+    q = try_build_group_topn(table, req)
+    assert q is not None
+    out_schema = q.output_schema()
+
+    for _ in range(args.warmup):
+        q.execute()
+        q.synchronize()
+    scan_ms, launches = [], 0
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        q.execute()
+        q.synchronize()  # reads the status word (table-overflow retry check) each step
+        st = q.stats()
+        scan_ms.append(st.scan_ms)
+        launches += st.kernel_launches
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    total_ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    st = q.stats()
+    res = q.collect()
+    ms_per_step = total_ms / args.steps
+    if dist:
+        tt = torch.tensor([ms_per_step], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_per_step = float(tt.item())
+    value = n * world / (ms_per_step / 1e3)
+    q.close()
+
+    # end to end through the C ABI from pinned host buffers
+    e2e_steps = max(1, min(args.steps, 5))
+    d2h = sum(c.elem_bytes for c in out_schema) * st.result_rows
+    e2e_times = []
+    for i in range(e2e_steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        t2 = Table(columns_of(inputs, ndv), compute_ndv=False, stream=stream.cuda_stream)
+        q2 = try_build_group_topn(t2, make_request(args.workload, stream=stream.cuda_stream))
+        r2 = q2.collect()
+        q2.close()
+        t2.close()
+        dt = time.perf_counter() - t0
+        if i > 0:  # the first pass warms the allocator
+            e2e_times.append(dt)
+    e2e_value = n / statistics.median(e2e_times)
+
+    peak, peak_kind = load_peak()
+    scan_avg = statistics.mean(scan_ms)
+    alg_bytes = n * wl["bytes_per_row"]
+    achieved = alg_bytes / (scan_avg / 1e3) / 1e9
+    traffic = load_traffic(args.workload)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        n_sample = cpu_sample_rows(args.workload)
+        v, dt = run_oracle_sample(args.workload, n_sample, threads)
+        cpu = {"value": v, "unit": "rows/s", "cores": threads, "kind": "port",
+               "sample": f"first {n_sample:,} rows of the workload ({dt:.1f} s), all host threads; C++ "
+                         "restatement of thinDB's silo executor (Zig toolchain absent)"}
+
+    if rank == 0:
+        line = {
+            "metric": "GROUP BY rows/s", "value": value, "unit": "rows/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": wl["dtype"], "data": "synthetic (seeded generator)",
+            "config": {"workload": wl["name"], "rows": n, "l2": "inputs larger than L2 (no flush)",
+                       "selectivity": st.rows_selected / max(1, st.rows_scanned), "groups": st.groups,
+                       "route": "shared-memory" if st.route == 1 else "global table",
+                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "scan_group_kernel", "kernel_ms": scan_avg,
+                         "algorithmic_bytes": alg_bytes, "peak_kind": peak_kind},
+            "e2e": {"value": e2e_value, "unit": "rows/s", "h2d_bytes_per_step": h2d_bytes,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": statistics.median(e2e_times) * 1e3},
+            "gpu_launches": launches,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    table.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="filtered", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        reference_arm(args, wl)
+    else:
+        gpu_arm(args, wl)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,321 @@
+/*
+ * thindb_gpu.h — plain-C boundary of the GB300 grouped-aggregation operator.
+ *
+ * This header is the whole interface between thinDB's Zig host and the CUDA
+ * engine: it uses only C scalar types, fixed-size structs and opaque handles,
+ * so Zig can `@cImport` it unchanged (no C++ and no torch types appear here).
+ *
+ * Reference interfaces replaced (paths inside the thinDB source tree):
+ *   - the operator handle `exec.Query` + `VTable`      src/exec/exec.zig:299-373, :903-1218
+ *   - `makeQuery` (operator -> Query)                  src/exec/exec.zig:1221-1239
+ *   - the routing points `tryBuildGroupTopN` /
+ *     `tryBuildLowCardGroup` (null = decline)          src/exec/v2_pipeline.zig:17-34,
+ *                                                      called from src/exec/engine_v2.zig:968-972
+ *   - the request `GroupTopNRequest`                   src/exec/v2_shape_group_topn.zig:63-101
+ *   - `AggSpec` / `AggFunc`                            src/exec/aggregate.zig:88, :237-267
+ *   - `SortSpec` (ORDER BY key + direction)            src/exec/sort.zig:28-31
+ *   - `Batch` / `ColumnView` output (bit 1 = valid)    src/exec/exec.zig:175-236,
+ *                                                      src/storage/column.zig:28-46, :207-210
+ *   - error set `exec.Error` (MemoryBudgetExceeded,
+ *     UnsupportedOperatorForType, QueryCancelled)      src/exec/exec.zig:87-110, :913-920,
+ *                                                      src/memory.zig:665
+ *
+ * Ownership: every handle is created and destroyed through this API.  Input
+ * columns may live on the host (copied into HBM at registration) or already on
+ * the device.  Output batches are written into CALLER-OWNED host buffers.
+ *
+ * Threading: all calls on one handle come from one thread at a time, except
+ * tgpu_query_cancel, which may be called from any thread at any time (it only
+ * sets a flag that kernels poll between scan tiles).
+ */
+#ifndef THINDB_GPU_H
+#define THINDB_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TGPU_ABI_VERSION 1
+
+/* ---------------------------------------------------------------- status -- */
+
+typedef enum tgpu_status {
+    TGPU_OK = 0,
+    /* The shape is outside what this operator runs: the caller tries its next
+     * route, exactly as a `tryBuild*` returning null (v2_pipeline.zig:17-34). */
+    TGPU_DECLINE = 1,
+    TGPU_ERR_INVALID_ARGUMENT = 2,
+    /* exec.Error.MemoryBudgetExceeded (exec.zig:915-919). */
+    TGPU_ERR_MEMORY_BUDGET = 3,
+    /* exec.Error.UnsupportedOperatorForType. */
+    TGPU_ERR_UNSUPPORTED_TYPE = 4,
+    /* error.QueryCancelled (memory.zig:665). */
+    TGPU_ERR_CANCELLED = 5,
+    /* A CUDA runtime call failed; tgpu_last_error_message() names it. */
+    TGPU_ERR_CUDA = 6,
+    /* A bounded device-side wait ran out; the context stays usable. */
+    TGPU_ERR_DEVICE_TIMEOUT = 7,
+    TGPU_ERR_INTERNAL = 8,
+    /* The CUDA extension found no usable GPU. */
+    TGPU_ERR_NO_DEVICE = 9
+} tgpu_status;
+
+/* ----------------------------------------------------------------- types -- */
+
+/* Column types, named after thinDB's `types.Type` (src/types.zig:375-383,
+ * :617): DECIMAL(p<=18,s) is a `decimal64` i64 mantissa, DATE is i32 days since
+ * 1970-01-01, DATETIME is i64 microseconds.  TGPU_DICT32 is a string column
+ * carried as int32 codes into a table-level dictionary (thinDB's packed table
+ * ids, src/exec/silo_group_core.zig:523-538); TGPU_DECIMAL128 only appears in
+ * outputs (SUM over a DECIMAL). */
+typedef enum tgpu_type {
+    TGPU_BOOLEAN = 1,    /* u8 0/1 */
+    TGPU_TINYINT = 2,    /* i8  */
+    TGPU_SMALLINT = 3,   /* i16 */
+    TGPU_INT = 4,        /* i32 */
+    TGPU_DATE = 5,       /* i32 days */
+    TGPU_BIGINT = 6,     /* i64 */
+    TGPU_DATETIME = 7,   /* i64 us */
+    TGPU_DECIMAL64 = 8,  /* i64 mantissa, scale in the column descriptor */
+    TGPU_FLOAT = 9,      /* f32 */
+    TGPU_DOUBLE = 10,    /* f64 */
+    TGPU_DECIMAL128 = 11,/* i128 little-endian (lo u64, hi i64): outputs only */
+    TGPU_DICT32 = 12     /* i32 code into the column's dictionary */
+} tgpu_type;
+
+typedef enum tgpu_location {
+    TGPU_LOC_HOST = 0,   /* pointers are host memory: copied into HBM */
+    TGPU_LOC_DEVICE = 1  /* pointers are device memory on the current device: used in place */
+} tgpu_location;
+
+/* One input column.  `validity` follows thinDB's ColumnView.nulls: NULL means
+ * NOT NULL; otherwise bit (row & 7) of byte (row >> 3) is 1 when the row holds
+ * a value (src/storage/column.zig:28-46, :207-210). */
+typedef struct tgpu_column_desc {
+    const char *name;
+    int32_t type;               /* tgpu_type */
+    uint8_t decimal_precision;  /* DECIMAL64 only */
+    uint8_t decimal_scale;      /* DECIMAL64 only */
+    uint8_t reserved[2];
+    const void *data;           /* n_rows elements of the type's width */
+    const uint8_t *validity;    /* optional validity bitmap */
+    /* DICT32 only: dictionary strings i live at dict_bytes[dict_offsets[i] ..
+     * dict_offsets[i+1]) (host memory, dict_size + 1 offsets). */
+    const uint32_t *dict_offsets;
+    const uint8_t *dict_bytes;
+    uint32_t dict_size;
+    uint32_t reserved2;
+    /* Optional distinct-count hint (thinDB keeps HLL NDV stats per segment);
+     * 0 = estimate it at registration with a device HyperLogLog pass. */
+    uint64_t ndv_hint;
+} tgpu_column_desc;
+
+/* An immutable table: one segment of `n_rows` rows cut into row groups of
+ * `row_group_rows` (thinDB's default 65,536, src/api/api.zig:140). */
+typedef struct tgpu_table_desc {
+    const tgpu_column_desc *columns;
+    uint32_t n_columns;
+    uint32_t row_group_rows;    /* 0 = 65536 */
+    uint64_t n_rows;
+    int32_t location;           /* tgpu_location */
+    int32_t compute_ndv;        /* 1 = run the HLL pass for columns without ndv_hint */
+    void *stream;               /* cudaStream_t for the copies / stats, NULL = library stream */
+} tgpu_table_desc;
+
+typedef struct tgpu_table tgpu_table;
+typedef struct tgpu_query tgpu_query;
+
+/* ------------------------------------------------------------- requests -- */
+
+/* thinDB AggFunc members this operator folds (src/exec/aggregate.zig:88). */
+typedef enum tgpu_agg_func {
+    TGPU_AGG_COUNT = 1,          /* COUNT(*) when column < 0, else COUNT(col) */
+    TGPU_AGG_SUM = 2,
+    TGPU_AGG_AVG = 3,
+    TGPU_AGG_MIN = 4,
+    TGPU_AGG_MAX = 5,
+    TGPU_AGG_COUNT_DISTINCT = 6
+} tgpu_agg_func;
+
+typedef struct tgpu_agg_spec {
+    int32_t func;                /* tgpu_agg_func */
+    int32_t column;              /* input column index, -1 for COUNT(*) */
+    const char *as;              /* output column name (may be NULL) */
+} tgpu_agg_spec;
+
+/* One conjunct of the fused WHERE (thinDB's scan fuses the conjunction of
+ * column-vs-constant leaves, src/exec/scan.zig:2808; BETWEEN lowers to two
+ * inclusive leaves, src/sql/parse_predicate.zig:671).  Integer, DATE and
+ * DECIMAL64 columns compare as i64 against lo/hi (DECIMAL bounds are
+ * mantissas at the column's scale); FLOAT/DOUBLE columns compare against
+ * flo/fhi.  A NULL row never satisfies a comparison. */
+typedef enum tgpu_pred_op {
+    TGPU_PRED_BETWEEN = 1,       /* lo <= x <= hi */
+    TGPU_PRED_NOT_BETWEEN = 2,   /* x < lo or x > hi */
+    TGPU_PRED_EQ = 3,            /* x == lo */
+    TGPU_PRED_NE = 4,            /* x != lo */
+    TGPU_PRED_LT = 5,            /* x <  lo */
+    TGPU_PRED_LE = 6,            /* x <= lo */
+    TGPU_PRED_GT = 7,            /* x >  lo */
+    TGPU_PRED_GE = 8,            /* x >= lo */
+    TGPU_PRED_IS_NULL = 9,
+    TGPU_PRED_IS_NOT_NULL = 10
+} tgpu_pred_op;
+
+typedef struct tgpu_predicate {
+    int32_t column;
+    int32_t op;                  /* tgpu_pred_op */
+    int64_t lo, hi;
+    double flo, fhi;
+} tgpu_predicate;
+
+/* HAVING conjunct over an aggregate's EMITTED value (a BIGINT SUM compares
+ * wrapped, v2_shape_group_topn.zig:1448-1453).  Integer-valued outputs compare
+ * as i128 against `ival`; DOUBLE outputs against `fval`.  A NULL aggregate
+ * never satisfies it. */
+typedef struct tgpu_having {
+    int32_t agg;                 /* index into the request's aggs */
+    int32_t op;                  /* TGPU_PRED_EQ .. TGPU_PRED_GE */
+    int64_t ival;
+    double fval;
+} tgpu_having;
+
+typedef enum tgpu_sort_target {
+    TGPU_SORT_KEY = 1,           /* index = position in group_cols */
+    TGPU_SORT_AGG = 2            /* index = position in aggs */
+} tgpu_sort_target;
+
+typedef struct tgpu_sort_spec {
+    int32_t target;              /* tgpu_sort_target */
+    int32_t index;
+    int32_t desc;
+    int32_t reserved;
+} tgpu_sort_spec;
+
+#define TGPU_NO_LIMIT UINT64_MAX
+
+/* Mirror of GroupTopNRequest (v2_shape_group_topn.zig:63-101) in plain C. */
+typedef struct tgpu_request {
+    const int32_t *group_cols;   uint32_t n_group_cols;
+    const tgpu_agg_spec *aggs;   uint32_t n_aggs;
+    const tgpu_predicate *where; uint32_t n_where;
+    const tgpu_having *having;   uint32_t n_having;
+    const tgpu_sort_spec *order; uint32_t n_order;
+    uint64_t limit;              /* TGPU_NO_LIMIT for none */
+    uint64_t offset;
+    uint64_t expected_groups;    /* allocation hint, 0 = estimate from stats */
+    uint64_t memory_budget_bytes;/* 0 = unlimited */
+    void *stream;                /* cudaStream_t, NULL = library stream */
+    int32_t flags;               /* TGPU_FLAG_* */
+    int32_t reserved;
+} tgpu_request;
+
+/* Record per-phase CUDA event times (tgpu_query_stats.*_ms). */
+#define TGPU_FLAG_TIMING 0x1
+/* Force the global-table route even when the groups fit a CTA's shared memory. */
+#define TGPU_FLAG_FORCE_GLOBAL 0x2
+/* Load every needed column densely instead of gathering only survivors. */
+#define TGPU_FLAG_DENSE_SCAN 0x4
+/* Disable the in-warp __match_any_sync pre-combine (tuning / tests). */
+#define TGPU_FLAG_NO_WARP_COMBINE 0x8
+
+/* ----------------------------------------------------------------- output -- */
+
+typedef struct tgpu_output_column {
+    char name[64];
+    int32_t type;                /* tgpu_type of the emitted column */
+    uint8_t decimal_precision;
+    uint8_t decimal_scale;
+    uint8_t nullable;
+    uint8_t reserved;
+    uint32_t elem_bytes;         /* width of one value in the data buffer */
+    uint32_t reserved2;
+} tgpu_output_column;
+
+/* Caller-owned host buffers for one `next()`.  values[c] holds capacity_rows
+ * values of column c; validity[c] (optional, may be NULL) receives a thinDB
+ * validity bitmap (bit 1 = valid) of ceil(capacity_rows / 8) bytes. */
+typedef struct tgpu_batch {
+    uint32_t n_columns;
+    uint32_t reserved;
+    void **values;
+    uint8_t **validity;
+    uint64_t capacity_rows;
+    uint64_t row_count;          /* filled by tgpu_query_next */
+} tgpu_batch;
+
+typedef struct tgpu_query_stats {
+    uint64_t rows_scanned;       /* rows in row groups that survived zone maps */
+    uint64_t rows_selected;      /* rows that passed the WHERE */
+    uint64_t groups;             /* groups before HAVING */
+    uint64_t result_rows;        /* rows the query emits (after OFFSET/LIMIT) */
+    uint64_t table_capacity;     /* global group-table slots */
+    uint64_t distinct_capacity;  /* (group, value) set slots, 0 if none */
+    uint32_t row_groups_total;
+    uint32_t row_groups_pruned;
+    uint32_t route;              /* 1 = shared-memory (lowcard) route, 2 = global table */
+    uint32_t retries;            /* group-table regrowths */
+    uint32_t kernel_launches;    /* kernels the last execute launched */
+    uint32_t reserved;
+    double scan_ms;              /* filter + group + fold kernel (TGPU_FLAG_TIMING) */
+    double finalize_ms;          /* compaction + ranking + output gather */
+    double total_ms;             /* whole execute on the device */
+    uint64_t device_bytes;       /* workspace bytes held by the query */
+} tgpu_query_stats;
+
+/* -------------------------------------------------------------- the API -- */
+
+/* ABI version and a short build string (arch, CUDA version). */
+uint32_t tgpu_abi_version(void);
+const char *tgpu_build_info(void);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *tgpu_last_error_message(void);
+
+/* Register an immutable table: copies host columns into HBM (or adopts device
+ * pointers), builds per-row-group zone maps (min/max) and NDV estimates.
+ * Replaces opening an `api.Table` snapshot for the scan (scan.zig:470). */
+tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out);
+tgpu_status tgpu_table_destroy(tgpu_table *table);
+/* Row count, row-group count and a column's NDV estimate (-1 column = none). */
+tgpu_status tgpu_table_info(const tgpu_table *table, int32_t column,
+                            uint64_t *n_rows, uint32_t *n_row_groups, uint64_t *ndv);
+
+/* tryBuildLowCardGroup / tryBuildGroupTopN in one call: validates the shape
+ * (validateShape, v2_shape_group_topn.zig:2051-2370), plans key packing and
+ * state slots, sizes the workspace.  Returns TGPU_DECLINE for shapes thinDB's
+ * V2 core also declines or that this engine leaves to another route. */
+tgpu_status tgpu_query_create(tgpu_table *table, const tgpu_request *request, tgpu_query **out);
+
+/* The result schema (`outputSchema`).  Writes up to `cap` columns. */
+tgpu_status tgpu_query_output_schema(const tgpu_query *q, tgpu_output_column *cols,
+                                     uint32_t cap, uint32_t *n_columns);
+
+/* Run the whole query on its stream (asynchronous; results stay in HBM).
+ * `next` calls this on first use, as GroupTopNPipeline.execute runs on the
+ * first `next()` (v2_shape_group_topn.zig:646-681).  Executing again reruns
+ * the query over the same table. */
+tgpu_status tgpu_query_execute(tgpu_query *q);
+
+/* `Query.next`: copies up to batch->capacity_rows result rows into the
+ * caller's buffers; *done = 1 once every row has been returned. */
+tgpu_status tgpu_query_next(tgpu_query *q, tgpu_batch *batch, int32_t *done);
+
+/* Async-safe cancellation flag; the next tile boundary or `next` returns
+ * TGPU_ERR_CANCELLED. */
+tgpu_status tgpu_query_cancel(tgpu_query *q);
+
+tgpu_status tgpu_query_get_stats(const tgpu_query *q, tgpu_query_stats *out);
+tgpu_status tgpu_query_destroy(tgpu_query *q);
+
+/* Synchronise the library stream / the query's stream (tests and benches). */
+tgpu_status tgpu_query_synchronize(tgpu_query *q);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* THINDB_GPU_H */

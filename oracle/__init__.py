@@ -1,0 +1,131 @@
+"""Python binding of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this;
+the product never imports it.  `run(columns, request)` evaluates a GROUP BY
+with the C++ restatement of thinDB's semantics (oracle.cpp) over host numpy
+columns and returns {output name: (values, validity or None)}.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+from thindb_gb300 import abi
+from thindb_gb300.engine import NP_DTYPES, Column, Request, build_request
+
+from . import build as _build
+
+_LIB: Optional[C.CDLL] = None
+
+
+def lib() -> C.CDLL:
+    global _LIB
+    if _LIB is None:
+        so = _build.SO
+        if not os.path.exists(so):
+            _build.build()
+        L = C.CDLL(so)
+        L.orc_group_by.restype = C.c_int
+        L.orc_group_by.argtypes = [C.POINTER(abi.TableDesc), C.POINTER(abi.Request), C.c_int, C.POINTER(C.c_void_p)]
+        L.orc_result_rows.restype = C.c_uint64
+        L.orc_result_rows.argtypes = [C.c_void_p]
+        L.orc_result_cols.restype = C.c_uint32
+        L.orc_result_cols.argtypes = [C.c_void_p]
+        L.orc_result_groups.restype = C.c_uint64
+        L.orc_result_groups.argtypes = [C.c_void_p]
+        L.orc_result_selected.restype = C.c_uint64
+        L.orc_result_selected.argtypes = [C.c_void_p]
+        L.orc_result_data.restype = C.c_void_p
+        L.orc_result_data.argtypes = [C.c_void_p, C.c_uint32]
+        L.orc_result_valid.restype = C.c_void_p
+        L.orc_result_valid.argtypes = [C.c_void_p, C.c_uint32]
+        L.orc_result_schema.restype = C.c_int
+        L.orc_result_schema.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(abi.OutputColumn)]
+        L.orc_result_free.argtypes = [C.c_void_p]
+        L.orc_last_error.restype = C.c_char_p
+        L.orc_i128_to_f64.restype = C.c_double
+        L.orc_i128_to_f64.argtypes = [C.c_uint64, C.c_int64]
+        L.orc_avg_decimal.restype = C.c_double
+        L.orc_avg_decimal.argtypes = [C.c_uint64, C.c_int64, C.c_uint64, C.c_int32]
+        _LIB = L
+    return _LIB
+
+
+class HostTable:
+    """Host columns described like engine.Table (names, types, validity)."""
+
+    def __init__(self, columns: Sequence[Column], row_group_rows: int = 65536):
+        self.columns = list(columns)
+        self.row_group_rows = row_group_rows
+        self.n_rows = len(self.columns[0].data)
+        self._keep: list = []
+        self.descs = (abi.ColumnDesc * len(self.columns))()
+        for i, c in enumerate(self.columns):
+            d = self.descs[i]
+            nm = c.name.encode()
+            arr = np.ascontiguousarray(c.data, dtype=NP_DTYPES[c.type])
+            self._keep += [nm, arr]
+            d.name = nm
+            d.type = c.type
+            d.decimal_precision = c.precision
+            d.decimal_scale = c.scale
+            d.data = arr.ctypes.data
+            if c.validity is not None:
+                bm = np.packbits(np.asarray(c.validity, dtype=bool), bitorder="little")
+                self._keep.append(bm)
+                d.validity = bm.ctypes.data
+        self.desc = abi.TableDesc()
+        self.desc.columns = self.descs
+        self.desc.n_columns = len(self.columns)
+        self.desc.row_group_rows = row_group_rows
+        self.desc.n_rows = self.n_rows
+        self.desc.location = abi.LOC_HOST
+
+    def col_index(self, name: str) -> int:
+        for i, c in enumerate(self.columns):
+            if c.name.lower() == name.lower():
+                return i
+        raise KeyError(name)
+
+
+class OracleDecline(Exception):
+    pass
+
+
+def run(table: HostTable, req: Request, threads: int = 1) -> dict:
+    """Evaluate `req`; raises OracleDecline for shapes the engine declines."""
+    r, keep = build_request(table, req)
+    h = C.c_void_p()
+    st = lib().orc_group_by(C.byref(table.desc), C.byref(r), threads, C.byref(h))
+    if st == abi.DECLINE:
+        raise OracleDecline(lib().orc_last_error().decode())
+    if st != abi.OK:
+        raise RuntimeError(f"oracle status {st}: {lib().orc_last_error().decode()}")
+    try:
+        rows = lib().orc_result_rows(h)
+        out = {}
+        for c in range(lib().orc_result_cols(h)):
+            oc = abi.OutputColumn()
+            lib().orc_result_schema(h, c, C.byref(oc))
+            eb = oc.elem_bytes
+            raw = C.string_at(lib().orc_result_data(h, c), rows * eb) if rows else b""
+            if oc.type == abi.DECIMAL128:
+                vals = np.frombuffer(raw, dtype=np.int64).reshape(-1, 2).copy()
+            else:
+                vals = np.frombuffer(raw, dtype=NP_DTYPES[oc.type]).copy()
+            ok = np.frombuffer(C.string_at(lib().orc_result_valid(h, c), rows) if rows else b"",
+                               dtype=np.uint8).astype(bool)
+            out[oc.name.decode()] = (vals, ok if oc.nullable else None)
+        out["__groups__"] = lib().orc_result_groups(h)
+        out["__selected__"] = lib().orc_result_selected(h)
+        return out
+    finally:
+        lib().orc_result_free(h)
+        del keep
+
+
+def i128_to_f64(lo: int, hi: int) -> float:
+    return lib().orc_i128_to_f64(lo & ((1 << 64) - 1), hi)

@@ -1,0 +1,240 @@
+"""CUDA engine parity: the reference's known answers and the oracle, bit-exact
+for integers/DECIMAL, FP64 sums within 1e-12 relative (the summation order
+differs from the oracle's)."""
+import numpy as np
+import pytest
+
+import cases
+import oracle
+from helpers import check_known_answer, compare_results, load_known_answers, to_rows
+from thindb_gb300 import abi, datagen
+from thindb_gb300.engine import (AggSpec, Column, MemoryBudgetExceeded, Pred, QueryCancelled, Request, SortSpec,
+                                 HavingSpec, Table, try_build_group_topn)
+
+pytestmark = pytest.mark.gpu
+KNOWN = load_known_answers()
+FP64_REL = 1e-12
+
+
+def run_gpu(cols, req, rg=65536, **kw):
+    t = Table(cols, row_group_rows=rg, **kw)
+    q = try_build_group_topn(t, req)
+    assert q is not None, "declined"
+    res = q.collect()
+    st = q.stats()
+    q.close()
+    t.close()
+    return res, st
+
+
+def run_both(cols, req, rg=65536, ordered=None, rel=FP64_REL, **kw):
+    got, st = run_gpu(cols, req, rg, **kw)
+    want = oracle.run(oracle.HostTable(cols, rg), req, threads=1)
+    if ordered is None:
+        ordered = bool(req.order_specs) or req.limit is not None
+    compare_results(got, want, len(req.group_cols), ordered, rel=rel)
+    assert st.groups == want["__groups__"], (st.groups, want["__groups__"])
+    assert st.rows_selected == want["__selected__"]
+    return got, st
+
+
+# ------------------------------------------------------------ known answers --
+
+@pytest.mark.parametrize("case_fn", cases.ALL_CASES, ids=[f.__name__ for f in cases.ALL_CASES])
+@pytest.mark.parametrize("flags", [0, abi.FLAG_FORCE_GLOBAL | abi.FLAG_NO_WARP_COMBINE])
+def test_engine_known_answers(case_fn, flags):
+    c = case_fn()
+    t = Table(c.columns, row_group_rows=c.row_group_rows)
+    for q in c.queries:
+        q.request.flags = flags
+        qq = try_build_group_topn(t, q.request)
+        assert qq is not None, q.name
+        check_known_answer(c, q, KNOWN[c.name][q.name], qq.collect())
+        qq.close()
+    t.close()
+
+
+# -------------------------------------------------------- workload shapes --
+
+def plain_cols(n):
+    d = datagen.plain(n, seed=7)
+    return [Column("k", abi.BIGINT, d["k"]), Column("v", abi.INT, d["v"])]
+
+
+@pytest.mark.parametrize("flags", [0, abi.FLAG_FORCE_GLOBAL, abi.FLAG_NO_WARP_COMBINE,
+                                   abi.FLAG_FORCE_GLOBAL | abi.FLAG_NO_WARP_COMBINE])
+def test_plain_lowcard(flags):
+    cols = plain_cols(1 << 20)
+    req = Request(["k"], [AggSpec("count", None, "c"), AggSpec("sum", "v", "s"), AggSpec("min", "v", "mn"),
+                          AggSpec("max", "v", "mx")], flags=flags)
+    _, st = run_both(cols, req)
+    assert st.groups == 1024
+    assert st.route == (2 if flags & abi.FLAG_FORCE_GLOBAL else 1)
+
+
+def filtered_cols(n, n_keys):
+    d = datagen.filtered(n, seed=5, n_keys=n_keys)
+    return [Column("k", abi.BIGINT, d["k"]), Column("amount", abi.DECIMAL64, d["amount"], scale=2, precision=18),
+            Column("d", abi.DATE, d["d"])]
+
+
+FILTER = [Pred("d", "between", datagen.FILTER_LO, datagen.FILTER_HI)]
+C2_AGGS = [AggSpec("count", None, "c"), AggSpec("sum", "amount", "s"), AggSpec("avg", "amount", "a")]
+
+
+@pytest.mark.parametrize("flags", [0, abi.FLAG_DENSE_SCAN, abi.FLAG_NO_WARP_COMBINE, abi.FLAG_FORCE_GLOBAL])
+def test_filtered_top10(flags):
+    cols = filtered_cols(2_000_000, 200_000)
+    req = Request(["k"], C2_AGGS, [SortSpec("s", True)], limit=10, where=FILTER, flags=flags)
+    got, st = run_both(cols, req)
+    assert st.result_rows == 10
+    # the sum is DECIMAL(38,2) and AVG is f64(sum)/count/100, bit-exact
+    assert got["s"][0].shape == (10, 2)
+
+
+def test_filtered_all_groups():
+    cols = filtered_cols(1_000_000, 100_000)
+    req = Request(["k"], C2_AGGS, where=FILTER)
+    got, st = run_both(cols, req)
+    assert st.route == 2
+
+
+def test_filtered_sorted_page():
+    cols = filtered_cols(1_000_000, 50_000)
+    req = Request(["k"], C2_AGGS, [SortSpec("a", False), SortSpec("c", True)], limit=500, offset=1234, where=FILTER)
+    run_both(cols, req)
+
+
+def distinct_cols(n, n_users):
+    d = datagen.distinct(n, seed=9, n_users=n_users)
+    return [Column("region", abi.SMALLINT, d["region"]), Column("url", abi.DICT32, d["url"]),
+            Column("user_id", abi.BIGINT, d["user_id"]), Column("latency_ms", abi.DOUBLE, d["latency_ms"])]
+
+
+def test_distinct_composite():
+    cols = distinct_cols(1_000_000, 50_000)
+    req = Request(["region", "url"], [AggSpec("count", None, "c"), AggSpec("count_distinct", "user_id", "u"),
+                                      AggSpec("sum", "latency_ms", "lat")])
+    got, st = run_both(cols, req)
+    assert st.groups > 100_000
+
+
+def test_distinct_rerun_epochs():
+    """The distinct set is reused across executions (epoch tags): results repeat."""
+    cols = distinct_cols(300_000, 20_000)
+    req = Request(["region"], [AggSpec("count_distinct", "user_id", "u"), AggSpec("count", None, "c")],
+                  [SortSpec("region")])
+    t = Table(cols)
+    q = try_build_group_topn(t, req)
+    first = to_rows(q.collect())
+    for _ in range(3):
+        q.execute()
+        assert to_rows(q.collect()) == first
+    q.close()
+    want = oracle.run(oracle.HostTable(cols), req)
+    assert to_rows(want) == first
+
+
+# ------------------------------------------------------------- semantics --
+
+def mixed_cols(n, seed=3):
+    rng = np.random.default_rng(seed)
+    k1 = rng.integers(-3, 4, n).astype(np.int8)
+    k2 = rng.integers(-200, 200, n).astype(np.int16)
+    k1_ok = rng.random(n) > 0.1
+    f = rng.normal(0, 100, n).astype(np.float32)
+    f_ok = rng.random(n) > 0.2
+    big = rng.integers(-(1 << 62), 1 << 62, n).astype(np.int64)
+    big_ok = rng.random(n) > 0.3
+    dt = rng.integers(18000, 21000, n).astype(np.int32)
+    b = (rng.random(n) > 0.5).astype(np.uint8)
+    dbl = rng.normal(0, 1e6, n)
+    return [Column("k1", abi.TINYINT, k1, validity=k1_ok), Column("k2", abi.SMALLINT, k2),
+            Column("f", abi.FLOAT, f, validity=f_ok), Column("big", abi.BIGINT, big, validity=big_ok),
+            Column("dt", abi.DATE, dt), Column("b", abi.BOOLEAN, b), Column("dbl", abi.DOUBLE, dbl)]
+
+
+def test_mixed_types_nulls():
+    cols = mixed_cols(300_000)
+    aggs = [AggSpec("count", None, "c"), AggSpec("count", "f", "cf"), AggSpec("sum", "big", "sb"),
+            AggSpec("avg", "big", "ab"), AggSpec("min", "f", "mnf"), AggSpec("max", "f", "mxf"),
+            AggSpec("min", "dt", "mnd"), AggSpec("max", "big", "mxb"), AggSpec("sum", "f", "sf"),
+            AggSpec("sum", "b", "sbool"), AggSpec("count_distinct", "k2", "dk2")]
+    req = Request(["k1", "b"], aggs)
+    run_both(cols, req, rel=1e-9)  # float32 inputs summed in f64: 1e-9 covers reordering
+
+
+def test_wide_key_and_nullable_order():
+    cols = mixed_cols(200_000, seed=11)
+    req = Request(["big", "k1", "k2"], [AggSpec("count", None, "c"), AggSpec("max", "dbl", "m")],
+                  [SortSpec("k1", True), SortSpec("m")], limit=700, offset=3)
+    run_both(cols, req)
+
+
+def test_order_by_key_desc_nulls_and_having():
+    cols = mixed_cols(200_000, seed=5)
+    req = Request(["k1"], [AggSpec("sum", "big", "s"), AggSpec("count", None, "c"), AggSpec("avg", "f", "af")],
+                  [SortSpec("k1", True)], having=[HavingSpec("c", ">", 10)])
+    run_both(cols, req, rel=1e-9)
+
+
+def test_empty_and_all_filtered():
+    cols = plain_cols(100_000)
+    req = Request(["k"], [AggSpec("count", None, "c")], where=[Pred("v", ">", 10_000_000)])
+    got, st = run_both(cols, req)
+    assert st.result_rows == 0 and st.groups == 0
+    empty = [Column("k", abi.BIGINT, np.zeros(0, np.int64)), Column("v", abi.INT, np.zeros(0, np.int32))]
+    got, st = run_gpu(empty, Request(["k"], [AggSpec("count", None, "c")]))
+    assert st.result_rows == 0
+
+
+def test_zone_map_pruning():
+    n = 1 << 20
+    d = np.sort(np.random.default_rng(1).integers(0, 1000, n)).astype(np.int32)
+    k = (np.arange(n) % 777).astype(np.int64)
+    cols = [Column("k", abi.BIGINT, k), Column("d", abi.DATE, d)]
+    req = Request(["k"], [AggSpec("count", None, "c"), AggSpec("max", "d", "md")], where=[Pred("d", "between", 300, 320)])
+    got, st = run_both(cols, req)
+    assert st.row_groups_pruned > 0
+
+
+def test_regrow_when_estimate_too_small():
+    cols = filtered_cols(500_000, 100_000)
+    req = Request(["k"], C2_AGGS, expected_groups=16, flags=abi.FLAG_FORCE_GLOBAL)
+    got, st = run_both(cols, req)
+    assert st.retries >= 1
+
+
+def test_memory_budget_and_cancel():
+    cols = plain_cols(100_000)
+    t = Table(cols)
+    with pytest.raises(MemoryBudgetExceeded):
+        try_build_group_topn(t, Request(["k"], [AggSpec("count", None, "c")], memory_budget=1024))
+    q = try_build_group_topn(t, Request(["k"], [AggSpec("count", None, "c")]))
+    q.cancel()
+    with pytest.raises(QueryCancelled):
+        q.next()
+    q.close()
+    t.close()
+
+
+def test_declines_like_reference():
+    cols = mixed_cols(1000)
+    t = Table(cols)
+    assert try_build_group_topn(t, Request(["dbl"], [AggSpec("count", None, "c")])) is None  # float key
+    assert try_build_group_topn(t, Request(["dt"], [AggSpec("sum", "dt", "s")])) is None  # SUM(DATE)
+    many = [AggSpec("sum", "big", f"s{i}") for i in range(9)]  # 9 x (2 + valid) slots > 16
+    assert try_build_group_topn(t, Request(["k2"], many)) is None
+    t.close()
+
+
+def test_device_resident_columns():
+    torch = pytest.importorskip("torch")
+    d = datagen.filtered(300_000, seed=4, n_keys=30_000)
+    host = [Column("k", abi.BIGINT, d["k"]), Column("amount", abi.DECIMAL64, d["amount"], scale=2),
+            Column("d", abi.DATE, d["d"])]
+    dev = [Column(c.name, c.type, torch.from_numpy(c.data).cuda(), scale=c.scale) for c in host]
+    req = Request(["k"], C2_AGGS, [SortSpec("s", True)], limit=10, where=FILTER)
+    got, _ = run_gpu(dev, req, location="device")
+    want = oracle.run(oracle.HostTable(host), req)
+    compare_results(got, want, 1, True)

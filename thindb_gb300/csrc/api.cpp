@@ -1,0 +1,1131 @@
+// api.cpp — host runtime behind include/thindb_gpu.h.
+//
+// Table registration (HBM residency, zone maps, NDV), query planning (thinDB's
+// validateShape: key packing and state slots, v2_shape_group_topn.zig:2051-2370),
+// group-table sizing (expectedTotalGroups, silo_group_core.zig:11398), a
+// workspace pool of self-cleaning group tables and epoch-tagged distinct sets,
+// and the execute / next / cancel life cycle of thinDB's `exec.Query`
+// (exec.zig:903-1218).
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+
+using namespace tgpu;
+
+namespace {
+
+thread_local std::string g_err;
+
+tgpu_status fail(tgpu_status s, const std::string &msg) {
+    g_err = msg;
+    return s;
+}
+
+#define CU(call)                                                                                 \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess) {                                                                 \
+            return fail(TGPU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));      \
+        }                                                                                        \
+    } while (0)
+
+int type_bytes(int t) {
+    switch (t) {
+        case TGPU_BOOLEAN: case TGPU_TINYINT: return 1;
+        case TGPU_SMALLINT: return 2;
+        case TGPU_INT: case TGPU_DATE: case TGPU_DICT32: case TGPU_FLOAT: return 4;
+        case TGPU_DECIMAL128: return 16;
+        default: return 8;
+    }
+}
+// intTypeBits (v2_shape_group_topn.zig:2698-2706) plus packed string ids.
+int type_bits(int t) {
+    switch (t) {
+        case TGPU_BOOLEAN: case TGPU_TINYINT: return 8;
+        case TGPU_SMALLINT: return 16;
+        case TGPU_INT: case TGPU_DATE: case TGPU_DICT32: return 32;
+        case TGPU_BIGINT: case TGPU_DATETIME: case TGPU_DECIMAL64: return 64;
+        default: return 0;
+    }
+}
+bool is_float_t(int t) { return t == TGPU_FLOAT || t == TGPU_DOUBLE; }
+bool is_temporal(int t) { return t == TGPU_DATE || t == TGPU_DATETIME; }
+bool is_i64_phys(int t) { return t == TGPU_BIGINT || t == TGPU_DATETIME || t == TGPU_DECIMAL64; }
+
+uint64_t next_pow2(uint64_t x) {
+    uint64_t p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+// ------------------------------------------------------------ device --
+
+struct DeviceCtx {
+    int id = -1;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+};
+
+std::mutex g_dev_mu;
+DeviceCtx g_dev;
+
+tgpu_status device_ctx(DeviceCtx **out) {
+    std::lock_guard<std::mutex> lk(g_dev_mu);
+    if (g_dev.id < 0) {
+        int n = 0;
+        cudaError_t e = cudaGetDeviceCount(&n);
+        if (e != cudaSuccess || n == 0)
+            return fail(TGPU_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+        int id = 0;
+        CU(cudaGetDevice(&id));
+        CU(cudaDeviceGetAttribute(&g_dev.sms, cudaDevAttrMultiProcessorCount, id));
+        CU(cudaStreamCreateWithFlags(&g_dev.stream, cudaStreamNonBlocking));
+        g_dev.id = id;
+    }
+    *out = &g_dev;
+    return TGPU_OK;
+}
+
+// ------------------------------------------------------- workspace pool --
+
+// Group tables come back all-zero (the clear kernel zeroes every slot it
+// used), distinct sets carry an epoch so old entries read as free: neither
+// needs a memset between queries.
+struct Buffer {
+    void *p = nullptr;
+    size_t bytes = 0;
+    bool dirty = false;     // contents unknown: must be zeroed before use
+    uint32_t epoch = 0;     // distinct sets: last epoch written
+};
+
+struct Pool {
+    std::mutex mu;
+    std::vector<Buffer> free_;
+    tgpu_status take(size_t bytes, cudaStream_t s, Buffer *out) {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            int best = -1;
+            for (size_t i = 0; i < free_.size(); ++i)
+                if (free_[i].bytes >= bytes && free_[i].bytes <= 2 * bytes + (1u << 20) &&
+                    (best < 0 || free_[i].bytes < free_[best].bytes))
+                    best = (int)i;
+            if (best >= 0) {
+                *out = free_[best];
+                free_.erase(free_.begin() + best);
+                if (out->dirty) {
+                    CU(cudaMemsetAsync(out->p, 0, out->bytes, s));
+                    out->dirty = false;
+                    out->epoch = 0;
+                }
+                return TGPU_OK;
+            }
+        }
+        Buffer b;
+        b.bytes = bytes;
+        cudaError_t e = cudaMalloc(&b.p, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            // release cached buffers and retry once
+            trim();
+            e = cudaMalloc(&b.p, bytes);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                return fail(TGPU_ERR_MEMORY_BUDGET, "device allocation of " + std::to_string(bytes) + " bytes failed");
+            }
+        }
+        CU(cudaMemsetAsync(b.p, 0, bytes, s));
+        *out = b;
+        return TGPU_OK;
+    }
+    void give(Buffer b) {
+        if (!b.p) return;
+        std::lock_guard<std::mutex> lk(mu);
+        free_.push_back(b);
+    }
+    void trim() {
+        std::lock_guard<std::mutex> lk(mu);
+        for (auto &b : free_) cudaFree(b.p);
+        free_.clear();
+    }
+};
+
+Pool g_pool;
+
+// ----------------------------------------------------------------- table --
+
+struct Column {
+    std::string name;
+    int type = 0;
+    int precision = 0, scale = 0;
+    void *d_data = nullptr;
+    uint32_t *d_valid = nullptr;
+    bool owned = false;
+    bool nullable = false;
+    uint64_t ndv = 0;
+    std::vector<int64_t> zmin, zmax;
+    std::vector<double> zfmin, zfmax;
+    std::vector<uint32_t> znull;
+    std::vector<uint32_t> dict_offsets;
+    std::vector<uint8_t> dict_bytes;
+};
+
+}  // namespace
+
+struct tgpu_table {
+    uint64_t n_rows = 0;
+    uint32_t rg_rows = 65536;
+    uint32_t n_rg = 0;
+    std::vector<Column> cols;
+    ~tgpu_table() {
+        for (auto &c : cols) {
+            if (c.owned) cudaFree(c.d_data);
+            cudaFree(c.d_valid);
+        }
+    }
+};
+
+namespace {
+
+double hll_estimate(const std::vector<uint32_t> &regs) {
+    const double m = (double)regs.size();
+    double sum = 0;
+    int zeros = 0;
+    for (uint32_t r : regs) {
+        sum += std::ldexp(1.0, -(int)r);
+        if (r == 0) ++zeros;
+    }
+    double alpha = 0.7213 / (1.0 + 1.079 / m);
+    double e = alpha * m * m / sum;
+    if (e <= 2.5 * m && zeros > 0) e = m * std::log(m / zeros);  // linear counting
+    return e;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------- query --
+
+namespace {
+
+enum RankMode { RANK_NONE = 0, RANK_TOPK = 1, RANK_SORT = 2 };
+
+}  // namespace
+
+struct tgpu_query {
+    tgpu_table *t = nullptr;
+    cudaStream_t stream = nullptr;
+    int flags = 0;
+    uint64_t limit = TGPU_NO_LIMIT, offset = 0;
+    uint64_t budget = 0;
+    std::vector<tgpu_output_column> schema;
+    DevQuery dq{};
+    DevFinal df{};
+    std::vector<int> out_types;
+    int route = 0;
+    uint64_t groups_est = 0, sel_est = 0, rows_scanned = 0;
+    uint32_t rg_total = 0, rg_pruned = 0;
+    int rank = RANK_NONE;
+    uint32_t k = 0;
+    uint64_t out_rows_max = 0;
+    int grid = 0;
+    // workspace
+    Buffer table_buf, occ_buf;
+    std::vector<Buffer> dset_bufs;
+    std::vector<uint64_t> dset_need;   // distinct entries estimated per set
+    void *scratch = nullptr;           // per-query small buffers (one allocation)
+    size_t scratch_bytes = 0;
+    uint32_t *d_rg_list = nullptr;
+    unsigned int *d_ctrl = nullptr;            // [0] tile counter, [1] status
+    unsigned long long *d_counts = nullptr;    // [0..3] counts, [4] selected rows
+    uint32_t *d_block_counts = nullptr;
+    uint32_t n_cpt_blocks = 0;
+    uint32_t *d_gids = nullptr;
+    unsigned long long *d_cand_keys = nullptr;
+    uint32_t *d_cand_gids = nullptr;
+    uint32_t n_cand_blocks = 0;
+    uint32_t *d_sel = nullptr;
+    unsigned long long *d_sort_keys[2] = {nullptr, nullptr};
+    uint32_t *d_sort_ids[2] = {nullptr, nullptr};
+    std::vector<void *> d_out;
+    std::vector<uint8_t *> d_outvalid;
+    void **d_out_ptrs = nullptr;
+    uint8_t **d_valid_ptrs = nullptr;
+    std::vector<uint32_t> rg_list;
+    // host pinned
+    int *h_cancel = nullptr;
+    int *d_cancel = nullptr;
+    unsigned long long *h_counts = nullptr;   // [0..4] counts + selected, [5] status
+    // state
+    bool executed = false, synced = false;
+    uint64_t returned = 0, result_rows = 0;
+    uint32_t retries = 0;
+    uint32_t launches = 0;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    tgpu_query_stats stats{};
+
+    ~tgpu_query() {
+        if (stream) cudaStreamSynchronize(stream);
+        release_workspace();
+        if (scratch) cudaFree(scratch);
+        if (h_cancel) cudaFreeHost(h_cancel);
+        if (h_counts) cudaFreeHost(h_counts);
+        for (auto e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+    void release_workspace() {
+        // a table the clear kernel never ran on (failed/cancelled execute) is dirty
+        g_pool.give(table_buf);
+        g_pool.give(occ_buf);
+        table_buf = occ_buf = Buffer();
+        for (auto &b : dset_bufs) g_pool.give(b);
+        dset_bufs.clear();
+    }
+};
+
+namespace {
+
+// Could row group `rg` hold a row satisfying `p`?  (statsOverlapPredicate,
+// predicate.zig:3380; rowGroupCanMatch, scan.zig:3539)
+bool rg_may_match(const tgpu_table *t, const Column &c, uint32_t rg, const tgpu_predicate &p) {
+    uint64_t rows = std::min<uint64_t>(t->rg_rows, t->n_rows - (uint64_t)rg * t->rg_rows);
+    uint64_t nulls = c.znull[rg];
+    uint64_t valid = rows - nulls;
+    if (p.op == TGPU_PRED_IS_NULL) return nulls > 0;
+    if (p.op == TGPU_PRED_IS_NOT_NULL) return valid > 0;
+    if (valid == 0) return false;
+    if (is_float_t(c.type)) {
+        double mn = c.zfmin[rg], mx = c.zfmax[rg];
+        switch (p.op) {
+            case TGPU_PRED_BETWEEN: return mx >= p.flo && mn <= p.fhi;
+            case TGPU_PRED_NOT_BETWEEN: return mn < p.flo || mx > p.fhi;
+            case TGPU_PRED_EQ: return p.flo >= mn && p.flo <= mx;
+            case TGPU_PRED_NE: return true;
+            case TGPU_PRED_LT: return mn < p.flo;
+            case TGPU_PRED_LE: return mn <= p.flo;
+            case TGPU_PRED_GT: return mx > p.flo;
+            default: return mx >= p.flo;
+        }
+    }
+    int64_t mn = c.zmin[rg], mx = c.zmax[rg];
+    switch (p.op) {
+        case TGPU_PRED_BETWEEN: return mx >= p.lo && mn <= p.hi;
+        case TGPU_PRED_NOT_BETWEEN: return mn < p.lo || mx > p.hi;
+        case TGPU_PRED_EQ: return p.lo >= mn && p.lo <= mx;
+        case TGPU_PRED_NE: return !(mn == mx && mn == p.lo);
+        case TGPU_PRED_LT: return mn < p.lo;
+        case TGPU_PRED_LE: return mn <= p.lo;
+        case TGPU_PRED_GT: return mx > p.lo;
+        default: return mx >= p.lo;
+    }
+}
+
+// Fraction of a column's values a predicate keeps, assuming values spread
+// uniformly between the column's global min and max (an allocation hint).
+double pred_selectivity(const tgpu_table *t, const Column &c, const tgpu_predicate &p) {
+    uint64_t nulls = 0;
+    for (uint32_t v : c.znull) nulls += v;
+    double valid_frac = t->n_rows ? 1.0 - (double)nulls / (double)t->n_rows : 1.0;
+    if (p.op == TGPU_PRED_IS_NULL) return 1.0 - valid_frac;
+    if (p.op == TGPU_PRED_IS_NOT_NULL) return valid_frac;
+    double lo, hi;
+    bool have = false;
+    double gmin = 0, gmax = 0;
+    for (uint32_t rg = 0; rg < t->n_rg; ++rg) {
+        uint64_t rows = std::min<uint64_t>(t->rg_rows, t->n_rows - (uint64_t)rg * t->rg_rows);
+        if (c.znull[rg] >= rows) continue;
+        double mn = is_float_t(c.type) ? c.zfmin[rg] : (double)c.zmin[rg];
+        double mx = is_float_t(c.type) ? c.zfmax[rg] : (double)c.zmax[rg];
+        if (!have) {
+            gmin = mn;
+            gmax = mx;
+            have = true;
+        } else {
+            gmin = std::min(gmin, mn);
+            gmax = std::max(gmax, mx);
+        }
+    }
+    if (!have) return 0.0;
+    const bool f = is_float_t(c.type);
+    lo = f ? p.flo : (double)p.lo;
+    hi = f ? p.fhi : (double)p.hi;
+    double span = gmax - gmin + (f ? 0.0 : 1.0);
+    if (span <= 0) span = 1.0;
+    auto frac = [&](double a, double b) {
+        double x = std::max(a, gmin), y = std::min(b, gmax);
+        if (y < x) return 0.0;
+        return std::min(1.0, (y - x + (f ? 0.0 : 1.0)) / span);
+    };
+    double s;
+    switch (p.op) {
+        case TGPU_PRED_BETWEEN: s = frac(lo, hi); break;
+        case TGPU_PRED_NOT_BETWEEN: s = 1.0 - frac(lo, hi); break;
+        case TGPU_PRED_EQ: s = 1.0 / (double)std::max<uint64_t>(1, c.ndv); break;
+        case TGPU_PRED_NE: s = 1.0; break;
+        case TGPU_PRED_LT: case TGPU_PRED_LE: s = frac(gmin, lo); break;
+        default: s = frac(lo, gmax); break;
+    }
+    return std::max(0.0, std::min(1.0, s)) * valid_frac;
+}
+
+int used_col(DevQuery &dq, std::vector<int> &map, const tgpu_table *t, int c) {
+    if (map[c] >= 0) return map[c];
+    if (dq.n_cols >= MAX_QCOLS) return -1;
+    const Column &col = t->cols[c];
+    DevCol &d = dq.cols[dq.n_cols];
+    d.data = col.d_data;
+    d.valid = col.d_valid;
+    d.type = col.type;
+    d.bytes = type_bytes(col.type);
+    map[c] = dq.n_cols++;
+    return map[c];
+}
+
+// validateShape (v2_shape_group_topn.zig:2051-2370) for this engine: integer /
+// DATE / DECIMAL64 / packed-id keys up to 128 packed bits, COUNT/SUM/AVG/MIN/
+// MAX/COUNT(DISTINCT) within thinDB's 16 state slots.  Strings other than
+// packed ids (hashed keys) decline to the next route.
+tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *req) {
+    DevQuery &dq = q->dq;
+    DevFinal &df = q->df;
+    std::memset(&dq, 0, sizeof(dq));
+    std::memset(&df, 0, sizeof(df));
+    std::vector<int> map(t->cols.size(), -1);
+
+    if (req->n_group_cols == 0 || req->n_group_cols > (uint32_t)MAX_GROUP_KEYS)
+        return fail(TGPU_DECLINE, "group key count");
+    if (req->n_aggs == 0 || req->n_aggs > (uint32_t)MAX_AGGS) return fail(TGPU_DECLINE, "aggregate count");
+    if (req->n_where > (uint32_t)MAX_PREDS) return fail(TGPU_DECLINE, "too many WHERE conjuncts");
+    if (req->n_order > (uint32_t)MAX_ORDER) return fail(TGPU_DECLINE, "too many ORDER BY keys");
+    if (req->n_having > (uint32_t)MAX_AGGS) return fail(TGPU_DECLINE, "too many HAVING conjuncts");
+
+    // WHERE
+    for (uint32_t i = 0; i < req->n_where; ++i) {
+        const tgpu_predicate &w = req->where[i];
+        if (w.column < 0 || (size_t)w.column >= t->cols.size())
+            return fail(TGPU_ERR_INVALID_ARGUMENT, "predicate column index");
+        if (w.op < TGPU_PRED_BETWEEN || w.op > TGPU_PRED_IS_NOT_NULL) return fail(TGPU_DECLINE, "predicate op");
+        const Column &c = t->cols[w.column];
+        if (c.type == TGPU_DICT32 && !(w.op == TGPU_PRED_EQ || w.op == TGPU_PRED_NE || w.op == TGPU_PRED_IS_NULL ||
+                                       w.op == TGPU_PRED_IS_NOT_NULL))
+            return fail(TGPU_DECLINE, "string range predicate");
+        DevPred &p = dq.preds[dq.n_preds++];
+        p.col = used_col(dq, map, t, w.column);
+        if (p.col < 0) return fail(TGPU_DECLINE, "too many columns");
+        p.op = w.op;
+        p.is_float = is_float_t(c.type);
+        p.lo = w.lo;
+        p.hi = w.hi;
+        p.flo = w.flo;
+        p.fhi = w.fhi;
+    }
+
+    // key layout
+    int off = 0;
+    for (uint32_t i = 0; i < req->n_group_cols; ++i) {
+        int c = req->group_cols[i];
+        if (c < 0 || (size_t)c >= t->cols.size()) return fail(TGPU_ERR_INVALID_ARGUMENT, "group column index");
+        const Column &col = t->cols[c];
+        int bits = type_bits(col.type);
+        if (bits == 0) return fail(TGPU_DECLINE, "group key type");
+        DevKeyPart &kp = dq.parts[dq.n_parts];
+        kp.col = used_col(dq, map, t, c);
+        if (kp.col < 0) return fail(TGPU_DECLINE, "too many columns");
+        kp.offset = off;
+        kp.payload = bits;
+        kp.nullable = col.nullable ? 1 : 0;
+        df.parts[dq.n_parts] = kp;
+        df.part_types[dq.n_parts] = col.type;
+        dq.n_parts++;
+        off += bits + kp.nullable;
+        tgpu_output_column oc{};
+        std::snprintf(oc.name, sizeof(oc.name), "%s", col.name.c_str());
+        oc.type = col.type;
+        oc.decimal_precision = (uint8_t)col.precision;
+        oc.decimal_scale = (uint8_t)col.scale;
+        oc.nullable = col.nullable;
+        oc.elem_bytes = type_bytes(col.type);
+        q->schema.push_back(oc);
+    }
+    if (off > 128) return fail(TGPU_DECLINE, "packed key wider than 128 bits (hashed keys)");
+    dq.key_words = off > 64 ? 2 : 1;
+
+    // aggregates and state words (word 0 = the group's row count)
+    int next = 1;
+    for (uint32_t i = 0; i < req->n_aggs; ++i) {
+        const tgpu_agg_spec &a = req->aggs[i];
+        DevAgg &g = dq.aggs[dq.n_aggs];
+        DevOut &o = df.outs[dq.n_aggs];
+        g.col = -1;
+        g.vword = -1;
+        o.vword = -1;
+        o.func = a.func;
+        int in_type = 0, scale = 0;
+        bool nullable = false;
+        if (a.column >= 0) {
+            if ((size_t)a.column >= t->cols.size()) return fail(TGPU_ERR_INVALID_ARGUMENT, "aggregate column index");
+            const Column &col = t->cols[a.column];
+            in_type = col.type;
+            nullable = col.nullable;
+            scale = col.type == TGPU_DECIMAL64 ? col.scale : 0;
+            g.col = used_col(dq, map, t, a.column);
+            if (g.col < 0) return fail(TGPU_DECLINE, "too many columns");
+            g.is_float_in = is_float_t(in_type);
+        }
+        int out_type = TGPU_BIGINT;
+        switch (a.func) {
+            case TGPU_AGG_COUNT:
+                if (nullable) {
+                    if (next > MAX_AGGS) return fail(TGPU_DECLINE, "aggregate state count");
+                    g.kind = AK_COUNT_VALID;
+                    g.word = next++;
+                } else {
+                    g.kind = AK_COUNT_ROWS;
+                    g.word = 0;
+                }
+                break;
+            case TGPU_AGG_SUM: case TGPU_AGG_AVG: case TGPU_AGG_MIN: case TGPU_AGG_MAX: {
+                if (a.column < 0) return fail(TGPU_ERR_INVALID_ARGUMENT, "aggregate column");
+                if (in_type == TGPU_DICT32) return fail(TGPU_DECLINE, "string aggregate");
+                bool sum = a.func == TGPU_AGG_SUM || a.func == TGPU_AGG_AVG;
+                if (sum && is_temporal(in_type)) return fail(TGPU_DECLINE, "temporal read as a number");
+                bool wide = sum && is_i64_phys(in_type);
+                int width = (wide ? 2 : 1) + (nullable ? 1 : 0);
+                if (next + width - 1 > MAX_AGGS) return fail(TGPU_DECLINE, "aggregate state count");
+                g.word = next;
+                g.vword = nullable ? next + width - 1 : -1;
+                next += width;
+                if (sum) {
+                    g.kind = is_float_t(in_type) ? AK_SUM_F64 : (wide ? AK_SUM_I128 : AK_SUM_I64);
+                    if (a.func == TGPU_AGG_SUM)
+                        out_type = in_type == TGPU_DECIMAL64 ? TGPU_DECIMAL128 : (is_float_t(in_type) ? TGPU_DOUBLE : TGPU_BIGINT);
+                    else
+                        out_type = TGPU_DOUBLE;
+                } else {
+                    bool mn = a.func == TGPU_AGG_MIN;
+                    g.kind = is_float_t(in_type) ? (mn ? AK_MIN_F : AK_MAX_F) : (mn ? AK_MIN_I : AK_MAX_I);
+                    out_type = in_type;
+                }
+                break;
+            }
+            case TGPU_AGG_COUNT_DISTINCT:
+                if (a.column < 0) return fail(TGPU_ERR_INVALID_ARGUMENT, "count distinct column");
+                if (dq.n_dsets >= MAX_DISTINCT) return fail(TGPU_DECLINE, "count distinct slot count");
+                if (next > MAX_AGGS) return fail(TGPU_DECLINE, "aggregate state count");
+                g.kind = AK_DISTINCT;
+                g.word = next++;
+                g.dset = dq.n_dsets++;
+                dq.needs_gid = 1;
+                break;
+            default:
+                return fail(TGPU_DECLINE, "aggregate func");
+        }
+        o.kind = g.kind;
+        o.word = g.word;
+        o.vword = g.vword;
+        o.out_type = out_type;
+        o.in_type = in_type;
+        o.scale = scale;
+        o.nullable = (nullable && (a.func == TGPU_AGG_SUM || a.func == TGPU_AGG_AVG || a.func == TGPU_AGG_MIN ||
+                                   a.func == TGPU_AGG_MAX)) ? 1 : 0;
+        dq.n_aggs++;
+        q->out_types.push_back(out_type);
+        tgpu_output_column oc{};
+        std::snprintf(oc.name, sizeof(oc.name), "%s", a.as ? a.as : "");
+        oc.type = out_type;
+        oc.nullable = o.nullable;
+        if (out_type == TGPU_DECIMAL128) {
+            oc.decimal_precision = 38;
+            oc.decimal_scale = (uint8_t)scale;
+        } else if (out_type == TGPU_DECIMAL64) {
+            oc.decimal_precision = (uint8_t)t->cols[a.column].precision;
+            oc.decimal_scale = (uint8_t)scale;
+        }
+        oc.elem_bytes = type_bytes(out_type);
+        q->schema.push_back(oc);
+    }
+    dq.state_words = next;
+    dq.slot_words = (int)next_pow2((uint64_t)(dq.key_words + dq.state_words));
+
+    for (uint32_t i = 0; i < req->n_order; ++i) {
+        const tgpu_sort_spec &s = req->order[i];
+        if (!((s.target == TGPU_SORT_KEY && s.index >= 0 && (uint32_t)s.index < req->n_group_cols) ||
+              (s.target == TGPU_SORT_AGG && s.index >= 0 && (uint32_t)s.index < req->n_aggs)))
+            return fail(TGPU_DECLINE, "order key");
+        df.order[i] = DevOrder{s.target, s.index, s.desc ? 1 : 0, 0};
+    }
+    for (uint32_t i = 0; i < req->n_having; ++i) {
+        const tgpu_having &h = req->having[i];
+        if (h.agg < 0 || (uint32_t)h.agg >= req->n_aggs || h.op < TGPU_PRED_EQ || h.op > TGPU_PRED_GE)
+            return fail(TGPU_DECLINE, "having");
+        df.having[i] = DevHaving{h.agg, h.op, h.ival, h.fval};
+    }
+    df.n_parts = dq.n_parts;
+    df.n_aggs = dq.n_aggs;
+    df.n_order = (int32_t)req->n_order;
+    df.n_having = (int32_t)req->n_having;
+    df.key_words = dq.key_words;
+    df.slot_words = dq.slot_words;
+    df.sort_words = 2 * (int32_t)req->n_order + 2;
+
+    // zone-map pruning -> the row groups the scan visits
+    q->rg_total = t->n_rg;
+    q->rg_list.clear();
+    uint64_t rows_scanned = 0;
+    for (uint32_t rg = 0; rg < t->n_rg; ++rg) {
+        bool keep = true;
+        for (uint32_t i = 0; i < req->n_where && keep; ++i)
+            keep = rg_may_match(t, t->cols[req->where[i].column], rg, req->where[i]);
+        if (keep) {
+            q->rg_list.push_back(rg);
+            rows_scanned += std::min<uint64_t>(t->rg_rows, t->n_rows - (uint64_t)rg * t->rg_rows);
+        }
+    }
+    q->rg_pruned = t->n_rg - (uint32_t)q->rg_list.size();
+    q->rows_scanned = rows_scanned;
+
+    double sel = 1.0;
+    for (uint32_t i = 0; i < req->n_where; ++i) sel *= pred_selectivity(t, t->cols[req->where[i].column], req->where[i]);
+    uint64_t sel_rows = (uint64_t)std::ceil((double)rows_scanned * std::min(1.0, sel * 1.25));
+    q->sel_est = sel_rows;
+    uint64_t groups = 1;
+    for (uint32_t i = 0; i < req->n_group_cols; ++i) {
+        const Column &c = t->cols[req->group_cols[i]];
+        uint64_t nd = std::max<uint64_t>(1, c.ndv) + (c.nullable ? 1 : 0);
+        groups = (groups > (1ULL << 40) / nd) ? (1ULL << 40) : groups * nd;
+    }
+    groups = std::min<uint64_t>(groups, std::max<uint64_t>(1, sel_rows));
+    if (req->expected_groups) groups = req->expected_groups;
+    q->groups_est = groups;
+    for (int d = 0; d < dq.n_dsets; ++d) {
+        // pairs <= rows that reach the fold, and <= groups * distinct values
+        int col = -1;
+        for (uint32_t i = 0; i < req->n_aggs; ++i)
+            if (dq.aggs[i].kind == AK_DISTINCT && dq.aggs[i].dset == d) col = req->aggs[i].column;
+        uint64_t ndv = std::max<uint64_t>(1, t->cols[col].ndv);
+        uint64_t pairs = groups > (1ULL << 40) / ndv ? (1ULL << 40) : groups * ndv;
+        pairs = std::min<uint64_t>(pairs, std::max<uint64_t>(1, sel_rows));
+        q->dset_need.push_back(pairs);
+    }
+    return TGPU_OK;
+}
+
+// Shared-memory cache size for a state width: the largest power of two that
+// keeps two CTAs per SM (<= ~100 KB each).
+int cache_slots_for(int state_words) {
+    size_t per = 12 + 8 * (size_t)state_words;
+    int c = 4096;
+    while (c > 64 && (size_t)c * per + SCAN_WARPS * 64 * 4 + 16 > 100 * 1024) c >>= 1;
+    return c;
+}
+
+tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
+    DevQuery &dq = q->dq;
+    DevFinal &df = q->df;
+    cap = std::max<uint64_t>(cap, 64);
+    if (cap > (1ULL << 31)) return fail(TGPU_ERR_MEMORY_BUDGET, "group table would exceed 2^31 slots");
+    dq.cap = cap;
+    df.cap = cap;
+
+    // route: the shared-memory cache holds every group (lowcard), pre-folds
+    // hot keys with periodic flushes (global route), or is off.
+    dq.cache_slots = 0;
+    dq.cache_flush_at = 0;
+    q->route = 2;
+    if (dq.key_words == 1 && !(q->flags & TGPU_FLAG_FORCE_GLOBAL)) {
+        int C = cache_slots_for(dq.state_words);
+        if (q->groups_est * 2 <= (uint64_t)C) {
+            dq.cache_slots = C;
+            dq.cache_flush_at = C;  // resident: never flushed before the end
+            q->route = 1;
+        } else if (!dq.needs_gid) {
+            dq.cache_slots = C;
+            dq.cache_flush_at = C * 3 / 4;
+        }
+    }
+    dq.warp_combine = (q->flags & TGPU_FLAG_NO_WARP_COMBINE) ? 0 : 1;
+    dq.gather = (dq.n_preds > 0 && !(q->flags & TGPU_FLAG_DENSE_SCAN)) ? 1 : 0;
+
+    // ranking
+    if (df.n_order == 0 && q->limit == TGPU_NO_LIMIT && q->offset == 0) {
+        q->rank = RANK_NONE;
+        q->out_rows_max = cap + 1;
+    } else if (q->limit != TGPU_NO_LIMIT && q->offset + q->limit <= 32) {
+        q->rank = RANK_TOPK;
+        q->k = (uint32_t)(q->offset + q->limit);
+        q->out_rows_max = q->limit;
+    } else {
+        q->rank = RANK_SORT;
+        q->out_rows_max = q->limit == TGPU_NO_LIMIT ? cap + 1 : std::min<uint64_t>(q->limit, cap + 1);
+    }
+
+    // bytes
+    const uint64_t slots = cap + 1;
+    const size_t table_bytes = slots * (size_t)dq.slot_words * 8;
+    const size_t occ_bytes = ((slots + 31) / 32) * 4;
+    std::vector<uint64_t> dcap;
+    size_t dset_bytes = 0;
+    for (uint64_t need : q->dset_need) {
+        uint64_t c = next_pow2(std::max<uint64_t>(64, need * 2));
+        dcap.push_back(c);
+        dset_bytes += c * 16;
+    }
+    q->n_cpt_blocks = compact_blocks(cap);
+    q->n_cand_blocks = 152;
+    size_t row_bytes = 0;
+    for (auto &oc : q->schema) row_bytes += oc.elem_bytes + 1;
+    const size_t sw = (size_t)df.sort_words;
+    size_t scratch = 0;
+    auto add = [&](size_t b) {
+        size_t o = scratch;
+        scratch += (b + 255) & ~(size_t)255;
+        return o;
+    };
+    size_t o_ctrl = add(16), o_counts = add(8 * 8), o_bc = add(4 * (size_t)q->n_cpt_blocks), o_gids = add(4 * slots);
+    size_t o_ck = 0, o_cg = 0, o_sel = 0, o_sk0 = 0, o_sk1 = 0, o_si0 = 0, o_si1 = 0;
+    if (q->rank == RANK_TOPK) {
+        o_ck = add((size_t)q->n_cand_blocks * 32 * sw * 8);
+        o_cg = add((size_t)q->n_cand_blocks * 32 * 4);
+        o_sel = add(32 * 4);
+    } else if (q->rank == RANK_SORT) {
+        o_sk0 = add(slots * sw * 8);
+        o_sk1 = add(slots * sw * 8);
+        o_si0 = add(slots * 4);
+        o_si1 = add(slots * 4);
+    }
+    size_t o_rg = add(4 * std::max<size_t>(1, q->rg_list.size()));
+    std::vector<size_t> o_out, o_val;
+    for (auto &oc : q->schema) {
+        o_out.push_back(add(q->out_rows_max * oc.elem_bytes));
+        o_val.push_back(add(q->out_rows_max));
+    }
+    size_t o_ptrs = add(q->schema.size() * 8), o_vptrs = add(q->schema.size() * 8);
+    (void)row_bytes;
+
+    const size_t total = table_bytes + occ_bytes + dset_bytes + scratch;
+    if (q->budget && total > q->budget)
+        return fail(TGPU_ERR_MEMORY_BUDGET, "query needs " + std::to_string(total) + " device bytes, budget " +
+                                                std::to_string(q->budget));
+
+    q->release_workspace();
+    tgpu_status st;
+    if ((st = g_pool.take(table_bytes, q->stream, &q->table_buf)) != TGPU_OK) return st;
+    if ((st = g_pool.take(occ_bytes, q->stream, &q->occ_buf)) != TGPU_OK) return st;
+    for (size_t d = 0; d < dcap.size(); ++d) {
+        Buffer b;
+        if ((st = g_pool.take(dcap[d] * 16, q->stream, &b)) != TGPU_OK) return st;
+        q->dset_bufs.push_back(b);
+        dq.dset[d] = (unsigned long long *)b.p;
+        dq.dset_cap[d] = dcap[d];
+    }
+    if (scratch > q->scratch_bytes) {
+        if (q->scratch) CU(cudaFree(q->scratch));
+        q->scratch = nullptr;
+        CU(cudaMalloc(&q->scratch, scratch));
+        q->scratch_bytes = scratch;
+    }
+    char *base = (char *)q->scratch;
+    q->d_ctrl = (unsigned int *)(base + o_ctrl);
+    q->d_counts = (unsigned long long *)(base + o_counts);
+    q->d_block_counts = (uint32_t *)(base + o_bc);
+    q->d_gids = (uint32_t *)(base + o_gids);
+    q->d_cand_keys = q->rank == RANK_TOPK ? (unsigned long long *)(base + o_ck) : nullptr;
+    q->d_cand_gids = q->rank == RANK_TOPK ? (uint32_t *)(base + o_cg) : nullptr;
+    q->d_sel = q->rank == RANK_TOPK ? (uint32_t *)(base + o_sel) : nullptr;
+    if (q->rank == RANK_SORT) {
+        q->d_sort_keys[0] = (unsigned long long *)(base + o_sk0);
+        q->d_sort_keys[1] = (unsigned long long *)(base + o_sk1);
+        q->d_sort_ids[0] = (uint32_t *)(base + o_si0);
+        q->d_sort_ids[1] = (uint32_t *)(base + o_si1);
+    }
+    q->d_rg_list = (uint32_t *)(base + o_rg);
+    q->d_out.clear();
+    q->d_outvalid.clear();
+    for (size_t c = 0; c < q->schema.size(); ++c) {
+        q->d_out.push_back(base + o_out[c]);
+        q->d_outvalid.push_back((uint8_t *)(base + o_val[c]));
+    }
+    q->d_out_ptrs = (void **)(base + o_ptrs);
+    q->d_valid_ptrs = (uint8_t **)(base + o_vptrs);
+    CU(cudaMemcpyAsync(q->d_out_ptrs, q->d_out.data(), q->schema.size() * 8, cudaMemcpyHostToDevice, q->stream));
+    CU(cudaMemcpyAsync(q->d_valid_ptrs, q->d_outvalid.data(), q->schema.size() * 8, cudaMemcpyHostToDevice, q->stream));
+    if (!q->rg_list.empty())
+        CU(cudaMemcpyAsync(q->d_rg_list, q->rg_list.data(), 4 * q->rg_list.size(), cudaMemcpyHostToDevice, q->stream));
+    // the host vectors above are read by the copies: finish them before returning
+    CU(cudaStreamSynchronize(q->stream));
+
+    dq.table = (unsigned long long *)q->table_buf.p;
+    dq.occ = (uint32_t *)q->occ_buf.p;
+    df.table = dq.table;
+    df.occ = dq.occ;
+    dq.tile_counter = q->d_ctrl;
+    dq.status = q->d_ctrl + 1;
+    dq.selected_rows = q->d_counts + 4;
+    dq.cancel = (const volatile int *)q->d_cancel;
+    const tgpu_table *t = q->t;
+    dq.n_rows = t->n_rows;
+    dq.rg_rows = t->rg_rows;
+    const bool pruned = q->rg_list.size() != t->n_rg;
+    if (pruned) {
+        dq.rg_list = q->d_rg_list;
+        dq.n_rg = (uint32_t)q->rg_list.size();
+        dq.tiles_per_rg = (t->rg_rows + TILE_ROWS - 1) / TILE_ROWS;
+        dq.n_tiles = dq.n_rg * dq.tiles_per_rg;
+    } else {
+        dq.rg_list = nullptr;
+        dq.n_rg = t->n_rg;
+        dq.tiles_per_rg = 0;
+        dq.n_tiles = (uint32_t)((t->n_rows + TILE_ROWS - 1) / TILE_ROWS);
+    }
+    return TGPU_OK;
+}
+
+tgpu_status enqueue(tgpu_query *q) {
+    DevQuery &dq = q->dq;
+    DevFinal &df = q->df;
+    cudaStream_t s = q->stream;
+    q->launches = 0;
+    // epochs for the distinct sets
+    uint32_t epoch = 0;
+    for (auto &b : q->dset_bufs) epoch = std::max(epoch, b.epoch);
+    ++epoch;
+    if (epoch == 0xFFFFFFFFu) {
+        for (auto &b : q->dset_bufs) {
+            CU(cudaMemsetAsync(b.p, 0, b.bytes, s));
+            b.epoch = 0;
+        }
+        epoch = 1;
+    }
+    for (auto &b : q->dset_bufs) b.epoch = epoch;
+    dq.epoch = epoch;
+    q->table_buf.dirty = true;  // until the clear kernel has run
+    q->occ_buf.dirty = true;
+
+    CU(cudaMemsetAsync(q->d_ctrl, 0, 16, s));
+    CU(cudaMemsetAsync(q->d_counts, 0, 8 * 8, s));
+    const bool timing = (q->flags & TGPU_FLAG_TIMING) != 0;
+    if (timing) CU(cudaEventRecord(q->ev[0], s));
+    if (dq.n_tiles > 0) {
+        CU(launch_scan(dq, q->grid, s));
+        q->launches++;
+    }
+    if (timing) CU(cudaEventRecord(q->ev[1], s));
+    CU(launch_compact(df, q->d_block_counts, q->n_cpt_blocks, q->d_gids, q->d_counts, s));
+    q->launches += 2;
+    const uint32_t *sel = q->d_gids;
+    uint64_t gather_offset = 0, gather_rows = q->out_rows_max;
+    if (q->rank == RANK_NONE) {
+        CU(launch_sel_all(q->d_counts, s));
+        q->launches++;
+    } else if (q->rank == RANK_TOPK) {
+        CU(launch_topk(df, q->d_gids, q->d_counts, q->k, q->d_cand_keys, q->d_cand_gids, q->n_cand_blocks, q->d_sel, s));
+        q->launches += 2;
+        sel = q->d_sel;
+        gather_offset = q->offset;
+        gather_rows = q->limit;
+    } else {
+        uint32_t *sorted = nullptr;
+        CU(launch_sort(df, q->d_gids, q->d_counts, dq.cap + 1, q->d_sort_keys[0], q->d_sort_keys[1], q->d_sort_ids[0],
+                       q->d_sort_ids[1], &sorted, s));
+        uint64_t passes = 0;
+        for (uint64_t w = 1024; w < dq.cap + 1; w <<= 1) ++passes;
+        q->launches += 3 + (uint32_t)passes;
+        sel = sorted;
+        gather_offset = q->offset;
+        gather_rows = q->out_rows_max;
+    }
+    CU(launch_gather(df, sel, q->d_counts, gather_offset, gather_rows, q->d_out_ptrs, q->d_valid_ptrs, s));
+    CU(launch_clear(dq.table, dq.cap, dq.slot_words, dq.occ, s));
+    q->launches += 2;
+    if (timing) CU(cudaEventRecord(q->ev[2], s));
+    CU(cudaMemcpyAsync(q->h_counts, q->d_counts, 5 * 8, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(q->h_counts + 5, q->d_ctrl + 1, 4, cudaMemcpyDeviceToHost, s));
+    q->executed = true;
+    q->synced = false;
+    q->returned = 0;
+    return TGPU_OK;
+}
+
+tgpu_status finish(tgpu_query *q) {
+    for (;;) {
+        CU(cudaStreamSynchronize(q->stream));
+        q->table_buf.dirty = false;
+        q->occ_buf.dirty = false;
+        const uint32_t status = (uint32_t)(q->h_counts[5] & 0xFFFFFFFFu);
+        if (status & ST_CANCELLED) {
+            q->synced = true;
+            q->result_rows = 0;
+            return fail(TGPU_ERR_CANCELLED, "query cancelled");
+        }
+        if (status & (ST_TABLE_FULL | ST_DISTINCT_FULL)) {
+            if (++q->retries > 4) return fail(TGPU_ERR_INTERNAL, "group table kept overflowing");
+            if (status & ST_TABLE_FULL) q->groups_est = std::max<uint64_t>(q->groups_est * 4, 1024);
+            if (status & ST_DISTINCT_FULL)
+                for (auto &n : q->dset_need) n *= 4;
+            tgpu_status st = size_workspace(q, next_pow2(q->groups_est * 2));
+            if (st != TGPU_OK) return st;
+            st = enqueue(q);
+            if (st != TGPU_OK) return st;
+            continue;
+        }
+        break;
+    }
+    q->synced = true;
+    q->result_rows = q->h_counts[2];
+    tgpu_query_stats &s = q->stats;
+    s.rows_scanned = q->rows_scanned;
+    s.rows_selected = q->h_counts[4];
+    s.groups = q->h_counts[0];
+    s.result_rows = q->h_counts[2];
+    s.table_capacity = q->dq.cap;
+    s.distinct_capacity = q->dq.n_dsets ? q->dq.dset_cap[0] : 0;
+    s.row_groups_total = q->rg_total;
+    s.row_groups_pruned = q->rg_pruned;
+    s.route = (uint32_t)q->route;
+    s.retries = q->retries;
+    s.kernel_launches = q->launches;
+    s.device_bytes = q->table_buf.bytes + q->occ_buf.bytes + q->scratch_bytes;
+    for (auto &b : q->dset_bufs) s.device_bytes += b.bytes;
+    if (q->flags & TGPU_FLAG_TIMING) {
+        float a = 0, b = 0, c = 0;
+        CU(cudaEventElapsedTime(&a, q->ev[0], q->ev[1]));
+        CU(cudaEventElapsedTime(&b, q->ev[1], q->ev[2]));
+        CU(cudaEventElapsedTime(&c, q->ev[0], q->ev[2]));
+        s.scan_ms = a;
+        s.finalize_ms = b;
+        s.total_ms = c;
+    }
+    return TGPU_OK;
+}
+
+}  // namespace
+
+// ================================================================ C ABI ====
+
+extern "C" {
+
+uint32_t tgpu_abi_version(void) { return TGPU_ABI_VERSION; }
+
+const char *tgpu_build_info(void) {
+    static char buf[128];
+    std::snprintf(buf, sizeof(buf), "thindb_gpu sm_103a cuda %d.%d", CUDART_VERSION / 1000, (CUDART_VERSION % 1000) / 10);
+    return buf;
+}
+
+const char *tgpu_last_error_message(void) { return g_err.c_str(); }
+
+tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out) {
+    if (!desc || !out) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
+    if (desc->n_columns == 0 || !desc->columns) return fail(TGPU_ERR_INVALID_ARGUMENT, "no columns");
+    DeviceCtx *dev;
+    tgpu_status st = device_ctx(&dev);
+    if (st != TGPU_OK) return st;
+    cudaStream_t s = desc->stream ? (cudaStream_t)desc->stream : dev->stream;
+    std::unique_ptr<tgpu_table> t(new tgpu_table());
+    t->n_rows = desc->n_rows;
+    t->rg_rows = desc->row_group_rows ? desc->row_group_rows : 65536u;
+    t->n_rg = (uint32_t)((t->n_rows + t->rg_rows - 1) / t->rg_rows);
+    const uint64_t n = t->n_rows;
+    const uint64_t vwords = (n + 31) / 32 + 1;
+    int64_t *d_imin = nullptr, *d_imax = nullptr;
+    double *d_fmin = nullptr, *d_fmax = nullptr;
+    uint32_t *d_nulls = nullptr, *d_regs = nullptr;
+    const size_t nrg = std::max<uint32_t>(1, t->n_rg);
+    CU(cudaMallocAsync((void **)&d_imin, nrg * 8, s));
+    CU(cudaMallocAsync((void **)&d_imax, nrg * 8, s));
+    CU(cudaMallocAsync((void **)&d_fmin, nrg * 8, s));
+    CU(cudaMallocAsync((void **)&d_fmax, nrg * 8, s));
+    CU(cudaMallocAsync((void **)&d_nulls, nrg * 4, s));
+    CU(cudaMallocAsync((void **)&d_regs, (1u << HLL_P) * 4, s));
+    for (uint32_t i = 0; i < desc->n_columns; ++i) {
+        const tgpu_column_desc &cd = desc->columns[i];
+        if (cd.type < TGPU_BOOLEAN || cd.type > TGPU_DICT32 || cd.type == TGPU_DECIMAL128)
+            return fail(TGPU_ERR_UNSUPPORTED_TYPE, "column type");
+        if (n && !cd.data) return fail(TGPU_ERR_INVALID_ARGUMENT, "column without data");
+        t->cols.emplace_back();
+        Column &c = t->cols.back();
+        c.name = cd.name ? cd.name : "";
+        c.type = cd.type;
+        c.precision = cd.decimal_precision;
+        c.scale = cd.decimal_scale;
+        c.nullable = cd.validity != nullptr;
+        const size_t bytes = n * type_bytes(cd.type);
+        if (desc->location == TGPU_LOC_DEVICE) {
+            c.d_data = const_cast<void *>(cd.data);
+            c.owned = false;
+        } else {
+            CU(cudaMalloc(&c.d_data, std::max<size_t>(bytes, 16)));
+            c.owned = true;
+            if (bytes) CU(cudaMemcpyAsync(c.d_data, cd.data, bytes, cudaMemcpyHostToDevice, s));
+        }
+        if (cd.validity) {
+            CU(cudaMalloc((void **)&c.d_valid, vwords * 4));
+            CU(cudaMemsetAsync(c.d_valid, 0, vwords * 4, s));
+            CU(cudaMemcpyAsync(c.d_valid, cd.validity, (n + 7) / 8,
+                               desc->location == TGPU_LOC_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+        }
+        if (cd.type == TGPU_DICT32 && cd.dict_offsets && cd.dict_size) {
+            c.dict_offsets.assign(cd.dict_offsets, cd.dict_offsets + cd.dict_size + 1);
+            c.dict_bytes.assign(cd.dict_bytes, cd.dict_bytes + cd.dict_offsets[cd.dict_size]);
+        }
+        c.zmin.resize(t->n_rg);
+        c.zmax.resize(t->n_rg);
+        c.zfmin.resize(t->n_rg);
+        c.zfmax.resize(t->n_rg);
+        c.znull.resize(t->n_rg);
+        if (t->n_rg) {
+            CU(launch_zone_maps(c.d_data, c.d_valid, c.type, n, t->rg_rows, t->n_rg, d_imin, d_imax, d_fmin, d_fmax,
+                                d_nulls, s));
+            CU(cudaMemcpyAsync(c.zmin.data(), d_imin, t->n_rg * 8, cudaMemcpyDeviceToHost, s));
+            CU(cudaMemcpyAsync(c.zmax.data(), d_imax, t->n_rg * 8, cudaMemcpyDeviceToHost, s));
+            CU(cudaMemcpyAsync(c.zfmin.data(), d_fmin, t->n_rg * 8, cudaMemcpyDeviceToHost, s));
+            CU(cudaMemcpyAsync(c.zfmax.data(), d_fmax, t->n_rg * 8, cudaMemcpyDeviceToHost, s));
+            CU(cudaMemcpyAsync(c.znull.data(), d_nulls, t->n_rg * 4, cudaMemcpyDeviceToHost, s));
+            CU(cudaStreamSynchronize(s));
+        }
+        c.ndv = cd.ndv_hint;
+        if (!c.ndv && desc->compute_ndv && n) {
+            CU(cudaMemsetAsync(d_regs, 0, (1u << HLL_P) * 4, s));
+            CU(launch_hll(c.d_data, c.d_valid, c.type, n, d_regs, s));
+            std::vector<uint32_t> regs(1u << HLL_P);
+            CU(cudaMemcpyAsync(regs.data(), d_regs, regs.size() * 4, cudaMemcpyDeviceToHost, s));
+            CU(cudaStreamSynchronize(s));
+            c.ndv = (uint64_t)std::llround(hll_estimate(regs));
+        }
+        if (!c.ndv) {
+            // without a sketch: bounded by the type's domain and the row count
+            uint64_t dom = type_bits(c.type) && type_bits(c.type) < 40 ? (1ULL << type_bits(c.type)) : n;
+            if (c.type == TGPU_DICT32 && c.dict_offsets.size() > 1) dom = c.dict_offsets.size() - 1;
+            c.ndv = std::max<uint64_t>(1, std::min<uint64_t>(dom, n));
+        }
+    }
+    CU(cudaFreeAsync(d_imin, s));
+    CU(cudaFreeAsync(d_imax, s));
+    CU(cudaFreeAsync(d_fmin, s));
+    CU(cudaFreeAsync(d_fmax, s));
+    CU(cudaFreeAsync(d_nulls, s));
+    CU(cudaFreeAsync(d_regs, s));
+    CU(cudaStreamSynchronize(s));
+    *out = t.release();
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_table_destroy(tgpu_table *table) {
+    if (!table) return fail(TGPU_ERR_INVALID_ARGUMENT, "null table");
+    delete table;
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_table_info(const tgpu_table *t, int32_t column, uint64_t *n_rows, uint32_t *n_rg, uint64_t *ndv) {
+    if (!t) return fail(TGPU_ERR_INVALID_ARGUMENT, "null table");
+    if (n_rows) *n_rows = t->n_rows;
+    if (n_rg) *n_rg = t->n_rg;
+    if (ndv) {
+        if (column < 0 || (size_t)column >= t->cols.size()) *ndv = 0;
+        else *ndv = t->cols[column].ndv;
+    }
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_query_create(tgpu_table *table, const tgpu_request *req, tgpu_query **out) {
+    if (!table || !req || !out) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
+    DeviceCtx *dev;
+    tgpu_status st = device_ctx(&dev);
+    if (st != TGPU_OK) return st;
+    std::unique_ptr<tgpu_query> q(new tgpu_query());
+    q->t = table;
+    q->stream = req->stream ? (cudaStream_t)req->stream : dev->stream;
+    q->flags = req->flags;
+    q->limit = req->limit;
+    q->offset = req->offset;
+    q->budget = req->memory_budget_bytes;
+    st = plan_query(q.get(), table, req);
+    if (st != TGPU_OK) return st;
+    CU(cudaHostAlloc((void **)&q->h_cancel, sizeof(int), cudaHostAllocMapped));
+    *q->h_cancel = 0;
+    CU(cudaHostGetDevicePointer((void **)&q->d_cancel, q->h_cancel, 0));
+    CU(cudaHostAlloc((void **)&q->h_counts, 8 * 8, cudaHostAllocDefault));
+    std::memset(q->h_counts, 0, 64);
+    for (auto &e : q->ev) CU(cudaEventCreate(&e));
+    st = size_workspace(q.get(), next_pow2(std::max<uint64_t>(64, q->groups_est * 2)));
+    if (st != TGPU_OK) return st;
+    q->grid = scan_grid_size(q->dq, dev->sms);
+    *out = q.release();
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_query_output_schema(const tgpu_query *q, tgpu_output_column *cols, uint32_t cap, uint32_t *n) {
+    if (!q) return fail(TGPU_ERR_INVALID_ARGUMENT, "null query");
+    if (n) *n = (uint32_t)q->schema.size();
+    for (uint32_t i = 0; cols && i < cap && i < q->schema.size(); ++i) cols[i] = q->schema[i];
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_query_execute(tgpu_query *q) {
+    if (!q) return fail(TGPU_ERR_INVALID_ARGUMENT, "null query");
+    if (*q->h_cancel) return fail(TGPU_ERR_CANCELLED, "query cancelled");
+    return enqueue(q);
+}
+
+tgpu_status tgpu_query_synchronize(tgpu_query *q) {
+    if (!q) return fail(TGPU_ERR_INVALID_ARGUMENT, "null query");
+    if (!q->executed) return TGPU_OK;
+    if (!q->synced) return finish(q);
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_query_next(tgpu_query *q, tgpu_batch *b, int32_t *done) {
+    if (!q || !b || !done) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
+    if (*q->h_cancel) return fail(TGPU_ERR_CANCELLED, "query cancelled");  // Query.next checks first (exec.zig:914)
+    tgpu_status st;
+    if (!q->executed && (st = enqueue(q)) != TGPU_OK) return st;
+    if (!q->synced && (st = finish(q)) != TGPU_OK) return st;
+    if (b->n_columns != q->schema.size()) return fail(TGPU_ERR_INVALID_ARGUMENT, "batch column count");
+    const uint64_t n = std::min<uint64_t>(b->capacity_rows, q->result_rows - q->returned);
+    std::vector<uint8_t> vbytes(n);
+    for (size_t c = 0; c < q->schema.size(); ++c) {
+        const size_t eb = q->schema[c].elem_bytes;
+        if (n && b->values && b->values[c])
+            CU(cudaMemcpyAsync(b->values[c], (char *)q->d_out[c] + q->returned * eb, n * eb, cudaMemcpyDeviceToHost,
+                               q->stream));
+        if (n && b->validity && b->validity[c]) {
+            CU(cudaMemcpyAsync(vbytes.data(), q->d_outvalid[c] + q->returned, n, cudaMemcpyDeviceToHost, q->stream));
+            CU(cudaStreamSynchronize(q->stream));
+            uint8_t *bm = b->validity[c];
+            std::memset(bm, 0, (n + 7) / 8);
+            for (uint64_t r = 0; r < n; ++r)
+                if (vbytes[r]) bm[r >> 3] |= (uint8_t)(1u << (r & 7));
+        }
+    }
+    CU(cudaStreamSynchronize(q->stream));
+    q->returned += n;
+    b->row_count = n;
+    *done = q->returned >= q->result_rows ? 1 : 0;
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_query_cancel(tgpu_query *q) {
+    if (!q) return fail(TGPU_ERR_INVALID_ARGUMENT, "null query");
+    __atomic_store_n(q->h_cancel, 1, __ATOMIC_SEQ_CST);
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_query_get_stats(const tgpu_query *q, tgpu_query_stats *out) {
+    if (!q || !out) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
+    *out = q->stats;
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_query_destroy(tgpu_query *q) {
+    if (!q) return fail(TGPU_ERR_INVALID_ARGUMENT, "null query");
+    delete q;
+    return TGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,208 @@
+// engine.h — internal plan, device descriptors and launch entry points of the
+// GB300 grouped-aggregation engine (behind include/thindb_gpu.h).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/thindb_gpu.h"
+
+namespace tgpu {
+
+constexpr int MAX_GROUP_KEYS = 8;   // thinDB MAX_GROUP_KEYS (v2_shape_group_topn.zig:50)
+constexpr int MAX_AGGS = 16;        // thinDB MAX_AGGS (v2_shape_group_topn.zig:54)
+constexpr int MAX_STATE_WORDS = 17; // the row count + 16 numeric slots
+constexpr int MAX_DISTINCT = 8;     // thinDB MAX_DISTINCT_AGG_SLOTS (v2_shape_group_topn.zig:62)
+constexpr int MAX_PREDS = 8;
+constexpr int MAX_QCOLS = 24;       // distinct columns one query reads
+constexpr int MAX_ORDER = 6;
+constexpr int MAX_SORT_WORDS = 2 * MAX_ORDER + 2;
+
+// Scan geometry: persistent CTAs claim tiles of TILE_ROWS rows; each of the
+// CTA's warps owns TILE_ROWS / WARPS consecutive rows of the tile.
+constexpr int SCAN_THREADS = 512;
+constexpr int SCAN_WARPS = SCAN_THREADS / 32;
+constexpr int TILE_ROWS = 8192;
+constexpr int WARP_ROWS = TILE_ROWS / SCAN_WARPS;  // 512
+
+// Status bits the kernels OR into the query's device status word.
+constexpr unsigned ST_TABLE_FULL = 1u;      // a probe ran past MAX_PROBE: regrow and rerun
+constexpr unsigned ST_DISTINCT_FULL = 2u;   // a distinct set probe ran past MAX_PROBE
+constexpr unsigned ST_CANCELLED = 4u;       // the host cancel flag was seen
+constexpr unsigned ST_BAD_INDEX = 8u;       // a bounds check caught an index (never expected)
+constexpr unsigned MAX_PROBE = 4096;
+
+// Aggregate fold kinds (one state word each unless noted).
+enum AggKind : int32_t {
+    AK_COUNT_ROWS = 0,   // COUNT(*) / non-nullable COUNT(col): word 0
+    AK_COUNT_VALID = 1,  // nullable COUNT(col): own word
+    AK_SUM_I64 = 2,      // SUM/AVG over 8/16/32-bit ints: wrapping u64 word
+    AK_SUM_I128 = 3,     // SUM/AVG over 64-bit ints / DECIMAL64: lo, hi words
+    AK_SUM_F64 = 4,      // SUM/AVG over FLOAT/DOUBLE: f64 word
+    AK_MIN_I = 5,        // ~enc_i64 word, folded by atomicMax
+    AK_MAX_I = 6,        // enc_i64 word
+    AK_MIN_F = 7,        // ~enc_f64 word
+    AK_MAX_F = 8,        // enc_f64 word
+    AK_DISTINCT = 9      // count word + a (group, value) set
+};
+
+struct DevCol {
+    const void *data;
+    const uint32_t *valid;  // validity bitmap as little-endian u32 words, nullptr = NOT NULL
+    int32_t type;           // tgpu_type
+    int32_t bytes;          // element width
+};
+
+struct DevPred {
+    int32_t col;            // index into DevQuery::cols
+    int32_t op;             // tgpu_pred_op
+    int32_t is_float;
+    int32_t pad;
+    int64_t lo, hi;
+    double flo, fhi;
+};
+
+struct DevKeyPart {
+    int32_t col;
+    int32_t offset;         // bit offset in the packed key
+    int32_t payload;        // payload bits (type width)
+    int32_t nullable;       // validity bit at offset + payload
+};
+
+struct DevAgg {
+    int32_t kind;           // AggKind
+    int32_t col;            // DevQuery::cols index, -1 for COUNT(*)
+    int32_t word;           // first state word
+    int32_t vword;          // valid-count word, -1 = none
+    int32_t dset;           // distinct set index (AK_DISTINCT)
+    int32_t is_float_in;    // input column is FLOAT/DOUBLE
+};
+
+// Everything a scan launch needs, passed by value (kernel parameter).
+struct DevQuery {
+    // rows
+    uint64_t n_rows;
+    const uint32_t *rg_list;  // surviving row groups, nullptr = every row group
+    uint32_t n_rg;            // row groups iterated (list length or total)
+    uint32_t rg_rows;
+    uint32_t tiles_per_rg;
+    uint32_t n_tiles;
+    // columns / predicates / key / aggregates
+    DevCol cols[MAX_QCOLS];
+    int32_t n_cols;
+    int32_t n_preds;
+    DevPred preds[MAX_PREDS];
+    DevKeyPart parts[MAX_GROUP_KEYS];
+    int32_t n_parts;
+    int32_t key_words;        // 1 or 2
+    DevAgg aggs[MAX_AGGS];
+    int32_t n_aggs;
+    int32_t state_words;      // row count + slots
+    int32_t slot_words;       // key_words + state_words rounded to a power of two
+    int32_t needs_gid;        // a distinct aggregate needs each row's group slot
+    // global group table: capacity + 1 slots (the last one holds the all-zero key)
+    unsigned long long *table;
+    uint64_t cap;             // power of two
+    uint32_t *occ;            // occupancy bitmap, cap + 1 bits
+    // distinct sets: entries of {value u64, gid u32 | epoch << 32}
+    unsigned long long *dset[MAX_DISTINCT];
+    uint64_t dset_cap[MAX_DISTINCT];
+    uint32_t epoch;
+    int32_t n_dsets;
+    // shared-memory pre-aggregation (0 slots = off)
+    int32_t cache_slots;      // power of two
+    int32_t cache_flush_at;   // flush + clear once this many entries are live
+    int32_t warp_combine;     // __match_any_sync pre-combine on/off
+    int32_t gather;           // 1 = compact survivors, then gather; 0 = process rows in place
+    // control
+    unsigned int *tile_counter;
+    unsigned int *status;
+    const volatile int *cancel;           // host-mapped cancel flag (may be nullptr)
+    unsigned long long *selected_rows;    // rows that passed WHERE
+};
+
+// Ranking / emit descriptors -------------------------------------------------
+
+struct DevOrder {
+    int32_t target;           // TGPU_SORT_KEY / TGPU_SORT_AGG
+    int32_t index;            // key part / aggregate index
+    int32_t desc;
+    int32_t pad;
+};
+
+// How one output aggregate column is finalised from the state words.
+struct DevOut {
+    int32_t func;             // tgpu_agg_func
+    int32_t kind;             // AggKind of the state
+    int32_t word;
+    int32_t vword;
+    int32_t out_type;         // tgpu_type of the emitted column
+    int32_t in_type;
+    int32_t scale;            // DECIMAL input scale (AVG divides by 10^scale)
+    int32_t nullable;         // all-NULL input groups emit NULL
+};
+
+struct DevHaving {
+    int32_t agg;
+    int32_t op;
+    int64_t ival;
+    double fval;
+};
+
+struct DevFinal {
+    const unsigned long long *table;
+    uint64_t cap;
+    const uint32_t *occ;
+    int32_t key_words;
+    int32_t slot_words;
+    int32_t n_parts;
+    int32_t n_aggs;
+    int32_t n_order;
+    int32_t n_having;
+    int32_t sort_words;       // words of one encoded sort key
+    int32_t pad;
+    DevKeyPart parts[MAX_GROUP_KEYS];
+    int32_t part_types[MAX_GROUP_KEYS];
+    DevOut outs[MAX_AGGS];
+    DevOrder order[MAX_ORDER];
+    DevHaving having[MAX_AGGS];
+};
+
+// Launchers (scan.cu / finalize.cu / table.cu) --------------------------------
+
+int scan_grid_size(const DevQuery &q, int device_sms);
+size_t scan_smem_bytes(const DevQuery &q);
+cudaError_t launch_scan(const DevQuery &q, int grid, cudaStream_t s);
+
+// compaction: dense list of occupied slots that pass HAVING
+cudaError_t launch_compact(const DevFinal &f, uint32_t *block_counts, uint32_t n_blocks,
+                           uint32_t *gids_out, unsigned long long *counts /*[0]=groups,[1]=kept*/,
+                           cudaStream_t s);
+uint32_t compact_blocks(uint64_t cap);
+// counts[] (device): [0] groups, [1] groups kept by HAVING, [2] result rows,
+// [3] entries in the selection list.
+// top-k (k <= 32) over the dense list -> sel_out, counts[3]
+cudaError_t launch_topk(const DevFinal &f, const uint32_t *gids, unsigned long long *counts, uint32_t k,
+                        unsigned long long *cand_keys, uint32_t *cand_gids, uint32_t n_cand_blocks,
+                        uint32_t *sel_out, cudaStream_t s);
+// full sort of the dense list (ORDER BY without a small LIMIT) -> *sorted_out, counts[3]
+cudaError_t launch_sort(const DevFinal &f, const uint32_t *gids, unsigned long long *counts, uint64_t max_n,
+                        unsigned long long *keys_a, unsigned long long *keys_b, uint32_t *ids_a, uint32_t *ids_b,
+                        uint32_t **sorted_out, cudaStream_t s);
+// the dense list itself is the selection: counts[3] = counts[1]
+cudaError_t launch_sel_all(unsigned long long *counts, cudaStream_t s);
+// output columns for rows [offset, offset + max_rows) of `sel` -> counts[2]
+cudaError_t launch_gather(const DevFinal &f, const uint32_t *sel, unsigned long long *counts, uint64_t offset,
+                          uint64_t max_rows, void *const *out_cols, uint8_t *const *out_valid, cudaStream_t s);
+// zero the occupied slots and the bitmap (leaves the table ready for reuse)
+cudaError_t launch_clear(unsigned long long *table, uint64_t cap, int32_t slot_words, uint32_t *occ, cudaStream_t s);
+
+// table statistics
+cudaError_t launch_zone_maps(const void *data, const uint32_t *valid, int32_t type, uint64_t n_rows,
+                             uint32_t rg_rows, uint32_t n_rg, int64_t *imin, int64_t *imax, double *fmin,
+                             double *fmax, uint32_t *nulls, cudaStream_t s);
+cudaError_t launch_hll(const void *data, const uint32_t *valid, int32_t type, uint64_t n_rows, uint32_t *regs,
+                       cudaStream_t s);
+constexpr int HLL_P = 14;
+
+}  // namespace tgpu

@@ -1,0 +1,671 @@
+// finalize.cu — from the folded group table to the result rows.
+//
+// thinDB's emit stage (silo_group_core.zig emitAllGroupsNumeric :4802,
+// emitRankedGroups :4856, TopSet :5083; v2_shape_group_topn.zig
+// applyHaving :2586, rankedFinalRows :1137, rowOrderBefore :1327-1335,
+// avgValue :1438-1446, integerAggValue :1448-1453, emitResultStage :1514):
+//
+//   compact   occupancy bitmap -> dense list of group slots passing HAVING
+//             (two passes, block counts then ordered writes: deterministic)
+//   rank      k <= 32: warp-register top-k per warp, merged per CTA, then by
+//             one warp; otherwise a merge sort (bitonic 1024-runs + merge
+//             passes).  Keys are encoded into unsigned words compared
+//             lexicographically: each ORDER BY value (NULL first), then the
+//             packed group key ascending.
+//   gather    result rows -> typed output columns + validity bytes
+//   clear     zero every used slot and the bitmap so the table is reusable
+//             without a full memset.
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace tgpu {
+
+namespace {
+
+constexpr unsigned FULL = 0xFFFFFFFFu;
+
+__device__ __constant__ double POW10[19] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8, 1e9,
+                                            1e10, 1e11, 1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18};
+
+struct EmitVal {
+    bool null;
+    bool is_f;
+    uint64_t lo;   // i128 low word (integers)
+    int64_t hi;    // i128 high word
+    double f;
+};
+
+__device__ __forceinline__ const unsigned long long *slot_states(const DevFinal &f, uint32_t gid) {
+    return f.table + (uint64_t)gid * f.slot_words + f.key_words;
+}
+
+// The emitted value of aggregate `a` (countValue / aggIsNull / avgValue /
+// integerAggValue, v2_shape_group_topn.zig:1399-1453).
+__device__ EmitVal emit_agg(const DevFinal &f, const unsigned long long *st, int a) {
+    const DevOut &o = f.outs[a];
+    EmitVal v{false, false, 0, 0, 0.0};
+    const uint64_t rows = st[0];
+    if (o.func == TGPU_AGG_COUNT) {
+        v.lo = o.kind == AK_COUNT_VALID ? st[o.word] : rows;
+        return v;
+    }
+    if (o.func == TGPU_AGG_COUNT_DISTINCT) {
+        v.lo = st[o.word];
+        return v;
+    }
+    const uint64_t den = o.vword >= 0 ? st[o.vword] : rows;
+    if (o.nullable && den == 0) {
+        v.null = true;
+        return v;
+    }
+    switch (o.func) {
+        case TGPU_AGG_SUM:
+            if (o.kind == AK_SUM_F64) {
+                v.is_f = true;
+                v.f = bits_f64(st[o.word]);
+            } else if (o.kind == AK_SUM_I64) {
+                v.lo = st[o.word];
+                v.hi = (int64_t)v.lo < 0 ? -1 : 0;
+            } else {
+                v.lo = st[o.word];
+                v.hi = (int64_t)st[o.word + 1];
+                if (o.out_type == TGPU_BIGINT) v.hi = (int64_t)v.lo < 0 ? -1 : 0;  // wraps to BIGINT
+            }
+            return v;
+        case TGPU_AGG_AVG: {
+            v.is_f = true;
+            if (den == 0) return v;
+            if (o.kind == AK_SUM_F64) {
+                v.f = bits_f64(st[o.word]) / (double)den;
+            } else {
+                uint64_t lo = st[o.word];
+                int64_t hi = o.kind == AK_SUM_I128 ? (int64_t)st[o.word + 1] : ((int64_t)lo < 0 ? -1 : 0);
+                v.f = i128_to_f64(lo, hi) / (double)den / POW10[o.scale];
+            }
+            return v;
+        }
+        default: {  // MIN / MAX
+            uint64_t e = st[o.word];
+            if (o.func == TGPU_AGG_MIN) e = ~e;
+            if (o.kind == AK_MIN_F || o.kind == AK_MAX_F) {
+                v.is_f = true;
+                v.f = bits_f64(dec_f64_bits(e));
+            } else {
+                v.lo = (uint64_t)dec_i64(e);
+                v.hi = (int64_t)v.lo < 0 ? -1 : 0;
+            }
+            return v;
+        }
+    }
+}
+
+__device__ __forceinline__ void slot_key(const DevFinal &f, uint32_t gid, uint64_t &k0, uint64_t &k1) {
+    const unsigned long long *s = f.table + (uint64_t)gid * f.slot_words;
+    k0 = s[0];
+    k1 = f.key_words == 2 ? s[1] : 0;
+}
+
+// keyPartIsNull / keyPartValue (v2_shape_group_topn.zig:1426-1470).
+__device__ EmitVal emit_key(const DevFinal &f, uint64_t k0, uint64_t k1, int p) {
+    const DevKeyPart &kp = f.parts[p];
+    EmitVal v{false, false, 0, 0, 0.0};
+    auto bit = [&](int b) -> uint64_t { return b < 64 ? (k0 >> b) & 1 : (k1 >> (b - 64)) & 1; };
+    if (kp.nullable && !bit(kp.offset + kp.payload)) {
+        v.null = true;
+        return v;
+    }
+    uint64_t raw;
+    int off = kp.offset;
+    if (off >= 64) raw = k1 >> (off - 64);
+    else raw = (k0 >> off) | (off ? (k1 << (64 - off)) : 0);
+    if (kp.payload < 64) raw &= (1ULL << kp.payload) - 1;
+    int64_t s;
+    switch (f.part_types[p]) {
+        case TGPU_BOOLEAN: case TGPU_TINYINT: s = (int8_t)(uint8_t)raw; break;
+        case TGPU_SMALLINT: s = (int16_t)(uint16_t)raw; break;
+        case TGPU_INT: case TGPU_DATE: case TGPU_DICT32: s = (int32_t)(uint32_t)raw; break;
+        default: s = (int64_t)raw; break;
+    }
+    v.lo = (uint64_t)s;
+    v.hi = s < 0 ? -1 : 0;
+    return v;
+}
+
+__device__ __forceinline__ int cmp_i128(uint64_t alo, int64_t ahi, uint64_t blo, int64_t bhi) {
+    if (ahi != bhi) return ahi < bhi ? -1 : 1;
+    if (alo != blo) return alo < blo ? -1 : 1;
+    return 0;
+}
+
+__device__ bool having_pass(const DevFinal &f, const unsigned long long *st) {
+    for (int i = 0; i < f.n_having; ++i) {
+        const DevHaving &h = f.having[i];
+        EmitVal v = emit_agg(f, st, h.agg);
+        if (v.null) return false;
+        int c;
+        if (v.is_f) {
+            if (v.f != v.f || h.fval != h.fval) {
+                if (h.op != TGPU_PRED_NE) return false;
+                continue;
+            }
+            c = v.f < h.fval ? -1 : (v.f > h.fval ? 1 : 0);
+        } else {
+            c = cmp_i128(v.lo, v.hi, (uint64_t)h.ival, h.ival < 0 ? -1 : 0);
+        }
+        bool ok;
+        switch (h.op) {
+            case TGPU_PRED_EQ: ok = c == 0; break;
+            case TGPU_PRED_NE: ok = c != 0; break;
+            case TGPU_PRED_LT: ok = c < 0; break;
+            case TGPU_PRED_LE: ok = c <= 0; break;
+            case TGPU_PRED_GT: ok = c > 0; break;
+            default: ok = c >= 0; break;
+        }
+        if (!ok) return false;
+    }
+    return true;
+}
+
+// Encoded sort key: per ORDER BY value a 128-bit word pair (NULL = 0, a value
+// = its order-preserving image + 1, complemented for DESC), then the packed
+// key.  Smaller words = earlier row.
+__device__ void encode_sort_key(const DevFinal &f, uint32_t gid, uint64_t *w) {
+    uint64_t k0, k1;
+    slot_key(f, gid, k0, k1);
+    const unsigned long long *st = slot_states(f, gid);
+    int n = 0;
+    for (int i = 0; i < f.n_order; ++i) {
+        const DevOrder &o = f.order[i];
+        EmitVal v = o.target == TGPU_SORT_KEY ? emit_key(f, k0, k1, o.index) : emit_agg(f, st, o.index);
+        uint64_t hi = 0, lo = 0;
+        if (!v.null) {
+            if (v.is_f) {
+                double d = v.f;
+                uint64_t b = (d != d) ? 0x7FF8000000000000ULL : (d == 0.0 ? 0ULL : f64_bits(d));
+                lo = enc_f64_bits(b);
+                hi = 0;
+            } else {
+                lo = v.lo;
+                hi = (uint64_t)v.hi ^ 0x8000000000000000ULL;
+            }
+            lo += 1;
+            if (lo == 0) hi += 1;
+        }
+        if (o.desc) {
+            hi = ~hi;
+            lo = ~lo;
+        }
+        w[n++] = hi;
+        w[n++] = lo;
+    }
+    w[n++] = k1;
+    w[n++] = k0;
+}
+
+template <typename A, typename B>
+__device__ __forceinline__ bool key_less(const A *a, const B *b, int sw) {
+#pragma unroll
+    for (int i = 0; i < MAX_SORT_WORDS; ++i) {
+        if (i >= sw) break;
+        if (a[i] != b[i]) return a[i] < b[i];
+    }
+    return false;
+}
+
+// -------------------------------------------------------------- compact --
+
+constexpr int CPT_THREADS = 256;
+constexpr int CPT_WORDS_PER_THREAD = 8;
+constexpr int CPT_WORDS_PER_BLOCK = CPT_THREADS * CPT_WORDS_PER_THREAD;
+
+__device__ __forceinline__ int block_excl_scan(int v, int *sh, int &total) {
+    // Kogge-Stone over warps
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(FULL, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int nw = blockDim.x >> 5;
+        int s = lane < nw ? sh[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(FULL, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < nw) sh[lane] = s;
+    }
+    __syncthreads();
+    int before = warp ? sh[warp - 1] : 0;
+    total = sh[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+__global__ void __launch_bounds__(CPT_THREADS) compact_count_kernel(const __grid_constant__ DevFinal f, uint64_t n_words,
+                                                                    uint32_t *block_counts,
+                                                                    unsigned long long *counts) {
+    __shared__ int sh[32];
+    uint64_t w0 = (uint64_t)blockIdx.x * CPT_WORDS_PER_BLOCK + threadIdx.x * CPT_WORDS_PER_THREAD;
+    int groups = 0, kept = 0;
+    for (int i = 0; i < CPT_WORDS_PER_THREAD; ++i) {
+        uint64_t w = w0 + i;
+        if (w >= n_words) break;
+        uint32_t bits = f.occ[w];
+        while (bits) {
+            int b = __ffs(bits) - 1;
+            bits &= bits - 1;
+            uint32_t gid = (uint32_t)(w * 32 + b);
+            ++groups;
+            if (f.n_having == 0 || having_pass(f, slot_states(f, gid))) ++kept;
+        }
+    }
+    int tg, tk;
+    block_excl_scan(groups, sh, tg);
+    block_excl_scan(kept, sh, tk);
+    if (threadIdx.x == 0) {
+        block_counts[blockIdx.x] = (uint32_t)tk;
+        if (tg) atomicAdd(&counts[0], (unsigned long long)tg);
+    }
+}
+
+__global__ void __launch_bounds__(CPT_THREADS) compact_write_kernel(const __grid_constant__ DevFinal f, uint64_t n_words,
+                                                                    const uint32_t *block_counts,
+                                                                    uint32_t n_blocks, uint32_t *gids_out,
+                                                                    unsigned long long *counts) {
+    __shared__ int sh[32];
+    __shared__ unsigned long long base_sh;
+    // this block's output offset = sum of the previous blocks' counts
+    unsigned long long part = 0;
+    for (uint32_t b = threadIdx.x; b < blockIdx.x; b += blockDim.x) part += block_counts[b];
+    for (int o = 16; o; o >>= 1) part += __shfl_down_sync(FULL, part, o);
+    if (threadIdx.x == 0) base_sh = 0;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0 && part) atomicAdd(&base_sh, part);
+    __syncthreads();
+    const unsigned long long base = base_sh;
+
+    uint64_t w0 = (uint64_t)blockIdx.x * CPT_WORDS_PER_BLOCK + threadIdx.x * CPT_WORDS_PER_THREAD;
+    int kept = 0;
+    for (int i = 0; i < CPT_WORDS_PER_THREAD; ++i) {
+        uint64_t w = w0 + i;
+        if (w >= n_words) break;
+        uint32_t bits = f.occ[w];
+        while (bits) {
+            int b = __ffs(bits) - 1;
+            bits &= bits - 1;
+            uint32_t gid = (uint32_t)(w * 32 + b);
+            if (f.n_having == 0 || having_pass(f, slot_states(f, gid))) ++kept;
+        }
+    }
+    int total;
+    int pos = block_excl_scan(kept, sh, total);
+    for (int i = 0; i < CPT_WORDS_PER_THREAD; ++i) {
+        uint64_t w = w0 + i;
+        if (w >= n_words) break;
+        uint32_t bits = f.occ[w];
+        while (bits) {
+            int b = __ffs(bits) - 1;
+            bits &= bits - 1;
+            uint32_t gid = (uint32_t)(w * 32 + b);
+            if (f.n_having == 0 || having_pass(f, slot_states(f, gid))) gids_out[base + pos++] = gid;
+        }
+    }
+    if (blockIdx.x == n_blocks - 1 && threadIdx.x == 0) counts[1] = base + total;
+}
+
+// ----------------------------------------------------------------- top-k --
+
+constexpr int TOPK_THREADS = 256;
+
+// A warp's sorted list of up to k (<= 32) best entries, one per lane.
+struct WarpTop {
+    uint64_t key[MAX_SORT_WORDS];
+    uint32_t gid;
+    int count;  // warp-uniform
+};
+
+__device__ __forceinline__ void warp_top_init(WarpTop &t, int sw) {
+    for (int i = 0; i < MAX_SORT_WORDS; ++i) t.key[i] = ~0ULL;
+    t.gid = 0xFFFFFFFFu;
+    t.count = 0;
+    (void)sw;
+}
+
+// Offer each lane's candidate (valid flag) to the warp's list.
+__device__ void warp_top_offer(WarpTop &t, const uint64_t *cand, uint32_t cgid, bool valid, int k, int sw) {
+    const int lane = threadIdx.x & 31;
+    unsigned m = __ballot_sync(FULL, valid);
+    while (m) {
+        const int src = __ffs(m) - 1;
+        m &= m - 1;
+        uint64_t c[MAX_SORT_WORDS];
+#pragma unroll
+        for (int i = 0; i < MAX_SORT_WORDS; ++i)
+            c[i] = (i < sw) ? (uint64_t)__shfl_sync(FULL, (long long)cand[i], src) : 0;
+        const uint32_t g = __shfl_sync(FULL, cgid, src);
+        // worst kept entry (lane k-1) when the list is full
+        if (t.count == k) {
+            uint64_t worst[MAX_SORT_WORDS];
+#pragma unroll
+            for (int i = 0; i < MAX_SORT_WORDS; ++i)
+                worst[i] = (i < sw) ? (uint64_t)__shfl_sync(FULL, (long long)t.key[i], k - 1) : 0;
+            if (!key_less(c, worst, sw)) continue;
+        }
+        const bool before = lane < t.count && key_less(t.key, c, sw);
+        const int pos = __popc(__ballot_sync(FULL, before));
+        // shift lanes >= pos down by one
+        uint64_t up[MAX_SORT_WORDS];
+#pragma unroll
+        for (int i = 0; i < MAX_SORT_WORDS; ++i)
+            up[i] = (i < sw) ? (uint64_t)__shfl_up_sync(FULL, (long long)t.key[i], 1) : 0;
+        uint32_t upg = __shfl_up_sync(FULL, t.gid, 1);
+        if (lane > pos && lane < k) {
+#pragma unroll
+            for (int i = 0; i < MAX_SORT_WORDS; ++i) t.key[i] = up[i];
+            t.gid = upg;
+        }
+        if (lane == pos) {
+#pragma unroll
+            for (int i = 0; i < MAX_SORT_WORDS; ++i) t.key[i] = c[i];
+            t.gid = g;
+        }
+        if (t.count < k) t.count++;
+    }
+}
+
+// Per-CTA top-k of the dense list; each warp scans a strided share, then
+// warp 0 merges the warps' lists.
+__global__ void __launch_bounds__(TOPK_THREADS) topk_partial_kernel(const __grid_constant__ DevFinal f, const uint32_t *gids,
+                                                                    const unsigned long long *counts, int k,
+                                                                    unsigned long long *cand_keys,
+                                                                    uint32_t *cand_gids) {
+    extern __shared__ unsigned long long tk_sh[];
+    const int sw = f.sort_words;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = TOPK_THREADS / 32;
+    const uint64_t n = counts[1];
+    WarpTop t;
+    warp_top_init(t, sw);
+    const uint64_t stride = (uint64_t)gridDim.x * TOPK_THREADS;
+    for (uint64_t base = (uint64_t)blockIdx.x * TOPK_THREADS + warp * 32; base < n; base += stride) {
+        const uint64_t i = base + lane;
+        uint64_t c[MAX_SORT_WORDS];
+        uint32_t g = 0;
+        const bool valid = i < n;
+        if (valid) {
+            g = gids[i];
+            encode_sort_key(f, g, c);
+        }
+        warp_top_offer(t, c, g, valid, k, sw);
+    }
+    // park every warp's list in shared memory
+    unsigned long long *keys = tk_sh;                                  // nwarps*32*sw
+    uint32_t *ids = (uint32_t *)(keys + (size_t)nwarps * 32 * sw);     // nwarps*32
+    int *cnt = (int *)(ids + nwarps * 32);
+    for (int i = 0; i < sw; ++i) keys[((size_t)warp * 32 + lane) * sw + i] = t.key[i];
+    ids[warp * 32 + lane] = t.gid;
+    if (lane == 0) cnt[warp] = t.count;
+    __syncthreads();
+    if (warp == 0) {
+        WarpTop m;
+        warp_top_init(m, sw);
+        for (int w = 0; w < nwarps; ++w) {
+            uint64_t c[MAX_SORT_WORDS];
+            for (int i = 0; i < sw; ++i) c[i] = keys[((size_t)w * 32 + lane) * sw + i];
+            warp_top_offer(m, c, ids[w * 32 + lane], lane < cnt[w], k, sw);
+        }
+        for (int i = 0; i < sw; ++i) cand_keys[((size_t)blockIdx.x * 32 + lane) * sw + i] = m.key[i];
+        cand_gids[blockIdx.x * 32 + lane] = lane < m.count ? m.gid : 0xFFFFFFFFu;
+    }
+}
+
+__global__ void topk_final_kernel(const __grid_constant__ DevFinal f, const unsigned long long *cand_keys, const uint32_t *cand_gids,
+                                  uint32_t n_blocks, int k, uint32_t *sel_out, unsigned long long *counts) {
+    const int sw = f.sort_words;
+    const int lane = threadIdx.x & 31;
+    WarpTop t;
+    warp_top_init(t, sw);
+    for (uint32_t b = 0; b < n_blocks; ++b) {
+        uint64_t c[MAX_SORT_WORDS];
+        for (int i = 0; i < sw; ++i) c[i] = cand_keys[((size_t)b * 32 + lane) * sw + i];
+        uint32_t g = cand_gids[b * 32 + lane];
+        warp_top_offer(t, c, g, g != 0xFFFFFFFFu, k, sw);
+    }
+    if (lane < t.count) sel_out[lane] = t.gid;
+    if (lane == 0) counts[3] = (unsigned long long)t.count;  // rows in `sel`
+}
+
+// ------------------------------------------------------------ merge sort --
+
+constexpr int SORT_TILE = 1024;
+constexpr int SORT_THREADS = 512;
+
+__global__ void sort_keys_kernel(const __grid_constant__ DevFinal f, const uint32_t *gids, const unsigned long long *counts,
+                                 unsigned long long *keys, uint32_t *ids) {
+    const uint64_t n = counts[1];
+    const int sw = f.sort_words;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t w[MAX_SORT_WORDS];
+        encode_sort_key(f, gids[i], w);
+        for (int j = 0; j < sw; ++j) keys[i * sw + j] = w[j];
+        ids[i] = gids[i];
+    }
+}
+
+__global__ void __launch_bounds__(SORT_THREADS) sort_tile_kernel(int sw, const unsigned long long *counts,
+                                                                 unsigned long long *keys, uint32_t *ids) {
+    extern __shared__ unsigned long long st_sh[];
+    unsigned long long *k = st_sh;                       // SORT_TILE * sw
+    uint32_t *id = (uint32_t *)(k + (size_t)SORT_TILE * sw);
+    const uint64_t n = counts[1];
+    const uint64_t base = (uint64_t)blockIdx.x * SORT_TILE;
+    if (base >= n) return;
+    for (int i = threadIdx.x; i < SORT_TILE; i += blockDim.x) {
+        uint64_t gi = base + i;
+        for (int j = 0; j < sw; ++j) k[i * sw + j] = gi < n ? keys[gi * sw + j] : ~0ULL;
+        id[i] = gi < n ? ids[gi] : 0xFFFFFFFFu;
+    }
+    __syncthreads();
+    for (int size = 2; size <= SORT_TILE; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = threadIdx.x; t < SORT_TILE / 2; t += blockDim.x) {
+                int lo = 2 * t - (t & (stride - 1));
+                int hi = lo + stride;
+                bool asc = ((lo & size) == 0);
+                bool less = key_less(k + (size_t)hi * sw, k + (size_t)lo * sw, sw);
+                if (less == asc) {
+                    for (int j = 0; j < sw; ++j) {
+                        unsigned long long x = k[lo * sw + j];
+                        k[lo * sw + j] = k[hi * sw + j];
+                        k[hi * sw + j] = x;
+                    }
+                    uint32_t x = id[lo];
+                    id[lo] = id[hi];
+                    id[hi] = x;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < SORT_TILE; i += blockDim.x) {
+        uint64_t gi = base + i;
+        if (gi >= n) break;
+        for (int j = 0; j < sw; ++j) keys[gi * sw + j] = k[i * sw + j];
+        ids[gi] = id[i];
+    }
+}
+
+// Merge adjacent sorted runs of `width` (keys unique): each element's output
+// position is its rank in its own run plus its rank in the partner run.
+__global__ void merge_pass_kernel(int sw, const unsigned long long *counts, uint64_t width,
+                                  const unsigned long long *kin, const uint32_t *iin, unsigned long long *kout,
+                                  uint32_t *iout) {
+    const uint64_t n = counts[1];
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t run = i / width;
+        const uint64_t run_start = run * width;
+        const uint64_t pair_start = (run & ~1ULL) * width;
+        const uint64_t partner = run ^ 1ULL;
+        const uint64_t p_start = partner * width;
+        uint64_t out;
+        if (p_start >= n) {
+            out = i;
+        } else {
+            const uint64_t p_end = min(p_start + width, n);
+            const unsigned long long *me = kin + i * sw;
+            // first partner element that is not less than me
+            uint64_t lo = p_start, hi = p_end;
+            while (lo < hi) {
+                uint64_t mid = (lo + hi) >> 1;
+                if (key_less(kin + mid * sw, me, sw)) lo = mid + 1;
+                else hi = mid;
+            }
+            out = pair_start + (i - run_start) + (lo - p_start);
+        }
+        for (int j = 0; j < sw; ++j) kout[out * sw + j] = kin[i * sw + j];
+        iout[out] = iin[i];
+    }
+}
+
+// Every kept group is a selection candidate: counts[3] = counts[1].
+__global__ void sel_count_kernel(unsigned long long *counts) { counts[3] = counts[1]; }
+
+// ---------------------------------------------------------------- gather --
+
+__global__ void gather_kernel(const __grid_constant__ DevFinal f, const uint32_t *sel, uint64_t offset, uint64_t max_rows,
+                              void *const *out_cols, uint8_t *const *out_valid, unsigned long long *counts) {
+    const uint64_t ns = counts[3];
+    const uint64_t avail = ns > offset ? ns - offset : 0;
+    const uint64_t rows = avail < max_rows ? avail : max_rows;
+    if (blockIdx.x == 0 && threadIdx.x == 0) counts[2] = rows;
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t gid = sel[offset + r];
+        uint64_t k0, k1;
+        slot_key(f, gid, k0, k1);
+        for (int p = 0; p < f.n_parts; ++p) {
+            EmitVal v = emit_key(f, k0, k1, p);
+            out_valid[p][r] = v.null ? 0 : 1;
+            void *col = out_cols[p];
+            switch (f.part_types[p]) {
+                case TGPU_BOOLEAN: case TGPU_TINYINT: ((int8_t *)col)[r] = (int8_t)v.lo; break;
+                case TGPU_SMALLINT: ((int16_t *)col)[r] = (int16_t)v.lo; break;
+                case TGPU_INT: case TGPU_DATE: case TGPU_DICT32: ((int32_t *)col)[r] = (int32_t)v.lo; break;
+                default: ((int64_t *)col)[r] = (int64_t)v.lo; break;
+            }
+        }
+        const unsigned long long *st = slot_states(f, gid);
+        for (int a = 0; a < f.n_aggs; ++a) {
+            const int c = f.n_parts + a;
+            EmitVal v = emit_agg(f, st, a);
+            out_valid[c][r] = v.null ? 0 : 1;
+            void *col = out_cols[c];
+            switch (f.outs[a].out_type) {
+                case TGPU_DOUBLE: ((double *)col)[r] = v.null ? 0.0 : v.f; break;
+                case TGPU_FLOAT: ((float *)col)[r] = v.null ? 0.0f : (float)v.f; break;
+                case TGPU_DECIMAL128:
+                    ((uint64_t *)col)[2 * r] = v.null ? 0 : v.lo;
+                    ((int64_t *)col)[2 * r + 1] = v.null ? 0 : v.hi;
+                    break;
+                case TGPU_BOOLEAN: case TGPU_TINYINT: ((int8_t *)col)[r] = v.null ? 0 : (int8_t)v.lo; break;
+                case TGPU_SMALLINT: ((int16_t *)col)[r] = v.null ? 0 : (int16_t)v.lo; break;
+                case TGPU_INT: case TGPU_DATE: case TGPU_DICT32: ((int32_t *)col)[r] = v.null ? 0 : (int32_t)v.lo; break;
+                default: ((int64_t *)col)[r] = v.null ? 0 : (int64_t)v.lo; break;
+            }
+        }
+    }
+}
+
+// ----------------------------------------------------------------- clear --
+
+__global__ void clear_kernel(unsigned long long *table, uint64_t n_words, int32_t slot_words, uint32_t *occ) {
+    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < n_words; w += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t bits = occ[w];
+        if (!bits) continue;
+        while (bits) {
+            int b = __ffs(bits) - 1;
+            bits &= bits - 1;
+            unsigned long long *s = table + (w * 32 + b) * (uint64_t)slot_words;
+            for (int i = 0; i < slot_words; ++i) s[i] = 0;
+        }
+        occ[w] = 0;
+    }
+}
+
+inline uint64_t occ_words(uint64_t cap) { return (cap + 1 + 31) / 32; }
+
+}  // namespace
+
+uint32_t compact_blocks(uint64_t cap) {
+    return (uint32_t)((occ_words(cap) + CPT_WORDS_PER_BLOCK - 1) / CPT_WORDS_PER_BLOCK);
+}
+
+cudaError_t launch_compact(const DevFinal &f, uint32_t *block_counts, uint32_t n_blocks, uint32_t *gids_out,
+                           unsigned long long *counts, cudaStream_t s) {
+    const uint64_t nw = occ_words(f.cap);
+    compact_count_kernel<<<n_blocks, CPT_THREADS, 0, s>>>(f, nw, block_counts, counts);
+    compact_write_kernel<<<n_blocks, CPT_THREADS, 0, s>>>(f, nw, block_counts, n_blocks, gids_out, counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_topk(const DevFinal &f, const uint32_t *gids, unsigned long long *counts, uint32_t k,
+                        unsigned long long *cand_keys, uint32_t *cand_gids, uint32_t n_cand_blocks,
+                        uint32_t *sel_out, cudaStream_t s) {
+    const int nwarps = TOPK_THREADS / 32;
+    size_t smem = (size_t)nwarps * 32 * f.sort_words * 8 + nwarps * 32 * 4 + nwarps * 4;
+    topk_partial_kernel<<<n_cand_blocks, TOPK_THREADS, smem, s>>>(f, gids, counts, (int)k, cand_keys, cand_gids);
+    topk_final_kernel<<<1, 32, 0, s>>>(f, cand_keys, cand_gids, n_cand_blocks, (int)k, sel_out, counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sort(const DevFinal &f, const uint32_t *gids, unsigned long long *counts, uint64_t max_n,
+                        unsigned long long *keys_a, unsigned long long *keys_b, uint32_t *ids_a, uint32_t *ids_b,
+                        uint32_t **sorted_out, cudaStream_t s) {
+    const int sw = f.sort_words;
+    int grid = (int)std::min<uint64_t>((max_n + 255) / 256, 4096);
+    if (grid < 1) grid = 1;
+    sort_keys_kernel<<<grid, 256, 0, s>>>(f, gids, counts, keys_a, ids_a);
+    uint64_t tiles = (max_n + SORT_TILE - 1) / SORT_TILE;
+    if (tiles < 1) tiles = 1;
+    size_t smem = (size_t)SORT_TILE * sw * 8 + SORT_TILE * 4;
+    cudaError_t e = cudaFuncSetAttribute(sort_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    sort_tile_kernel<<<(unsigned)tiles, SORT_THREADS, smem, s>>>(sw, counts, keys_a, ids_a);
+    unsigned long long *kin = keys_a, *kout = keys_b;
+    uint32_t *iin = ids_a, *iout = ids_b;
+    for (uint64_t width = SORT_TILE; width < max_n; width <<= 1) {
+        merge_pass_kernel<<<grid, 256, 0, s>>>(sw, counts, width, kin, iin, kout, iout);
+        std::swap(kin, kout);
+        std::swap(iin, iout);
+    }
+    *sorted_out = iin;
+    sel_count_kernel<<<1, 1, 0, s>>>(counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sel_all(unsigned long long *counts, cudaStream_t s) {
+    sel_count_kernel<<<1, 1, 0, s>>>(counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather(const DevFinal &f, const uint32_t *sel, unsigned long long *counts, uint64_t offset,
+                          uint64_t max_rows, void *const *out_cols, uint8_t *const *out_valid, cudaStream_t s) {
+    int grid = (int)std::min<uint64_t>((max_rows + 255) / 256, 2048);
+    if (grid < 1) grid = 1;
+    gather_kernel<<<grid, 256, 0, s>>>(f, sel, offset, max_rows, out_cols, out_valid, counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_clear(unsigned long long *table, uint64_t cap, int32_t slot_words, uint32_t *occ, cudaStream_t s) {
+    uint64_t nw = occ_words(cap);
+    int grid = (int)std::min<uint64_t>((nw + 255) / 256, 4096);
+    if (grid < 1) grid = 1;
+    clear_kernel<<<grid, 256, 0, s>>>(table, nw, slot_words, occ);
+    return cudaGetLastError();
+}
+
+}  // namespace tgpu

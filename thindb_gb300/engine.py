@@ -1,0 +1,408 @@
+"""Host-side mirror of thinDB's grouped-aggregation operator interface.
+
+The names follow the reference so tests read like its own:
+
+    Table            a registered immutable table (an `api.Table` snapshot in HBM)
+    AggSpec          exec.AggSpec {func, col, as}          (src/exec/aggregate.zig:237)
+    SortSpec         sort.SortSpec {col, desc}             (src/exec/sort.zig:28)
+    Request          GroupTopNRequest                      (src/exec/v2_shape_group_topn.zig:63)
+    try_build_group_topn(table, request) -> Query | None  (v2_pipeline.tryBuildGroupTopN:
+                     None means "decline", exactly as the Zig routing point returns null)
+    Query.next() -> Batch | None                           (exec.Query.next, src/exec/exec.zig:913)
+
+Every call goes through the C ABI of libthindb_gpu.so (include/thindb_gpu.h);
+there is no CPU path: without the built extension, importing the library
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+from typing import Any, Optional, Sequence
+
+import numpy as np
+
+from . import abi
+
+_LIB: Optional[C.CDLL] = None
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libthindb_gpu.so")
+
+
+def lib() -> C.CDLL:
+    """Load libthindb_gpu.so (built in-tree by thindb_gb300.build)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"thindb_gb300 CUDA extension missing at {LIB_PATH}: run thindb_gb300.build first")
+        L = C.CDLL(LIB_PATH)
+        for name, res, args in abi.SIGNATURES:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+class EngineError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{abi.STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class MemoryBudgetExceeded(EngineError):
+    pass
+
+
+class QueryCancelled(EngineError):
+    pass
+
+
+def _check(status: int) -> None:
+    if status == abi.OK:
+        return
+    msg = (lib().tgpu_last_error_message() or b"").decode(errors="replace")
+    if status == abi.ERR_MEMORY_BUDGET:
+        raise MemoryBudgetExceeded(status, msg)
+    if status == abi.ERR_CANCELLED:
+        raise QueryCancelled(status, msg)
+    raise EngineError(status, msg)
+
+
+NP_DTYPES = {abi.BOOLEAN: np.uint8, abi.TINYINT: np.int8, abi.SMALLINT: np.int16, abi.INT: np.int32,
+             abi.DATE: np.int32, abi.BIGINT: np.int64, abi.DATETIME: np.int64, abi.DECIMAL64: np.int64,
+             abi.FLOAT: np.float32, abi.DOUBLE: np.float64, abi.DICT32: np.int32}
+
+
+def decimal128_to_ints(raw: np.ndarray) -> list[int]:
+    """(n, 2) little-endian words of an i128 column -> Python ints."""
+    pairs = np.asarray(raw).reshape(-1, 2).view(np.uint64)
+    out = []
+    for lo, hi in pairs:
+        v = (int(hi) << 64) | int(lo)
+        if v >= 1 << 127:
+            v -= 1 << 128
+        out.append(v)
+    return out
+
+
+@dataclass
+class Column:
+    """One input column: host numpy array or device tensor (anything with data_ptr())."""
+    name: str
+    type: int
+    data: Any
+    validity: Optional[np.ndarray] = None   # bool per row (True = value), None = NOT NULL
+    scale: int = 0
+    precision: int = 18
+    dictionary: Optional[Sequence[str]] = None  # DICT32 strings
+    ndv_hint: int = 0
+
+
+def _ptr(x: Any) -> int:
+    if hasattr(x, "data_ptr"):
+        return int(x.data_ptr())
+    return int(x.ctypes.data)
+
+
+class Table:
+    """An immutable, HBM-resident table with zone maps and NDV sketches."""
+
+    def __init__(self, columns: Sequence[Column], row_group_rows: int = 65536, location: str = "host",
+                 compute_ndv: bool = True, stream: int = 0):
+        self.columns = list(columns)
+        if not self.columns:
+            raise ValueError("a table needs columns")
+        n = len(self.columns[0].data) if not hasattr(self.columns[0].data, "numel") else int(self.columns[0].data.numel())
+        self.n_rows = n
+        self._keep: list[Any] = []
+        descs = (abi.ColumnDesc * len(self.columns))()
+        for i, c in enumerate(self.columns):
+            cn = len(c.data) if not hasattr(c.data, "numel") else int(c.data.numel())
+            if cn != n:
+                raise ValueError(f"column {c.name} has {cn} rows, expected {n}")
+            d = descs[i]
+            nm = c.name.encode()
+            self._keep.append(nm)
+            d.name = nm
+            d.type = c.type
+            d.decimal_precision = c.precision
+            d.decimal_scale = c.scale
+            if location == "host":
+                arr = np.ascontiguousarray(c.data, dtype=NP_DTYPES[c.type]) if not hasattr(c.data, "data_ptr") else c.data
+                self._keep.append(arr)
+                d.data = _ptr(arr)
+            else:
+                d.data = _ptr(c.data)
+            if c.validity is not None:
+                bm = np.packbits(np.asarray(c.validity, dtype=bool), bitorder="little")
+                if location == "device":
+                    import torch
+                    bm = torch.from_numpy(bm).cuda()
+                self._keep.append(bm)
+                d.validity = _ptr(bm)
+            if c.type == abi.DICT32 and c.dictionary is not None:
+                enc = [s.encode() if isinstance(s, str) else bytes(s) for s in c.dictionary]
+                offs = np.zeros(len(enc) + 1, dtype=np.uint32)
+                offs[1:] = np.cumsum([len(s) for s in enc])
+                blob = np.frombuffer(b"".join(enc) or b"\0", dtype=np.uint8).copy()
+                self._keep += [offs, blob]
+                d.dict_offsets = _ptr(offs)
+                d.dict_bytes = _ptr(blob)
+                d.dict_size = len(enc)
+            d.ndv_hint = c.ndv_hint
+        td = abi.TableDesc()
+        td.columns = descs
+        td.n_columns = len(self.columns)
+        td.row_group_rows = row_group_rows
+        td.n_rows = n
+        td.location = abi.LOC_HOST if location == "host" else abi.LOC_DEVICE
+        td.compute_ndv = 1 if compute_ndv else 0
+        td.stream = stream or None
+        h = C.c_void_p()
+        _check(lib().tgpu_table_register(C.byref(td), C.byref(h)))
+        self.handle = h
+        if location == "host":
+            self._keep = []  # copied into HBM
+        self.row_group_rows = row_group_rows
+
+    def col_index(self, name: str) -> int:
+        for i, c in enumerate(self.columns):
+            if c.name.lower() == name.lower():
+                return i
+        raise KeyError(name)
+
+    def ndv(self, name: str) -> int:
+        v = C.c_uint64()
+        _check(lib().tgpu_table_info(self.handle, self.col_index(name), None, None, C.byref(v)))
+        return v.value
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().tgpu_table_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class AggSpec:
+    func: str            # count | sum | avg | min | max | count_distinct
+    col: Optional[str] = None
+    as_: str = ""
+
+
+@dataclass
+class SortSpec:
+    col: str             # a group column or an aggregate's output name
+    desc: bool = False
+
+
+@dataclass
+class Pred:
+    col: str
+    op: str              # between | not_between | = | != | < | <= | > | >= | is_null | is_not_null
+    lo: Any = 0
+    hi: Any = 0
+
+
+@dataclass
+class HavingSpec:
+    agg: str             # aggregate output name
+    op: str              # = != < <= > >=
+    value: Any = 0
+
+
+@dataclass
+class Request:
+    group_cols: Sequence[str]
+    aggs: Sequence[AggSpec]
+    order_specs: Sequence[SortSpec] = ()
+    limit: Optional[int] = None
+    offset: int = 0
+    where: Sequence[Pred] = ()
+    having: Sequence[HavingSpec] = ()
+    expected_groups: int = 0
+    memory_budget: int = 0
+    flags: int = 0
+    stream: int = 0
+
+
+def build_request(table: Table, req: Request) -> tuple[abi.Request, list]:
+    """Translate a name-based Request into the C struct (keeps the arrays alive)."""
+    keep: list = []
+    g = (C.c_int32 * len(req.group_cols))(*[table.col_index(c) for c in req.group_cols])
+    aggs = (abi.AggSpec * len(req.aggs))()
+    for i, a in enumerate(req.aggs):
+        aggs[i].func = abi.AGG_BY_NAME[a.func]
+        aggs[i].column = -1 if a.col is None else table.col_index(a.col)
+        nm = (a.as_ or f"{a.func}_{a.col or 'star'}").encode()
+        keep.append(nm)
+        aggs[i].as_ = nm
+    where = (abi.Predicate * max(1, len(req.where)))()
+    for i, p in enumerate(req.where):
+        ci = table.col_index(p.col)
+        where[i].column = ci
+        where[i].op = abi.PRED_BY_NAME[p.op]
+        if table.columns[ci].type in (abi.FLOAT, abi.DOUBLE):
+            where[i].flo, where[i].fhi = float(p.lo), float(p.hi)
+        else:
+            where[i].lo, where[i].hi = int(p.lo), int(p.hi)
+    names = [a.as_ or f"{a.func}_{a.col or 'star'}" for a in req.aggs]
+    having = (abi.Having * max(1, len(req.having)))()
+    for i, h in enumerate(req.having):
+        having[i].agg = names.index(h.agg)
+        having[i].op = abi.PRED_BY_NAME[h.op]
+        having[i].ival = int(h.value) if not isinstance(h.value, float) else int(h.value)
+        having[i].fval = float(h.value)
+    order = (abi.SortSpec * max(1, len(req.order_specs)))()
+    lower_keys = [c.lower() for c in req.group_cols]
+    lower_aggs = [n.lower() for n in names]
+    for i, s in enumerate(req.order_specs):
+        if s.col.lower() in lower_aggs:
+            order[i].target, order[i].index = abi.SORT_AGG, lower_aggs.index(s.col.lower())
+        elif s.col.lower() in lower_keys:
+            order[i].target, order[i].index = abi.SORT_KEY, lower_keys.index(s.col.lower())
+        else:
+            raise KeyError(f"ORDER BY {s.col}: not an output column")
+        order[i].desc = 1 if s.desc else 0
+    r = abi.Request()
+    r.group_cols, r.n_group_cols = g, len(req.group_cols)
+    r.aggs, r.n_aggs = aggs, len(req.aggs)
+    r.where, r.n_where = where, len(req.where)
+    r.having, r.n_having = having, len(req.having)
+    r.order, r.n_order = order, len(req.order_specs)
+    r.limit = abi.NO_LIMIT if req.limit is None else int(req.limit)
+    r.offset = int(req.offset)
+    r.expected_groups = int(req.expected_groups)
+    r.memory_budget_bytes = int(req.memory_budget)
+    r.stream = req.stream or None
+    r.flags = int(req.flags)
+    keep += [g, aggs, where, having, order]
+    return r, keep
+
+
+@dataclass
+class Batch:
+    """One result batch: schema + column arrays (+ validity as bool arrays, None = NOT NULL)."""
+    schema: list
+    values: list
+    validity: list
+    row_count: int
+
+
+@dataclass
+class OutCol:
+    name: str
+    type: int
+    nullable: bool
+    elem_bytes: int
+    precision: int = 0
+    scale: int = 0
+
+
+class Query:
+    """A planned GPU GROUP BY operator (the `exec.Query` the shim would wrap)."""
+
+    def __init__(self, handle: C.c_void_p, table: Table):
+        self.handle = handle
+        self.table = table
+        n = C.c_uint32()
+        _check(lib().tgpu_query_output_schema(handle, None, 0, C.byref(n)))
+        cols = (abi.OutputColumn * n.value)()
+        _check(lib().tgpu_query_output_schema(handle, cols, n.value, C.byref(n)))
+        self.schema = [OutCol(c.name.decode(), c.type, bool(c.nullable), c.elem_bytes, c.decimal_precision,
+                              c.decimal_scale) for c in cols]
+
+    def output_schema(self) -> list:
+        return self.schema
+
+    def execute(self) -> None:
+        _check(lib().tgpu_query_execute(self.handle))
+
+    def synchronize(self) -> None:
+        _check(lib().tgpu_query_synchronize(self.handle))
+
+    def next(self, capacity: int = 1 << 16) -> Optional[Batch]:
+        vals = []
+        valid = []
+        for c in self.schema:
+            if c.type == abi.DECIMAL128:
+                vals.append(np.zeros((capacity, 2), dtype=np.int64))
+            else:
+                vals.append(np.zeros(capacity, dtype=NP_DTYPES[c.type]))
+            valid.append(np.zeros((capacity + 7) // 8, dtype=np.uint8))
+        b = abi.Batch()
+        b.n_columns = len(self.schema)
+        vp = (C.c_void_p * len(vals))(*[v.ctypes.data for v in vals])
+        bp = (C.c_void_p * len(valid))(*[v.ctypes.data for v in valid])
+        b.values = vp
+        b.validity = bp
+        b.capacity_rows = capacity
+        done = C.c_int32()
+        _check(lib().tgpu_query_next(self.handle, C.byref(b), C.byref(done)))
+        n = b.row_count
+        if n == 0 and done.value:
+            return None
+        out_v = [v[:n] for v in vals]
+        out_ok = [np.unpackbits(bm, bitorder="little")[:n].astype(bool) if c.nullable else None
+                  for bm, c in zip(valid, self.schema)]
+        return Batch(self.schema, out_v, out_ok, n)
+
+    def collect(self, capacity: int = 1 << 20) -> dict:
+        """Drain the query: {column name: (values, validity or None)} in result order."""
+        parts: list[Batch] = []
+        while True:
+            b = self.next(capacity)
+            if b is None:
+                break
+            parts.append(b)
+            if b.row_count < capacity:
+                # the next call returns the end marker
+                continue
+        out = {}
+        for i, c in enumerate(self.schema):
+            if parts:
+                v = np.concatenate([p.values[i] for p in parts])
+                ok = np.concatenate([p.validity[i] for p in parts]) if c.nullable else None
+            else:
+                v = np.zeros((0, 2) if c.type == abi.DECIMAL128 else 0,
+                             dtype=np.int64 if c.type == abi.DECIMAL128 else NP_DTYPES[c.type])
+                ok = np.zeros(0, dtype=bool) if c.nullable else None
+            out[c.name] = (v, ok)
+        return out
+
+    def cancel(self) -> None:
+        _check(lib().tgpu_query_cancel(self.handle))
+
+    def stats(self) -> abi.QueryStats:
+        s = abi.QueryStats()
+        _check(lib().tgpu_query_get_stats(self.handle, C.byref(s)))
+        return s
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().tgpu_query_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def try_build_group_topn(table: Table, req: Request) -> Optional[Query]:
+    """v2_pipeline.tryBuildGroupTopN: a Query, or None when the shape declines."""
+    r, keep = build_request(table, req)
+    h = C.c_void_p()
+    st = lib().tgpu_query_create(table.handle, C.byref(r), C.byref(h))
+    del keep
+    if st == abi.DECLINE:
+        return None
+    _check(st)
+    return Query(h, table)
