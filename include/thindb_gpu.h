@@ -210,7 +210,14 @@ typedef struct tgpu_request {
     uint64_t memory_budget_bytes;/* 0 = unlimited */
     void *stream;                /* cudaStream_t, NULL = library stream */
     int32_t flags;               /* TGPU_FLAG_* */
-    int32_t reserved;
+    /* Tuning knobs (0 = engine default; the autotuner sets them per shape):
+     * rows per scan tile (a multiple of 512, at most 65,536; default 8,192),
+     * shared-memory table slots (power of two; -1 = no shared-memory table),
+     * group-table load in percent (capacity = expected groups * 100 / load;
+     * default 50). */
+    int32_t tile_rows;
+    int32_t cache_slots;
+    int32_t table_load_pct;
 } tgpu_request;
 
 /* Record per-phase CUDA event times (tgpu_query_stats.*_ms). */

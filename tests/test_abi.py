@@ -48,7 +48,7 @@ def test_struct_sizes_match_c_layout():
     assert C.sizeof(abi.TableDesc) == 40
     assert C.sizeof(abi.AggSpec) == 16
     assert C.sizeof(abi.Predicate) == 40
-    assert C.sizeof(abi.Request) == 128
+    assert C.sizeof(abi.Request) == 136
     assert C.sizeof(abi.OutputColumn) == 80
     assert C.sizeof(abi.QueryStats) == 104
     assert C.sizeof(abi.Batch) == 40

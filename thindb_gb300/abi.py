@@ -83,7 +83,7 @@ class Request(C.Structure):
                 ("order", C.POINTER(SortSpec)), ("n_order", C.c_uint32),
                 ("limit", C.c_uint64), ("offset", C.c_uint64), ("expected_groups", C.c_uint64),
                 ("memory_budget_bytes", C.c_uint64), ("stream", C.c_void_p), ("flags", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("tile_rows", C.c_int32), ("cache_slots", C.c_int32), ("table_load_pct", C.c_int32)]
 
 
 class OutputColumn(C.Structure):

@@ -106,6 +106,8 @@ struct Buffer {
     uint32_t epoch = 0;     // distinct sets: last epoch written
 };
 
+void trim_all();
+
 struct Pool {
     std::mutex mu;
     std::vector<Buffer> free_;
@@ -134,7 +136,7 @@ struct Pool {
         if (e != cudaSuccess) {
             cudaGetLastError();
             // release cached buffers and retry once
-            trim();
+            trim_all();
             e = cudaMalloc(&b.p, bytes);
             if (e != cudaSuccess) {
                 cudaGetLastError();
@@ -157,7 +159,15 @@ struct Pool {
     }
 };
 
+// Zero-clean buffers (group tables, occupancy bitmaps) and epoch-tagged
+// distinct sets never mix: a set's stale entries are not zero.
 Pool g_pool;
+Pool g_set_pool;
+
+void trim_all() {
+    g_pool.trim();
+    g_set_pool.trim();
+}
 
 // ----------------------------------------------------------------- table --
 
@@ -235,6 +245,8 @@ struct tgpu_query {
     uint32_t k = 0;
     uint64_t out_rows_max = 0;
     int grid = 0;
+    int cache_req = 0;            // requested shared-memory slots (0 auto, -1 off)
+    int load_pct = 50;            // group-table load target
     // workspace
     Buffer table_buf, occ_buf;
     std::vector<Buffer> dset_bufs;
@@ -284,7 +296,7 @@ struct tgpu_query {
         g_pool.give(table_buf);
         g_pool.give(occ_buf);
         table_buf = occ_buf = Buffer();
-        for (auto &b : dset_bufs) g_pool.give(b);
+        for (auto &b : dset_bufs) g_set_pool.give(b);
         dset_bufs.clear();
     }
 };
@@ -638,9 +650,10 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     dq.cache_slots = 0;
     dq.cache_flush_at = 0;
     q->route = 2;
-    if (dq.key_words == 1 && !(q->flags & TGPU_FLAG_FORCE_GLOBAL)) {
+    if (dq.key_words == 1 && !(q->flags & TGPU_FLAG_FORCE_GLOBAL) && q->cache_req >= 0) {
         int C = cache_slots_for(dq.state_words);
-        if (q->groups_est * 2 <= (uint64_t)C) {
+        if (q->cache_req > 0) C = std::min(C, q->cache_req);
+        if (q->groups_est * 8 <= (uint64_t)C * 5) {
             dq.cache_slots = C;
             dq.cache_flush_at = C;  // resident: never flushed before the end
             q->route = 1;
@@ -719,7 +732,7 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     if ((st = g_pool.take(occ_bytes, q->stream, &q->occ_buf)) != TGPU_OK) return st;
     for (size_t d = 0; d < dcap.size(); ++d) {
         Buffer b;
-        if ((st = g_pool.take(dcap[d] * 16, q->stream, &b)) != TGPU_OK) return st;
+        if ((st = g_set_pool.take(dcap[d] * 16, q->stream, &b)) != TGPU_OK) return st;
         q->dset_bufs.push_back(b);
         dq.dset[d] = (unsigned long long *)b.p;
         dq.dset_cap[d] = dcap[d];
@@ -775,13 +788,13 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     if (pruned) {
         dq.rg_list = q->d_rg_list;
         dq.n_rg = (uint32_t)q->rg_list.size();
-        dq.tiles_per_rg = (t->rg_rows + TILE_ROWS - 1) / TILE_ROWS;
+        dq.tiles_per_rg = (t->rg_rows + dq.tile_rows - 1) / dq.tile_rows;
         dq.n_tiles = dq.n_rg * dq.tiles_per_rg;
     } else {
         dq.rg_list = nullptr;
         dq.n_rg = t->n_rg;
         dq.tiles_per_rg = 0;
-        dq.n_tiles = (uint32_t)((t->n_rows + TILE_ROWS - 1) / TILE_ROWS);
+        dq.n_tiles = (uint32_t)((t->n_rows + dq.tile_rows - 1) / dq.tile_rows);
     }
     return TGPU_OK;
 }
@@ -868,7 +881,7 @@ tgpu_status finish(tgpu_query *q) {
             if (status & ST_TABLE_FULL) q->groups_est = std::max<uint64_t>(q->groups_est * 4, 1024);
             if (status & ST_DISTINCT_FULL)
                 for (auto &n : q->dset_need) n *= 4;
-            tgpu_status st = size_workspace(q, next_pow2(q->groups_est * 2));
+            tgpu_status st = size_workspace(q, next_pow2(q->groups_est * 100 / q->load_pct));
             if (st != TGPU_OK) return st;
             st = enqueue(q);
             if (st != TGPU_OK) return st;
@@ -1045,7 +1058,17 @@ tgpu_status tgpu_query_create(tgpu_table *table, const tgpu_request *req, tgpu_q
     q->limit = req->limit;
     q->offset = req->offset;
     q->budget = req->memory_budget_bytes;
+    if (req->tile_rows < 0 || req->tile_rows % SCAN_THREADS != 0 || req->tile_rows > 65536)
+        return fail(TGPU_ERR_INVALID_ARGUMENT, "tile_rows must be a multiple of 512 up to 65536");
+    if (req->cache_slots > 0 && (req->cache_slots & (req->cache_slots - 1)))
+        return fail(TGPU_ERR_INVALID_ARGUMENT, "cache_slots must be a power of two");
+    if (req->table_load_pct < 0 || req->table_load_pct > 90)
+        return fail(TGPU_ERR_INVALID_ARGUMENT, "table_load_pct must be within 1..90");
+    q->cache_req = req->cache_slots;
+    q->load_pct = req->table_load_pct ? req->table_load_pct : 50;
     st = plan_query(q.get(), table, req);
+    q->dq.tile_rows = req->tile_rows ? (uint32_t)req->tile_rows : (uint32_t)TILE_ROWS;
+    q->dq.warp_rows = q->dq.tile_rows / SCAN_WARPS;
     if (st != TGPU_OK) return st;
     CU(cudaHostAlloc((void **)&q->h_cancel, sizeof(int), cudaHostAllocMapped));
     *q->h_cancel = 0;
@@ -1053,7 +1076,7 @@ tgpu_status tgpu_query_create(tgpu_table *table, const tgpu_request *req, tgpu_q
     CU(cudaHostAlloc((void **)&q->h_counts, 8 * 8, cudaHostAllocDefault));
     std::memset(q->h_counts, 0, 64);
     for (auto &e : q->ev) CU(cudaEventCreate(&e));
-    st = size_workspace(q.get(), next_pow2(std::max<uint64_t>(64, q->groups_est * 2)));
+    st = size_workspace(q.get(), next_pow2(std::max<uint64_t>(64, q->groups_est * 100 / q->load_pct)));
     if (st != TGPU_OK) return st;
     q->grid = scan_grid_size(q->dq, dev->sms);
     *out = q.release();

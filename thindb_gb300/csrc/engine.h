@@ -22,8 +22,7 @@ constexpr int MAX_SORT_WORDS = 2 * MAX_ORDER + 2;
 // CTA's warps owns TILE_ROWS / WARPS consecutive rows of the tile.
 constexpr int SCAN_THREADS = 512;
 constexpr int SCAN_WARPS = SCAN_THREADS / 32;
-constexpr int TILE_ROWS = 8192;
-constexpr int WARP_ROWS = TILE_ROWS / SCAN_WARPS;  // 512
+constexpr int TILE_ROWS = 8192;                    // default rows per scan tile
 
 // Status bits the kernels OR into the query's device status word.
 constexpr unsigned ST_TABLE_FULL = 1u;      // a probe ran past MAX_PROBE: regrow and rerun
@@ -87,6 +86,8 @@ struct DevQuery {
     uint32_t rg_rows;
     uint32_t tiles_per_rg;
     uint32_t n_tiles;
+    uint32_t tile_rows;       // rows per scan tile (multiple of SCAN_THREADS)
+    uint32_t warp_rows;       // tile_rows / SCAN_WARPS
     // columns / predicates / key / aggregates
     DevCol cols[MAX_QCOLS];
     int32_t n_cols;
@@ -168,11 +169,38 @@ struct DevFinal {
     DevHaving having[MAX_AGGS];
 };
 
+// Per-query finalize buffers of a batch (device array, one per query).
+struct DevFinalBufs {
+    uint32_t *block_counts;
+    uint32_t *gids;
+    unsigned long long *counts;      // [0] groups [1] kept [2] result rows [3] selection size [4] selected rows
+    unsigned long long *cand_keys;
+    uint32_t *cand_gids;
+    uint32_t *sel;                   // selection list read by gather (gids or the top-k)
+    void **out_cols;
+    uint8_t **out_valid;
+    uint64_t offset;
+    uint64_t gather_rows;
+    uint32_t n_cpt_blocks;
+    uint32_t n_cand_blocks;
+    uint32_t k;
+    int32_t rank;                    // 0 all groups, 1 top-k (k <= 32)
+};
+
 // Launchers (scan.cu / finalize.cu / table.cu) --------------------------------
 
 int scan_grid_size(const DevQuery &q, int device_sms);
 size_t scan_smem_bytes(const DevQuery &q);
 cudaError_t launch_scan(const DevQuery &q, int grid, cudaStream_t s);
+// many queries, one persistent kernel over (query, tile) work items
+int batch_scan_grid(int max_aggs, size_t smem, int sms);
+cudaError_t launch_batch_scan(const DevQuery *qs, const uint32_t *tile_start, uint32_t n_queries, int max_aggs,
+                              size_t smem, int grid, unsigned int *work_counter, const volatile int *cancel,
+                              unsigned int *status, cudaStream_t s);
+// compaction, top-k / all-groups selection, gather and clear for every query of a batch
+cudaError_t launch_finalize_batch(const DevFinal *fs, const DevFinalBufs *bs, uint32_t n_queries,
+                                  uint32_t max_cpt_blocks, uint32_t max_cand_blocks, int max_sort_words,
+                                  bool any_topk, uint64_t max_rows, uint64_t max_words, cudaStream_t s);
 
 // compaction: dense list of occupied slots that pass HAVING
 cudaError_t launch_compact(const DevFinal &f, uint32_t *block_counts, uint32_t n_blocks,

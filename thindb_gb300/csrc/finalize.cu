@@ -247,11 +247,10 @@ __device__ __forceinline__ int block_excl_scan(int v, int *sh, int &total) {
     return before + x - v;
 }
 
-__global__ void __launch_bounds__(CPT_THREADS) compact_count_kernel(const __grid_constant__ DevFinal f, uint64_t n_words,
-                                                                    uint32_t *block_counts,
-                                                                    unsigned long long *counts) {
+__device__ __forceinline__ void compact_count_body(const DevFinal &f, uint64_t n_words, uint32_t *block_counts,
+                                                   unsigned long long *counts, uint32_t bid) {
     __shared__ int sh[32];
-    uint64_t w0 = (uint64_t)blockIdx.x * CPT_WORDS_PER_BLOCK + threadIdx.x * CPT_WORDS_PER_THREAD;
+    uint64_t w0 = (uint64_t)bid * CPT_WORDS_PER_BLOCK + threadIdx.x * CPT_WORDS_PER_THREAD;
     int groups = 0, kept = 0;
     for (int i = 0; i < CPT_WORDS_PER_THREAD; ++i) {
         uint64_t w = w0 + i;
@@ -269,20 +268,25 @@ __global__ void __launch_bounds__(CPT_THREADS) compact_count_kernel(const __grid
     block_excl_scan(groups, sh, tg);
     block_excl_scan(kept, sh, tk);
     if (threadIdx.x == 0) {
-        block_counts[blockIdx.x] = (uint32_t)tk;
+        block_counts[bid] = (uint32_t)tk;
         if (tg) atomicAdd(&counts[0], (unsigned long long)tg);
     }
 }
 
-__global__ void __launch_bounds__(CPT_THREADS) compact_write_kernel(const __grid_constant__ DevFinal f, uint64_t n_words,
-                                                                    const uint32_t *block_counts,
-                                                                    uint32_t n_blocks, uint32_t *gids_out,
+__global__ void __launch_bounds__(CPT_THREADS) compact_count_kernel(const __grid_constant__ DevFinal f, uint64_t n_words,
+                                                                    uint32_t *block_counts,
                                                                     unsigned long long *counts) {
+    compact_count_body(f, n_words, block_counts, counts, blockIdx.x);
+}
+
+__device__ __forceinline__ void compact_write_body(const DevFinal &f, uint64_t n_words, const uint32_t *block_counts,
+                                                   uint32_t n_blocks, uint32_t *gids_out, unsigned long long *counts,
+                                                   uint32_t bid) {
     __shared__ int sh[32];
     __shared__ unsigned long long base_sh;
     // this block's output offset = sum of the previous blocks' counts
     unsigned long long part = 0;
-    for (uint32_t b = threadIdx.x; b < blockIdx.x; b += blockDim.x) part += block_counts[b];
+    for (uint32_t b = threadIdx.x; b < bid; b += blockDim.x) part += block_counts[b];
     for (int o = 16; o; o >>= 1) part += __shfl_down_sync(FULL, part, o);
     if (threadIdx.x == 0) base_sh = 0;
     __syncthreads();
@@ -290,7 +294,7 @@ __global__ void __launch_bounds__(CPT_THREADS) compact_write_kernel(const __grid
     __syncthreads();
     const unsigned long long base = base_sh;
 
-    uint64_t w0 = (uint64_t)blockIdx.x * CPT_WORDS_PER_BLOCK + threadIdx.x * CPT_WORDS_PER_THREAD;
+    uint64_t w0 = (uint64_t)bid * CPT_WORDS_PER_BLOCK + threadIdx.x * CPT_WORDS_PER_THREAD;
     int kept = 0;
     for (int i = 0; i < CPT_WORDS_PER_THREAD; ++i) {
         uint64_t w = w0 + i;
@@ -316,7 +320,14 @@ __global__ void __launch_bounds__(CPT_THREADS) compact_write_kernel(const __grid
             if (f.n_having == 0 || having_pass(f, slot_states(f, gid))) gids_out[base + pos++] = gid;
         }
     }
-    if (blockIdx.x == n_blocks - 1 && threadIdx.x == 0) counts[1] = base + total;
+    if (bid == n_blocks - 1 && threadIdx.x == 0) counts[1] = base + total;
+}
+
+__global__ void __launch_bounds__(CPT_THREADS) compact_write_kernel(const __grid_constant__ DevFinal f, uint64_t n_words,
+                                                                    const uint32_t *block_counts,
+                                                                    uint32_t n_blocks, uint32_t *gids_out,
+                                                                    unsigned long long *counts) {
+    compact_write_body(f, n_words, block_counts, n_blocks, gids_out, counts, blockIdx.x);
 }
 
 // ----------------------------------------------------------------- top-k --
@@ -381,18 +392,18 @@ __device__ void warp_top_offer(WarpTop &t, const uint64_t *cand, uint32_t cgid, 
 
 // Per-CTA top-k of the dense list; each warp scans a strided share, then
 // warp 0 merges the warps' lists.
-__global__ void __launch_bounds__(TOPK_THREADS) topk_partial_kernel(const __grid_constant__ DevFinal f, const uint32_t *gids,
-                                                                    const unsigned long long *counts, int k,
-                                                                    unsigned long long *cand_keys,
-                                                                    uint32_t *cand_gids) {
+__device__ __forceinline__ void topk_partial_body(const DevFinal &f, const uint32_t *gids,
+                                                  const unsigned long long *counts, int k,
+                                                  unsigned long long *cand_keys, uint32_t *cand_gids, uint32_t bid,
+                                                  uint32_t nblk) {
     extern __shared__ unsigned long long tk_sh[];
     const int sw = f.sort_words;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = TOPK_THREADS / 32;
     const uint64_t n = counts[1];
     WarpTop t;
     warp_top_init(t, sw);
-    const uint64_t stride = (uint64_t)gridDim.x * TOPK_THREADS;
-    for (uint64_t base = (uint64_t)blockIdx.x * TOPK_THREADS + warp * 32; base < n; base += stride) {
+    const uint64_t stride = (uint64_t)nblk * TOPK_THREADS;
+    for (uint64_t base = (uint64_t)bid * TOPK_THREADS + warp * 32; base < n; base += stride) {
         const uint64_t i = base + lane;
         uint64_t c[MAX_SORT_WORDS];
         uint32_t g = 0;
@@ -419,13 +430,21 @@ __global__ void __launch_bounds__(TOPK_THREADS) topk_partial_kernel(const __grid
             for (int i = 0; i < sw; ++i) c[i] = keys[((size_t)w * 32 + lane) * sw + i];
             warp_top_offer(m, c, ids[w * 32 + lane], lane < cnt[w], k, sw);
         }
-        for (int i = 0; i < sw; ++i) cand_keys[((size_t)blockIdx.x * 32 + lane) * sw + i] = m.key[i];
-        cand_gids[blockIdx.x * 32 + lane] = lane < m.count ? m.gid : 0xFFFFFFFFu;
+        for (int i = 0; i < sw; ++i) cand_keys[((size_t)bid * 32 + lane) * sw + i] = m.key[i];
+        cand_gids[bid * 32 + lane] = lane < m.count ? m.gid : 0xFFFFFFFFu;
     }
 }
 
-__global__ void topk_final_kernel(const __grid_constant__ DevFinal f, const unsigned long long *cand_keys, const uint32_t *cand_gids,
-                                  uint32_t n_blocks, int k, uint32_t *sel_out, unsigned long long *counts) {
+__global__ void __launch_bounds__(TOPK_THREADS) topk_partial_kernel(const __grid_constant__ DevFinal f, const uint32_t *gids,
+                                                                    const unsigned long long *counts, int k,
+                                                                    unsigned long long *cand_keys,
+                                                                    uint32_t *cand_gids) {
+    topk_partial_body(f, gids, counts, k, cand_keys, cand_gids, blockIdx.x, gridDim.x);
+}
+
+__device__ __forceinline__ void topk_final_body(const DevFinal &f, const unsigned long long *cand_keys,
+                                                const uint32_t *cand_gids, uint32_t n_blocks, int k, uint32_t *sel_out,
+                                                unsigned long long *counts) {
     const int sw = f.sort_words;
     const int lane = threadIdx.x & 31;
     WarpTop t;
@@ -438,6 +457,11 @@ __global__ void topk_final_kernel(const __grid_constant__ DevFinal f, const unsi
     }
     if (lane < t.count) sel_out[lane] = t.gid;
     if (lane == 0) counts[3] = (unsigned long long)t.count;  // rows in `sel`
+}
+
+__global__ void topk_final_kernel(const __grid_constant__ DevFinal f, const unsigned long long *cand_keys, const uint32_t *cand_gids,
+                                  uint32_t n_blocks, int k, uint32_t *sel_out, unsigned long long *counts) {
+    topk_final_body(f, cand_keys, cand_gids, n_blocks, k, sel_out, counts);
 }
 
 // ------------------------------------------------------------ merge sort --
@@ -537,13 +561,14 @@ __global__ void sel_count_kernel(unsigned long long *counts) { counts[3] = count
 
 // ---------------------------------------------------------------- gather --
 
-__global__ void gather_kernel(const __grid_constant__ DevFinal f, const uint32_t *sel, uint64_t offset, uint64_t max_rows,
-                              void *const *out_cols, uint8_t *const *out_valid, unsigned long long *counts) {
+__device__ __forceinline__ void gather_body(const DevFinal &f, const uint32_t *sel, uint64_t offset, uint64_t max_rows,
+                                            void *const *out_cols, uint8_t *const *out_valid,
+                                            unsigned long long *counts, uint32_t bid, uint32_t nblk) {
     const uint64_t ns = counts[3];
     const uint64_t avail = ns > offset ? ns - offset : 0;
     const uint64_t rows = avail < max_rows ? avail : max_rows;
-    if (blockIdx.x == 0 && threadIdx.x == 0) counts[2] = rows;
-    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (uint64_t)gridDim.x * blockDim.x) {
+    if (bid == 0 && threadIdx.x == 0) counts[2] = rows;
+    for (uint64_t r = (uint64_t)bid * blockDim.x + threadIdx.x; r < rows; r += (uint64_t)nblk * blockDim.x) {
         const uint32_t gid = sel[offset + r];
         uint64_t k0, k1;
         slot_key(f, gid, k0, k1);
@@ -580,10 +605,16 @@ __global__ void gather_kernel(const __grid_constant__ DevFinal f, const uint32_t
     }
 }
 
+__global__ void gather_kernel(const __grid_constant__ DevFinal f, const uint32_t *sel, uint64_t offset, uint64_t max_rows,
+                              void *const *out_cols, uint8_t *const *out_valid, unsigned long long *counts) {
+    gather_body(f, sel, offset, max_rows, out_cols, out_valid, counts, blockIdx.x, gridDim.x);
+}
+
 // ----------------------------------------------------------------- clear --
 
-__global__ void clear_kernel(unsigned long long *table, uint64_t n_words, int32_t slot_words, uint32_t *occ) {
-    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < n_words; w += (uint64_t)gridDim.x * blockDim.x) {
+__device__ __forceinline__ void clear_body(unsigned long long *table, uint64_t n_words, int32_t slot_words, uint32_t *occ,
+                                           uint32_t bid, uint32_t nblk) {
+    for (uint64_t w = (uint64_t)bid * blockDim.x + threadIdx.x; w < n_words; w += (uint64_t)nblk * blockDim.x) {
         uint32_t bits = occ[w];
         if (!bits) continue;
         while (bits) {
@@ -596,7 +627,56 @@ __global__ void clear_kernel(unsigned long long *table, uint64_t n_words, int32_
     }
 }
 
-inline uint64_t occ_words(uint64_t cap) { return (cap + 1 + 31) / 32; }
+__global__ void clear_kernel(unsigned long long *table, uint64_t n_words, int32_t slot_words, uint32_t *occ) {
+    clear_body(table, n_words, slot_words, occ, blockIdx.x, gridDim.x);
+}
+
+__host__ __device__ inline uint64_t occ_words(uint64_t cap) { return (cap + 1 + 31) / 32; }
+
+// ------------------------------------------------------ batched (y = query) --
+
+__global__ void __launch_bounds__(CPT_THREADS) compact_count_batch(const DevFinal *fs, const DevFinalBufs *bs) {
+    const DevFinal &f = fs[blockIdx.y];
+    const DevFinalBufs &b = bs[blockIdx.y];
+    if (blockIdx.x >= b.n_cpt_blocks) return;
+    compact_count_body(f, occ_words(f.cap), b.block_counts, b.counts, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(CPT_THREADS) compact_write_batch(const DevFinal *fs, const DevFinalBufs *bs) {
+    const DevFinal &f = fs[blockIdx.y];
+    const DevFinalBufs &b = bs[blockIdx.y];
+    if (blockIdx.x >= b.n_cpt_blocks) return;
+    compact_write_body(f, occ_words(f.cap), b.block_counts, b.n_cpt_blocks, b.gids, b.counts, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(TOPK_THREADS) topk_partial_batch(const DevFinal *fs, const DevFinalBufs *bs) {
+    const DevFinalBufs &b = bs[blockIdx.y];
+    if (b.rank != 1 || blockIdx.x >= b.n_cand_blocks) return;
+    topk_partial_body(fs[blockIdx.y], b.gids, b.counts, (int)b.k, b.cand_keys, b.cand_gids, blockIdx.x,
+                      b.n_cand_blocks);
+}
+
+__global__ void topk_final_batch(const DevFinal *fs, const DevFinalBufs *bs) {
+    const DevFinalBufs &b = bs[blockIdx.y];
+    if (b.rank == 0) {
+        if (threadIdx.x == 0) b.counts[3] = b.counts[1];
+        return;
+    }
+    if (b.rank != 1) return;
+    topk_final_body(fs[blockIdx.y], b.cand_keys, b.cand_gids, b.n_cand_blocks, (int)b.k, b.sel, b.counts);
+}
+
+__global__ void gather_batch(const DevFinal *fs, const DevFinalBufs *bs) {
+    const DevFinalBufs &b = bs[blockIdx.y];
+    gather_body(fs[blockIdx.y], b.sel, b.offset, b.gather_rows, b.out_cols, b.out_valid, b.counts, blockIdx.x,
+                gridDim.x);
+}
+
+__global__ void clear_batch(const DevFinal *fs, const DevFinalBufs *bs) {
+    const DevFinal &f = fs[blockIdx.y];
+    clear_body(const_cast<unsigned long long *>(f.table), occ_words(f.cap), f.slot_words,
+               const_cast<uint32_t *>(f.occ), blockIdx.x, gridDim.x);
+}
 
 }  // namespace
 
@@ -665,6 +745,26 @@ cudaError_t launch_clear(unsigned long long *table, uint64_t cap, int32_t slot_w
     int grid = (int)std::min<uint64_t>((nw + 255) / 256, 4096);
     if (grid < 1) grid = 1;
     clear_kernel<<<grid, 256, 0, s>>>(table, nw, slot_words, occ);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize_batch(const DevFinal *fs, const DevFinalBufs *bs, uint32_t n_queries,
+                                  uint32_t max_cpt_blocks, uint32_t max_cand_blocks, int max_sort_words,
+                                  bool any_topk, uint64_t max_rows, uint64_t max_words, cudaStream_t s) {
+    if (n_queries == 0) return cudaSuccess;
+    dim3 gc(std::max<uint32_t>(1, max_cpt_blocks), n_queries);
+    compact_count_batch<<<gc, CPT_THREADS, 0, s>>>(fs, bs);
+    compact_write_batch<<<gc, CPT_THREADS, 0, s>>>(fs, bs);
+    if (any_topk) {
+        const int nwarps = TOPK_THREADS / 32;
+        size_t smem = (size_t)nwarps * 32 * max_sort_words * 8 + nwarps * 32 * 4 + nwarps * 4;
+        topk_partial_batch<<<dim3(std::max<uint32_t>(1, max_cand_blocks), n_queries), TOPK_THREADS, smem, s>>>(fs, bs);
+    }
+    topk_final_batch<<<dim3(1, n_queries), 32, 0, s>>>(fs, bs);
+    unsigned gx = (unsigned)std::min<uint64_t>(std::max<uint64_t>(1, (max_rows + 255) / 256), 64);
+    gather_batch<<<dim3(gx, n_queries), 256, 0, s>>>(fs, bs);
+    unsigned cx = (unsigned)std::min<uint64_t>(std::max<uint64_t>(1, (max_words + 255) / 256), 512);
+    clear_batch<<<dim3(cx, n_queries), 256, 0, s>>>(fs, bs);
     return cudaGetLastError();
 }
 

@@ -5,8 +5,8 @@
 // -> stageBucketIds :9228 / scatterStageLane :9348 -> groupChunkRowsDirectKeys
 // :7456 -> foldKernel* :7832-8001 -> foldGroupDistinct :8003-8176):
 //
-//   1. CTAs claim tiles of TILE_ROWS rows (inside the row groups that survived
-//      the zone maps); each warp owns WARP_ROWS consecutive rows of the tile.
+//   1. CTAs claim tiles of q.tile_rows rows (inside the row groups that
+//      survived the zone maps); each warp owns q.warp_rows consecutive rows.
 //   2. The fused WHERE is evaluated 32 rows per warp step with coalesced loads;
 //      a warp ballot gives the survivors, which are compacted into a per-warp
 //      shared-memory ring (prefix = popc of the ballot below the lane).
@@ -526,23 +526,98 @@ __device__ __forceinline__ void process_batch(const DevQuery &q, ScanSmem &sm, u
 
 // ---------------------------------------------------------------- kernel --
 
-template <int NA>
-__global__ void __launch_bounds__(SCAN_THREADS, NA <= 4 ? 2 : 1) scan_group_kernel(const __grid_constant__ DevQuery q) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    ScanSmem sm = carve(q, smem_raw);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-
+__device__ __forceinline__ void cache_init(const DevQuery &q, ScanSmem &sm) {
     for (int e = threadIdx.x; e < q.cache_slots; e += blockDim.x) {
         sm.ckeys[e] = 0;
         sm.cgid[e] = NO_GID;
     }
     for (int e = threadIdx.x; e < q.cache_slots * q.state_words; e += blockDim.x) sm.cstate[e] = 0;
+}
+
+// Rows [row0, row_end) of scan tile t.
+__device__ __forceinline__ void tile_rows(const DevQuery &q, uint32_t t, uint64_t &row0, uint64_t &row_end) {
+    if (q.rg_list) {
+        uint32_t rgi = t / q.tiles_per_rg, sub = t % q.tiles_per_rg;
+        uint64_t rg = q.rg_list[rgi];
+        row0 = rg * q.rg_rows + (uint64_t)sub * q.tile_rows;
+        row_end = min(min(row0 + q.tile_rows, (rg + 1) * (uint64_t)q.rg_rows), q.n_rows);
+    } else {
+        row0 = (uint64_t)t * q.tile_rows;
+        row_end = min(row0 + q.tile_rows, q.n_rows);
+    }
+}
+
+// One warp's share of scan tile t: filter, compact, fold.
+template <int NA>
+__device__ __forceinline__ void scan_tile(const DevQuery &q, ScanSmem &sm, uint32_t t, unsigned long long &selected) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t *wb = sm.wbuf + warp * WBUF;
+    uint64_t row0, row_end;
+    tile_rows(q, t, row0, row_end);
+    const uint64_t wbase = row0 + (uint64_t)warp * q.warp_rows;
+    const uint64_t wend = min(wbase + q.warp_rows, row_end);
+    if (wbase >= wend) return;
+    if (q.n_preds == 0) {
+        for (uint64_t b = wbase; b < wend; b += 32) {
+            uint64_t r = b + lane;
+            unsigned act = __ballot_sync(FULL, r < wend);
+            selected += (lane == 0) ? __popc(act) : 0;
+            process_batch<NA>(q, sm, r, act, lane);
+        }
+    } else if (!q.gather) {
+        for (uint64_t b = wbase; b < wend; b += 32) {
+            uint64_t r = b + lane;
+            bool pass = r < wend && row_passes(q, r);
+            unsigned act = __ballot_sync(FULL, pass);
+            selected += (lane == 0) ? __popc(act) : 0;
+            if (act) process_batch<NA>(q, sm, r, act, lane);
+        }
+    } else {
+        int n = 0;  // survivors in this warp's ring
+        for (uint64_t b = wbase; b < wend; b += 128) {
+            bool pass[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                uint64_t r = b + u * 32 + lane;
+                pass[u] = r < wend && row_passes(q, r);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                unsigned m = __ballot_sync(FULL, pass[u]);
+                if (pass[u]) wb[n + __popc(m & ((1u << lane) - 1))] = (uint32_t)(b + u * 32 + lane - row0);
+                n += __popc(m);
+                selected += (lane == 0) ? __popc(m) : 0;
+                __syncwarp();
+                if (n >= 32) {
+                    uint64_t r = row0 + wb[lane];
+                    __syncwarp();
+                    if (lane < n - 32) wb[lane] = wb[32 + lane];
+                    n -= 32;
+                    __syncwarp();
+                    process_batch<NA>(q, sm, r, FULL, lane);
+                }
+            }
+        }
+        if (n > 0) {
+            uint64_t r = row0 + wb[lane < n ? lane : 0];
+            unsigned act = (n >= 32) ? FULL : ((1u << n) - 1);
+            __syncwarp();
+            process_batch<NA>(q, sm, r, act, lane);
+        }
+    }
+}
+
+template <int NA>
+__global__ void __launch_bounds__(SCAN_THREADS, NA <= 4 ? 2 : 1) scan_group_kernel(const __grid_constant__ DevQuery q) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ScanSmem sm = carve(q, smem_raw);
+    const int lane = threadIdx.x & 31;
+    cache_init(q, sm);
     if (threadIdx.x == 0) {
         *sm.live = 0;
         sm.flags[0] = 0;
         sm.flags[1] = 0;
     }
-    uint32_t *wb = sm.wbuf + warp * WBUF;
     unsigned long long selected = 0;
     __syncthreads();
 
@@ -560,75 +635,11 @@ __global__ void __launch_bounds__(SCAN_THREADS, NA <= 4 ? 2 : 1) scan_group_kern
         const uint32_t t = *sm.tile;
         if (sm.flags[0]) {
             cache_flush(q, sm);
-            __syncthreads();
             if (threadIdx.x == 0) *sm.live = 0;
+            __syncthreads();
         }
         if (t >= q.n_tiles) break;
-
-        // rows of this tile and of this warp
-        uint64_t row0, row_end;
-        if (q.rg_list) {
-            uint32_t rgi = t / q.tiles_per_rg, sub = t % q.tiles_per_rg;
-            uint64_t rg = q.rg_list[rgi];
-            row0 = rg * q.rg_rows + (uint64_t)sub * TILE_ROWS;
-            row_end = min(min(row0 + TILE_ROWS, (rg + 1) * (uint64_t)q.rg_rows), q.n_rows);
-        } else {
-            row0 = (uint64_t)t * TILE_ROWS;
-            row_end = min(row0 + TILE_ROWS, q.n_rows);
-        }
-        const uint64_t wbase = row0 + (uint64_t)warp * WARP_ROWS;
-        const uint64_t wend = min(wbase + WARP_ROWS, row_end);
-
-        if (wbase < wend) {
-            if (q.n_preds == 0) {
-                for (uint64_t b = wbase; b < wend; b += 32) {
-                    uint64_t r = b + lane;
-                    unsigned act = __ballot_sync(FULL, r < wend);
-                    selected += (lane == 0) ? __popc(act) : 0;
-                    process_batch<NA>(q, sm, r, act, lane);
-                }
-            } else if (!q.gather) {
-                for (uint64_t b = wbase; b < wend; b += 32) {
-                    uint64_t r = b + lane;
-                    bool pass = r < wend && row_passes(q, r);
-                    unsigned act = __ballot_sync(FULL, pass);
-                    selected += (lane == 0) ? __popc(act) : 0;
-                    if (act) process_batch<NA>(q, sm, r, act, lane);
-                }
-            } else {
-                int n = 0;  // survivors in this warp's ring
-                for (uint64_t b = wbase; b < wend; b += 128) {
-                    bool pass[4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        uint64_t r = b + u * 32 + lane;
-                        pass[u] = r < wend && row_passes(q, r);
-                    }
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        unsigned m = __ballot_sync(FULL, pass[u]);
-                        if (pass[u]) wb[n + __popc(m & ((1u << lane) - 1))] = (uint32_t)(b + u * 32 + lane - row0);
-                        n += __popc(m);
-                        selected += (lane == 0) ? __popc(m) : 0;
-                        __syncwarp();
-                        if (n >= 32) {
-                            uint64_t r = row0 + wb[lane];
-                            __syncwarp();
-                            if (lane < n - 32) wb[lane] = wb[32 + lane];
-                            n -= 32;
-                            __syncwarp();
-                            process_batch<NA>(q, sm, r, FULL, lane);
-                        }
-                    }
-                }
-                if (n > 0) {
-                    uint64_t r = row0 + wb[lane < n ? lane : 0];
-                    unsigned act = (n >= 32) ? FULL : ((1u << n) - 1);
-                    __syncwarp();
-                    process_batch<NA>(q, sm, r, act, lane);
-                }
-            }
-        }
+        scan_tile<NA>(q, sm, t, selected);
         __syncthreads();
     }
     if (q.cache_slots) {
@@ -638,35 +649,97 @@ __global__ void __launch_bounds__(SCAN_THREADS, NA <= 4 ? 2 : 1) scan_group_kern
     if (lane == 0 && selected) atomicAdd(q.selected_rows, selected);
 }
 
+// Many queries in one persistent kernel: work items are (query, tile) pairs,
+// query-major (item i belongs to the query whose [tile_start[q],
+// tile_start[q+1]) range holds it).  A CTA keeps one query's shared-memory
+// table at a time and flushes it when its next item belongs to another query.
+template <int NA>
+__global__ void __launch_bounds__(SCAN_THREADS, NA <= 4 ? 2 : 1)
+    batch_scan_kernel(const DevQuery *__restrict__ qs, const uint32_t *__restrict__ tile_start, uint32_t n_queries,
+                      unsigned int *work_counter, const volatile int *cancel, unsigned int *batch_status) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint32_t s_item, s_query;
+    const int lane = threadIdx.x & 31;
+    const uint32_t total = tile_start[n_queries];
+    int cur = -1;
+    ScanSmem sm{};
+    unsigned long long selected = 0;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            uint32_t item = atomicAdd(work_counter, 1u);
+            if (cancel && *cancel) {
+                atomicOr(batch_status, ST_CANCELLED);
+                item = 0xFFFFFFFFu;
+            }
+            uint32_t qi = 0;
+            if (item < total) {
+                uint32_t lo = 0, hi = n_queries;  // last q with tile_start[q] <= item
+                while (hi - lo > 1) {
+                    uint32_t mid = (lo + hi) >> 1;
+                    if (tile_start[mid] <= item) lo = mid;
+                    else hi = mid;
+                }
+                qi = lo;
+            }
+            s_item = item;
+            s_query = qi;
+        }
+        __syncthreads();
+        const uint32_t item = s_item;
+        const int qn = item < total ? (int)s_query : -1;
+        if (qn != cur && cur >= 0) {
+            const DevQuery &old = qs[cur];
+            if (old.cache_slots) cache_flush(old, sm);
+            if (lane == 0 && selected) atomicAdd(old.selected_rows, selected);
+            selected = 0;
+            __syncthreads();
+        }
+        if (qn < 0) break;
+        const DevQuery &q = qs[qn];
+        if (qn != cur) {
+            sm = carve(q, smem_raw);
+            cache_init(q, sm);
+            if (threadIdx.x == 0) *sm.live = 0;
+            cur = qn;
+            __syncthreads();
+        } else if (q.cache_slots && *sm.live >= (uint32_t)q.cache_flush_at) {
+            __syncthreads();
+            cache_flush(q, sm);
+            if (threadIdx.x == 0) *sm.live = 0;
+            __syncthreads();
+        }
+        scan_tile<NA>(q, sm, item - tile_start[qn], selected);
+        __syncthreads();
+    }
+}
+
 }  // namespace
 
 size_t scan_smem_bytes(const DevQuery &q) {
     return (size_t)q.cache_slots * (8 + 8 * (size_t)q.state_words + 4) + SCAN_WARPS * WBUF * 4 + 16;
 }
 
-int scan_grid_size(const DevQuery &q, int sms) {
-    // persistent grid: every CTA that fits on an SM at once
+template <typename K>
+static int blocks_per_sm(K kernel, size_t smem) {
     int per_sm = 1;
-    size_t smem = scan_smem_bytes(q);
-    cudaError_t e;
-    if (q.n_aggs <= 4) {
-        cudaFuncSetAttribute(scan_group_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scan_group_kernel<4>, SCAN_THREADS, smem);
-    } else {
-        cudaFuncSetAttribute(scan_group_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scan_group_kernel<16>, SCAN_THREADS, smem);
-    }
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, SCAN_THREADS, smem);
     if (e != cudaSuccess || per_sm < 1) {
         cudaGetLastError();
         per_sm = 1;
     }
-    return sms * per_sm;
+    return per_sm;
+}
+
+int scan_grid_size(const DevQuery &q, int sms) {
+    // persistent grid: every CTA that fits on an SM at once
+    size_t smem = scan_smem_bytes(q);
+    return sms * (q.n_aggs <= 4 ? blocks_per_sm(scan_group_kernel<4>, smem) : blocks_per_sm(scan_group_kernel<16>, smem));
 }
 
 cudaError_t launch_scan(const DevQuery &q, int grid, cudaStream_t s) {
     size_t smem = scan_smem_bytes(q);
-    bool small = q.n_aggs <= 4;
-    if (small) {
+    if (q.n_aggs <= 4) {
         cudaError_t e = cudaFuncSetAttribute(scan_group_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         scan_group_kernel<4><<<grid, SCAN_THREADS, smem, s>>>(q);
@@ -674,6 +747,25 @@ cudaError_t launch_scan(const DevQuery &q, int grid, cudaStream_t s) {
         cudaError_t e = cudaFuncSetAttribute(scan_group_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         scan_group_kernel<16><<<grid, SCAN_THREADS, smem, s>>>(q);
+    }
+    return cudaGetLastError();
+}
+
+int batch_scan_grid(int max_aggs, size_t smem, int sms) {
+    return sms * (max_aggs <= 4 ? blocks_per_sm(batch_scan_kernel<4>, smem) : blocks_per_sm(batch_scan_kernel<16>, smem));
+}
+
+cudaError_t launch_batch_scan(const DevQuery *qs, const uint32_t *tile_start, uint32_t n_queries, int max_aggs,
+                              size_t smem, int grid, unsigned int *work_counter, const volatile int *cancel,
+                              unsigned int *status, cudaStream_t s) {
+    if (max_aggs <= 4) {
+        cudaError_t e = cudaFuncSetAttribute(batch_scan_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        batch_scan_kernel<4><<<grid, SCAN_THREADS, smem, s>>>(qs, tile_start, n_queries, work_counter, cancel, status);
+    } else {
+        cudaError_t e = cudaFuncSetAttribute(batch_scan_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        batch_scan_kernel<16><<<grid, SCAN_THREADS, smem, s>>>(qs, tile_start, n_queries, work_counter, cancel, status);
     }
     return cudaGetLastError();
 }

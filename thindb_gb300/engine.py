@@ -230,6 +230,9 @@ class Request:
     memory_budget: int = 0
     flags: int = 0
     stream: int = 0
+    tile_rows: int = 0
+    cache_slots: int = 0
+    table_load_pct: int = 0
 
 
 def build_request(table: Table, req: Request) -> tuple[abi.Request, list]:
@@ -282,6 +285,9 @@ def build_request(table: Table, req: Request) -> tuple[abi.Request, list]:
     r.memory_budget_bytes = int(req.memory_budget)
     r.stream = req.stream or None
     r.flags = int(req.flags)
+    r.tile_rows = int(req.tile_rows)
+    r.cache_slots = int(req.cache_slots)
+    r.table_load_pct = int(req.table_load_pct)
     keep += [g, aggs, where, having, order]
     return r, keep
 
