@@ -162,6 +162,14 @@ def make_request(workload: str, flags: int = 0, stream: int = 0):
                                        AggSpec("sum", "latency_ms", "lat")], flags=flags, stream=stream)
 
 
+def rows_of(result: dict) -> list:
+    """A result dict as a list of exact rows (bytes per column), for equality checks."""
+    cols = []
+    for name, (vals, ok) in result.items():
+        cols.append((name, np.ascontiguousarray(vals).tobytes(), None if ok is None else ok.tobytes()))
+    return cols
+
+
 def columns_of(inputs, ndv=None):
     from thindb_gb300.engine import Column
 
@@ -347,16 +355,98 @@ def gpu_arm(args, wl):
         dist.destroy_process_group()
 
 
+def batched_arm(args):
+    """256 GROUP BY queries over one resident 100M-row table: one batched
+    persistent kernel replayed from a CUDA graph vs 256 plain sequential
+    operator executions; identical results required."""
+    import torch
+
+    from thindb_gb300 import workloads
+    from thindb_gb300.engine import QueryBatch, Table, try_build_group_topn
+
+    n = args.rows or datagen.FILTERED_ROWS
+    torch.cuda.set_device(0)
+    inputs = make_inputs("filtered", n, pinned=True)
+    k10, k1k, k1m = (torch.empty(n, dtype=torch.int32, pin_memory=True) for _ in range(3))
+    datagen.lib().tdg_extra_keys(n, 2, k10.data_ptr(), k1k.data_ptr(), k1m.data_ptr(), 0)
+    inputs += [("k10", abi.INT, k10, 0), ("k1k", abi.INT, k1k, 0), ("k1m", abi.INT, k1m, 0)]
+    stream = torch.cuda.Stream()
+    table = Table(columns_of(inputs), compute_ndv=True, stream=stream.cuda_stream)
+    nq = args.queries
+    reqs = workloads.batched_requests(nq, seed=4)
+    for r in reqs:
+        r.stream = stream.cuda_stream
+
+    b = QueryBatch(table, reqs, graph=True, stream=stream.cuda_stream)
+    for _ in range(args.warmup):
+        b.execute()
+        b.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        b.execute()
+        b.synchronize()
+        batched_rows = [rows_of(b.collect(i)) for i in range(nq)]
+    batched_s = (time.perf_counter() - t0) / args.steps
+    clk = clocks.stop()
+    bst = b.stats()
+    b.close()
+
+    qs = [try_build_group_topn(table, r) for r in reqs]
+    for q in qs:  # warm every plain operator once
+        q.execute()
+        q.synchronize()
+    t0 = time.perf_counter()
+    plain_rows = []
+    for q in qs:
+        q.execute()
+        plain_rows.append(rows_of(q.collect()))
+    plain_s = time.perf_counter() - t0
+    for q in qs:
+        q.close()
+    identical = plain_rows == batched_rows
+    value = nq / batched_s
+    line = {
+        "metric": "batched GROUP BY queries/s", "value": value, "unit": "queries/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_s * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int64/int128", "data": "synthetic (seeded generator)",
+        "config": {"workload": f"{nq} concurrent GROUP BY queries over one resident {n:,}-row table "
+                               "(k Zipf 10M, k10, k1k, k1m keys; selectivity log-uniform 0.1%-50%; random "
+                               "COUNT/SUM/MIN/MAX subsets; ORDER BY first aggregate DESC LIMIT 10)",
+                   "step": "one batched execute (CUDA graph replay) + results of every query to the host"},
+        "plain": {"value": nq / plain_s, "unit": "queries/s",
+                  "how": f"{nq} plain operators executed one after another (execute + next each)"},
+        "speedup_vs_plain": plain_s / batched_s,
+        "identical_results": identical,
+        "batch": {"kernel_launches": bst.kernel_launches, "graph": bool(bst.graph), "work_items": bst.work_items,
+                  "device_ms": bst.total_ms, "rerun_queries": bst.rerun_queries},
+        "gpu_launches": bst.kernel_launches * args.steps,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    table.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="filtered", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="filtered", choices=sorted(WORKLOADS) + ["batched", "served"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--rows", type=int, default=0, help="rows of the workload (default: its full size)")
+    ap.add_argument("--queries", type=int, default=256, help="queries of the batched workload")
     args = ap.parse_args()
+    if args.workload == "batched":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the batched mode has no CPU reference arm; "
+                              "run the default workload"}))
+            return
+        batched_arm(args)
+        return
     wl = dict(WORKLOADS[args.workload])
     if args.rows:
         wl["rows"] = args.rows

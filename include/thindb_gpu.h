@@ -211,11 +211,12 @@ typedef struct tgpu_request {
     void *stream;                /* cudaStream_t, NULL = library stream */
     int32_t flags;               /* TGPU_FLAG_* */
     /* Tuning knobs (0 = engine default; the autotuner sets them per shape):
-     * rows per scan tile (a multiple of 512, at most 65,536; default 8,192),
+     * rows per warp chunk of the scan (a multiple of 256, at most 65,536;
+     * default: about eight chunks per warp of the persistent grid),
      * shared-memory table slots (power of two; -1 = no shared-memory table),
      * group-table load in percent (capacity = expected groups * 100 / load;
      * default 50). */
-    int32_t tile_rows;
+    int32_t chunk_rows;
     int32_t cache_slots;
     int32_t table_load_pct;
 } tgpu_request;
@@ -320,6 +321,42 @@ tgpu_status tgpu_query_destroy(tgpu_query *q);
 
 /* Synchronise the library stream / the query's stream (tests and benches). */
 tgpu_status tgpu_query_synchronize(tgpu_query *q);
+
+/* ------------------------------------------------------ batched execution -- */
+
+/* Many GROUP BY queries over one table run as ONE persistent kernel that
+ * drains a work queue of (query, row-group tile) items, then one set of
+ * batched compaction / top-k / gather / clear kernels (grid.y = query).  With
+ * TGPU_BATCH_GRAPH the whole sequence is captured once into a CUDA graph and
+ * every later execute replays it.  thinDB runs such queries one operator at a
+ * time (one `Query` per statement, exec.zig:903); this has no direct
+ * counterpart and produces, per query, exactly the rows `tgpu_query_next`
+ * would.  Each request must return all groups or a top-k page with
+ * offset + limit <= 32; other shapes decline the batch. */
+typedef struct tgpu_query_batch tgpu_query_batch;
+
+#define TGPU_BATCH_GRAPH 0x1
+
+typedef struct tgpu_batch_stats {
+    uint32_t n_queries;
+    uint32_t kernel_launches;    /* kernels one execute launches */
+    uint32_t graph;              /* 1 when executes replay a captured CUDA graph */
+    uint32_t rerun_queries;      /* queries rerun alone after a table overflow */
+    uint64_t work_items;         /* (query, tile) items of one execute */
+    double total_ms;             /* last execute on the device (CUDA events) */
+} tgpu_batch_stats;
+
+tgpu_status tgpu_batch_create(tgpu_table *table, const tgpu_request *requests, uint32_t n_requests,
+                              int32_t flags, void *stream, tgpu_query_batch **out);
+tgpu_status tgpu_batch_execute(tgpu_query_batch *b);
+tgpu_status tgpu_batch_synchronize(tgpu_query_batch *b);
+tgpu_status tgpu_batch_output_schema(const tgpu_query_batch *b, uint32_t query, tgpu_output_column *cols,
+                                     uint32_t cap, uint32_t *n_columns);
+/* `next` of query `query` of the last execute. */
+tgpu_status tgpu_batch_next(tgpu_query_batch *b, uint32_t query, tgpu_batch *batch, int32_t *done);
+tgpu_status tgpu_batch_cancel(tgpu_query_batch *b);
+tgpu_status tgpu_batch_get_stats(const tgpu_query_batch *b, tgpu_batch_stats *out);
+tgpu_status tgpu_batch_destroy(tgpu_query_batch *b);
 
 #ifdef __cplusplus
 }

@@ -83,7 +83,7 @@ class Request(C.Structure):
                 ("order", C.POINTER(SortSpec)), ("n_order", C.c_uint32),
                 ("limit", C.c_uint64), ("offset", C.c_uint64), ("expected_groups", C.c_uint64),
                 ("memory_budget_bytes", C.c_uint64), ("stream", C.c_void_p), ("flags", C.c_int32),
-                ("tile_rows", C.c_int32), ("cache_slots", C.c_int32), ("table_load_pct", C.c_int32)]
+                ("chunk_rows", C.c_int32), ("cache_slots", C.c_int32), ("table_load_pct", C.c_int32)]
 
 
 class OutputColumn(C.Structure):
@@ -124,4 +124,21 @@ SIGNATURES = [
     ("tgpu_query_get_stats", C.c_int, [C.c_void_p, C.POINTER(QueryStats)]),
     ("tgpu_query_destroy", C.c_int, [C.c_void_p]),
     ("tgpu_query_synchronize", C.c_int, [C.c_void_p]),
+    ("tgpu_batch_create", C.c_int, [C.c_void_p, C.POINTER(Request), C.c_uint32, C.c_int32, C.c_void_p,
+                                    C.POINTER(C.c_void_p)]),
+    ("tgpu_batch_execute", C.c_int, [C.c_void_p]),
+    ("tgpu_batch_synchronize", C.c_int, [C.c_void_p]),
+    ("tgpu_batch_output_schema", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(OutputColumn), C.c_uint32,
+                                           C.POINTER(C.c_uint32)]),
+    ("tgpu_batch_next", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(Batch), C.POINTER(C.c_int32)]),
+    ("tgpu_batch_cancel", C.c_int, [C.c_void_p]),
+    ("tgpu_batch_get_stats", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("tgpu_batch_destroy", C.c_int, [C.c_void_p]),
 ]
+
+BATCH_GRAPH = 0x1
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("n_queries", C.c_uint32), ("kernel_launches", C.c_uint32), ("graph", C.c_uint32),
+                ("rerun_queries", C.c_uint32), ("work_items", C.c_uint64), ("total_ms", C.c_double)]

@@ -246,6 +246,7 @@ struct tgpu_query {
     uint64_t out_rows_max = 0;
     int grid = 0;
     int cache_req = 0;            // requested shared-memory slots (0 auto, -1 off)
+    uint32_t chunk_req = 0;       // requested rows per warp chunk (0 auto)
     int load_pct = 50;            // group-table load target
     // workspace
     Buffer table_buf, occ_buf;
@@ -468,14 +469,22 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
     if (off > 128) return fail(TGPU_DECLINE, "packed key wider than 128 bits (hashed keys)");
     dq.key_words = off > 64 ? 2 : 1;
 
-    // aggregates and state words (word 0 = the group's row count)
-    int next = 1;
+    // aggregates and state words (word 0 = the group's row count).  `next`
+    // counts slots exactly as thinDB does (its 16-slot limit decides
+    // declines); `phys` allocates the device words, where SUM and AVG of one
+    // column share their sum (and valid-count) words.
+    int next = 1, phys = 1;
+    struct Shared {
+        int col, kind, word, vword;
+    };
+    std::vector<Shared> shared;
     for (uint32_t i = 0; i < req->n_aggs; ++i) {
         const tgpu_agg_spec &a = req->aggs[i];
         DevAgg &g = dq.aggs[dq.n_aggs];
         DevOut &o = df.outs[dq.n_aggs];
         g.col = -1;
         g.vword = -1;
+        g.owner = 1;
         o.vword = -1;
         o.func = a.func;
         int in_type = 0, scale = 0;
@@ -496,7 +505,8 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
                 if (nullable) {
                     if (next > MAX_AGGS) return fail(TGPU_DECLINE, "aggregate state count");
                     g.kind = AK_COUNT_VALID;
-                    g.word = next++;
+                    next++;
+                    g.word = phys++;
                 } else {
                     g.kind = AK_COUNT_ROWS;
                     g.word = 0;
@@ -510,18 +520,31 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
                 bool wide = sum && is_i64_phys(in_type);
                 int width = (wide ? 2 : 1) + (nullable ? 1 : 0);
                 if (next + width - 1 > MAX_AGGS) return fail(TGPU_DECLINE, "aggregate state count");
-                g.word = next;
-                g.vword = nullable ? next + width - 1 : -1;
                 next += width;
+                if (sum) g.kind = is_float_t(in_type) ? AK_SUM_F64 : (wide ? AK_SUM_I128 : AK_SUM_I64);
+                else {
+                    bool mn = a.func == TGPU_AGG_MIN;
+                    g.kind = is_float_t(in_type) ? (mn ? AK_MIN_F : AK_MAX_F) : (mn ? AK_MIN_I : AK_MAX_I);
+                }
+                const Shared *sh = nullptr;
+                for (const Shared &s2 : shared)
+                    if (s2.col == a.column && s2.kind == g.kind) sh = &s2;
+                if (sh) {
+                    g.word = sh->word;
+                    g.vword = sh->vword;
+                    g.owner = 0;
+                } else {
+                    g.word = phys;
+                    g.vword = nullable ? phys + width - 1 : -1;
+                    phys += width;
+                    shared.push_back(Shared{a.column, g.kind, g.word, g.vword});
+                }
                 if (sum) {
-                    g.kind = is_float_t(in_type) ? AK_SUM_F64 : (wide ? AK_SUM_I128 : AK_SUM_I64);
                     if (a.func == TGPU_AGG_SUM)
                         out_type = in_type == TGPU_DECIMAL64 ? TGPU_DECIMAL128 : (is_float_t(in_type) ? TGPU_DOUBLE : TGPU_BIGINT);
                     else
                         out_type = TGPU_DOUBLE;
                 } else {
-                    bool mn = a.func == TGPU_AGG_MIN;
-                    g.kind = is_float_t(in_type) ? (mn ? AK_MIN_F : AK_MAX_F) : (mn ? AK_MIN_I : AK_MAX_I);
                     out_type = in_type;
                 }
                 break;
@@ -531,13 +554,15 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
                 if (dq.n_dsets >= MAX_DISTINCT) return fail(TGPU_DECLINE, "count distinct slot count");
                 if (next > MAX_AGGS) return fail(TGPU_DECLINE, "aggregate state count");
                 g.kind = AK_DISTINCT;
-                g.word = next++;
+                next++;
+                g.word = phys++;
                 g.dset = dq.n_dsets++;
                 dq.needs_gid = 1;
                 break;
             default:
                 return fail(TGPU_DECLINE, "aggregate func");
         }
+        g.needs_value = (g.kind == AK_DISTINCT || (g.owner && g.kind != AK_COUNT_ROWS && g.kind != AK_COUNT_VALID)) ? 1 : 0;
         o.kind = g.kind;
         o.word = g.word;
         o.vword = g.vword;
@@ -562,7 +587,7 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
         oc.elem_bytes = type_bytes(out_type);
         q->schema.push_back(oc);
     }
-    dq.state_words = next;
+    dq.state_words = phys;
     dq.slot_words = (int)next_pow2((uint64_t)(dq.key_words + dq.state_words));
 
     for (uint32_t i = 0; i < req->n_order; ++i) {
@@ -630,10 +655,10 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
 
 // Shared-memory cache size for a state width: the largest power of two that
 // keeps two CTAs per SM (<= ~100 KB each).
-int cache_slots_for(int state_words) {
+int cache_slots_for(int state_words, size_t list_bytes) {
     size_t per = 12 + 8 * (size_t)state_words;
     int c = 4096;
-    while (c > 64 && (size_t)c * per + SCAN_WARPS * 64 * 4 + 16 > 100 * 1024) c >>= 1;
+    while (c >= 64 && (size_t)c * per + list_bytes + 16 > 110 * 1024) c >>= 1;
     return c;
 }
 
@@ -645,25 +670,42 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     dq.cap = cap;
     df.cap = cap;
 
-    // route: the shared-memory cache holds every group (lowcard), pre-folds
-    // hot keys with periodic flushes (global route), or is off.
-    dq.cache_slots = 0;
-    dq.cache_flush_at = 0;
-    q->route = 2;
-    if (dq.key_words == 1 && !(q->flags & TGPU_FLAG_FORCE_GLOBAL) && q->cache_req >= 0) {
-        int C = cache_slots_for(dq.state_words);
-        if (q->cache_req > 0) C = std::min(C, q->cache_req);
-        if (q->groups_est * 8 <= (uint64_t)C * 5) {
-            dq.cache_slots = C;
-            dq.cache_flush_at = C;  // resident: never flushed before the end
-            q->route = 1;
-        } else if (!dq.needs_gid) {
-            dq.cache_slots = C;
-            dq.cache_flush_at = C * 3 / 4;
-        }
-    }
     dq.warp_combine = (q->flags & TGPU_FLAG_NO_WARP_COMBINE) ? 0 : 1;
     dq.gather = (dq.n_preds > 0 && !(q->flags & TGPU_FLAG_DENSE_SCAN)) ? 1 : 0;
+
+    // chunking: about eight chunks per warp of a two-CTA-per-SM grid
+    {
+        DeviceCtx *dev;
+        tgpu_status st = device_ctx(&dev);
+        if (st != TGPU_OK) return st;
+        uint64_t warps = (uint64_t)dev->sms * 2 * SCAN_WARPS;
+        uint64_t chunk = q->chunk_req;
+        if (!chunk) {
+            chunk = std::max<uint64_t>(1, q->rows_scanned / (warps * 8));
+            chunk = std::max<uint64_t>(CHUNK_ALIGN, chunk / CHUNK_ALIGN * CHUNK_ALIGN);
+            chunk = std::min<uint64_t>(chunk, dq.gather ? 1024 : 4096);
+        }
+        dq.chunk_rows = (uint32_t)chunk;
+    }
+    const size_t list_bytes = dq.gather ? (size_t)SCAN_WARPS * dq.chunk_rows * 2 : 0;
+
+    // route: the shared-memory table holds every group (lowcard), keeps the
+    // first-seen (hottest) keys of a larger key space (global route), or is off
+    dq.cache_slots = 0;
+    dq.cache_probe = 0;
+    q->route = 2;
+    if (dq.key_words == 1 && !(q->flags & TGPU_FLAG_FORCE_GLOBAL) && q->cache_req >= 0) {
+        int C = cache_slots_for(dq.state_words, list_bytes);
+        if (q->cache_req > 0) C = std::min(C, q->cache_req);
+        if (C >= 64 && q->groups_est * 8 <= (uint64_t)C * 5) {
+            dq.cache_slots = C;
+            dq.cache_probe = C;  // resident: probe the whole table
+            q->route = 1;
+        } else if (C >= 64 && !dq.needs_gid) {
+            dq.cache_slots = C;
+            dq.cache_probe = 16;
+        }
+    }
 
     // ranking
     if (df.n_order == 0 && q->limit == TGPU_NO_LIMIT && q->offset == 0) {
@@ -788,13 +830,13 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     if (pruned) {
         dq.rg_list = q->d_rg_list;
         dq.n_rg = (uint32_t)q->rg_list.size();
-        dq.tiles_per_rg = (t->rg_rows + dq.tile_rows - 1) / dq.tile_rows;
-        dq.n_tiles = dq.n_rg * dq.tiles_per_rg;
+        dq.chunks_per_rg = (t->rg_rows + dq.chunk_rows - 1) / dq.chunk_rows;
+        dq.n_chunks = dq.n_rg * dq.chunks_per_rg;
     } else {
         dq.rg_list = nullptr;
         dq.n_rg = t->n_rg;
-        dq.tiles_per_rg = 0;
-        dq.n_tiles = (uint32_t)((t->n_rows + dq.tile_rows - 1) / dq.tile_rows);
+        dq.chunks_per_rg = 0;
+        dq.n_chunks = (uint32_t)((t->n_rows + dq.chunk_rows - 1) / dq.chunk_rows);
     }
     return TGPU_OK;
 }
@@ -824,7 +866,7 @@ tgpu_status enqueue(tgpu_query *q) {
     CU(cudaMemsetAsync(q->d_counts, 0, 8 * 8, s));
     const bool timing = (q->flags & TGPU_FLAG_TIMING) != 0;
     if (timing) CU(cudaEventRecord(q->ev[0], s));
-    if (dq.n_tiles > 0) {
+    if (dq.n_chunks > 0) {
         CU(launch_scan(dq, q->grid, s));
         q->launches++;
     }
@@ -1058,17 +1100,16 @@ tgpu_status tgpu_query_create(tgpu_table *table, const tgpu_request *req, tgpu_q
     q->limit = req->limit;
     q->offset = req->offset;
     q->budget = req->memory_budget_bytes;
-    if (req->tile_rows < 0 || req->tile_rows % SCAN_THREADS != 0 || req->tile_rows > 65536)
-        return fail(TGPU_ERR_INVALID_ARGUMENT, "tile_rows must be a multiple of 512 up to 65536");
+    if (req->chunk_rows < 0 || req->chunk_rows % CHUNK_ALIGN != 0 || req->chunk_rows > 65536)
+        return fail(TGPU_ERR_INVALID_ARGUMENT, "chunk_rows must be a multiple of 256 up to 65536");
     if (req->cache_slots > 0 && (req->cache_slots & (req->cache_slots - 1)))
         return fail(TGPU_ERR_INVALID_ARGUMENT, "cache_slots must be a power of two");
     if (req->table_load_pct < 0 || req->table_load_pct > 90)
         return fail(TGPU_ERR_INVALID_ARGUMENT, "table_load_pct must be within 1..90");
     q->cache_req = req->cache_slots;
+    q->chunk_req = (uint32_t)req->chunk_rows;
     q->load_pct = req->table_load_pct ? req->table_load_pct : 50;
     st = plan_query(q.get(), table, req);
-    q->dq.tile_rows = req->tile_rows ? (uint32_t)req->tile_rows : (uint32_t)TILE_ROWS;
-    q->dq.warp_rows = q->dq.tile_rows / SCAN_WARPS;
     if (st != TGPU_OK) return st;
     CU(cudaHostAlloc((void **)&q->h_cancel, sizeof(int), cudaHostAllocMapped));
     *q->h_cancel = 0;
@@ -1148,6 +1189,339 @@ tgpu_status tgpu_query_get_stats(const tgpu_query *q, tgpu_query_stats *out) {
 tgpu_status tgpu_query_destroy(tgpu_query *q) {
     if (!q) return fail(TGPU_ERR_INVALID_ARGUMENT, "null query");
     delete q;
+    return TGPU_OK;
+}
+
+}  // extern "C"
+
+// ====================================================== batched execution ==
+
+struct tgpu_query_batch {
+    tgpu_table *t = nullptr;
+    cudaStream_t stream = nullptr;
+    int flags = 0;
+    std::vector<tgpu_query *> qs;
+    std::vector<DevQuery> h_qs;
+    std::vector<DevFinal> h_fs;
+    std::vector<DevFinalBufs> h_bs;
+    std::vector<uint32_t> tile_start;
+    void *dev = nullptr;                    // one allocation for every array below
+    DevQuery *d_qs = nullptr;
+    DevFinal *d_fs = nullptr;
+    DevFinalBufs *d_bs = nullptr;
+    uint32_t *d_tile_start = nullptr;
+    unsigned int *d_ctrl = nullptr;         // [0] work counter, [1] status
+    unsigned long long *d_counts = nullptr; // 8 per query
+    unsigned int *d_qctrl = nullptr;        // 4 per query: tile counter, status
+    unsigned long long *h_counts = nullptr; // pinned: 8 per query, then Q statuses + batch status
+    int *h_cancel = nullptr, *d_cancel = nullptr;
+    bool any_distinct = false, any_topk = false;
+    int max_aggs = 0, max_sort_words = 2;
+    size_t smem = 0;
+    int grid = 0;
+    uint32_t max_cpt_blocks = 1, max_cand_blocks = 1;
+    uint64_t max_rows = 1, max_words = 1;
+    uint32_t epoch = 0;
+    bool descriptors_dirty = true;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool executed = false, synced = false;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    tgpu_batch_stats stats{};
+    ~tgpu_query_batch() {
+        if (stream) cudaStreamSynchronize(stream);
+        for (auto *q : qs) delete q;
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (dev) cudaFree(dev);
+        if (h_counts) cudaFreeHost(h_counts);
+        if (h_cancel) cudaFreeHost(h_cancel);
+        for (auto e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
+
+namespace {
+
+// Point every query's counters at the batch arrays and rebuild the device
+// descriptors (after create, and after a query was regrown on its own).
+tgpu_status batch_descriptors(tgpu_query_batch *b) {
+    const uint32_t Q = (uint32_t)b->qs.size();
+    b->h_qs.resize(Q);
+    b->h_fs.resize(Q);
+    b->h_bs.resize(Q);
+    b->tile_start.assign(Q + 1, 0);
+    b->max_aggs = 0;
+    b->max_sort_words = 2;
+    b->smem = 0;
+    b->max_cpt_blocks = 1;
+    b->max_cand_blocks = 1;
+    b->max_rows = 1;
+    b->max_words = 1;
+    b->any_distinct = b->any_topk = false;
+    for (uint32_t i = 0; i < Q; ++i) {
+        tgpu_query *q = b->qs[i];
+        q->d_counts = b->d_counts + 8 * (size_t)i;
+        q->d_ctrl = b->d_qctrl + 4 * (size_t)i;
+        DevQuery dq = q->dq;
+        dq.tile_counter = q->d_ctrl;
+        dq.status = q->d_ctrl + 1;
+        dq.selected_rows = q->d_counts + 4;
+        dq.cancel = (const volatile int *)b->d_cancel;
+        dq.epoch = b->epoch;
+        b->h_qs[i] = dq;
+        b->h_fs[i] = q->df;
+        DevFinalBufs &fb = b->h_bs[i];
+        fb.block_counts = q->d_block_counts;
+        fb.gids = q->d_gids;
+        fb.counts = q->d_counts;
+        fb.cand_keys = q->d_cand_keys;
+        fb.cand_gids = q->d_cand_gids;
+        fb.out_cols = q->d_out_ptrs;
+        fb.out_valid = q->d_valid_ptrs;
+        fb.n_cpt_blocks = q->n_cpt_blocks;
+        fb.n_cand_blocks = q->n_cand_blocks;
+        fb.k = q->k;
+        fb.rank = q->rank == RANK_TOPK ? 1 : 0;
+        fb.sel = q->rank == RANK_TOPK ? q->d_sel : q->d_gids;
+        fb.offset = q->rank == RANK_TOPK ? q->offset : 0;
+        fb.gather_rows = q->rank == RANK_TOPK ? q->limit : q->out_rows_max;
+        b->tile_start[i + 1] = b->tile_start[i] + (dq.n_chunks + SCAN_WARPS - 1) / SCAN_WARPS;
+        b->max_aggs = std::max(b->max_aggs, dq.n_aggs);
+        b->max_sort_words = std::max(b->max_sort_words, (int)q->df.sort_words);
+        b->smem = std::max(b->smem, scan_smem_bytes(dq));
+        b->max_cpt_blocks = std::max(b->max_cpt_blocks, q->n_cpt_blocks);
+        b->max_cand_blocks = std::max(b->max_cand_blocks, q->n_cand_blocks);
+        b->max_rows = std::max<uint64_t>(b->max_rows, fb.gather_rows);
+        b->max_words = std::max<uint64_t>(b->max_words, (dq.cap + 1 + 31) / 32);
+        b->any_distinct |= dq.n_dsets > 0;
+        b->any_topk |= fb.rank == 1;
+    }
+    CU(cudaMemcpyAsync(b->d_qs, b->h_qs.data(), sizeof(DevQuery) * Q, cudaMemcpyHostToDevice, b->stream));
+    CU(cudaMemcpyAsync(b->d_fs, b->h_fs.data(), sizeof(DevFinal) * Q, cudaMemcpyHostToDevice, b->stream));
+    CU(cudaMemcpyAsync(b->d_bs, b->h_bs.data(), sizeof(DevFinalBufs) * Q, cudaMemcpyHostToDevice, b->stream));
+    CU(cudaMemcpyAsync(b->d_tile_start, b->tile_start.data(), 4 * (Q + 1), cudaMemcpyHostToDevice, b->stream));
+    CU(cudaStreamSynchronize(b->stream));
+    DeviceCtx *dev;
+    tgpu_status st = device_ctx(&dev);
+    if (st != TGPU_OK) return st;
+    b->grid = batch_scan_grid(b->max_aggs, b->smem, dev->sms);
+    b->descriptors_dirty = false;
+    b->stats.work_items = b->tile_start[Q];
+    return TGPU_OK;
+}
+
+// The device work of one execute (also what a CUDA graph captures).
+tgpu_status batch_enqueue_work(tgpu_query_batch *b) {
+    const uint32_t Q = (uint32_t)b->qs.size();
+    cudaStream_t s = b->stream;
+    CU(cudaEventRecord(b->ev[0], s));
+    CU(cudaMemsetAsync(b->d_ctrl, 0, 8, s));
+    CU(cudaMemsetAsync(b->d_counts, 0, 64 * (size_t)Q, s));
+    CU(cudaMemsetAsync(b->d_qctrl, 0, 16 * (size_t)Q, s));
+    CU(launch_batch_scan(b->d_qs, b->d_tile_start, Q, b->max_aggs, b->smem, b->grid, b->d_ctrl,
+                         (const volatile int *)b->d_cancel, b->d_ctrl + 1, s));
+    CU(launch_finalize_batch(b->d_fs, b->d_bs, Q, b->max_cpt_blocks, b->max_cand_blocks, b->max_sort_words,
+                             b->any_topk, b->max_rows, b->max_words, s));
+    CU(cudaMemcpyAsync(b->h_counts, b->d_counts, 64 * (size_t)Q, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(b->h_counts + 8 * (size_t)Q, b->d_qctrl, 16 * (size_t)Q, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(b->h_counts + 10 * (size_t)Q, b->d_ctrl, 8, cudaMemcpyDeviceToHost, s));
+    CU(cudaEventRecord(b->ev[1], s));
+    b->stats.kernel_launches = 1 + 5 + (b->any_topk ? 1 : 0);
+    return TGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+tgpu_status tgpu_batch_create(tgpu_table *table, const tgpu_request *reqs, uint32_t n, int32_t flags, void *stream,
+                              tgpu_query_batch **out) {
+    if (!table || (!reqs && n) || !out) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
+    if (n == 0) return fail(TGPU_ERR_INVALID_ARGUMENT, "empty batch");
+    DeviceCtx *dev;
+    tgpu_status st = device_ctx(&dev);
+    if (st != TGPU_OK) return st;
+    std::unique_ptr<tgpu_query_batch> b(new tgpu_query_batch());
+    b->t = table;
+    b->stream = stream ? (cudaStream_t)stream : dev->stream;
+    b->flags = flags;
+    for (uint32_t i = 0; i < n; ++i) {
+        tgpu_request r = reqs[i];
+        r.stream = b->stream;
+        tgpu_query *q = nullptr;
+        st = tgpu_query_create(table, &r, &q);
+        if (st != TGPU_OK) return st;
+        b->qs.push_back(q);
+        if (q->rank == RANK_SORT) {
+            return fail(TGPU_DECLINE, "batched queries return all groups or a top-k with offset + limit <= 32");
+        }
+    }
+    const size_t Q = n;
+    size_t off = 0;
+    auto add = [&](size_t bytes) {
+        size_t o = off;
+        off += (bytes + 255) & ~(size_t)255;
+        return o;
+    };
+    size_t o_qs = add(sizeof(DevQuery) * Q), o_fs = add(sizeof(DevFinal) * Q), o_bs = add(sizeof(DevFinalBufs) * Q),
+           o_ts = add(4 * (Q + 1)), o_ctrl = add(16), o_counts = add(64 * Q), o_qctrl = add(16 * Q);
+    CU(cudaMalloc(&b->dev, off));
+    char *base = (char *)b->dev;
+    b->d_qs = (DevQuery *)(base + o_qs);
+    b->d_fs = (DevFinal *)(base + o_fs);
+    b->d_bs = (DevFinalBufs *)(base + o_bs);
+    b->d_tile_start = (uint32_t *)(base + o_ts);
+    b->d_ctrl = (unsigned int *)(base + o_ctrl);
+    b->d_counts = (unsigned long long *)(base + o_counts);
+    b->d_qctrl = (unsigned int *)(base + o_qctrl);
+    CU(cudaHostAlloc((void **)&b->h_counts, 8 * (11 * Q + 2), cudaHostAllocDefault));
+    std::memset(b->h_counts, 0, 8 * (11 * Q + 2));
+    CU(cudaHostAlloc((void **)&b->h_cancel, sizeof(int), cudaHostAllocMapped));
+    *b->h_cancel = 0;
+    CU(cudaHostGetDevicePointer((void **)&b->d_cancel, b->h_cancel, 0));
+    for (auto &e : b->ev) CU(cudaEventCreate(&e));
+    for (auto *q : b->qs)
+        for (auto &buf : q->dset_bufs) b->epoch = std::max(b->epoch, buf.epoch);
+    b->stats.n_queries = n;
+    st = batch_descriptors(b.get());
+    if (st != TGPU_OK) return st;
+    *out = b.release();
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_batch_execute(tgpu_query_batch *b) {
+    if (!b) return fail(TGPU_ERR_INVALID_ARGUMENT, "null batch");
+    if (*b->h_cancel) return fail(TGPU_ERR_CANCELLED, "batch cancelled");
+    tgpu_status st;
+    if (b->any_distinct) {
+        // distinct sets are reused across executes: a fresh epoch frees their entries
+        ++b->epoch;
+        if (b->epoch == 0xFFFFFFFFu) {
+            for (auto *q : b->qs)
+                for (auto &buf : q->dset_bufs) CU(cudaMemsetAsync(buf.p, 0, buf.bytes, b->stream));
+            b->epoch = 1;
+        }
+        for (auto *q : b->qs)
+            for (auto &buf : q->dset_bufs) buf.epoch = b->epoch;
+        b->descriptors_dirty = true;
+    }
+    if (b->descriptors_dirty) {
+        if ((st = batch_descriptors(b)) != TGPU_OK) return st;
+    }
+    for (auto *q : b->qs) {
+        q->table_buf.dirty = true;
+        q->occ_buf.dirty = true;
+    }
+    if (b->flags & TGPU_BATCH_GRAPH) {
+        if (!b->exec) {
+            CU(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+            st = batch_enqueue_work(b);
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+            if (st != TGPU_OK) {
+                if (g) cudaGraphDestroy(g);
+                return st;
+            }
+            CU(e);
+            b->graph = g;
+            CU(cudaGraphInstantiate(&b->exec, g, 0));
+        }
+        CU(cudaGraphLaunch(b->exec, b->stream));
+        b->stats.graph = 1;
+    } else {
+        if ((st = batch_enqueue_work(b)) != TGPU_OK) return st;
+        b->stats.graph = 0;
+    }
+    b->executed = true;
+    b->synced = false;
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_batch_synchronize(tgpu_query_batch *b) {
+    if (!b) return fail(TGPU_ERR_INVALID_ARGUMENT, "null batch");
+    if (!b->executed || b->synced) return TGPU_OK;
+    CU(cudaStreamSynchronize(b->stream));
+    const size_t Q = b->qs.size();
+    const uint32_t *qctrl = (const uint32_t *)(b->h_counts + 8 * Q);
+    const uint32_t bstatus = ((const uint32_t *)(b->h_counts + 10 * Q))[1];
+    float ms = 0;
+    CU(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
+    b->stats.total_ms = ms;
+    b->stats.rerun_queries = 0;
+    b->synced = true;
+    if (bstatus & ST_CANCELLED) return fail(TGPU_ERR_CANCELLED, "batch cancelled");
+    for (size_t i = 0; i < Q; ++i) {
+        tgpu_query *q = b->qs[i];
+        const uint32_t status = qctrl[4 * i + 1];
+        q->table_buf.dirty = false;
+        q->occ_buf.dirty = false;
+        if (status & (ST_TABLE_FULL | ST_DISTINCT_FULL)) {
+            // regrow this query and run it alone; its descriptors change
+            if (status & ST_TABLE_FULL) q->groups_est = std::max<uint64_t>(q->groups_est * 4, 1024);
+            if (status & ST_DISTINCT_FULL)
+                for (auto &nd : q->dset_need) nd *= 4;
+            tgpu_status st = size_workspace(q, next_pow2(q->groups_est * 100 / q->load_pct));
+            if (st != TGPU_OK) return st;
+            DeviceCtx *dev;
+            if ((st = device_ctx(&dev)) != TGPU_OK) return st;
+            q->grid = scan_grid_size(q->dq, dev->sms);
+            if ((st = enqueue(q)) != TGPU_OK) return st;
+            if ((st = finish(q)) != TGPU_OK) return st;
+            b->stats.rerun_queries++;
+            b->descriptors_dirty = true;
+            if (b->exec) {
+                cudaGraphExecDestroy(b->exec);
+                cudaGraphDestroy(b->graph);
+                b->exec = nullptr;
+                b->graph = nullptr;
+            }
+            continue;
+        }
+        const unsigned long long *c = b->h_counts + 8 * i;
+        q->executed = true;
+        q->synced = true;
+        q->returned = 0;
+        q->result_rows = c[2];
+        q->stats.rows_scanned = q->rows_scanned;
+        q->stats.rows_selected = c[4];
+        q->stats.groups = c[0];
+        q->stats.result_rows = c[2];
+        q->stats.table_capacity = q->dq.cap;
+        q->stats.route = (uint32_t)q->route;
+    }
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_batch_output_schema(const tgpu_query_batch *b, uint32_t i, tgpu_output_column *cols, uint32_t cap,
+                                     uint32_t *n) {
+    if (!b || i >= b->qs.size()) return fail(TGPU_ERR_INVALID_ARGUMENT, "query index");
+    return tgpu_query_output_schema(b->qs[i], cols, cap, n);
+}
+
+tgpu_status tgpu_batch_next(tgpu_query_batch *b, uint32_t i, tgpu_batch *out, int32_t *done) {
+    if (!b || i >= b->qs.size()) return fail(TGPU_ERR_INVALID_ARGUMENT, "query index");
+    tgpu_status st = tgpu_batch_synchronize(b);
+    if (st != TGPU_OK) return st;
+    if (!b->qs[i]->executed) return fail(TGPU_ERR_INVALID_ARGUMENT, "batch not executed");
+    return tgpu_query_next(b->qs[i], out, done);
+}
+
+tgpu_status tgpu_batch_cancel(tgpu_query_batch *b) {
+    if (!b) return fail(TGPU_ERR_INVALID_ARGUMENT, "null batch");
+    __atomic_store_n(b->h_cancel, 1, __ATOMIC_SEQ_CST);
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_batch_get_stats(const tgpu_query_batch *b, tgpu_batch_stats *out) {
+    if (!b || !out) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
+    *out = b->stats;
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_batch_destroy(tgpu_query_batch *b) {
+    if (!b) return fail(TGPU_ERR_INVALID_ARGUMENT, "null batch");
+    delete b;
     return TGPU_OK;
 }
 

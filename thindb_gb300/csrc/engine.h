@@ -18,11 +18,11 @@ constexpr int MAX_QCOLS = 24;       // distinct columns one query reads
 constexpr int MAX_ORDER = 6;
 constexpr int MAX_SORT_WORDS = 2 * MAX_ORDER + 2;
 
-// Scan geometry: persistent CTAs claim tiles of TILE_ROWS rows; each of the
-// CTA's warps owns TILE_ROWS / WARPS consecutive rows of the tile.
+// Scan geometry: persistent CTAs of SCAN_WARPS warps; each warp folds a
+// static, strided set of chunks of chunk_rows rows.
 constexpr int SCAN_THREADS = 512;
 constexpr int SCAN_WARPS = SCAN_THREADS / 32;
-constexpr int TILE_ROWS = 8192;                    // default rows per scan tile
+constexpr int CHUNK_ALIGN = 256;
 
 // Status bits the kernels OR into the query's device status word.
 constexpr unsigned ST_TABLE_FULL = 1u;      // a probe ran past MAX_PROBE: regrow and rerun
@@ -75,6 +75,8 @@ struct DevAgg {
     int32_t vword;          // valid-count word, -1 = none
     int32_t dset;           // distinct set index (AK_DISTINCT)
     int32_t is_float_in;    // input column is FLOAT/DOUBLE
+    int32_t owner;          // folds its state words (0 when an earlier aggregate shares them)
+    int32_t needs_value;    // the fold reads the input value (not only its validity)
 };
 
 // Everything a scan launch needs, passed by value (kernel parameter).
@@ -84,10 +86,10 @@ struct DevQuery {
     const uint32_t *rg_list;  // surviving row groups, nullptr = every row group
     uint32_t n_rg;            // row groups iterated (list length or total)
     uint32_t rg_rows;
-    uint32_t tiles_per_rg;
-    uint32_t n_tiles;
-    uint32_t tile_rows;       // rows per scan tile (multiple of SCAN_THREADS)
-    uint32_t warp_rows;       // tile_rows / SCAN_WARPS
+    uint32_t chunks_per_rg;
+    uint32_t n_chunks;        // warp-sized units of work
+    uint32_t chunk_rows;      // rows per chunk (multiple of 256)
+    uint32_t pad0;
     // columns / predicates / key / aggregates
     DevCol cols[MAX_QCOLS];
     int32_t n_cols;
@@ -112,7 +114,7 @@ struct DevQuery {
     int32_t n_dsets;
     // shared-memory pre-aggregation (0 slots = off)
     int32_t cache_slots;      // power of two
-    int32_t cache_flush_at;   // flush + clear once this many entries are live
+    int32_t cache_probe;      // probe limit (cache_slots when the table holds every group)
     int32_t warp_combine;     // __match_any_sync pre-combine on/off
     int32_t gather;           // 1 = compact survivors, then gather; 0 = process rows in place
     // control

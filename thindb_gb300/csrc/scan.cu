@@ -5,20 +5,25 @@
 // -> stageBucketIds :9228 / scatterStageLane :9348 -> groupChunkRowsDirectKeys
 // :7456 -> foldKernel* :7832-8001 -> foldGroupDistinct :8003-8176):
 //
-//   1. CTAs claim tiles of q.tile_rows rows (inside the row groups that
-//      survived the zone maps); each warp owns q.warp_rows consecutive rows.
-//   2. The fused WHERE is evaluated 32 rows per warp step with coalesced loads;
-//      a warp ballot gives the survivors, which are compacted into a per-warp
-//      shared-memory ring (prefix = popc of the ballot below the lane).
-//   3. Full batches of 32 survivors gather their key parts and aggregate
-//      inputs (only survivor rows are read: late materialisation), pack the
-//      key LSB-first exactly as thinDB (v2_shape_group_topn.zig:2076-2092).
+//   1. Every warp owns a static, strided set of chunks of q.chunk_rows rows
+//      (inside the row groups that survived the zone maps): no tile claims and
+//      no block barriers in the main loop.
+//   2. The fused WHERE is evaluated 32 rows per step with coalesced streaming
+//      loads, eight steps in flight; a warp ballot gives the survivors, whose
+//      chunk offsets are compacted into the warp's shared-memory list
+//      (position = popc of the ballot below the lane).
+//   3. Survivors are folded 32 at a time: their key parts and aggregate inputs
+//      are gathered (only surviving rows are read: late materialisation; the
+//      next batch's gathers are issued before the current batch folds), and the
+//      key is packed LSB-first exactly as thinDB (v2_shape_group_topn.zig:2076-2092).
 //   4. __match_any_sync finds equal keys in the warp; their inputs are
 //      pre-combined into the lowest lane with shuffles (i128 sums exact).
-//   5. Leaders fold into a shared-memory table (key -> global slot + states,
-//      shared atomics).  Misses (table full) and every flush go to the global
+//   5. Leaders fold into the CTA's shared-memory table (key -> global slot +
+//      states, shared atomics; insert-if-free, so the hottest keys, which
+//      arrive first, stay resident).  Misses fold into the global
 //      open-addressing table (atomicCAS claim, linear probing), whose slot
-//      index is the group id used by COUNT(DISTINCT)'s (gid, value) set.
+//      index is the group id COUNT(DISTINCT)'s (gid, value) set keys on.  The
+//      shared table is flushed into the global one once, when the CTA ends.
 //
 // No spin-waits: every probe loop is bounded by MAX_PROBE and reports
 // ST_TABLE_FULL / ST_DISTINCT_FULL through the status word instead.
@@ -30,7 +35,7 @@ namespace {
 
 constexpr unsigned FULL = 0xFFFFFFFFu;
 constexpr uint32_t NO_GID = 0xFFFFFFFFu;
-constexpr int WBUF = 64;  // per-warp survivor ring
+constexpr int FILTER_UNROLL = 8;  // 32-row filter steps in flight per warp
 
 __device__ __forceinline__ bool col_valid(const DevCol &c, uint64_t r) {
     return c.valid == nullptr || ((__ldg(c.valid + (r >> 5)) >> (r & 31)) & 1u);
@@ -90,25 +95,13 @@ __device__ __forceinline__ bool cmp_f(int op, double x, double lo, double hi) {
     }
 }
 
-__device__ __forceinline__ bool row_passes(const DevQuery &q, uint64_t r) {
-    for (int i = 0; i < q.n_preds; ++i) {
-        const DevPred &p = q.preds[i];
-        const DevCol &c = q.cols[p.col];
-        bool v = col_valid(c, r);
-        if (p.op == TGPU_PRED_IS_NULL) {
-            if (v) return false;
-            continue;
-        }
-        if (p.op == TGPU_PRED_IS_NOT_NULL) {
-            if (!v) return false;
-            continue;
-        }
-        if (!v) return false;
-        bool ok = p.is_float ? cmp_f(p.op, col_f64(c, r), p.flo, p.fhi)
-                             : cmp_int(p.op, col_int_stream(c, r), p.lo, p.hi);
-        if (!ok) return false;
-    }
-    return true;
+__device__ __forceinline__ bool pred_holds(const DevQuery &q, const DevPred &p, uint64_t r) {
+    const DevCol &c = q.cols[p.col];
+    bool v = col_valid(c, r);
+    if (p.op == TGPU_PRED_IS_NULL) return !v;
+    if (p.op == TGPU_PRED_IS_NOT_NULL) return v;
+    if (!v) return false;
+    return p.is_float ? cmp_f(p.op, col_f64(c, r), p.flo, p.fhi) : cmp_int(p.op, col_int_stream(c, r), p.lo, p.hi);
 }
 
 // Packed key: parts LSB-first, a nullable part's slice is payload | valid-bit
@@ -238,7 +231,8 @@ struct Acc {
 };
 
 // Apply a combined contribution to a slot's state words (shared or global:
-// the atomics resolve to the address space of `st`).
+// the atomics resolve to the address space of `st`).  Aggregates that share a
+// state word (SUM and AVG of one column) fold it once (g.owner).
 template <int NA>
 __device__ __forceinline__ void apply_states(const DevQuery &q, unsigned long long *st, const Acc<NA> &acc) {
     atomicAdd(st, (unsigned long long)acc.rows);
@@ -247,7 +241,7 @@ __device__ __forceinline__ void apply_states(const DevQuery &q, unsigned long lo
         if (a >= q.n_aggs) break;
         const DevAgg &g = q.aggs[a];
         const uint32_t vc = acc.vc[a];
-        if (vc == 0) continue;
+        if (vc == 0 || !g.owner) continue;
         unsigned long long *w = st + g.word;
         switch (g.kind) {
             case AK_COUNT_VALID: atomicAdd(w, (unsigned long long)vc); break;
@@ -334,10 +328,7 @@ struct ScanSmem {
     unsigned long long *ckeys;   // cache_slots
     unsigned long long *cstate;  // cache_slots * state_words
     uint32_t *cgid;              // cache_slots
-    uint32_t *wbuf;              // SCAN_WARPS * WBUF row offsets
-    uint32_t *live;              // live cache entries
-    uint32_t *tile;              // claimed tile
-    uint32_t *flags;             // [0] flush now, [1] stop
+    uint16_t *wlist;             // SCAN_WARPS * chunk_rows survivor offsets (gather mode)
 };
 
 __device__ __forceinline__ ScanSmem carve(const DevQuery &q, unsigned char *base) {
@@ -346,18 +337,23 @@ __device__ __forceinline__ ScanSmem carve(const DevQuery &q, unsigned char *base
     s.ckeys = (unsigned long long *)base;
     s.cstate = s.ckeys + C;
     s.cgid = (uint32_t *)(s.cstate + (size_t)C * q.state_words);
-    s.wbuf = s.cgid + C;
-    s.live = s.wbuf + SCAN_WARPS * WBUF;
-    s.tile = s.live + 1;
-    s.flags = s.tile + 1;
+    s.wlist = (uint16_t *)(s.cgid + C);
     return s;
+}
+
+__device__ __forceinline__ void cache_init(const DevQuery &q, const ScanSmem &sm) {
+    for (int e = threadIdx.x; e < q.cache_slots; e += blockDim.x) {
+        sm.ckeys[e] = 0;
+        sm.cgid[e] = NO_GID;
+    }
+    for (int e = threadIdx.x; e < q.cache_slots * q.state_words; e += blockDim.x) sm.cstate[e] = 0;
 }
 
 // Find or claim the cache entry of a non-zero one-word key; -1 when the
 // bounded probe finds neither (the caller folds into the global table).
-__device__ __forceinline__ int cache_find(const DevQuery &q, ScanSmem &sm, uint64_t k, bool &claimed) {
+__device__ __forceinline__ int cache_find(const DevQuery &q, const ScanSmem &sm, uint64_t k, bool &claimed) {
     const int C = q.cache_slots;
-    const int limit = q.cache_flush_at >= C ? C : 16;  // a resident (lowcard) cache probes all
+    const int limit = q.cache_probe;
     uint32_t h = (uint32_t)hash_key(k, 0) & (C - 1);
     claimed = false;
     for (int p = 0; p < limit; ++p) {
@@ -367,7 +363,6 @@ __device__ __forceinline__ int cache_find(const DevQuery &q, ScanSmem &sm, uint6
             cur = atomicCAS(&sm.ckeys[h], 0ULL, (unsigned long long)k);
             if (cur == 0) {
                 claimed = true;
-                atomicAdd(sm.live, 1u);
                 return (int)h;
             }
             if (cur == k) return (int)h;
@@ -377,83 +372,96 @@ __device__ __forceinline__ int cache_find(const DevQuery &q, ScanSmem &sm, uint6
     return -1;
 }
 
-// Fold every live cache entry into its global slot and clear the cache.
-__device__ void cache_flush(const DevQuery &q, ScanSmem &sm) {
+// Fold every live cache entry into its global slot.
+__device__ void cache_flush(const DevQuery &q, const ScanSmem &sm) {
     const int C = q.cache_slots, S = q.state_words;
     for (int e = threadIdx.x; e < C; e += blockDim.x) {
         unsigned long long k = sm.ckeys[e];
         if (k == 0) continue;
         uint32_t gid = sm.cgid[e];
-        unsigned long long *st = sm.cstate + (size_t)e * S;
-        if (gid != NO_GID) {
-            unsigned long long *gst = q.table + (uint64_t)gid * q.slot_words + q.key_words;
-            atomicAdd(gst, st[0]);
-            for (int a = 0; a < q.n_aggs; ++a) {
-                const DevAgg &g = q.aggs[a];
-                unsigned long long *w = gst + g.word;
-                switch (g.kind) {
-                    case AK_COUNT_VALID: case AK_SUM_I64:
-                        if (st[g.word]) atomicAdd(w, st[g.word]);
-                        break;
-                    case AK_SUM_I128: {
-                        unsigned long long lo = st[g.word], hi = st[g.word + 1];
-                        if (lo) {
-                            unsigned long long old = atomicAdd(w, lo);
-                            hi += (old + lo < old) ? 1ULL : 0ULL;
-                        }
-                        if (hi) atomicAdd(w + 1, hi);
-                        break;
+        const unsigned long long *st = sm.cstate + (size_t)e * S;
+        if (gid == NO_GID) continue;  // only when the global table overflowed (rerun follows)
+        unsigned long long *gst = q.table + (uint64_t)gid * q.slot_words + q.key_words;
+        atomicAdd(gst, st[0]);
+        for (int a = 0; a < q.n_aggs; ++a) {
+            const DevAgg &g = q.aggs[a];
+            if (!g.owner) continue;
+            unsigned long long *w = gst + g.word;
+            switch (g.kind) {
+                case AK_COUNT_VALID: case AK_SUM_I64:
+                    if (st[g.word]) atomicAdd(w, st[g.word]);
+                    break;
+                case AK_SUM_I128: {
+                    unsigned long long lo = st[g.word], hi = st[g.word + 1];
+                    if (lo) {
+                        unsigned long long old = atomicAdd(w, lo);
+                        hi += (old + lo < old) ? 1ULL : 0ULL;
                     }
-                    case AK_SUM_F64: {
-                        double v = __longlong_as_double((long long)st[g.word]);
-                        if (v != 0.0 || (st[g.word] >> 63)) atomicAdd((double *)w, v);
-                        break;
-                    }
-                    case AK_MIN_I: case AK_MAX_I: case AK_MIN_F: case AK_MAX_F:
-                        if (st[g.word]) atomicMax(w, st[g.word]);
-                        break;
-                    default: break;  // distinct counts live only in the global slot
+                    if (hi) atomicAdd(w + 1, hi);
+                    break;
                 }
-                if (g.vword >= 0 && st[g.vword]) atomicAdd(gst + g.vword, st[g.vword]);
+                case AK_SUM_F64:
+                    if (st[g.word]) atomicAdd((double *)w, __longlong_as_double((long long)st[g.word]));
+                    break;
+                case AK_MIN_I: case AK_MAX_I: case AK_MIN_F: case AK_MAX_F:
+                    if (st[g.word]) atomicMax(w, st[g.word]);
+                    break;
+                default: break;  // distinct counts live only in the global slot
             }
+            if (g.vword >= 0 && st[g.vword]) atomicAdd(gst + g.vword, st[g.vword]);
         }
-        sm.ckeys[e] = 0;
-        sm.cgid[e] = NO_GID;
-        for (int w = 0; w < S; ++w) st[w] = 0;
     }
 }
 
-// ------------------------------------------------------------- a batch --
+// ------------------------------------------------------------ a batch --
 
-// Fold up to 32 rows (lane i holds `row` when bit i of `active` is set).
+// The gathered inputs of one row (one lane).
 template <int NA>
-__device__ __forceinline__ void process_batch(const DevQuery &q, ScanSmem &sm, uint64_t row, unsigned active,
-                                              int lane) {
-    const bool me = (active >> lane) & 1u;
-    uint64_t k0 = 0, k1 = 0;
+struct RowVals {
+    uint64_t k0, k1;
     uint64_t val[NA];
-    unsigned ok = 0;
+    unsigned ok;   // bit a: aggregate a's input is non-NULL
+};
+
+template <int NA>
+__device__ __forceinline__ void load_row(const DevQuery &q, uint64_t row, bool me, RowVals<NA> &rv) {
+    rv.k0 = 0;
+    rv.k1 = 0;
+    rv.ok = 0;
 #pragma unroll
-    for (int a = 0; a < NA; ++a) val[a] = 0;
-    if (me) {
-        pack_key(q, row, k0, k1);
+    for (int a = 0; a < NA; ++a) rv.val[a] = 0;
+    if (!me) return;
+    pack_key(q, row, rv.k0, rv.k1);
 #pragma unroll
-        for (int a = 0; a < NA; ++a) {
-            if (a >= q.n_aggs) break;
-            const DevAgg &g = q.aggs[a];
-            if (g.col < 0) continue;
-            const DevCol &c = q.cols[g.col];
-            if (!col_valid(c, row)) continue;
-            ok |= 1u << a;
-            if (g.kind == AK_COUNT_VALID) continue;
-            if (g.is_float_in) val[a] = f64_bits(col_f64(c, row));
-            else val[a] = (uint64_t)col_int(c, row);
-            if (g.kind == AK_MIN_F || g.kind == AK_MAX_F) {
-                double d = bits_f64(val[a]);
-                if (d != d) val[a] = 0x7FF8000000000000ULL;  // one NaN, ordered largest
-            }
+    for (int a = 0; a < NA; ++a) {
+        if (a >= q.n_aggs) break;
+        const DevAgg &g = q.aggs[a];
+        if (g.col < 0) continue;
+        const DevCol &c = q.cols[g.col];
+        if (!col_valid(c, row)) continue;
+        rv.ok |= 1u << a;
+        if (g.kind == AK_COUNT_VALID || g.kind == AK_COUNT_ROWS || !g.needs_value) continue;
+        rv.val[a] = g.is_float_in ? f64_bits(col_f64(c, row)) : (uint64_t)col_int(c, row);
+    }
+}
+
+// Fold up to 32 gathered rows (bit i of `active` = lane i holds one).  One
+// out-of-line copy keeps the instruction footprint small.
+template <int NA>
+__device__ __noinline__ void fold_batch(const DevQuery &q, const ScanSmem &sm, const RowVals<NA> &in, unsigned active) {
+    const int lane = threadIdx.x & 31;
+    const bool me = (active >> lane) & 1u;
+    uint64_t val[NA];
+    const unsigned ok = in.ok;
+#pragma unroll
+    for (int a = 0; a < NA; ++a) {
+        val[a] = in.val[a];
+        if (a < q.n_aggs && (q.aggs[a].kind == AK_MIN_F || q.aggs[a].kind == AK_MAX_F)) {
+            double d = bits_f64(val[a]);
+            if (d != d) val[a] = 0x7FF8000000000000ULL;  // one NaN, ordered largest
         }
     }
+    const uint64_t k0 = in.k0, k1 = in.k1;
 
     // Equal keys in the warp: the lowest lane of each group folds for all.
     unsigned grp;
@@ -524,123 +532,116 @@ __device__ __forceinline__ void process_batch(const DevQuery &q, ScanSmem &sm, u
     }
 }
 
-// ---------------------------------------------------------------- kernel --
-
-__device__ __forceinline__ void cache_init(const DevQuery &q, ScanSmem &sm) {
-    for (int e = threadIdx.x; e < q.cache_slots; e += blockDim.x) {
-        sm.ckeys[e] = 0;
-        sm.cgid[e] = NO_GID;
-    }
-    for (int e = threadIdx.x; e < q.cache_slots * q.state_words; e += blockDim.x) sm.cstate[e] = 0;
-}
-
-// Rows [row0, row_end) of scan tile t.
-__device__ __forceinline__ void tile_rows(const DevQuery &q, uint32_t t, uint64_t &row0, uint64_t &row_end) {
+// Rows [row0, row_end) of chunk c.
+__device__ __forceinline__ void chunk_rows(const DevQuery &q, uint32_t c, uint64_t &row0, uint64_t &row_end) {
     if (q.rg_list) {
-        uint32_t rgi = t / q.tiles_per_rg, sub = t % q.tiles_per_rg;
+        uint32_t rgi = c / q.chunks_per_rg, sub = c % q.chunks_per_rg;
         uint64_t rg = q.rg_list[rgi];
-        row0 = rg * q.rg_rows + (uint64_t)sub * q.tile_rows;
-        row_end = min(min(row0 + q.tile_rows, (rg + 1) * (uint64_t)q.rg_rows), q.n_rows);
+        row0 = rg * q.rg_rows + (uint64_t)sub * q.chunk_rows;
+        row_end = min(min(row0 + q.chunk_rows, (rg + 1) * (uint64_t)q.rg_rows), q.n_rows);
     } else {
-        row0 = (uint64_t)t * q.tile_rows;
-        row_end = min(row0 + q.tile_rows, q.n_rows);
+        row0 = (uint64_t)c * q.chunk_rows;
+        row_end = min(row0 + q.chunk_rows, q.n_rows);
     }
 }
 
-// One warp's share of scan tile t: filter, compact, fold.
+// One warp folds chunk c: filter + compaction, then batches of 32 survivors
+// (each batch's gathers issued before the previous batch folds).
 template <int NA>
-__device__ __forceinline__ void scan_tile(const DevQuery &q, ScanSmem &sm, uint32_t t, unsigned long long &selected) {
+__device__ __forceinline__ void scan_chunk(const DevQuery &q, const ScanSmem &sm, uint32_t c,
+                                           unsigned long long &selected) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t *wb = sm.wbuf + warp * WBUF;
     uint64_t row0, row_end;
-    tile_rows(q, t, row0, row_end);
-    const uint64_t wbase = row0 + (uint64_t)warp * q.warp_rows;
-    const uint64_t wend = min(wbase + q.warp_rows, row_end);
-    if (wbase >= wend) return;
-    if (q.n_preds == 0) {
-        for (uint64_t b = wbase; b < wend; b += 32) {
-            uint64_t r = b + lane;
-            unsigned act = __ballot_sync(FULL, r < wend);
+    chunk_rows(q, c, row0, row_end);
+    if (row0 >= row_end) return;
+    if (q.n_preds == 0 || !q.gather) {
+        // every row (or every filtered row in place): 32 consecutive rows per batch
+        RowVals<NA> cur, nxt;
+        uint64_t r = row0 + lane;
+        bool pass = r < row_end && (q.n_preds == 0 || [&] {
+                        for (int i = 0; i < q.n_preds; ++i)
+                            if (!pred_holds(q, q.preds[i], r)) return false;
+                        return true;
+                    }());
+        load_row<NA>(q, r, pass, cur);
+        unsigned act = __ballot_sync(FULL, pass);
+        for (uint64_t b = row0; b < row_end; b += 32) {
+            const uint64_t rn = b + 32 + lane;
+            const bool pn = rn < row_end && (q.n_preds == 0 || [&] {
+                                for (int i = 0; i < q.n_preds; ++i)
+                                    if (!pred_holds(q, q.preds[i], rn)) return false;
+                                return true;
+                            }());
+            load_row<NA>(q, rn, pn, nxt);
+            const unsigned actn = __ballot_sync(FULL, pn);
             selected += (lane == 0) ? __popc(act) : 0;
-            process_batch<NA>(q, sm, r, act, lane);
+            if (act) fold_batch<NA>(q, sm, cur, act);
+            cur = nxt;
+            act = actn;
         }
-    } else if (!q.gather) {
-        for (uint64_t b = wbase; b < wend; b += 32) {
-            uint64_t r = b + lane;
-            bool pass = r < wend && row_passes(q, r);
-            unsigned act = __ballot_sync(FULL, pass);
-            selected += (lane == 0) ? __popc(act) : 0;
-            if (act) process_batch<NA>(q, sm, r, act, lane);
+        return;
+    }
+    // gather mode: the chunk's survivors first, then folds
+    uint16_t *list = sm.wlist + (size_t)warp * q.chunk_rows;
+    uint32_t n = 0;
+    for (uint64_t b = row0; b < row_end; b += 32 * FILTER_UNROLL) {
+        bool pass[FILTER_UNROLL];
+        // first predicate for all steps (its loads are independent), then the rest
+#pragma unroll
+        for (int u = 0; u < FILTER_UNROLL; ++u) {
+            const uint64_t r = b + u * 32 + lane;
+            pass[u] = r < row_end && pred_holds(q, q.preds[0], r);
         }
-    } else {
-        int n = 0;  // survivors in this warp's ring
-        for (uint64_t b = wbase; b < wend; b += 128) {
-            bool pass[4];
+        for (int i = 1; i < q.n_preds; ++i) {
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                uint64_t r = b + u * 32 + lane;
-                pass[u] = r < wend && row_passes(q, r);
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                unsigned m = __ballot_sync(FULL, pass[u]);
-                if (pass[u]) wb[n + __popc(m & ((1u << lane) - 1))] = (uint32_t)(b + u * 32 + lane - row0);
-                n += __popc(m);
-                selected += (lane == 0) ? __popc(m) : 0;
-                __syncwarp();
-                if (n >= 32) {
-                    uint64_t r = row0 + wb[lane];
-                    __syncwarp();
-                    if (lane < n - 32) wb[lane] = wb[32 + lane];
-                    n -= 32;
-                    __syncwarp();
-                    process_batch<NA>(q, sm, r, FULL, lane);
-                }
+            for (int u = 0; u < FILTER_UNROLL; ++u) {
+                const uint64_t r = b + u * 32 + lane;
+                if (pass[u]) pass[u] = pred_holds(q, q.preds[i], r);
             }
         }
-        if (n > 0) {
-            uint64_t r = row0 + wb[lane < n ? lane : 0];
-            unsigned act = (n >= 32) ? FULL : ((1u << n) - 1);
-            __syncwarp();
-            process_batch<NA>(q, sm, r, act, lane);
+#pragma unroll
+        for (int u = 0; u < FILTER_UNROLL; ++u) {
+            const unsigned m = __ballot_sync(FULL, pass[u]);
+            if (pass[u]) list[n + __popc(m & ((1u << lane) - 1))] = (uint16_t)(b + u * 32 + lane - row0);
+            n += __popc(m);
         }
     }
+    __syncwarp();
+    selected += (lane == 0) ? n : 0;
+    if (n == 0) return;
+    RowVals<NA> cur, nxt;
+    load_row<NA>(q, row0 + list[lane < n ? lane : 0], lane < n, cur);
+    for (uint32_t i = 0; i < n; i += 32) {
+        const uint32_t j = i + 32 + lane;
+        load_row<NA>(q, row0 + list[j < n ? j : 0], j < n, nxt);
+        const uint32_t left = n - i;
+        fold_batch<NA>(q, sm, cur, left >= 32 ? FULL : ((1u << left) - 1));
+        cur = nxt;
+    }
 }
+
+// ---------------------------------------------------------------- kernel --
 
 template <int NA>
 __global__ void __launch_bounds__(SCAN_THREADS, NA <= 4 ? 2 : 1) scan_group_kernel(const __grid_constant__ DevQuery q) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    ScanSmem sm = carve(q, smem_raw);
-    const int lane = threadIdx.x & 31;
+    const ScanSmem sm = carve(q, smem_raw);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     cache_init(q, sm);
-    if (threadIdx.x == 0) {
-        *sm.live = 0;
-        sm.flags[0] = 0;
-        sm.flags[1] = 0;
-    }
-    unsigned long long selected = 0;
     __syncthreads();
-
-    for (;;) {
-        if (threadIdx.x == 0) {
-            uint32_t t = atomicAdd(q.tile_counter, 1u);
-            *sm.tile = t;
-            sm.flags[0] = (q.cache_slots && *sm.live >= (uint32_t)q.cache_flush_at) ? 1u : 0u;
-            if (q.cancel && *q.cancel) {
-                atomicOr(q.status, ST_CANCELLED);
-                *sm.tile = 0xFFFFFFFFu;
+    unsigned long long selected = 0;
+    const uint32_t nw = gridDim.x * SCAN_WARPS;
+    uint32_t k = 0;
+    for (uint32_t c = blockIdx.x * SCAN_WARPS + warp; c < q.n_chunks; c += nw, ++k) {
+        if ((k & 31) == 31 && q.cancel) {  // poll the host-mapped cancel flag now and then
+            int stop = 0;
+            if (lane == 0) stop = *q.cancel;
+            if (__shfl_sync(FULL, stop, 0)) {
+                if (lane == 0) atomicOr(q.status, ST_CANCELLED);
+                break;
             }
         }
-        __syncthreads();
-        const uint32_t t = *sm.tile;
-        if (sm.flags[0]) {
-            cache_flush(q, sm);
-            if (threadIdx.x == 0) *sm.live = 0;
-            __syncthreads();
-        }
-        if (t >= q.n_tiles) break;
-        scan_tile<NA>(q, sm, t, selected);
-        __syncthreads();
+        scan_chunk<NA>(q, sm, c, selected);
     }
     if (q.cache_slots) {
         __syncthreads();
@@ -649,74 +650,64 @@ __global__ void __launch_bounds__(SCAN_THREADS, NA <= 4 ? 2 : 1) scan_group_kern
     if (lane == 0 && selected) atomicAdd(q.selected_rows, selected);
 }
 
-// Many queries in one persistent kernel: work items are (query, tile) pairs,
-// query-major (item i belongs to the query whose [tile_start[q],
-// tile_start[q+1]) range holds it).  A CTA keeps one query's shared-memory
-// table at a time and flushes it when its next item belongs to another query.
+// Many queries in one persistent kernel: work items are (query, tile of
+// SCAN_WARPS chunks) pairs, query-major.  CTA b takes items b, b + grid, ...;
+// all warps of a CTA work on one query's tile at a time, so the CTA's
+// shared-memory table belongs to that query until its next item moves on,
+// when the table is flushed.
 template <int NA>
 __global__ void __launch_bounds__(SCAN_THREADS, NA <= 4 ? 2 : 1)
     batch_scan_kernel(const DevQuery *__restrict__ qs, const uint32_t *__restrict__ tile_start, uint32_t n_queries,
                       unsigned int *work_counter, const volatile int *cancel, unsigned int *batch_status) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ uint32_t s_item, s_query;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t total = tile_start[n_queries];
+    (void)work_counter;
     int cur = -1;
+    uint32_t qi = 0;
     ScanSmem sm{};
     unsigned long long selected = 0;
-    for (;;) {
-        if (threadIdx.x == 0) {
-            uint32_t item = atomicAdd(work_counter, 1u);
-            if (cancel && *cancel) {
-                atomicOr(batch_status, ST_CANCELLED);
-                item = 0xFFFFFFFFu;
-            }
-            uint32_t qi = 0;
-            if (item < total) {
-                uint32_t lo = 0, hi = n_queries;  // last q with tile_start[q] <= item
-                while (hi - lo > 1) {
-                    uint32_t mid = (lo + hi) >> 1;
-                    if (tile_start[mid] <= item) lo = mid;
-                    else hi = mid;
-                }
-                qi = lo;
-            }
-            s_item = item;
-            s_query = qi;
+    uint32_t k = 0;
+    for (uint32_t item = blockIdx.x;; item += gridDim.x, ++k) {
+        bool stop = item >= total;
+        if (!stop && (k & 15) == 15 && cancel) {
+            int c = 0;
+            if (threadIdx.x == 0) c = *cancel;
+            stop = __syncthreads_or(c) != 0;
+            if (stop && threadIdx.x == 0) atomicOr(batch_status, ST_CANCELLED);
         }
-        __syncthreads();
-        const uint32_t item = s_item;
-        const int qn = item < total ? (int)s_query : -1;
-        if (qn != cur && cur >= 0) {
-            const DevQuery &old = qs[cur];
-            if (old.cache_slots) cache_flush(old, sm);
-            if (lane == 0 && selected) atomicAdd(old.selected_rows, selected);
-            selected = 0;
+        int qn = -1;
+        if (!stop) {
+            while (qi + 1 < n_queries && tile_start[qi + 1] <= item) ++qi;  // items only grow
+            qn = (int)qi;
+        }
+        if (qn != cur) {
+            if (cur >= 0) {
+                const DevQuery &old = qs[cur];
+                __syncthreads();
+                if (old.cache_slots) cache_flush(old, sm);
+                if (lane == 0 && selected) atomicAdd(old.selected_rows, selected);
+                selected = 0;
+            }
+            if (qn < 0) break;
+            __syncthreads();
+            sm = carve(qs[qn], smem_raw);
+            cache_init(qs[qn], sm);
+            cur = qn;
             __syncthreads();
         }
         if (qn < 0) break;
         const DevQuery &q = qs[qn];
-        if (qn != cur) {
-            sm = carve(q, smem_raw);
-            cache_init(q, sm);
-            if (threadIdx.x == 0) *sm.live = 0;
-            cur = qn;
-            __syncthreads();
-        } else if (q.cache_slots && *sm.live >= (uint32_t)q.cache_flush_at) {
-            __syncthreads();
-            cache_flush(q, sm);
-            if (threadIdx.x == 0) *sm.live = 0;
-            __syncthreads();
-        }
-        scan_tile<NA>(q, sm, item - tile_start[qn], selected);
-        __syncthreads();
+        const uint32_t c = (item - tile_start[qn]) * SCAN_WARPS + warp;
+        if (c < q.n_chunks) scan_chunk<NA>(q, sm, c, selected);
     }
 }
 
 }  // namespace
 
 size_t scan_smem_bytes(const DevQuery &q) {
-    return (size_t)q.cache_slots * (8 + 8 * (size_t)q.state_words + 4) + SCAN_WARPS * WBUF * 4 + 16;
+    size_t list = q.gather ? (size_t)SCAN_WARPS * q.chunk_rows * 2 : 0;
+    return (size_t)q.cache_slots * (8 + 8 * (size_t)q.state_words + 4) + list + 16;
 }
 
 template <typename K>

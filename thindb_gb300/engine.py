@@ -230,7 +230,7 @@ class Request:
     memory_budget: int = 0
     flags: int = 0
     stream: int = 0
-    tile_rows: int = 0
+    chunk_rows: int = 0
     cache_slots: int = 0
     table_load_pct: int = 0
 
@@ -285,7 +285,7 @@ def build_request(table: Table, req: Request) -> tuple[abi.Request, list]:
     r.memory_budget_bytes = int(req.memory_budget)
     r.stream = req.stream or None
     r.flags = int(req.flags)
-    r.tile_rows = int(req.tile_rows)
+    r.chunk_rows = int(req.chunk_rows)
     r.cache_slots = int(req.cache_slots)
     r.table_load_pct = int(req.table_load_pct)
     keep += [g, aggs, where, having, order]
@@ -321,8 +321,10 @@ class Query:
         _check(lib().tgpu_query_output_schema(handle, None, 0, C.byref(n)))
         cols = (abi.OutputColumn * n.value)()
         _check(lib().tgpu_query_output_schema(handle, cols, n.value, C.byref(n)))
-        self.schema = [OutCol(c.name.decode(), c.type, bool(c.nullable), c.elem_bytes, c.decimal_precision,
-                              c.decimal_scale) for c in cols]
+        self.schema = _schema(cols)
+
+    def _next_c(self, b, done) -> None:
+        _check(lib().tgpu_query_next(self.handle, C.byref(b), C.byref(done)))
 
     def output_schema(self) -> list:
         return self.schema
@@ -350,7 +352,7 @@ class Query:
         b.validity = bp
         b.capacity_rows = capacity
         done = C.c_int32()
-        _check(lib().tgpu_query_next(self.handle, C.byref(b), C.byref(done)))
+        self._next_c(b, done)
         n = b.row_count
         if n == 0 and done.value:
             return None
@@ -402,6 +404,11 @@ class Query:
             pass
 
 
+def _schema(cols) -> list:
+    return [OutCol(c.name.decode(), c.type, bool(c.nullable), c.elem_bytes, c.decimal_precision, c.decimal_scale)
+            for c in cols]
+
+
 def try_build_group_topn(table: Table, req: Request) -> Optional[Query]:
     """v2_pipeline.tryBuildGroupTopN: a Query, or None when the shape declines."""
     r, keep = build_request(table, req)
@@ -412,3 +419,75 @@ def try_build_group_topn(table: Table, req: Request) -> Optional[Query]:
         return None
     _check(st)
     return Query(h, table)
+
+
+class _BatchMember(Query):
+    """Result view of one query of a QueryBatch (same next/collect as Query)."""
+
+    def __init__(self, batch: "QueryBatch", index: int):
+        self.batch = batch
+        self.index = index
+        self.handle = None
+        self.table = batch.table
+        n = C.c_uint32()
+        _check(lib().tgpu_batch_output_schema(batch.handle, index, None, 0, C.byref(n)))
+        cols = (abi.OutputColumn * n.value)()
+        _check(lib().tgpu_batch_output_schema(batch.handle, index, cols, n.value, C.byref(n)))
+        self.schema = _schema(cols)
+
+    def _next_c(self, b, done) -> None:
+        _check(lib().tgpu_batch_next(self.batch.handle, self.index, C.byref(b), C.byref(done)))
+
+    def close(self) -> None:
+        pass
+
+
+class QueryBatch:
+    """Many GROUP BY queries over one table in one persistent kernel
+    (optionally replayed from a captured CUDA graph)."""
+
+    def __init__(self, table: Table, requests: Sequence[Request], graph: bool = True, stream: int = 0):
+        self.table = table
+        reqs = (abi.Request * len(requests))()
+        keep = []
+        for i, rq in enumerate(requests):
+            r, k = build_request(table, rq)
+            reqs[i] = r
+            keep.append(k)
+        h = C.c_void_p()
+        st = lib().tgpu_batch_create(table.handle, reqs, len(requests), abi.BATCH_GRAPH if graph else 0,
+                                     stream or None, C.byref(h))
+        del keep
+        if st == abi.DECLINE:
+            raise EngineError(st, (lib().tgpu_last_error_message() or b"").decode())
+        _check(st)
+        self.handle = h
+        self.members = [_BatchMember(self, i) for i in range(len(requests))]
+
+    def execute(self) -> None:
+        _check(lib().tgpu_batch_execute(self.handle))
+
+    def synchronize(self) -> None:
+        _check(lib().tgpu_batch_synchronize(self.handle))
+
+    def collect(self, i: int, capacity: int = 1 << 20) -> dict:
+        return self.members[i].collect(capacity)
+
+    def cancel(self) -> None:
+        _check(lib().tgpu_batch_cancel(self.handle))
+
+    def stats(self) -> abi.BatchStats:
+        s = abi.BatchStats()
+        _check(lib().tgpu_batch_get_stats(self.handle, C.addressof(s)))
+        return s
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().tgpu_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
