@@ -358,6 +358,74 @@ tgpu_status tgpu_batch_cancel(tgpu_query_batch *b);
 tgpu_status tgpu_batch_get_stats(const tgpu_query_batch *b, tgpu_batch_stats *out);
 tgpu_status tgpu_batch_destroy(tgpu_query_batch *b);
 
+/* --------------------------------------------------------------- serving -- */
+
+/* A request loop over resident tables (the serving side thinDB's
+ * thindb-server runs per connection, src/cmd/server.zig; here one native
+ * dispatcher thread).  Submitted requests are admitted while the sum of their
+ * estimated group-table + distinct-set + buffer bytes stays under
+ * `memory_budget_bytes` (thinDB's MemoryAccountant, src/memory.zig:626);
+ * admitted requests of one table are launched together as a wave (the
+ * batched persistent kernel) on one of several streams, so waves overlap on
+ * the device and requests that arrive while others run join the next wave.
+ * TGPU_SERVE_PLAIN instead runs one plain operator at a time, in arrival
+ * order (the baseline the continuous mode is compared with). */
+typedef struct tgpu_server tgpu_server;
+
+#define TGPU_SERVE_CONTINUOUS 0
+#define TGPU_SERVE_PLAIN 1
+
+typedef struct tgpu_server_options {
+    uint64_t memory_budget_bytes;  /* 0 = 120 GB */
+    uint32_t max_batch;            /* requests per wave, 0 = 256 */
+    uint32_t max_inflight;         /* waves on the device at once, 0 = 4 */
+    int32_t mode;                  /* TGPU_SERVE_* */
+    int32_t reserved;
+} tgpu_server_options;
+
+typedef struct tgpu_server_stats {
+    uint64_t submitted, completed, failed;
+    uint64_t waves;                /* launches (waves or plain queries) */
+    uint64_t peak_admitted_bytes;
+    uint64_t peak_queued;          /* most requests waiting for admission at once */
+} tgpu_server_stats;
+
+tgpu_status tgpu_server_create(tgpu_table *const *tables, uint32_t n_tables, const tgpu_server_options *opts,
+                               tgpu_server **out);
+/* Thread-safe; copies the request.  *ticket identifies the result. */
+tgpu_status tgpu_server_submit(tgpu_server *s, uint32_t table, const tgpu_request *req, uint64_t *ticket);
+/* Wait up to timeout_ms (-1 = no limit) for a ticket; *done = 1 when its result is ready. */
+tgpu_status tgpu_server_wait(tgpu_server *s, uint64_t ticket, int32_t timeout_ms, int32_t *done);
+tgpu_status tgpu_server_output_schema(tgpu_server *s, uint64_t ticket, tgpu_output_column *cols, uint32_t cap,
+                                      uint32_t *n_columns);
+/* Rows of a finished ticket (status of the request if it failed). */
+tgpu_status tgpu_server_next(tgpu_server *s, uint64_t ticket, tgpu_batch *batch, int32_t *done);
+tgpu_status tgpu_server_release(tgpu_server *s, uint64_t ticket);
+tgpu_status tgpu_server_get_stats(tgpu_server *s, tgpu_server_stats *out);
+tgpu_status tgpu_server_destroy(tgpu_server *s);
+
+/* Open-loop load: Poisson arrivals at `rate_qps` for `duration_s`, request i
+ * drawn as requests[j], j uniform (seeded), against table tables_of[j];
+ * latency = submit to result ready.  Waits for every submitted request. */
+typedef struct tgpu_load_spec {
+    const uint32_t *table_of;
+    const tgpu_request *requests;
+    uint32_t n_requests;
+    uint32_t reserved;
+    double rate_qps;
+    double duration_s;
+    uint64_t seed;
+} tgpu_load_spec;
+
+typedef struct tgpu_load_report {
+    uint64_t submitted, completed, failed;
+    double elapsed_s;              /* first submit to last completion */
+    double achieved_qps;           /* completed / elapsed_s */
+    double p50_ms, p99_ms, p999_ms, max_ms, mean_ms;
+} tgpu_load_report;
+
+tgpu_status tgpu_server_run_load(tgpu_server *s, const tgpu_load_spec *spec, tgpu_load_report *out);
+
 #ifdef __cplusplus
 }
 #endif

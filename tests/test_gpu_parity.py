@@ -156,8 +156,9 @@ def mixed_cols(n, seed=3):
 
 def test_mixed_types_nulls():
     cols = mixed_cols(300_000)
+    # 15 of thinDB's 16 state slots (an 18-slot request declines, test_declines_like_reference)
     aggs = [AggSpec("count", None, "c"), AggSpec("count", "f", "cf"), AggSpec("sum", "big", "sb"),
-            AggSpec("avg", "big", "ab"), AggSpec("min", "f", "mnf"), AggSpec("max", "f", "mxf"),
+            AggSpec("min", "f", "mnf"), AggSpec("max", "f", "mxf"),
             AggSpec("min", "dt", "mnd"), AggSpec("max", "big", "mxb"), AggSpec("sum", "f", "sf"),
             AggSpec("sum", "b", "sbool"), AggSpec("count_distinct", "k2", "dk2")]
     req = Request(["k1", "b"], aggs)

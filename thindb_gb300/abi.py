@@ -137,6 +137,44 @@ SIGNATURES = [
 ]
 
 BATCH_GRAPH = 0x1
+SERVE_CONTINUOUS, SERVE_PLAIN = 0, 1
+
+
+class ServerOptions(C.Structure):
+    _fields_ = [("memory_budget_bytes", C.c_uint64), ("max_batch", C.c_uint32), ("max_inflight", C.c_uint32),
+                ("mode", C.c_int32), ("reserved", C.c_int32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("waves", C.c_uint64), ("peak_admitted_bytes", C.c_uint64), ("peak_queued", C.c_uint64)]
+
+
+class LoadSpec(C.Structure):
+    _fields_ = [("table_of", C.POINTER(C.c_uint32)), ("requests", C.POINTER(Request)), ("n_requests", C.c_uint32),
+                ("reserved", C.c_uint32), ("rate_qps", C.c_double), ("duration_s", C.c_double),
+                ("seed", C.c_uint64)]
+
+
+class LoadReport(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("elapsed_s", C.c_double), ("achieved_qps", C.c_double), ("p50_ms", C.c_double),
+                ("p99_ms", C.c_double), ("p999_ms", C.c_double), ("max_ms", C.c_double), ("mean_ms", C.c_double)]
+
+
+SIGNATURES += [
+    ("tgpu_server_create", C.c_int, [C.POINTER(C.c_void_p), C.c_uint32, C.POINTER(ServerOptions),
+                                     C.POINTER(C.c_void_p)]),
+    ("tgpu_server_submit", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(Request), C.POINTER(C.c_uint64)]),
+    ("tgpu_server_wait", C.c_int, [C.c_void_p, C.c_uint64, C.c_int32, C.POINTER(C.c_int32)]),
+    ("tgpu_server_output_schema", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(OutputColumn), C.c_uint32,
+                                            C.POINTER(C.c_uint32)]),
+    ("tgpu_server_next", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Batch), C.POINTER(C.c_int32)]),
+    ("tgpu_server_release", C.c_int, [C.c_void_p, C.c_uint64]),
+    ("tgpu_server_get_stats", C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
+    ("tgpu_server_destroy", C.c_int, [C.c_void_p]),
+    ("tgpu_server_run_load", C.c_int, [C.c_void_p, C.POINTER(LoadSpec), C.POINTER(LoadReport)]),
+]
 
 
 class BatchStats(C.Structure):

@@ -8,12 +8,18 @@
 // (exec.zig:903-1218).
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <memory>
 #include <mutex>
+#include <random>
 #include <string>
+#include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "engine.h"
@@ -33,6 +39,7 @@ tgpu_status fail(tgpu_status s, const std::string &msg) {
     do {                                                                                         \
         cudaError_t e_ = (call);                                                                 \
         if (e_ != cudaSuccess) {                                                                 \
+            cudaGetLastError(); /* a non-sticky error must not resurface in a later launch */    \
             return fail(TGPU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));      \
         }                                                                                        \
     } while (0)
@@ -275,6 +282,9 @@ struct tgpu_query {
     int *h_cancel = nullptr;
     int *d_cancel = nullptr;
     unsigned long long *h_counts = nullptr;   // [0..4] counts + selected, [5] status
+    // results packed into host memory by a batch (nullptr: read the device outputs)
+    const uint8_t *h_packed = nullptr;
+    uint64_t pack_rows = 0;
     // state
     bool executed = false, synced = false;
     uint64_t returned = 0, result_rows = 0;
@@ -437,6 +447,33 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
         p.hi = w.hi;
         p.flo = w.flo;
         p.fhi = w.fhi;
+    }
+
+    // one NOT NULL integer range test: the scan's width-specialised fast filter
+    dq.fp_bytes = 0;
+    if (req->n_where == 1) {
+        const tgpu_predicate &w = req->where[0];
+        const Column &c = t->cols[w.column];
+        if (!c.nullable && !is_float_t(c.type) && w.op >= TGPU_PRED_BETWEEN && w.op <= TGPU_PRED_GE) {
+            const int64_t MN = INT64_MIN, MX = INT64_MAX;
+            int64_t lo = 1, hi = 0;  // empty
+            int neg = 0;
+            switch (w.op) {
+                case TGPU_PRED_BETWEEN: lo = w.lo; hi = w.hi; break;
+                case TGPU_PRED_NOT_BETWEEN: lo = w.lo; hi = w.hi; neg = 1; break;
+                case TGPU_PRED_EQ: lo = hi = w.lo; break;
+                case TGPU_PRED_NE: lo = hi = w.lo; neg = 1; break;
+                case TGPU_PRED_LT: if (w.lo != MN) { lo = MN; hi = w.lo - 1; } break;
+                case TGPU_PRED_LE: lo = MN; hi = w.lo; break;
+                case TGPU_PRED_GT: if (w.lo != MX) { lo = w.lo + 1; hi = MX; } break;
+                default: lo = w.lo; hi = MX; break;
+            }
+            dq.fp_data = c.d_data;
+            dq.fp_lo = lo;
+            dq.fp_hi = hi;
+            dq.fp_negate = neg;
+            dq.fp_bytes = type_bytes(c.type);
+        }
     }
 
     // key layout
@@ -904,6 +941,7 @@ tgpu_status enqueue(tgpu_query *q) {
     q->executed = true;
     q->synced = false;
     q->returned = 0;
+    q->h_packed = nullptr;
     return TGPU_OK;
 }
 
@@ -1152,22 +1190,42 @@ tgpu_status tgpu_query_next(tgpu_query *q, tgpu_batch *b, int32_t *done) {
     if (!q->synced && (st = finish(q)) != TGPU_OK) return st;
     if (b->n_columns != q->schema.size()) return fail(TGPU_ERR_INVALID_ARGUMENT, "batch column count");
     const uint64_t n = std::min<uint64_t>(b->capacity_rows, q->result_rows - q->returned);
-    std::vector<uint8_t> vbytes(n);
-    for (size_t c = 0; c < q->schema.size(); ++c) {
-        const size_t eb = q->schema[c].elem_bytes;
-        if (n && b->values && b->values[c])
-            CU(cudaMemcpyAsync(b->values[c], (char *)q->d_out[c] + q->returned * eb, n * eb, cudaMemcpyDeviceToHost,
-                               q->stream));
-        if (n && b->validity && b->validity[c]) {
-            CU(cudaMemcpyAsync(vbytes.data(), q->d_outvalid[c] + q->returned, n, cudaMemcpyDeviceToHost, q->stream));
-            CU(cudaStreamSynchronize(q->stream));
-            uint8_t *bm = b->validity[c];
-            std::memset(bm, 0, (n + 7) / 8);
-            for (uint64_t r = 0; r < n; ++r)
-                if (vbytes[r]) bm[r >> 3] |= (uint8_t)(1u << (r & 7));
+    const size_t nc = q->schema.size();
+    std::vector<std::vector<uint8_t>> vbytes(nc);
+    if (q->h_packed) {
+        // rows a batch already packed into host memory
+        size_t off = 8;
+        for (size_t c = 0; c < nc; ++c) {
+            const size_t eb = q->schema[c].elem_bytes;
+            if (n && b->values && b->values[c])
+                std::memcpy(b->values[c], q->h_packed + off + q->returned * eb, n * eb);
+            off += q->pack_rows * eb;
         }
+        for (size_t c = 0; c < nc; ++c) {
+            vbytes[c].assign(q->h_packed + off + q->returned, q->h_packed + off + q->returned + n);
+            off += q->pack_rows;
+        }
+    } else {
+        for (size_t c = 0; c < nc; ++c) {
+            const size_t eb = q->schema[c].elem_bytes;
+            if (n && b->values && b->values[c])
+                CU(cudaMemcpyAsync(b->values[c], (char *)q->d_out[c] + q->returned * eb, n * eb,
+                                   cudaMemcpyDeviceToHost, q->stream));
+            if (n && b->validity && b->validity[c]) {
+                vbytes[c].resize(n);
+                CU(cudaMemcpyAsync(vbytes[c].data(), q->d_outvalid[c] + q->returned, n, cudaMemcpyDeviceToHost,
+                                   q->stream));
+            }
+        }
+        CU(cudaStreamSynchronize(q->stream));
     }
-    CU(cudaStreamSynchronize(q->stream));
+    for (size_t c = 0; c < nc; ++c) {
+        if (!(n && b->validity && b->validity[c])) continue;
+        uint8_t *bm = b->validity[c];
+        std::memset(bm, 0, (n + 7) / 8);
+        for (uint64_t r = 0; r < n; ++r)
+            if (vbytes[c][r]) bm[r >> 3] |= (uint8_t)(1u << (r & 7));
+    }
     q->returned += n;
     b->row_count = n;
     *done = q->returned >= q->result_rows ? 1 : 0;
@@ -1215,6 +1273,10 @@ struct tgpu_query_batch {
     unsigned int *d_qctrl = nullptr;        // 4 per query: tile counter, status
     unsigned long long *h_counts = nullptr; // pinned: 8 per query, then Q statuses + batch status
     int *h_cancel = nullptr, *d_cancel = nullptr;
+    uint8_t *h_stage = nullptr, *d_stage = nullptr;  // mapped pinned: packed result rows
+    size_t stage_bytes = 0;
+    std::vector<size_t> stage_off;
+    std::vector<uint64_t> stage_rows;
     bool any_distinct = false, any_topk = false;
     int max_aggs = 0, max_sort_words = 2;
     size_t smem = 0;
@@ -1235,6 +1297,7 @@ struct tgpu_query_batch {
         if (graph) cudaGraphDestroy(graph);
         if (dev) cudaFree(dev);
         if (h_counts) cudaFreeHost(h_counts);
+        if (h_stage) cudaFreeHost(h_stage);
         if (h_cancel) cudaFreeHost(h_cancel);
         for (auto e : ev)
             if (e) cudaEventDestroy(e);
@@ -1259,6 +1322,27 @@ tgpu_status batch_descriptors(tgpu_query_batch *b) {
     b->max_rows = 1;
     b->max_words = 1;
     b->any_distinct = b->any_topk = false;
+    // layout of the packed results (queries with at most 4,096 result rows)
+    b->stage_off.assign(Q, 0);
+    b->stage_rows.assign(Q, 0);
+    size_t stage = 0;
+    for (uint32_t i = 0; i < Q; ++i) {
+        tgpu_query *q = b->qs[i];
+        uint64_t rows = q->rank == RANK_TOPK ? q->limit : q->out_rows_max;
+        if (rows > 4096) continue;
+        size_t bytes = 8;
+        for (auto &oc : q->schema) bytes += rows * (oc.elem_bytes + 1);
+        b->stage_off[i] = stage;
+        b->stage_rows[i] = rows;
+        stage += (bytes + 15) & ~(size_t)15;
+    }
+    if (stage > b->stage_bytes) {
+        if (b->h_stage) CU(cudaFreeHost(b->h_stage));
+        b->h_stage = nullptr;
+        CU(cudaHostAlloc((void **)&b->h_stage, stage, cudaHostAllocMapped));
+        CU(cudaHostGetDevicePointer((void **)&b->d_stage, b->h_stage, 0));
+        b->stage_bytes = stage;
+    }
     for (uint32_t i = 0; i < Q; ++i) {
         tgpu_query *q = b->qs[i];
         q->d_counts = b->d_counts + 8 * (size_t)i;
@@ -1286,6 +1370,10 @@ tgpu_status batch_descriptors(tgpu_query_batch *b) {
         fb.sel = q->rank == RANK_TOPK ? q->d_sel : q->d_gids;
         fb.offset = q->rank == RANK_TOPK ? q->offset : 0;
         fb.gather_rows = q->rank == RANK_TOPK ? q->limit : q->out_rows_max;
+        fb.pack_rows = b->stage_rows[i];
+        fb.pack_dst = fb.pack_rows ? b->d_stage + b->stage_off[i] : nullptr;
+        fb.n_out = (uint32_t)q->schema.size();
+        for (size_t c = 0; c < q->schema.size(); ++c) fb.out_bytes[c] = q->schema[c].elem_bytes;
         b->tile_start[i + 1] = b->tile_start[i] + (dq.n_chunks + SCAN_WARPS - 1) / SCAN_WARPS;
         b->max_aggs = std::max(b->max_aggs, dq.n_aggs);
         b->max_sort_words = std::max(b->max_sort_words, (int)q->df.sort_words);
@@ -1312,10 +1400,10 @@ tgpu_status batch_descriptors(tgpu_query_batch *b) {
 }
 
 // The device work of one execute (also what a CUDA graph captures).
-tgpu_status batch_enqueue_work(tgpu_query_batch *b) {
+tgpu_status batch_enqueue_work(tgpu_query_batch *b, bool capturing) {
     const uint32_t Q = (uint32_t)b->qs.size();
     cudaStream_t s = b->stream;
-    CU(cudaEventRecord(b->ev[0], s));
+    if (!capturing) CU(cudaEventRecord(b->ev[0], s));
     CU(cudaMemsetAsync(b->d_ctrl, 0, 8, s));
     CU(cudaMemsetAsync(b->d_counts, 0, 64 * (size_t)Q, s));
     CU(cudaMemsetAsync(b->d_qctrl, 0, 16 * (size_t)Q, s));
@@ -1326,8 +1414,8 @@ tgpu_status batch_enqueue_work(tgpu_query_batch *b) {
     CU(cudaMemcpyAsync(b->h_counts, b->d_counts, 64 * (size_t)Q, cudaMemcpyDeviceToHost, s));
     CU(cudaMemcpyAsync(b->h_counts + 8 * (size_t)Q, b->d_qctrl, 16 * (size_t)Q, cudaMemcpyDeviceToHost, s));
     CU(cudaMemcpyAsync(b->h_counts + 10 * (size_t)Q, b->d_ctrl, 8, cudaMemcpyDeviceToHost, s));
-    CU(cudaEventRecord(b->ev[1], s));
-    b->stats.kernel_launches = 1 + 5 + (b->any_topk ? 1 : 0);
+    if (!capturing) CU(cudaEventRecord(b->ev[1], s));
+    b->stats.kernel_launches = 1 + 6 + (b->any_topk ? 1 : 0);
     return TGPU_OK;
 }
 
@@ -1416,7 +1504,7 @@ tgpu_status tgpu_batch_execute(tgpu_query_batch *b) {
     if (b->flags & TGPU_BATCH_GRAPH) {
         if (!b->exec) {
             CU(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-            st = batch_enqueue_work(b);
+            st = batch_enqueue_work(b, true);
             cudaGraph_t g = nullptr;
             cudaError_t e = cudaStreamEndCapture(b->stream, &g);
             if (st != TGPU_OK) {
@@ -1427,10 +1515,13 @@ tgpu_status tgpu_batch_execute(tgpu_query_batch *b) {
             b->graph = g;
             CU(cudaGraphInstantiate(&b->exec, g, 0));
         }
+        // events bracket the replay (an event recorded during capture is not a record node)
+        CU(cudaEventRecord(b->ev[0], b->stream));
         CU(cudaGraphLaunch(b->exec, b->stream));
+        CU(cudaEventRecord(b->ev[1], b->stream));
         b->stats.graph = 1;
     } else {
-        if ((st = batch_enqueue_work(b)) != TGPU_OK) return st;
+        if ((st = batch_enqueue_work(b, false)) != TGPU_OK) return st;
         b->stats.graph = 0;
     }
     b->executed = true;
@@ -1483,6 +1574,8 @@ tgpu_status tgpu_batch_synchronize(tgpu_query_batch *b) {
         q->synced = true;
         q->returned = 0;
         q->result_rows = c[2];
+        q->pack_rows = b->stage_rows[i];
+        q->h_packed = q->pack_rows ? b->h_stage + b->stage_off[i] : nullptr;
         q->stats.rows_scanned = q->rows_scanned;
         q->stats.rows_selected = c[4];
         q->stats.groups = c[0];
@@ -1522,6 +1615,514 @@ tgpu_status tgpu_batch_get_stats(const tgpu_query_batch *b, tgpu_batch_stats *ou
 tgpu_status tgpu_batch_destroy(tgpu_query_batch *b) {
     if (!b) return fail(TGPU_ERR_INVALID_ARGUMENT, "null batch");
     delete b;
+    return TGPU_OK;
+}
+
+}  // extern "C"
+
+// ================================================================ serving ==
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+// A request with its own copies of every array it points to.
+struct OwnedRequest {
+    tgpu_request r{};
+    std::vector<int32_t> group_cols;
+    std::vector<tgpu_agg_spec> aggs;
+    std::vector<std::string> names;
+    std::vector<tgpu_predicate> where;
+    std::vector<tgpu_having> having;
+    std::vector<tgpu_sort_spec> order;
+    void set(const tgpu_request &in) {
+        r = in;
+        group_cols.assign(in.group_cols, in.group_cols + in.n_group_cols);
+        aggs.assign(in.aggs, in.aggs + in.n_aggs);
+        names.clear();
+        for (auto &a : aggs) names.push_back(a.as ? a.as : "");
+        for (size_t i = 0; i < aggs.size(); ++i) aggs[i].as = names[i].c_str();
+        where.assign(in.where, in.where + in.n_where);
+        having.assign(in.having, in.having + in.n_having);
+        order.assign(in.order, in.order + in.n_order);
+        r.group_cols = group_cols.data();
+        r.aggs = aggs.data();
+        r.where = where.data();
+        r.having = having.data();
+        r.order = order.data();
+        r.stream = nullptr;
+    }
+};
+
+struct Ticket {
+    uint64_t id = 0;
+    uint32_t table = 0;
+    OwnedRequest req;
+    uint64_t est_bytes = 0;
+    Clock::time_point submitted, done_at;
+    int state = 0;  // 0 queued, 1 running, 2 done
+    tgpu_status status = TGPU_OK;
+    std::string error;
+    std::vector<tgpu_output_column> schema;
+    std::vector<std::vector<uint8_t>> data;
+    std::vector<std::vector<uint8_t>> valid;  // one byte per row
+    uint64_t rows = 0, returned = 0;
+};
+
+struct Wave {
+    std::vector<Ticket *> tickets;
+    tgpu_query_batch *batch = nullptr;
+    tgpu_query *query = nullptr;
+    int slot = 0;
+    cudaEvent_t done = nullptr;
+    uint64_t bytes = 0;
+};
+
+// Estimated device bytes of a request: group table + occupancy bitmap +
+// distinct sets + id list and outputs (thinDB's accountant reserves before
+// it allocates, src/memory.zig:841).
+tgpu_status estimate_bytes(tgpu_table *t, const tgpu_request *req, uint64_t *out) {
+    std::unique_ptr<tgpu_query> q(new tgpu_query());
+    q->t = t;
+    q->flags = req->flags;
+    q->limit = req->limit;
+    q->offset = req->offset;
+    q->load_pct = req->table_load_pct ? req->table_load_pct : 50;
+    tgpu_status st = plan_query(q.get(), t, req);
+    if (st != TGPU_OK) return st;
+    uint64_t cap = next_pow2(std::max<uint64_t>(64, q->groups_est * 100 / q->load_pct));
+    uint64_t slots = cap + 1;
+    uint64_t bytes = slots * (uint64_t)q->dq.slot_words * 8 + slots / 8 + slots * 4;
+    for (uint64_t need : q->dset_need) bytes += next_pow2(std::max<uint64_t>(64, need * 2)) * 16;
+    uint64_t rows = req->limit != TGPU_NO_LIMIT ? std::min<uint64_t>(req->limit, slots) : slots;
+    for (auto &oc : q->schema) bytes += rows * (oc.elem_bytes + 1);
+    *out = bytes;
+    return TGPU_OK;
+}
+
+}  // namespace
+
+struct tgpu_server {
+    std::vector<tgpu_table *> tables;
+    tgpu_server_options opt{};
+    std::mutex mu;
+    std::condition_variable cv_submit, cv_done;
+    std::deque<Ticket *> pending;
+    std::unordered_map<uint64_t, std::unique_ptr<Ticket>> tickets;
+    uint64_t next_id = 1;
+    uint64_t admitted_bytes = 0;
+    bool stop = false;
+    int device = 0;
+    std::vector<cudaStream_t> streams;
+    std::vector<bool> slot_busy;
+    std::vector<Wave> inflight;   // dispatcher thread only
+    tgpu_server_stats stats{};
+    std::thread th;
+
+    ~tgpu_server() {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            stop = true;
+        }
+        cv_submit.notify_all();
+        if (th.joinable()) th.join();
+        for (auto s : streams) cudaStreamDestroy(s);
+    }
+
+    void finish_wave(Wave &w) {
+        cudaEventSynchronize(w.done);
+        cudaEventDestroy(w.done);
+        std::vector<std::pair<Ticket *, tgpu_status>> results;
+        for (size_t i = 0; i < w.tickets.size(); ++i) {
+            Ticket *tk = w.tickets[i];
+            tgpu_status st = TGPU_OK;
+            tgpu_query *q = w.batch ? w.batch->qs[i] : w.query;
+            if (w.batch) st = tgpu_batch_synchronize(w.batch);
+            else st = tgpu_query_synchronize(q);
+            if (st == TGPU_OK) {
+                tk->schema = q->schema;
+                const size_t nc = q->schema.size();
+                std::vector<void *> vals(nc);
+                std::vector<uint8_t *> bms(nc);
+                uint64_t rows = q->result_rows;
+                tk->data.assign(nc, {});
+                tk->valid.assign(nc, {});
+                std::vector<std::vector<uint8_t>> bits(nc);
+                for (size_t c = 0; c < nc; ++c) {
+                    tk->data[c].resize(std::max<uint64_t>(1, rows) * q->schema[c].elem_bytes);
+                    bits[c].resize(std::max<uint64_t>(1, (rows + 7) / 8));
+                    vals[c] = tk->data[c].data();
+                    bms[c] = bits[c].data();
+                }
+                tgpu_batch ob{};
+                ob.n_columns = (uint32_t)nc;
+                ob.values = vals.data();
+                ob.validity = bms.data();
+                ob.capacity_rows = std::max<uint64_t>(1, rows);
+                int32_t d = 0;
+                st = tgpu_query_next(q, &ob, &d);
+                tk->rows = ob.row_count;
+                for (size_t c = 0; c < nc; ++c) {
+                    tk->valid[c].resize(tk->rows);
+                    for (uint64_t r = 0; r < tk->rows; ++r) tk->valid[c][r] = (bits[c][r >> 3] >> (r & 7)) & 1;
+                }
+            }
+            results.push_back({tk, st});
+        }
+        std::string err = g_err;
+        if (w.batch) tgpu_batch_destroy(w.batch);
+        if (w.query) tgpu_query_destroy(w.query);
+        auto now = Clock::now();
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            for (auto &pr : results) {
+                pr.first->status = pr.second;
+                if (pr.second != TGPU_OK) {
+                    pr.first->error = err;
+                    stats.failed++;
+                }
+                pr.first->state = 2;
+                pr.first->done_at = now;
+                stats.completed++;
+            }
+            admitted_bytes -= w.bytes;
+            slot_busy[w.slot] = false;
+        }
+        cv_done.notify_all();
+    }
+
+    void fail_tickets(const std::vector<Ticket *> &tks, tgpu_status st, uint64_t bytes, int slot) {
+        std::string err = g_err;
+        auto now = Clock::now();
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            for (Ticket *tk : tks) {
+                tk->status = st;
+                tk->error = err;
+                tk->state = 2;
+                tk->done_at = now;
+                stats.failed++;
+                stats.completed++;
+            }
+            admitted_bytes -= bytes;
+            if (slot >= 0) slot_busy[slot] = false;
+        }
+        cv_done.notify_all();
+    }
+
+    // Take the next wave: the oldest request's table, then every queued
+    // request of that table that fits the budget (FIFO within the table).
+    bool take_wave(std::vector<Ticket *> &out, uint32_t &table, uint64_t &bytes, int &slot) {
+        std::lock_guard<std::mutex> lk(mu);
+        if (pending.empty()) return false;
+        slot = -1;
+        for (size_t i = 0; i < slot_busy.size(); ++i)
+            if (!slot_busy[i]) {
+                slot = (int)i;
+                break;
+            }
+        if (slot < 0) return false;
+        const uint32_t max_batch = opt.mode == TGPU_SERVE_PLAIN ? 1 : (opt.max_batch ? opt.max_batch : 256);
+        table = pending.front()->table;
+        bytes = 0;
+        for (auto it = pending.begin(); it != pending.end() && out.size() < max_batch;) {
+            Ticket *tk = *it;
+            if (tk->table != table) {
+                ++it;
+                continue;
+            }
+            if (admitted_bytes + bytes + tk->est_bytes > opt.memory_budget_bytes && !(out.empty() && admitted_bytes == 0))
+                break;  // wait for memory to free up (a request larger than the budget runs alone)
+            bytes += tk->est_bytes;
+            tk->state = 1;
+            out.push_back(tk);
+            it = pending.erase(it);
+        }
+        if (out.empty()) return false;
+        admitted_bytes += bytes;
+        stats.peak_admitted_bytes = std::max(stats.peak_admitted_bytes, admitted_bytes);
+        slot_busy[slot] = true;
+        return true;
+    }
+
+    void launch(std::vector<Ticket *> &tks, uint32_t table, uint64_t bytes, int slot) {
+        Wave w;
+        w.tickets = tks;
+        w.slot = slot;
+        w.bytes = bytes;
+        cudaStream_t s = streams[slot];
+        tgpu_status st;
+        if (opt.mode == TGPU_SERVE_PLAIN || tks.size() == 1) {
+            tgpu_request r = tks[0]->req.r;
+            r.stream = s;
+            st = tgpu_query_create(tables[table], &r, &w.query);
+            if (st == TGPU_OK) st = tgpu_query_execute(w.query);
+        } else {
+            std::vector<tgpu_request> reqs;
+            for (Ticket *tk : tks) reqs.push_back(tk->req.r);
+            st = tgpu_batch_create(tables[table], reqs.data(), (uint32_t)reqs.size(), 0, s, &w.batch);
+            if (st == TGPU_DECLINE) {
+                // a shape the batch does not run: run each request alone, in order
+                for (Ticket *tk : tks) {
+                    std::vector<Ticket *> one{tk};
+                    launch_one_sync(one, table, s);
+                }
+                std::lock_guard<std::mutex> lk(mu);
+                admitted_bytes -= bytes;
+                slot_busy[slot] = false;
+                return;
+            }
+            if (st == TGPU_OK) st = tgpu_batch_execute(w.batch);
+        }
+        if (st != TGPU_OK) {
+            if (w.batch) tgpu_batch_destroy(w.batch);
+            if (w.query) tgpu_query_destroy(w.query);
+            fail_tickets(tks, st, bytes, slot);
+            return;
+        }
+        cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming);
+        cudaEventRecord(w.done, s);
+        stats.waves++;
+        inflight.push_back(w);
+    }
+
+    void launch_one_sync(std::vector<Ticket *> &one, uint32_t table, cudaStream_t s) {
+        Wave w;
+        w.tickets = one;
+        w.slot = 0;
+        w.bytes = 0;
+        tgpu_request r = one[0]->req.r;
+        r.stream = s;
+        tgpu_status st = tgpu_query_create(tables[table], &r, &w.query);
+        if (st == TGPU_OK) st = tgpu_query_execute(w.query);
+        if (st != TGPU_OK) {
+            if (w.query) tgpu_query_destroy(w.query);
+            fail_tickets(one, st, 0, -1);
+            return;
+        }
+        cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming);
+        cudaEventRecord(w.done, s);
+        stats.waves++;
+        // completes before the dispatcher launches more on this stream
+        bool busy = slot_busy[0];
+        finish_wave(w);
+        std::lock_guard<std::mutex> lk(mu);
+        slot_busy[0] = busy;
+    }
+
+    void run() {
+        cudaSetDevice(device);
+        for (;;) {
+            bool progressed = false;
+            for (size_t i = 0; i < inflight.size();) {
+                if (cudaEventQuery(inflight[i].done) == cudaSuccess) {
+                    finish_wave(inflight[i]);
+                    inflight.erase(inflight.begin() + i);
+                    progressed = true;
+                } else {
+                    cudaGetLastError();
+                    ++i;
+                }
+            }
+            for (;;) {
+                std::vector<Ticket *> tks;
+                uint32_t table = 0;
+                uint64_t bytes = 0;
+                int slot = -1;
+                if (!take_wave(tks, table, bytes, slot)) break;
+                launch(tks, table, bytes, slot);
+                progressed = true;
+            }
+            std::unique_lock<std::mutex> lk(mu);
+            if (stop && pending.empty() && inflight.empty()) break;
+            if (!progressed) {
+                if (inflight.empty()) cv_submit.wait_for(lk, std::chrono::milliseconds(2));
+                else {
+                    lk.unlock();
+                    std::this_thread::sleep_for(std::chrono::microseconds(20));
+                }
+            }
+        }
+    }
+};
+
+extern "C" {
+
+tgpu_status tgpu_server_create(tgpu_table *const *tables, uint32_t n, const tgpu_server_options *opts,
+                               tgpu_server **out) {
+    if (!tables || !n || !out) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
+    DeviceCtx *dev;
+    tgpu_status st = device_ctx(&dev);
+    if (st != TGPU_OK) return st;
+    std::unique_ptr<tgpu_server> s(new tgpu_server());
+    s->tables.assign(tables, tables + n);
+    if (opts) s->opt = *opts;
+    if (!s->opt.memory_budget_bytes) s->opt.memory_budget_bytes = 120ULL << 30;
+    if (!s->opt.max_inflight) s->opt.max_inflight = 4;
+    if (s->opt.mode == TGPU_SERVE_PLAIN) s->opt.max_inflight = 1;
+    s->device = dev->id;
+    for (uint32_t i = 0; i < s->opt.max_inflight; ++i) {
+        cudaStream_t st2;
+        CU(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
+        s->streams.push_back(st2);
+        s->slot_busy.push_back(false);
+    }
+    tgpu_server *raw = s.get();
+    s->th = std::thread([raw] { raw->run(); });
+    *out = s.release();
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_server_submit(tgpu_server *s, uint32_t table, const tgpu_request *req, uint64_t *ticket) {
+    if (!s || !req || !ticket) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
+    if (table >= s->tables.size()) return fail(TGPU_ERR_INVALID_ARGUMENT, "table index");
+    std::unique_ptr<Ticket> tk(new Ticket());
+    tk->table = table;
+    tk->req.set(*req);
+    tgpu_status st = estimate_bytes(s->tables[table], &tk->req.r, &tk->est_bytes);
+    if (st != TGPU_OK) return st;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        tk->id = s->next_id++;
+        tk->submitted = Clock::now();
+        *ticket = tk->id;
+        s->pending.push_back(tk.get());
+        s->stats.submitted++;
+        s->stats.peak_queued = std::max<uint64_t>(s->stats.peak_queued, s->pending.size());
+        s->tickets[tk->id] = std::move(tk);
+    }
+    s->cv_submit.notify_one();
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_server_wait(tgpu_server *s, uint64_t ticket, int32_t timeout_ms, int32_t *done) {
+    if (!s || !done) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->tickets.find(ticket);
+    if (it == s->tickets.end()) return fail(TGPU_ERR_INVALID_ARGUMENT, "unknown ticket");
+    Ticket *tk = it->second.get();
+    if (timeout_ms < 0) s->cv_done.wait(lk, [&] { return tk->state == 2; });
+    else s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return tk->state == 2; });
+    *done = tk->state == 2 ? 1 : 0;
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_server_output_schema(tgpu_server *s, uint64_t ticket, tgpu_output_column *cols, uint32_t cap,
+                                      uint32_t *n) {
+    if (!s) return fail(TGPU_ERR_INVALID_ARGUMENT, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->tickets.find(ticket);
+    if (it == s->tickets.end() || it->second->state != 2) return fail(TGPU_ERR_INVALID_ARGUMENT, "ticket not done");
+    Ticket *tk = it->second.get();
+    if (tk->status != TGPU_OK) return fail(tk->status, tk->error);
+    if (n) *n = (uint32_t)tk->schema.size();
+    for (uint32_t i = 0; cols && i < cap && i < tk->schema.size(); ++i) cols[i] = tk->schema[i];
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_server_next(tgpu_server *s, uint64_t ticket, tgpu_batch *b, int32_t *done) {
+    if (!s || !b || !done) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->tickets.find(ticket);
+    if (it == s->tickets.end() || it->second->state != 2) return fail(TGPU_ERR_INVALID_ARGUMENT, "ticket not done");
+    Ticket *tk = it->second.get();
+    if (tk->status != TGPU_OK) return fail(tk->status, tk->error);
+    if (b->n_columns != tk->schema.size()) return fail(TGPU_ERR_INVALID_ARGUMENT, "batch column count");
+    const uint64_t n = std::min<uint64_t>(b->capacity_rows, tk->rows - tk->returned);
+    for (size_t c = 0; c < tk->schema.size(); ++c) {
+        const size_t eb = tk->schema[c].elem_bytes;
+        if (n && b->values && b->values[c]) std::memcpy(b->values[c], tk->data[c].data() + tk->returned * eb, n * eb);
+        if (n && b->validity && b->validity[c]) {
+            std::memset(b->validity[c], 0, (n + 7) / 8);
+            for (uint64_t r = 0; r < n; ++r)
+                if (tk->valid[c][tk->returned + r]) b->validity[c][r >> 3] |= (uint8_t)(1u << (r & 7));
+        }
+    }
+    tk->returned += n;
+    b->row_count = n;
+    *done = tk->returned >= tk->rows ? 1 : 0;
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_server_release(tgpu_server *s, uint64_t ticket) {
+    if (!s) return fail(TGPU_ERR_INVALID_ARGUMENT, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->tickets.find(ticket);
+    if (it == s->tickets.end()) return fail(TGPU_ERR_INVALID_ARGUMENT, "unknown ticket");
+    if (it->second->state != 2) return fail(TGPU_ERR_INVALID_ARGUMENT, "ticket still running");
+    s->tickets.erase(it);
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_server_get_stats(tgpu_server *s, tgpu_server_stats *out) {
+    if (!s || !out) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    *out = s->stats;
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_server_destroy(tgpu_server *s) {
+    if (!s) return fail(TGPU_ERR_INVALID_ARGUMENT, "null server");
+    delete s;
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_server_run_load(tgpu_server *s, const tgpu_load_spec *spec, tgpu_load_report *out) {
+    if (!s || !spec || !out || !spec->n_requests || spec->rate_qps <= 0)
+        return fail(TGPU_ERR_INVALID_ARGUMENT, "bad load spec");
+    std::mt19937_64 rng(spec->seed);
+    std::exponential_distribution<double> gap(spec->rate_qps);
+    std::uniform_int_distribution<uint32_t> pick(0, spec->n_requests - 1);
+    std::vector<uint64_t> ids;
+    const auto t0 = Clock::now();
+    auto next = t0;
+    const auto end = t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(spec->duration_s));
+    while (next < end) {
+        // open loop: each arrival is scheduled from the previous arrival time, not from completions
+        while (Clock::now() < next) std::this_thread::yield();
+        uint32_t j = pick(rng);
+        uint64_t id = 0;
+        tgpu_status st = tgpu_server_submit(s, spec->table_of ? spec->table_of[j] : 0, &spec->requests[j], &id);
+        if (st != TGPU_OK) return st;
+        ids.push_back(id);
+        next += std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(gap(rng)));
+    }
+    std::vector<double> lat;
+    lat.reserve(ids.size());
+    uint64_t failed = 0;
+    Clock::time_point first = Clock::time_point::max(), last = t0;
+    for (uint64_t id : ids) {
+        int32_t done = 0;
+        tgpu_status st = tgpu_server_wait(s, id, 600000, &done);
+        if (st != TGPU_OK) return st;
+        if (!done) return fail(TGPU_ERR_DEVICE_TIMEOUT, "a request did not finish within 600 s");
+        std::lock_guard<std::mutex> lk(s->mu);
+        Ticket *tk = s->tickets[id].get();
+        lat.push_back(std::chrono::duration<double, std::milli>(tk->done_at - tk->submitted).count());
+        if (tk->status != TGPU_OK) ++failed;
+        first = std::min(first, tk->submitted);
+        last = std::max(last, tk->done_at);
+    }
+    for (uint64_t id : ids) tgpu_server_release(s, id);
+    std::sort(lat.begin(), lat.end());
+    auto pct = [&](double p) {
+        if (lat.empty()) return 0.0;
+        size_t i = (size_t)std::ceil(p * lat.size()) - 1;
+        return lat[std::min(i, lat.size() - 1)];
+    };
+    std::memset(out, 0, sizeof(*out));
+    out->submitted = ids.size();
+    out->completed = lat.size();
+    out->failed = failed;
+    out->elapsed_s = lat.empty() ? 0 : std::chrono::duration<double>(last - first).count();
+    out->achieved_qps = out->elapsed_s > 0 ? (double)lat.size() / out->elapsed_s : 0;
+    out->p50_ms = pct(0.50);
+    out->p99_ms = pct(0.99);
+    out->p999_ms = pct(0.999);
+    out->max_ms = lat.empty() ? 0 : lat.back();
+    double sum = 0;
+    for (double x : lat) sum += x;
+    out->mean_ms = lat.empty() ? 0 : sum / lat.size();
     return TGPU_OK;
 }
 

@@ -95,6 +95,12 @@ struct DevQuery {
     int32_t n_cols;
     int32_t n_preds;
     DevPred preds[MAX_PREDS];
+    // A WHERE that is one range test on a NOT NULL integer column:
+    // (fp_lo <= x <= fp_hi) != fp_negate, read with width-specialised loads.
+    const void *fp_data;
+    int64_t fp_lo, fp_hi;
+    int32_t fp_bytes;        // 0 = no fast predicate
+    int32_t fp_negate;
     DevKeyPart parts[MAX_GROUP_KEYS];
     int32_t n_parts;
     int32_t key_words;        // 1 or 2
@@ -187,6 +193,12 @@ struct DevFinalBufs {
     uint32_t n_cand_blocks;
     uint32_t k;
     int32_t rank;                    // 0 all groups, 1 top-k (k <= 32)
+    // result packing into mapped host memory (pack_rows == 0: not packed):
+    // [u64 rows][column c: pack_rows * elem_bytes[c]]...[column c validity: pack_rows bytes]...
+    uint8_t *pack_dst;
+    uint64_t pack_rows;
+    uint32_t n_out;
+    uint32_t out_bytes[MAX_GROUP_KEYS + MAX_AGGS];
 };
 
 // Launchers (scan.cu / finalize.cu / table.cu) --------------------------------

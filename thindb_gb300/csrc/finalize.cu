@@ -351,7 +351,16 @@ __device__ __forceinline__ void warp_top_init(WarpTop &t, int sw) {
 // Offer each lane's candidate (valid flag) to the warp's list.
 __device__ void warp_top_offer(WarpTop &t, const uint64_t *cand, uint32_t cgid, bool valid, int k, int sw) {
     const int lane = threadIdx.x & 31;
-    unsigned m = __ballot_sync(FULL, valid);
+    // once the list is full only candidates better than its worst entry matter
+    bool offer = valid;
+    if (t.count == k) {
+        uint64_t worst[MAX_SORT_WORDS];
+#pragma unroll
+        for (int i = 0; i < MAX_SORT_WORDS; ++i)
+            worst[i] = (i < sw) ? (uint64_t)__shfl_sync(FULL, (long long)t.key[i], k - 1) : 0;
+        offer = valid && key_less(cand, worst, sw);
+    }
+    unsigned m = __ballot_sync(FULL, offer);
     while (m) {
         const int src = __ffs(m) - 1;
         m &= m - 1;
@@ -672,6 +681,28 @@ __global__ void gather_batch(const DevFinal *fs, const DevFinalBufs *bs) {
                 gridDim.x);
 }
 
+// Every query's result rows into one mapped host buffer (no per-column copies).
+__global__ void pack_batch(const DevFinalBufs *bs) {
+    const DevFinalBufs &b = bs[blockIdx.y];
+    if (b.pack_rows == 0) return;
+    const uint64_t rows = min((uint64_t)b.counts[2], b.pack_rows);
+    uint8_t *dst = b.pack_dst;
+    if (threadIdx.x == 0) *(volatile unsigned long long *)dst = rows;
+    uint64_t off = 8;
+    for (uint32_t c = 0; c < b.n_out; ++c) {
+        const uint8_t *src = (const uint8_t *)b.out_cols[c];
+        const uint64_t n = rows * b.out_bytes[c];
+        for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) dst[off + i] = src[i];
+        off += b.pack_rows * b.out_bytes[c];
+    }
+    for (uint32_t c = 0; c < b.n_out; ++c) {
+        const uint8_t *src = b.out_valid[c];
+        for (uint64_t i = threadIdx.x; i < rows; i += blockDim.x) dst[off + i] = src[i];
+        off += b.pack_rows;
+    }
+    __threadfence_system();
+}
+
 __global__ void clear_batch(const DevFinal *fs, const DevFinalBufs *bs) {
     const DevFinal &f = fs[blockIdx.y];
     clear_body(const_cast<unsigned long long *>(f.table), occ_words(f.cap), f.slot_words,
@@ -763,6 +794,7 @@ cudaError_t launch_finalize_batch(const DevFinal *fs, const DevFinalBufs *bs, ui
     topk_final_batch<<<dim3(1, n_queries), 32, 0, s>>>(fs, bs);
     unsigned gx = (unsigned)std::min<uint64_t>(std::max<uint64_t>(1, (max_rows + 255) / 256), 64);
     gather_batch<<<dim3(gx, n_queries), 256, 0, s>>>(fs, bs);
+    pack_batch<<<dim3(1, n_queries), 256, 0, s>>>(bs);
     unsigned cx = (unsigned)std::min<uint64_t>(std::max<uint64_t>(1, (max_words + 255) / 256), 512);
     clear_batch<<<dim3(cx, n_queries), 256, 0, s>>>(fs, bs);
     return cudaGetLastError();

@@ -236,7 +236,7 @@ struct Acc {
 template <int NA>
 __device__ __forceinline__ void apply_states(const DevQuery &q, unsigned long long *st, const Acc<NA> &acc) {
     atomicAdd(st, (unsigned long long)acc.rows);
-#pragma unroll
+#pragma unroll 1
     for (int a = 0; a < NA; ++a) {
         if (a >= q.n_aggs) break;
         const DevAgg &g = q.aggs[a];
@@ -271,7 +271,7 @@ __device__ __forceinline__ void apply_states(const DevQuery &q, unsigned long lo
 template <int NA>
 __device__ __forceinline__ void acc_init(const DevQuery &q, Acc<NA> &acc, const uint64_t *val, unsigned ok) {
     acc.rows = 1;
-#pragma unroll
+#pragma unroll 1
     for (int a = 0; a < NA; ++a) {
         acc.lo[a] = 0;
         acc.hi[a] = 0;
@@ -296,7 +296,7 @@ __device__ __forceinline__ void acc_init(const DevQuery &q, Acc<NA> &acc, const 
 template <int NA>
 __device__ __forceinline__ void acc_add(const DevQuery &q, Acc<NA> &acc, const uint64_t *x, unsigned ok) {
     acc.rows += 1;
-#pragma unroll
+#pragma unroll 1
     for (int a = 0; a < NA; ++a) {
         if (a >= q.n_aggs || !((ok >> a) & 1u)) continue;
         const int kind = q.aggs[a].kind;
@@ -428,11 +428,11 @@ __device__ __forceinline__ void load_row(const DevQuery &q, uint64_t row, bool m
     rv.k0 = 0;
     rv.k1 = 0;
     rv.ok = 0;
-#pragma unroll
+#pragma unroll 1
     for (int a = 0; a < NA; ++a) rv.val[a] = 0;
     if (!me) return;
     pack_key(q, row, rv.k0, rv.k1);
-#pragma unroll
+#pragma unroll 1
     for (int a = 0; a < NA; ++a) {
         if (a >= q.n_aggs) break;
         const DevAgg &g = q.aggs[a];
@@ -453,7 +453,7 @@ __device__ __noinline__ void fold_batch(const DevQuery &q, const ScanSmem &sm, c
     const bool me = (active >> lane) & 1u;
     uint64_t val[NA];
     const unsigned ok = in.ok;
-#pragma unroll
+#pragma unroll 1
     for (int a = 0; a < NA; ++a) {
         val[a] = in.val[a];
         if (a < q.n_aggs && (q.aggs[a].kind == AK_MIN_F || q.aggs[a].kind == AK_MAX_F)) {
@@ -483,7 +483,7 @@ __device__ __noinline__ void fold_batch(const DevQuery &q, const ScanSmem &sm, c
             const int src = rem ? __ffs(rem) - 1 : lane;
             const unsigned ob = __shfl_sync(FULL, ok, src);
             uint64_t x[NA];
-#pragma unroll
+#pragma unroll 1
             for (int a = 0; a < NA; ++a) x[a] = (a < q.n_aggs) ? shfl64(val[a], src) : 0;
             if (rem) {
                 acc_add<NA>(q, acc, x, ob);
@@ -520,7 +520,7 @@ __device__ __noinline__ void fold_batch(const DevQuery &q, const ScanSmem &sm, c
         gid = __shfl_sync(FULL, gid, leader_lane);
         if (me && gid != NO_GID) {
             unsigned long long *gst = q.table + (uint64_t)gid * q.slot_words + q.key_words;
-#pragma unroll
+#pragma unroll 1
             for (int a = 0; a < NA; ++a) {
                 if (a >= q.n_aggs) break;
                 const DevAgg &g = q.aggs[a];
@@ -543,6 +543,35 @@ __device__ __forceinline__ void chunk_rows(const DevQuery &q, uint32_t c, uint64
         row0 = (uint64_t)c * q.chunk_rows;
         row_end = min(row0 + q.chunk_rows, q.n_rows);
     }
+}
+
+// The fast WHERE: one range test on a NOT NULL integer column of type T,
+// FILTER_UNROLL coalesced streaming loads in flight per lane.
+template <typename T>
+__device__ __forceinline__ uint32_t filter_range(const DevQuery &q, uint64_t row0, uint64_t row_end, uint16_t *list) {
+    const int lane = threadIdx.x & 31;
+    const T *col = (const T *)q.fp_data;
+    const int64_t lo = q.fp_lo, hi = q.fp_hi;
+    const bool neg = q.fp_negate != 0;
+    uint32_t n = 0;
+    for (uint64_t b = row0; b < row_end; b += 32 * FILTER_UNROLL) {
+        T v[FILTER_UNROLL];
+#pragma unroll
+        for (int u = 0; u < FILTER_UNROLL; ++u) {
+            const uint64_t r = b + u * 32 + lane;
+            v[u] = r < row_end ? __ldcs(col + r) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < FILTER_UNROLL; ++u) {
+            const uint64_t r = b + u * 32 + lane;
+            const int64_t x = (int64_t)v[u];
+            const bool pass = r < row_end && ((x >= lo && x <= hi) != neg);
+            const unsigned m = __ballot_sync(FULL, pass);
+            if (pass) list[n + __popc(m & ((1u << lane) - 1))] = (uint16_t)(r - row0);
+            n += __popc(m);
+        }
+    }
+    return n;
 }
 
 // One warp folds chunk c: filter + compaction, then batches of 32 survivors
@@ -584,7 +613,14 @@ __device__ __forceinline__ void scan_chunk(const DevQuery &q, const ScanSmem &sm
     // gather mode: the chunk's survivors first, then folds
     uint16_t *list = sm.wlist + (size_t)warp * q.chunk_rows;
     uint32_t n = 0;
-    for (uint64_t b = row0; b < row_end; b += 32 * FILTER_UNROLL) {
+    switch (q.fp_bytes) {
+        case 1: n = filter_range<signed char>(q, row0, row_end, list); break;
+        case 2: n = filter_range<short>(q, row0, row_end, list); break;
+        case 4: n = filter_range<int>(q, row0, row_end, list); break;
+        case 8: n = filter_range<long long>(q, row0, row_end, list); break;
+        default: break;
+    }
+    for (uint64_t b = row0; q.fp_bytes == 0 && b < row_end; b += 32 * FILTER_UNROLL) {
         bool pass[FILTER_UNROLL];
         // first predicate for all steps (its loads are independent), then the rest
 #pragma unroll

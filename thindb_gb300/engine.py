@@ -491,3 +491,98 @@ class QueryBatch:
             self.close()
         except Exception:
             pass
+
+
+class _ServerResult(Query):
+    """Result view of one finished server ticket (same next/collect as Query)."""
+
+    def __init__(self, server: "Server", ticket: int):
+        self.server = server
+        self.ticket = ticket
+        self.handle = None
+        self.table = None
+        n = C.c_uint32()
+        _check(lib().tgpu_server_output_schema(server.handle, ticket, None, 0, C.byref(n)))
+        cols = (abi.OutputColumn * n.value)()
+        _check(lib().tgpu_server_output_schema(server.handle, ticket, cols, n.value, C.byref(n)))
+        self.schema = _schema(cols)
+
+    def _next_c(self, b, done) -> None:
+        _check(lib().tgpu_server_next(self.server.handle, self.ticket, C.byref(b), C.byref(done)))
+
+    def close(self) -> None:
+        pass
+
+
+class Server:
+    """Continuous-batching request loop over resident tables (native dispatcher)."""
+
+    def __init__(self, tables: Sequence[Table], mode: str = "continuous", memory_budget: int = 0,
+                 max_batch: int = 0, max_inflight: int = 0):
+        self.tables = list(tables)
+        arr = (C.c_void_p * len(self.tables))(*[t.handle.value for t in self.tables])
+        o = abi.ServerOptions()
+        o.memory_budget_bytes = memory_budget
+        o.max_batch = max_batch
+        o.max_inflight = max_inflight
+        o.mode = abi.SERVE_PLAIN if mode == "plain" else abi.SERVE_CONTINUOUS
+        h = C.c_void_p()
+        _check(lib().tgpu_server_create(arr, len(self.tables), C.byref(o), C.byref(h)))
+        self.handle = h
+
+    def submit(self, table_index: int, req: Request) -> int:
+        r, keep = build_request(self.tables[table_index], req)
+        t = C.c_uint64()
+        _check(lib().tgpu_server_submit(self.handle, table_index, C.byref(r), C.byref(t)))
+        del keep
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1) -> bool:
+        d = C.c_int32()
+        _check(lib().tgpu_server_wait(self.handle, ticket, timeout_ms, C.byref(d)))
+        return bool(d.value)
+
+    def result(self, ticket: int) -> dict:
+        self.wait(ticket)
+        return _ServerResult(self, ticket).collect()
+
+    def release(self, ticket: int) -> None:
+        _check(lib().tgpu_server_release(self.handle, ticket))
+
+    def stats(self) -> abi.ServerStats:
+        s = abi.ServerStats()
+        _check(lib().tgpu_server_get_stats(self.handle, C.byref(s)))
+        return s
+
+    def run_load(self, mix: Sequence[tuple], rate_qps: float, duration_s: float, seed: int = 1) -> dict:
+        """Open-loop Poisson load over `mix` = [(table index, Request)]; latency percentiles in ms."""
+        reqs = (abi.Request * len(mix))()
+        tabs = (C.c_uint32 * len(mix))()
+        keep = []
+        for i, (ti, rq) in enumerate(mix):
+            r, k = build_request(self.tables[ti], rq)
+            reqs[i] = r
+            tabs[i] = ti
+            keep.append(k)
+        spec = abi.LoadSpec()
+        spec.table_of = tabs
+        spec.requests = reqs
+        spec.n_requests = len(mix)
+        spec.rate_qps = rate_qps
+        spec.duration_s = duration_s
+        spec.seed = seed
+        rep = abi.LoadReport()
+        _check(lib().tgpu_server_run_load(self.handle, C.byref(spec), C.byref(rep)))
+        del keep
+        return {f: getattr(rep, f) for f, _ in abi.LoadReport._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().tgpu_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -44,3 +44,30 @@ def batched_request(seed: int, i: int, flags: int = 0) -> Request:
 
 def batched_requests(n: int = 256, seed: int = 4, flags: int = 0) -> list:
     return [batched_request(seed, i, flags) for i in range(n)]
+
+
+# Served mix: tables are [plain, filtered, distinct, batched]; shapes come from
+# the filtered, distinct and batched families (one third each).
+SERVED_TABLES = ["plain", "filtered", "distinct", "batched"]
+
+
+def served_request(seed: int, i: int) -> tuple:
+    """(table index, Request) of served request template i."""
+    rng = np.random.default_rng([seed, 7, i])
+    fam = i % 3
+    if fam == 0:  # filtered DECIMAL top-10 over a random DATE window of 1-36 days
+        days = int(rng.integers(1, 37))
+        start = int(rng.integers(0, 365 - days + 1))
+        where = [Pred("d", "between", datagen.DATE_BASE + start, datagen.DATE_BASE + start + days - 1)]
+        return 1, Request(["k"], [AggSpec("count", None, "c"), AggSpec("sum", "amount", "s"),
+                                  AggSpec("avg", "amount", "a")], [SortSpec("s", True)], limit=10, where=where)
+    if fam == 1:  # composite key + COUNT(DISTINCT) for one region, top-10 by distinct users
+        r = int(rng.integers(0, 64))
+        return 2, Request(["region", "url"], [AggSpec("count", None, "c"), AggSpec("count_distinct", "user_id", "u"),
+                                              AggSpec("sum", "latency_ms", "lat")], [SortSpec("u", True)], limit=10,
+                          where=[Pred("region", "=", r)])
+    return 3, batched_request(seed, 100_000 + i)
+
+
+def served_mix(n: int = 96, seed: int = 5) -> list:
+    return [served_request(seed, i) for i in range(n)]
