@@ -35,6 +35,12 @@ tgpu_status fail(tgpu_status s, const std::string &msg) {
     return s;
 }
 
+}  // namespace
+
+void tgpu::set_error(const char *msg) { g_err = msg ? msg : ""; }
+
+namespace {
+
 #define CU(call)                                                                                 \
     do {                                                                                         \
         cudaError_t e_ = (call);                                                                 \
@@ -626,6 +632,29 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
     }
     dq.state_words = phys;
     dq.slot_words = (int)next_pow2((uint64_t)(dq.key_words + dq.state_words));
+
+    // compiled fast fold: NOT NULL key parts and inputs, at most four owner
+    // aggregates (the scan falls back to the interpreter when no compiled
+    // signature matches)
+    dq.fast_km = 0;
+    dq.n_faggs = 0;
+    {
+        bool ok = true;
+        for (int i = 0; i < dq.n_parts; ++i) ok = ok && !dq.parts[i].nullable;
+        for (int a = 0; a < dq.n_aggs && ok; ++a) {
+            const DevAgg &g = dq.aggs[a];
+            if (g.kind == AK_COUNT_ROWS || !g.owner) continue;
+            if (g.kind == AK_COUNT_VALID || g.vword >= 0 || (g.kind == AK_DISTINCT && g.is_float_in) ||
+                dq.n_faggs >= 4) {
+                ok = false;
+                break;
+            }
+            dq.faggs[dq.n_faggs++] = g;
+        }
+        if (ok) dq.fast_km = dq.n_parts == 1 ? 1 : 2;
+        else dq.n_faggs = 0;
+        dq.fast_id = fast_fold_id(dq);
+    }
 
     for (uint32_t i = 0; i < req->n_order; ++i) {
         const tgpu_sort_spec &s = req->order[i];

@@ -106,6 +106,13 @@ struct DevQuery {
     int32_t key_words;        // 1 or 2
     DevAgg aggs[MAX_AGGS];
     int32_t n_aggs;
+    // compiled fast fold: key mode (0 = none, 1 = one NOT NULL part, 2 = several
+    // NOT NULL parts) and the owner aggregates it folds, in plan order
+    int32_t fast_km;
+    int32_t n_faggs;
+    DevAgg faggs[4];
+    int32_t fast_id;          // index of the matching compiled fold, -1 = interpreter
+    int32_t pad1;
     int32_t state_words;      // row count + slots
     int32_t slot_words;       // key_words + state_words rounded to a power of two
     int32_t needs_gid;        // a distinct aggregate needs each row's group slot
@@ -201,9 +208,14 @@ struct DevFinalBufs {
     uint32_t out_bytes[MAX_GROUP_KEYS + MAX_AGGS];
 };
 
+// Message returned by tgpu_last_error_message() on this thread (api.cpp).
+void set_error(const char *msg);
+
 // Launchers (scan.cu / finalize.cu / table.cu) --------------------------------
 
 int scan_grid_size(const DevQuery &q, int device_sms);
+// index of the compiled fast fold matching the plan (-1: the interpreter runs it)
+int fast_fold_id(const DevQuery &q);
 size_t scan_smem_bytes(const DevQuery &q);
 cudaError_t launch_scan(const DevQuery &q, int grid, cudaStream_t s);
 // many queries, one persistent kernel over (query, tile) work items

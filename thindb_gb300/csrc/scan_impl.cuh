@@ -1,0 +1,902 @@
+// scan_impl.cuh — device code of the fused scan + GROUP BY fold (shared by the
+// single-query kernels in scan.cu and the batched kernel in scan_batch.cu).
+//
+// One persistent kernel does thinDB's whole per-row hot loop
+// (silo_group_core.zig: runGridScanBurst :10705 -> appendBatchRawChunks :5364
+// -> stageBucketIds :9228 / scatterStageLane :9348 -> groupChunkRowsDirectKeys
+// :7456 -> foldKernel* :7832-8001 -> foldGroupDistinct :8003-8176):
+//
+//   1. Every warp owns a static, strided set of chunks of q.chunk_rows rows
+//      (inside the row groups that survived the zone maps): no tile claims and
+//      no block barriers in the main loop.
+//   2. The fused WHERE is evaluated 32 rows per step with coalesced streaming
+//      loads, eight steps in flight; a warp ballot gives the survivors, whose
+//      chunk offsets are compacted into the warp's shared-memory list
+//      (position = popc of the ballot below the lane).
+//   3. Survivors are folded 32 at a time: their key parts and aggregate inputs
+//      are gathered (only surviving rows are read: late materialisation; the
+//      next batch's gathers are issued before the current batch folds), and the
+//      key is packed LSB-first exactly as thinDB (v2_shape_group_topn.zig:2076-2092).
+//   4. __match_any_sync finds equal keys in the warp; their inputs are
+//      pre-combined into the lowest lane with shuffles (i128 sums exact).
+//   5. Leaders fold into the CTA's shared-memory table (key -> global slot +
+//      states, shared atomics; insert-if-free, so the hottest keys, which
+//      arrive first, stay resident).  Misses fold into the global
+//      open-addressing table (atomicCAS claim, linear probing), whose slot
+//      index is the group id COUNT(DISTINCT)'s (gid, value) set keys on.  The
+//      shared table is flushed into the global one once, when the CTA ends.
+//
+// No spin-waits: every probe loop is bounded by MAX_PROBE and reports
+// ST_TABLE_FULL / ST_DISTINCT_FULL through the status word instead.
+#pragma once
+
+#include "common.cuh"
+
+namespace tgpu {
+
+namespace {
+
+constexpr unsigned FULL = 0xFFFFFFFFu;
+constexpr uint32_t NO_GID = 0xFFFFFFFFu;
+constexpr int FILTER_UNROLL = 8;  // 32-row filter steps in flight per warp
+
+__device__ __forceinline__ bool col_valid(const DevCol &c, uint64_t r) {
+    return c.valid == nullptr || ((__ldg(c.valid + (r >> 5)) >> (r & 31)) & 1u);
+}
+
+// Sign-extended integer value (BOOLEAN zero-extended).
+__device__ __forceinline__ int64_t col_int(const DevCol &c, uint64_t r) {
+    switch (c.bytes) {
+        case 1:
+            return c.type == TGPU_BOOLEAN ? (int64_t)__ldg((const uint8_t *)c.data + r)
+                                          : (int64_t)(int8_t)__ldg((const int8_t *)c.data + r);
+        case 2: return (int64_t)__ldg((const int16_t *)c.data + r);
+        case 4: return (int64_t)__ldg((const int32_t *)c.data + r);
+        default: return (int64_t)__ldg((const long long *)c.data + r);
+    }
+}
+
+__device__ __forceinline__ double col_f64(const DevCol &c, uint64_t r) {
+    if (c.bytes == 4) return (double)__ldg((const float *)c.data + r);
+    return __ldg((const double *)c.data + r);
+}
+
+// Streaming (evict-first) loads for the predicate columns: read once.
+__device__ __forceinline__ int64_t col_int_stream(const DevCol &c, uint64_t r) {
+    switch (c.bytes) {
+        case 1:
+            return c.type == TGPU_BOOLEAN ? (int64_t)__ldcs((const unsigned char *)c.data + r)
+                                          : (int64_t)(signed char)__ldcs((const signed char *)c.data + r);
+        case 2: return (int64_t)__ldcs((const short *)c.data + r);
+        case 4: return (int64_t)__ldcs((const int *)c.data + r);
+        default: return (int64_t)__ldcs((const long long *)c.data + r);
+    }
+}
+
+__device__ __forceinline__ bool cmp_int(int op, int64_t x, int64_t lo, int64_t hi) {
+    switch (op) {
+        case TGPU_PRED_BETWEEN: return x >= lo && x <= hi;
+        case TGPU_PRED_NOT_BETWEEN: return x < lo || x > hi;
+        case TGPU_PRED_EQ: return x == lo;
+        case TGPU_PRED_NE: return x != lo;
+        case TGPU_PRED_LT: return x < lo;
+        case TGPU_PRED_LE: return x <= lo;
+        case TGPU_PRED_GT: return x > lo;
+        default: return x >= lo;
+    }
+}
+__device__ __forceinline__ bool cmp_f(int op, double x, double lo, double hi) {
+    switch (op) {
+        case TGPU_PRED_BETWEEN: return x >= lo && x <= hi;
+        case TGPU_PRED_NOT_BETWEEN: return x < lo || x > hi;
+        case TGPU_PRED_EQ: return x == lo;
+        case TGPU_PRED_NE: return x != lo;
+        case TGPU_PRED_LT: return x < lo;
+        case TGPU_PRED_LE: return x <= lo;
+        case TGPU_PRED_GT: return x > lo;
+        default: return x >= lo;
+    }
+}
+
+__device__ __forceinline__ bool pred_holds(const DevQuery &q, const DevPred &p, uint64_t r) {
+    const DevCol &c = q.cols[p.col];
+    bool v = col_valid(c, r);
+    if (p.op == TGPU_PRED_IS_NULL) return !v;
+    if (p.op == TGPU_PRED_IS_NOT_NULL) return v;
+    if (!v) return false;
+    return p.is_float ? cmp_f(p.op, col_f64(c, r), p.flo, p.fhi) : cmp_int(p.op, col_int_stream(c, r), p.lo, p.hi);
+}
+
+// Packed key: parts LSB-first, a nullable part's slice is payload | valid-bit
+// and all-zero for NULL (v2_shape_group_topn.zig:105-119, :2076-2092).
+__device__ __forceinline__ void pack_key(const DevQuery &q, uint64_t r, uint64_t &k0, uint64_t &k1) {
+    k0 = 0;
+    k1 = 0;
+    for (int i = 0; i < q.n_parts; ++i) {
+        const DevKeyPart &kp = q.parts[i];
+        const DevCol &c = q.cols[kp.col];
+        uint64_t slice = 0;
+        if (!kp.nullable || col_valid(c, r)) {
+            uint64_t raw = (uint64_t)col_int(c, r);
+            if (kp.payload < 64) raw &= (1ULL << kp.payload) - 1;
+            slice = raw;
+            if (kp.nullable) {
+                // validity bit sits right above the payload (bit 64 of a 64-bit part)
+                if (kp.payload < 64) {
+                    slice |= 1ULL << kp.payload;
+                } else {
+                    int vb = kp.offset + 64;
+                    if (vb < 64) k0 |= 1ULL << vb;
+                    else k1 |= 1ULL << (vb - 64);
+                }
+            }
+        }
+        int off = kp.offset;
+        if (off < 64) {
+            k0 |= slice << off;
+            if (off > 0) k1 |= slice >> (64 - off);
+        } else {
+            k1 |= slice << (off - 64);
+        }
+    }
+}
+
+__device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
+    return (uint64_t)__shfl_sync(FULL, (long long)v, src);
+}
+
+// ---------------------------------------------------------------- tables --
+
+// Slot of `key` in the global table, inserting it if absent.  Slot `cap`
+// holds the all-zero key (zero is the empty marker).
+__device__ uint64_t global_slot(const DevQuery &q, uint64_t k0, uint64_t k1) {
+    const uint64_t mask = q.cap - 1;
+    if (k0 == 0 && k1 == 0) {
+        uint32_t w = (uint32_t)(q.cap >> 5), b = 1u << (q.cap & 31);
+        if (!(*((volatile uint32_t *)q.occ + w) & b)) atomicOr(q.occ + w, b);
+        return q.cap;
+    }
+    uint64_t h = hash_key(k0, k1) & mask;
+    if (q.key_words == 1) {
+        for (unsigned p = 0; p < MAX_PROBE; ++p) {
+            unsigned long long *sp = q.table + h * (uint64_t)q.slot_words;
+            unsigned long long cur = ld_relaxed(sp);
+            if (cur == k0) return h;
+            if (cur == 0) {
+                cur = atomicCAS(sp, 0ULL, (unsigned long long)k0);
+                if (cur == 0) {
+                    atomicOr(q.occ + (h >> 5), 1u << (h & 31));
+                    return h;
+                }
+                if (cur == k0) return h;
+            }
+            h = (h + 1) & mask;
+        }
+    } else {
+        const ulonglong2 want = make_ulonglong2(k0, k1);
+        for (unsigned p = 0; p < MAX_PROBE; ++p) {
+            unsigned long long *sp = q.table + h * (uint64_t)q.slot_words;
+            // The CAS itself is the read: a plain 16-byte load may see the
+            // halves of two different writes.
+            ulonglong2 cur = cas128(sp, make_ulonglong2(0, 0), want);
+            if (cur.x == 0 && cur.y == 0) {
+                atomicOr(q.occ + (h >> 5), 1u << (h & 31));
+                return h;
+            }
+            if (cur.x == k0 && cur.y == k1) return h;
+            h = (h + 1) & mask;
+        }
+    }
+    atomicOr(q.status, ST_TABLE_FULL);
+    return NO_GID;
+}
+
+// Insert (gid, value bits) into a distinct set; true when the pair is new.
+// Entries are {value, gid | epoch << 32}; an entry from an older epoch is free.
+__device__ bool distinct_insert(const DevQuery &q, int d, uint32_t gid, uint64_t bits) {
+    unsigned long long *set = q.dset[d];
+    const uint64_t mask = q.dset_cap[d] - 1;
+    const uint64_t tag = (uint64_t)gid | ((uint64_t)q.epoch << 32);
+    uint64_t h = mix64(bits ^ mix64((uint64_t)gid)) & mask;
+    for (unsigned p = 0; p < MAX_PROBE; ++p) {
+        unsigned long long *sp = set + 2 * h;
+        ulonglong2 cur = ld128(sp);  // a hint; every decision below is confirmed atomically
+        bool next = false;
+        for (int tries = 0; tries < 16 && !next; ++tries) {
+            if ((uint32_t)(cur.y >> 32) == q.epoch) {
+                ulonglong2 a = cas128(sp, cur, cur);
+                if (a.x != cur.x || a.y != cur.y) {
+                    cur = a;
+                    continue;
+                }
+                if (cur.x == bits && cur.y == tag) return false;
+                next = true;
+            } else {
+                ulonglong2 a = cas128(sp, cur, make_ulonglong2(bits, tag));
+                if (a.x == cur.x && a.y == cur.y) return true;
+                cur = a;
+            }
+        }
+        h = (h + 1) & mask;
+    }
+    atomicOr(q.status, ST_DISTINCT_FULL);
+    return false;
+}
+
+// ------------------------------------------------------- fold of states --
+
+template <int NA>
+struct Acc {
+    uint64_t lo[NA];   // i64 sum / i128 lo / f64 bits / encoded extreme
+    uint64_t hi[NA];   // i128 hi
+    uint32_t vc[NA];   // valid inputs folded
+    uint32_t rows;     // rows folded (COUNT(*))
+};
+
+// Apply a combined contribution to a slot's state words (shared or global:
+// the atomics resolve to the address space of `st`).  Aggregates that share a
+// state word (SUM and AVG of one column) fold it once (g.owner).
+template <int NA>
+__device__ __forceinline__ void apply_states(const DevQuery &q, unsigned long long *st, const Acc<NA> &acc) {
+    atomicAdd(st, (unsigned long long)acc.rows);
+#pragma unroll 1
+    for (int a = 0; a < NA; ++a) {
+        if (a >= q.n_aggs) break;
+        const DevAgg &g = q.aggs[a];
+        const uint32_t vc = acc.vc[a];
+        if (vc == 0 || !g.owner) continue;
+        unsigned long long *w = st + g.word;
+        switch (g.kind) {
+            case AK_COUNT_VALID: atomicAdd(w, (unsigned long long)vc); break;
+            case AK_SUM_I64:
+                if (acc.lo[a]) atomicAdd(w, (unsigned long long)acc.lo[a]);
+                break;
+            case AK_SUM_I128: {
+                unsigned long long lo = acc.lo[a], hi = acc.hi[a];
+                if (lo) {
+                    unsigned long long old = atomicAdd(w, lo);
+                    hi += (old + lo < old) ? 1ULL : 0ULL;
+                }
+                if (hi) atomicAdd(w + 1, hi);
+                break;
+            }
+            case AK_SUM_F64: atomicAdd((double *)w, __longlong_as_double((long long)acc.lo[a])); break;
+            case AK_MIN_I: case AK_MAX_I: case AK_MIN_F: case AK_MAX_F:
+                atomicMax(w, (unsigned long long)acc.lo[a]);
+                break;
+            default: break;
+        }
+        if (g.vword >= 0) atomicAdd(st + g.vword, (unsigned long long)vc);
+    }
+}
+
+// One lane's own contribution, already in folded form.
+template <int NA>
+__device__ __forceinline__ void acc_init(const DevQuery &q, Acc<NA> &acc, const uint64_t *val, unsigned ok) {
+    acc.rows = 1;
+#pragma unroll 1
+    for (int a = 0; a < NA; ++a) {
+        acc.lo[a] = 0;
+        acc.hi[a] = 0;
+        acc.vc[a] = 0;
+        if (a >= q.n_aggs || !((ok >> a) & 1u)) continue;
+        const int kind = q.aggs[a].kind;
+        const uint64_t v = val[a];
+        acc.vc[a] = 1;
+        switch (kind) {
+            case AK_SUM_I64: acc.lo[a] = v; break;
+            case AK_SUM_I128: acc.lo[a] = v; acc.hi[a] = ((int64_t)v < 0) ? ~0ULL : 0ULL; break;
+            case AK_SUM_F64: acc.lo[a] = v; break;
+            case AK_MAX_I: acc.lo[a] = enc_i64((int64_t)v); break;
+            case AK_MIN_I: acc.lo[a] = ~enc_i64((int64_t)v); break;
+            case AK_MAX_F: acc.lo[a] = enc_f64_bits(v); break;
+            case AK_MIN_F: acc.lo[a] = ~enc_f64_bits(v); break;
+            default: break;
+        }
+    }
+}
+
+template <int NA>
+__device__ __forceinline__ void acc_add(const DevQuery &q, Acc<NA> &acc, const uint64_t *x, unsigned ok) {
+    acc.rows += 1;
+#pragma unroll 1
+    for (int a = 0; a < NA; ++a) {
+        if (a >= q.n_aggs || !((ok >> a) & 1u)) continue;
+        const int kind = q.aggs[a].kind;
+        const uint64_t v = x[a];
+        acc.vc[a] += 1;
+        switch (kind) {
+            case AK_SUM_I64: acc.lo[a] += v; break;
+            case AK_SUM_I128: {
+                uint64_t lo = acc.lo[a] + v;
+                acc.hi[a] += (((int64_t)v < 0) ? ~0ULL : 0ULL) + (lo < acc.lo[a] ? 1ULL : 0ULL);
+                acc.lo[a] = lo;
+                break;
+            }
+            case AK_SUM_F64:
+                acc.lo[a] = f64_bits(bits_f64(acc.lo[a]) + bits_f64(v));
+                break;
+            case AK_MAX_I: acc.lo[a] = max(acc.lo[a], (uint64_t)enc_i64((int64_t)v)); break;
+            case AK_MIN_I: acc.lo[a] = max(acc.lo[a], ~enc_i64((int64_t)v)); break;
+            case AK_MAX_F: acc.lo[a] = max(acc.lo[a], enc_f64_bits(v)); break;
+            case AK_MIN_F: acc.lo[a] = max(acc.lo[a], ~enc_f64_bits(v)); break;
+            default: break;
+        }
+    }
+}
+
+// ------------------------------------------------------ shared memory --
+
+struct ScanSmem {
+    unsigned long long *ckeys;   // cache_slots
+    unsigned long long *cstate;  // cache_slots * state_words
+    uint32_t *cgid;              // cache_slots
+    uint16_t *wlist;             // SCAN_WARPS * chunk_rows survivor offsets (gather mode)
+};
+
+__device__ __forceinline__ ScanSmem carve(const DevQuery &q, unsigned char *base) {
+    ScanSmem s;
+    const int C = q.cache_slots;
+    s.ckeys = (unsigned long long *)base;
+    s.cstate = s.ckeys + C;
+    s.cgid = (uint32_t *)(s.cstate + (size_t)C * q.state_words);
+    s.wlist = (uint16_t *)(s.cgid + C);
+    return s;
+}
+
+__device__ __forceinline__ void cache_init(const DevQuery &q, const ScanSmem &sm) {
+    for (int e = threadIdx.x; e < q.cache_slots; e += blockDim.x) {
+        sm.ckeys[e] = 0;
+        sm.cgid[e] = NO_GID;
+    }
+    for (int e = threadIdx.x; e < q.cache_slots * q.state_words; e += blockDim.x) sm.cstate[e] = 0;
+}
+
+// Find or claim the cache entry of a non-zero one-word key; -1 when the
+// bounded probe finds neither (the caller folds into the global table).
+__device__ __forceinline__ int cache_find(const DevQuery &q, const ScanSmem &sm, uint64_t k, bool &claimed) {
+    const int C = q.cache_slots;
+    const int limit = q.cache_probe;
+    uint32_t h = (uint32_t)hash_key(k, 0) & (C - 1);
+    claimed = false;
+    for (int p = 0; p < limit; ++p) {
+        unsigned long long cur = sm.ckeys[h];
+        if (cur == k) return (int)h;
+        if (cur == 0) {
+            cur = atomicCAS(&sm.ckeys[h], 0ULL, (unsigned long long)k);
+            if (cur == 0) {
+                claimed = true;
+                return (int)h;
+            }
+            if (cur == k) return (int)h;
+        }
+        h = (h + 1) & (C - 1);
+    }
+    return -1;
+}
+
+// Fold every live cache entry into its global slot.
+__device__ void cache_flush(const DevQuery &q, const ScanSmem &sm) {
+    const int C = q.cache_slots, S = q.state_words;
+    for (int e = threadIdx.x; e < C; e += blockDim.x) {
+        unsigned long long k = sm.ckeys[e];
+        if (k == 0) continue;
+        uint32_t gid = sm.cgid[e];
+        const unsigned long long *st = sm.cstate + (size_t)e * S;
+        if (gid == NO_GID) continue;  // only when the global table overflowed (rerun follows)
+        unsigned long long *gst = q.table + (uint64_t)gid * q.slot_words + q.key_words;
+        atomicAdd(gst, st[0]);
+        for (int a = 0; a < q.n_aggs; ++a) {
+            const DevAgg &g = q.aggs[a];
+            if (!g.owner) continue;
+            unsigned long long *w = gst + g.word;
+            switch (g.kind) {
+                case AK_COUNT_VALID: case AK_SUM_I64:
+                    if (st[g.word]) atomicAdd(w, st[g.word]);
+                    break;
+                case AK_SUM_I128: {
+                    unsigned long long lo = st[g.word], hi = st[g.word + 1];
+                    if (lo) {
+                        unsigned long long old = atomicAdd(w, lo);
+                        hi += (old + lo < old) ? 1ULL : 0ULL;
+                    }
+                    if (hi) atomicAdd(w + 1, hi);
+                    break;
+                }
+                case AK_SUM_F64:
+                    if (st[g.word]) atomicAdd((double *)w, __longlong_as_double((long long)st[g.word]));
+                    break;
+                case AK_MIN_I: case AK_MAX_I: case AK_MIN_F: case AK_MAX_F:
+                    if (st[g.word]) atomicMax(w, st[g.word]);
+                    break;
+                default: break;  // distinct counts live only in the global slot
+            }
+            if (g.vword >= 0 && st[g.vword]) atomicAdd(gst + g.vword, st[g.vword]);
+        }
+    }
+}
+
+// ------------------------------------------------------------ a batch --
+
+// The gathered inputs of one row (one lane).
+template <int NA>
+struct RowVals {
+    uint64_t k0, k1;
+    uint64_t val[NA];
+    unsigned ok;   // bit a: aggregate a's input is non-NULL
+};
+
+template <int NA>
+__device__ __forceinline__ void load_row(const DevQuery &q, uint64_t row, bool me, RowVals<NA> &rv) {
+    rv.k0 = 0;
+    rv.k1 = 0;
+    rv.ok = 0;
+#pragma unroll 1
+    for (int a = 0; a < NA; ++a) rv.val[a] = 0;
+    if (!me) return;
+    pack_key(q, row, rv.k0, rv.k1);
+#pragma unroll 1
+    for (int a = 0; a < NA; ++a) {
+        if (a >= q.n_aggs) break;
+        const DevAgg &g = q.aggs[a];
+        if (g.col < 0) continue;
+        const DevCol &c = q.cols[g.col];
+        if (!col_valid(c, row)) continue;
+        rv.ok |= 1u << a;
+        if (g.kind == AK_COUNT_VALID || g.kind == AK_COUNT_ROWS || !g.needs_value) continue;
+        rv.val[a] = g.is_float_in ? f64_bits(col_f64(c, row)) : (uint64_t)col_int(c, row);
+    }
+}
+
+// Fold up to 32 gathered rows (bit i of `active` = lane i holds one).  One
+// out-of-line copy keeps the instruction footprint small.
+template <int NA>
+__device__ __noinline__ void fold_batch(const DevQuery &q, const ScanSmem &sm, const RowVals<NA> &in, unsigned active) {
+    const int lane = threadIdx.x & 31;
+    const bool me = (active >> lane) & 1u;
+    uint64_t val[NA];
+    const unsigned ok = in.ok;
+#pragma unroll 1
+    for (int a = 0; a < NA; ++a) {
+        val[a] = in.val[a];
+        if (a < q.n_aggs && (q.aggs[a].kind == AK_MIN_F || q.aggs[a].kind == AK_MAX_F)) {
+            double d = bits_f64(val[a]);
+            if (d != d) val[a] = 0x7FF8000000000000ULL;  // one NaN, ordered largest
+        }
+    }
+    const uint64_t k0 = in.k0, k1 = in.k1;
+
+    // Equal keys in the warp: the lowest lane of each group folds for all.
+    unsigned grp;
+    if (q.warp_combine) {
+        grp = __match_any_sync(FULL, k0);
+        if (q.key_words == 2) grp &= __match_any_sync(FULL, k1);
+        grp &= active;
+    } else {
+        grp = 1u << lane;
+    }
+    const int leader_lane = me ? __ffs(grp) - 1 : lane;
+    const bool leader = me && leader_lane == lane;
+
+    Acc<NA> acc;
+    acc_init<NA>(q, acc, val, ok);
+    if (q.warp_combine) {
+        unsigned rem = leader ? (grp & ~(1u << lane)) : 0u;
+        while (__any_sync(FULL, rem != 0)) {
+            const int src = rem ? __ffs(rem) - 1 : lane;
+            const unsigned ob = __shfl_sync(FULL, ok, src);
+            uint64_t x[NA];
+#pragma unroll 1
+            for (int a = 0; a < NA; ++a) x[a] = (a < q.n_aggs) ? shfl64(val[a], src) : 0;
+            if (rem) {
+                acc_add<NA>(q, acc, x, ob);
+                rem &= rem - 1;
+            }
+        }
+    }
+
+    uint32_t gid = NO_GID;
+    if (leader) {
+        bool done = false;
+        if (q.cache_slots && q.key_words == 1 && k0 != 0) {
+            bool claimed;
+            int e = cache_find(q, sm, k0, claimed);
+            if (e >= 0) {
+                if (claimed) {
+                    gid = (uint32_t)global_slot(q, k0, 0);
+                    sm.cgid[e] = gid;
+                } else if (q.needs_gid) {
+                    gid = *((volatile uint32_t *)sm.cgid + e);
+                    if (gid == NO_GID) gid = (uint32_t)global_slot(q, k0, 0);
+                }
+                apply_states<NA>(q, sm.cstate + (size_t)e * q.state_words, acc);
+                done = true;
+            }
+        }
+        if (!done) {
+            gid = (uint32_t)global_slot(q, k0, k1);
+            if (gid != NO_GID) apply_states<NA>(q, q.table + (uint64_t)gid * q.slot_words + q.key_words, acc);
+        }
+    }
+
+    if (q.needs_gid) {
+        gid = __shfl_sync(FULL, gid, leader_lane);
+        if (me && gid != NO_GID) {
+            unsigned long long *gst = q.table + (uint64_t)gid * q.slot_words + q.key_words;
+#pragma unroll 1
+            for (int a = 0; a < NA; ++a) {
+                if (a >= q.n_aggs) break;
+                const DevAgg &g = q.aggs[a];
+                if (g.kind != AK_DISTINCT || !((ok >> a) & 1u)) continue;
+                uint64_t bits = g.is_float_in ? canon_f64_bits(bits_f64(val[a])) : val[a];
+                if (distinct_insert(q, g.dset, gid, bits)) atomicAdd(gst + g.word, 1ULL);
+            }
+        }
+    }
+}
+
+// Rows [row0, row_end) of chunk c.
+__device__ __forceinline__ void chunk_rows(const DevQuery &q, uint32_t c, uint64_t &row0, uint64_t &row_end) {
+    if (q.rg_list) {
+        uint32_t rgi = c / q.chunks_per_rg, sub = c % q.chunks_per_rg;
+        uint64_t rg = q.rg_list[rgi];
+        row0 = rg * q.rg_rows + (uint64_t)sub * q.chunk_rows;
+        row_end = min(min(row0 + q.chunk_rows, (rg + 1) * (uint64_t)q.rg_rows), q.n_rows);
+    } else {
+        row0 = (uint64_t)c * q.chunk_rows;
+        row_end = min(row0 + q.chunk_rows, q.n_rows);
+    }
+}
+
+// The fast WHERE: one range test on a NOT NULL integer column of type T,
+// FILTER_UNROLL coalesced streaming loads in flight per lane.
+template <typename T>
+__device__ __forceinline__ uint32_t filter_range(const DevQuery &q, uint64_t row0, uint64_t row_end, uint16_t *list) {
+    const int lane = threadIdx.x & 31;
+    const T *col = (const T *)q.fp_data;
+    const int64_t lo = q.fp_lo, hi = q.fp_hi;
+    const bool neg = q.fp_negate != 0;
+    uint32_t n = 0;
+    for (uint64_t b = row0; b < row_end; b += 32 * FILTER_UNROLL) {
+        T v[FILTER_UNROLL];
+#pragma unroll
+        for (int u = 0; u < FILTER_UNROLL; ++u) {
+            const uint64_t r = b + u * 32 + lane;
+            v[u] = r < row_end ? __ldcs(col + r) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < FILTER_UNROLL; ++u) {
+            const uint64_t r = b + u * 32 + lane;
+            const int64_t x = (int64_t)v[u];
+            const bool pass = r < row_end && ((x >= lo && x <= hi) != neg);
+            const unsigned m = __ballot_sync(FULL, pass);
+            if (pass) list[n + __popc(m & ((1u << lane) - 1))] = (uint16_t)(r - row0);
+            n += __popc(m);
+        }
+    }
+    return n;
+}
+
+// ------------------------------------------------------ fold policies --
+
+// The interpreter: any plan, aggregate kinds read from the plan at run time.
+template <int NA>
+struct GenericFold {
+    using Row = RowVals<NA>;
+    __device__ __forceinline__ static void load(const DevQuery &q, uint64_t r, bool me, Row &rv) {
+        load_row<NA>(q, r, me, rv);
+    }
+    __device__ __forceinline__ static void fold(const DevQuery &q, const ScanSmem &sm, const Row &rv, unsigned act) {
+        fold_batch<NA>(q, sm, rv, act);
+    }
+};
+
+// A plan whose NOT NULL inputs fold with the compile-time kinds K0..K3 (the
+// owner aggregates of q.faggs, AK_NONE = none) and whose key is one NOT NULL
+// integer part (KM = 1) or several NOT NULL parts (KM = 2): no per-row kind
+// dispatch, no validity checks, the accumulators stay in registers.
+constexpr int AK_NONE = -1;
+
+template <int KM, int K0, int K1, int K2, int K3>
+struct FastFold {
+    static constexpr int NA = (K0 != AK_NONE) + (K1 != AK_NONE) + (K2 != AK_NONE) + (K3 != AK_NONE);
+    static constexpr int NV = NA > 0 ? NA : 1;
+    __host__ __device__ static constexpr int kind(int a) { return a == 0 ? K0 : a == 1 ? K1 : a == 2 ? K2 : K3; }
+    __host__ __device__ static constexpr bool is_f(int a) {
+        return kind(a) == AK_SUM_F64 || kind(a) == AK_MIN_F || kind(a) == AK_MAX_F;
+    }
+    static constexpr bool DISTINCT = K0 == AK_DISTINCT || K1 == AK_DISTINCT || K2 == AK_DISTINCT || K3 == AK_DISTINCT;
+
+    struct Row {
+        uint64_t k0, k1;
+        uint64_t val[NV];
+    };
+
+    __device__ __forceinline__ static void load(const DevQuery &q, uint64_t r, bool me, Row &rv) {
+        rv.k0 = 0;
+        rv.k1 = 0;
+#pragma unroll
+        for (int a = 0; a < NV; ++a) rv.val[a] = 0;
+        if (!me) return;
+        if (KM == 1) {
+            const DevKeyPart &kp = q.parts[0];
+            uint64_t raw = (uint64_t)col_int(q.cols[kp.col], r);
+            rv.k0 = kp.payload < 64 ? (raw & ((1ULL << kp.payload) - 1)) : raw;
+        } else {
+            for (int i = 0; i < q.n_parts; ++i) {
+                const DevKeyPart &kp = q.parts[i];
+                uint64_t raw = (uint64_t)col_int(q.cols[kp.col], r);
+                if (kp.payload < 64) raw &= (1ULL << kp.payload) - 1;
+                const int off = kp.offset;
+                if (off < 64) {
+                    rv.k0 |= raw << off;
+                    if (off > 0) rv.k1 |= raw >> (64 - off);
+                } else {
+                    rv.k1 |= raw << (off - 64);
+                }
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < NA; ++a) {
+            const DevCol &c = q.cols[q.faggs[a].col];
+            rv.val[a] = is_f(a) ? f64_bits(col_f64(c, r)) : (uint64_t)col_int(c, r);
+        }
+    }
+
+    __device__ __noinline__ static void fold(const DevQuery &q, const ScanSmem &sm, const Row &in, unsigned active) {
+        const int lane = threadIdx.x & 31;
+        const bool me = (active >> lane) & 1u;
+        uint64_t val[NV];
+#pragma unroll
+        for (int a = 0; a < NV; ++a) {
+            val[a] = in.val[a];
+            if (a < NA && (kind(a) == AK_MIN_F || kind(a) == AK_MAX_F)) {
+                const double d = bits_f64(val[a]);
+                if (d != d) val[a] = 0x7FF8000000000000ULL;
+            }
+        }
+        const uint64_t k0 = in.k0, k1 = in.k1;
+        unsigned grp;
+        if (q.warp_combine) {
+            grp = __match_any_sync(FULL, k0);
+            if (q.key_words == 2) grp &= __match_any_sync(FULL, k1);
+            grp &= active;
+        } else {
+            grp = 1u << lane;
+        }
+        const int leader_lane = me ? __ffs(grp) - 1 : lane;
+        const bool leader = me && leader_lane == lane;
+
+        // own contribution in folded form
+        uint32_t rows = 1;
+        uint64_t lo[NV], hi[NV];
+#pragma unroll
+        for (int a = 0; a < NV; ++a) {
+            lo[a] = 0;
+            hi[a] = 0;
+            if (a >= NA) continue;
+            const uint64_t v = val[a];
+            switch (kind(a)) {
+                case AK_SUM_I64: case AK_SUM_F64: lo[a] = v; break;
+                case AK_SUM_I128: lo[a] = v; hi[a] = ((int64_t)v < 0) ? ~0ULL : 0ULL; break;
+                case AK_MAX_I: lo[a] = enc_i64((int64_t)v); break;
+                case AK_MIN_I: lo[a] = ~enc_i64((int64_t)v); break;
+                case AK_MAX_F: lo[a] = enc_f64_bits(v); break;
+                case AK_MIN_F: lo[a] = ~enc_f64_bits(v); break;
+                default: break;
+            }
+        }
+        if (q.warp_combine) {
+            unsigned rem = leader ? (grp & ~(1u << lane)) : 0u;
+            while (__any_sync(FULL, rem != 0)) {
+                const int src = rem ? __ffs(rem) - 1 : lane;
+                uint64_t x[NV];
+#pragma unroll
+                for (int a = 0; a < NV; ++a) x[a] = a < NA ? shfl64(val[a], src) : 0;
+                if (rem) {
+                    rows += 1;
+#pragma unroll
+                    for (int a = 0; a < NV; ++a) {
+                        if (a >= NA) continue;
+                        const uint64_t v = x[a];
+                        switch (kind(a)) {
+                            case AK_SUM_I64: lo[a] += v; break;
+                            case AK_SUM_I128: {
+                                const uint64_t l = lo[a] + v;
+                                hi[a] += (((int64_t)v < 0) ? ~0ULL : 0ULL) + (l < lo[a] ? 1ULL : 0ULL);
+                                lo[a] = l;
+                                break;
+                            }
+                            case AK_SUM_F64: lo[a] = f64_bits(bits_f64(lo[a]) + bits_f64(v)); break;
+                            case AK_MAX_I: lo[a] = max(lo[a], (uint64_t)enc_i64((int64_t)v)); break;
+                            case AK_MIN_I: lo[a] = max(lo[a], ~enc_i64((int64_t)v)); break;
+                            case AK_MAX_F: lo[a] = max(lo[a], enc_f64_bits(v)); break;
+                            case AK_MIN_F: lo[a] = max(lo[a], ~enc_f64_bits(v)); break;
+                            default: break;
+                        }
+                    }
+                    rem &= rem - 1;
+                }
+            }
+        }
+
+        uint32_t gid = NO_GID;
+        if (leader) {
+            unsigned long long *st = nullptr;
+            if (q.cache_slots && q.key_words == 1 && k0 != 0) {
+                bool claimed;
+                const int e = cache_find(q, sm, k0, claimed);
+                if (e >= 0) {
+                    if (claimed) {
+                        gid = (uint32_t)global_slot(q, k0, 0);
+                        sm.cgid[e] = gid;
+                    } else if (DISTINCT) {
+                        gid = *((volatile uint32_t *)sm.cgid + e);
+                        if (gid == NO_GID) gid = (uint32_t)global_slot(q, k0, 0);
+                    }
+                    st = sm.cstate + (size_t)e * q.state_words;
+                }
+            }
+            if (!st) {
+                gid = (uint32_t)global_slot(q, k0, k1);
+                if (gid != NO_GID) st = q.table + (uint64_t)gid * q.slot_words + q.key_words;
+            }
+            if (st) {
+                atomicAdd(st, (unsigned long long)rows);
+#pragma unroll
+                for (int a = 0; a < NV; ++a) {
+                    if (a >= NA) continue;
+                    unsigned long long *w = st + q.faggs[a].word;
+                    switch (kind(a)) {
+                        case AK_SUM_I64:
+                            if (lo[a]) atomicAdd(w, (unsigned long long)lo[a]);
+                            break;
+                        case AK_SUM_I128: {
+                            unsigned long long l = lo[a], h = hi[a];
+                            if (l) {
+                                const unsigned long long old = atomicAdd(w, l);
+                                h += (old + l < old) ? 1ULL : 0ULL;
+                            }
+                            if (h) atomicAdd(w + 1, h);
+                            break;
+                        }
+                        case AK_SUM_F64: atomicAdd((double *)w, bits_f64(lo[a])); break;
+                        case AK_MIN_I: case AK_MAX_I: case AK_MIN_F: case AK_MAX_F:
+                            atomicMax(w, (unsigned long long)lo[a]);
+                            break;
+                        default: break;
+                    }
+                }
+            }
+        }
+        if (DISTINCT) {
+            gid = __shfl_sync(FULL, gid, leader_lane);
+            if (me && gid != NO_GID) {
+                unsigned long long *gst = q.table + (uint64_t)gid * q.slot_words + q.key_words;
+#pragma unroll
+                for (int a = 0; a < NV; ++a) {
+                    if (a >= NA || kind(a) != AK_DISTINCT) continue;
+                    if (distinct_insert(q, q.faggs[a].dset, gid, val[a])) atomicAdd(gst + q.faggs[a].word, 1ULL);
+                }
+            }
+        }
+    }
+};
+
+// One warp folds chunk c: filter + compaction, then batches of 32 survivors
+// (each batch's gathers issued before the previous batch folds).
+template <class P>
+__device__ __forceinline__ void scan_chunk(const DevQuery &q, const ScanSmem &sm, uint32_t c,
+                                           unsigned long long &selected) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint64_t row0, row_end;
+    chunk_rows(q, c, row0, row_end);
+    if (row0 >= row_end) return;
+    if (q.n_preds == 0 || !q.gather) {
+        // every row (or every filtered row in place): 32 consecutive rows per batch
+        typename P::Row cur, nxt;
+        uint64_t r = row0 + lane;
+        bool pass = r < row_end && (q.n_preds == 0 || [&] {
+                        for (int i = 0; i < q.n_preds; ++i)
+                            if (!pred_holds(q, q.preds[i], r)) return false;
+                        return true;
+                    }());
+        P::load(q, r, pass, cur);
+        unsigned act = __ballot_sync(FULL, pass);
+        for (uint64_t b = row0; b < row_end; b += 32) {
+            const uint64_t rn = b + 32 + lane;
+            const bool pn = rn < row_end && (q.n_preds == 0 || [&] {
+                                for (int i = 0; i < q.n_preds; ++i)
+                                    if (!pred_holds(q, q.preds[i], rn)) return false;
+                                return true;
+                            }());
+            P::load(q, rn, pn, nxt);
+            const unsigned actn = __ballot_sync(FULL, pn);
+            selected += (lane == 0) ? __popc(act) : 0;
+            if (act) P::fold(q, sm, cur, act);
+            cur = nxt;
+            act = actn;
+        }
+        return;
+    }
+    // gather mode: the chunk's survivors first, then folds
+    uint16_t *list = sm.wlist + (size_t)warp * q.chunk_rows;
+    uint32_t n = 0;
+    switch (q.fp_bytes) {
+        case 1: n = filter_range<signed char>(q, row0, row_end, list); break;
+        case 2: n = filter_range<short>(q, row0, row_end, list); break;
+        case 4: n = filter_range<int>(q, row0, row_end, list); break;
+        case 8: n = filter_range<long long>(q, row0, row_end, list); break;
+        default: break;
+    }
+    for (uint64_t b = row0; q.fp_bytes == 0 && b < row_end; b += 32 * FILTER_UNROLL) {
+        bool pass[FILTER_UNROLL];
+        // first predicate for all steps (its loads are independent), then the rest
+#pragma unroll
+        for (int u = 0; u < FILTER_UNROLL; ++u) {
+            const uint64_t r = b + u * 32 + lane;
+            pass[u] = r < row_end && pred_holds(q, q.preds[0], r);
+        }
+        for (int i = 1; i < q.n_preds; ++i) {
+#pragma unroll
+            for (int u = 0; u < FILTER_UNROLL; ++u) {
+                const uint64_t r = b + u * 32 + lane;
+                if (pass[u]) pass[u] = pred_holds(q, q.preds[i], r);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < FILTER_UNROLL; ++u) {
+            const unsigned m = __ballot_sync(FULL, pass[u]);
+            if (pass[u]) list[n + __popc(m & ((1u << lane) - 1))] = (uint16_t)(b + u * 32 + lane - row0);
+            n += __popc(m);
+        }
+    }
+    __syncwarp();
+    selected += (lane == 0) ? n : 0;
+    if (n == 0) return;
+    typename P::Row cur, nxt;
+    P::load(q, row0 + list[lane < n ? lane : 0], lane < n, cur);
+    for (uint32_t i = 0; i < n; i += 32) {
+        const uint32_t j = i + 32 + lane;
+        P::load(q, row0 + list[j < n ? j : 0], j < n, nxt);
+        const uint32_t left = n - i;
+        P::fold(q, sm, cur, left >= 32 ? FULL : ((1u << left) - 1));
+        cur = nxt;
+    }
+}
+
+// The compiled fast-fold signatures: (index, key mode, owner aggregate kinds).
+#define TGPU_FAST_FOLDS(X)                                             \
+    X(0, 1, AK_SUM_I64, AK_MIN_I, AK_MAX_I, AK_NONE)                   \
+    X(1, 1, AK_SUM_I128, AK_NONE, AK_NONE, AK_NONE)                    \
+    X(2, 1, AK_SUM_I128, AK_MIN_I, AK_MAX_I, AK_NONE)                  \
+    X(3, 1, AK_SUM_I128, AK_MIN_I, AK_NONE, AK_NONE)                   \
+    X(4, 1, AK_SUM_I128, AK_MAX_I, AK_NONE, AK_NONE)                   \
+    X(5, 1, AK_MIN_I, AK_MAX_I, AK_NONE, AK_NONE)                      \
+    X(6, 1, AK_MIN_I, AK_NONE, AK_NONE, AK_NONE)                       \
+    X(7, 1, AK_MAX_I, AK_NONE, AK_NONE, AK_NONE)                       \
+    X(8, 1, AK_NONE, AK_NONE, AK_NONE, AK_NONE)                        \
+    X(9, 1, AK_SUM_I64, AK_NONE, AK_NONE, AK_NONE)                     \
+    X(10, 2, AK_DISTINCT, AK_SUM_F64, AK_NONE, AK_NONE)                \
+    X(11, 2, AK_NONE, AK_NONE, AK_NONE, AK_NONE)
+
+// The same work as scan_chunk<P> for the fold the plan's fast_id names.
+template <int NA>
+__device__ __forceinline__ void scan_chunk_dispatch(const DevQuery &q, const ScanSmem &sm, uint32_t c,
+                                                    unsigned long long &selected) {
+    if constexpr (NA > 4) {
+        scan_chunk<GenericFold<NA>>(q, sm, c, selected);  // wide plans: the interpreter
+    } else {
+        switch (q.fast_id) {
+#define TGPU_CASE(I, KM, A, B, C2, D) \
+    case I: scan_chunk<FastFold<KM, A, B, C2, D>>(q, sm, c, selected); break;
+            TGPU_FAST_FOLDS(TGPU_CASE)
+#undef TGPU_CASE
+            default: scan_chunk<GenericFold<NA>>(q, sm, c, selected); break;
+        }
+    }
+}
+
+}  // namespace
+
+}  // namespace tgpu
