@@ -426,6 +426,32 @@ typedef struct tgpu_load_report {
 
 tgpu_status tgpu_server_run_load(tgpu_server *s, const tgpu_load_spec *spec, tgpu_load_report *out);
 
+/* ------------------------------------------------- allocation-free call -- */
+
+/* No counterpart in thinDB.  For callers that cannot let the library
+ * allocate device memory (a host that reserves the GPU's memory for its own
+ * arena up front, a plugin running inside another runtime's memory pool, a
+ * latency-critical loop that must not block in cudaMalloc/cudaFree):
+ *
+ *   SELECT key, COUNT(*), SUM(value), MIN(value), MAX(value) GROUP BY key
+ *
+ * over two NOT NULL BIGINT device columns of n_rows rows, with the same
+ * kernels as tgpu_query_create.  Nothing is allocated: the group table lives
+ * in one fixed array of about 9.6 MB inside the library (held on every GPU
+ * that loads it until the process exits).  Outputs are caller-provided device
+ * buffers of TGPU_NOALLOC_MAX_GROUPS values each; *out_groups (device memory)
+ * receives the number of groups.  SUM is BIGINT and wraps, as thinDB's.
+ * More than TGPU_NOALLOC_MAX_GROUPS distinct keys returns
+ * TGPU_ERR_INVALID_ARGUMENT.  The first call on a device looks up the
+ * array's device address and zeroes it: make that first call before any
+ * stream capture.  The call is synchronous (it reads back a status word).
+ * All calls share the array: calls that overlap on the GPU race. */
+#define TGPU_NOALLOC_MAX_GROUPS 65536
+tgpu_status tgpu_group_by_i64_noalloc(const int64_t *keys, const int64_t *values, uint64_t n_rows,
+                                      int64_t *out_keys, int64_t *out_count, int64_t *out_sum,
+                                      int64_t *out_min, int64_t *out_max, uint64_t *out_groups,
+                                      void *stream);
+
 #ifdef __cplusplus
 }
 #endif
