@@ -798,7 +798,14 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
         dset_bytes += c * 16;
     }
     q->n_cpt_blocks = compact_blocks(cap);
-    q->n_cand_blocks = 152;
+    {
+        // enough CTAs to stream the group list, a few per SM at most
+        DeviceCtx *dev;
+        tgpu_status st = device_ctx(&dev);
+        if (st != TGPU_OK) return st;
+        const uint64_t want = (std::min<uint64_t>(q->groups_est, cap + 1) + 2047) / 2048;
+        q->n_cand_blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)dev->sms * 4));
+    }
     size_t row_bytes = 0;
     for (auto &oc : q->schema) row_bytes += oc.elem_bytes + 1;
     const size_t sw = (size_t)df.sort_words;
@@ -811,7 +818,7 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     size_t o_ctrl = add(16), o_counts = add(8 * 8), o_bc = add(4 * (size_t)q->n_cpt_blocks), o_gids = add(4 * slots);
     size_t o_ck = 0, o_cg = 0, o_sel = 0, o_sk0 = 0, o_sk1 = 0, o_si0 = 0, o_si1 = 0;
     if (q->rank == RANK_TOPK) {
-        o_ck = add((size_t)q->n_cand_blocks * 32 * sw * 8);
+        o_ck = add((size_t)q->n_cand_blocks * 32 * topk_width((int)sw) * 8);
         o_cg = add((size_t)q->n_cand_blocks * 32 * 4);
         o_sel = add(32 * 4);
     } else if (q->rank == RANK_SORT) {
@@ -1307,7 +1314,8 @@ struct tgpu_query_batch {
     std::vector<size_t> stage_off;
     std::vector<uint64_t> stage_rows;
     bool any_distinct = false, any_topk = false;
-    int max_aggs = 0, max_sort_words = 2;
+    int max_aggs = 0;
+    uint32_t topk_widths = 0;  // TOPK_W* classes of the top-k queries
     size_t smem = 0;
     int grid = 0;
     uint32_t max_cpt_blocks = 1, max_cand_blocks = 1;
@@ -1344,7 +1352,7 @@ tgpu_status batch_descriptors(tgpu_query_batch *b) {
     b->h_bs.resize(Q);
     b->tile_start.assign(Q + 1, 0);
     b->max_aggs = 0;
-    b->max_sort_words = 2;
+    b->topk_widths = 0;
     b->smem = 0;
     b->max_cpt_blocks = 1;
     b->max_cand_blocks = 1;
@@ -1405,7 +1413,7 @@ tgpu_status batch_descriptors(tgpu_query_batch *b) {
         for (size_t c = 0; c < q->schema.size(); ++c) fb.out_bytes[c] = q->schema[c].elem_bytes;
         b->tile_start[i + 1] = b->tile_start[i] + (dq.n_chunks + SCAN_WARPS - 1) / SCAN_WARPS;
         b->max_aggs = std::max(b->max_aggs, dq.n_aggs);
-        b->max_sort_words = std::max(b->max_sort_words, (int)q->df.sort_words);
+        if (fb.rank == 1) b->topk_widths |= topk_width_bit(q->df.sort_words);
         b->smem = std::max(b->smem, scan_smem_bytes(dq));
         b->max_cpt_blocks = std::max(b->max_cpt_blocks, q->n_cpt_blocks);
         b->max_cand_blocks = std::max(b->max_cand_blocks, q->n_cand_blocks);
@@ -1438,13 +1446,13 @@ tgpu_status batch_enqueue_work(tgpu_query_batch *b, bool capturing) {
     CU(cudaMemsetAsync(b->d_qctrl, 0, 16 * (size_t)Q, s));
     CU(launch_batch_scan(b->d_qs, b->d_tile_start, Q, b->max_aggs, b->smem, b->grid, b->d_ctrl,
                          (const volatile int *)b->d_cancel, b->d_ctrl + 1, s));
-    CU(launch_finalize_batch(b->d_fs, b->d_bs, Q, b->max_cpt_blocks, b->max_cand_blocks, b->max_sort_words,
-                             b->any_topk, b->max_rows, b->max_words, s));
+    CU(launch_finalize_batch(b->d_fs, b->d_bs, Q, b->max_cpt_blocks, b->max_cand_blocks, b->topk_widths,
+                             b->max_rows, b->max_words, s));
     CU(cudaMemcpyAsync(b->h_counts, b->d_counts, 64 * (size_t)Q, cudaMemcpyDeviceToHost, s));
     CU(cudaMemcpyAsync(b->h_counts + 8 * (size_t)Q, b->d_qctrl, 16 * (size_t)Q, cudaMemcpyDeviceToHost, s));
     CU(cudaMemcpyAsync(b->h_counts + 10 * (size_t)Q, b->d_ctrl, 8, cudaMemcpyDeviceToHost, s));
     if (!capturing) CU(cudaEventRecord(b->ev[1], s));
-    b->stats.kernel_launches = 1 + 6 + (b->any_topk ? 1 : 0);
+    b->stats.kernel_launches = 1 + 5 + std::max(1, 2 * __builtin_popcount(b->topk_widths));
     return TGPU_OK;
 }
 

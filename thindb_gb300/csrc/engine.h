@@ -18,6 +18,15 @@ constexpr int MAX_QCOLS = 24;       // distinct columns one query reads
 constexpr int MAX_ORDER = 6;
 constexpr int MAX_SORT_WORDS = 2 * MAX_ORDER + 2;
 
+// Key-width class of the top-k kernels for an encoded sort key of `sw` words
+// (one to six ORDER BY entries): the candidate buffers hold this many words
+// per entry.
+__host__ __device__ constexpr int topk_width(int sw) { return sw <= 4 ? 4 : sw <= 6 ? 6 : sw <= 8 ? 8 : 14; }
+constexpr uint32_t TOPK_W4 = 1, TOPK_W6 = 2, TOPK_W8 = 4, TOPK_W14 = 8;
+__host__ __device__ constexpr uint32_t topk_width_bit(int sw) {
+    return sw <= 4 ? TOPK_W4 : sw <= 6 ? TOPK_W6 : sw <= 8 ? TOPK_W8 : TOPK_W14;
+}
+
 // Scan geometry: persistent CTAs of SCAN_WARPS warps; each warp folds a
 // static, strided set of chunks of chunk_rows rows.
 constexpr int SCAN_THREADS = 512;
@@ -224,9 +233,10 @@ cudaError_t launch_batch_scan(const DevQuery *qs, const uint32_t *tile_start, ui
                               size_t smem, int grid, unsigned int *work_counter, const volatile int *cancel,
                               unsigned int *status, cudaStream_t s);
 // compaction, top-k / all-groups selection, gather and clear for every query of a batch
+// topk_widths: TOPK_W* bits of the key-width classes of the batch's top-k queries
 cudaError_t launch_finalize_batch(const DevFinal *fs, const DevFinalBufs *bs, uint32_t n_queries,
-                                  uint32_t max_cpt_blocks, uint32_t max_cand_blocks, int max_sort_words,
-                                  bool any_topk, uint64_t max_rows, uint64_t max_words, cudaStream_t s);
+                                  uint32_t max_cpt_blocks, uint32_t max_cand_blocks, uint32_t topk_widths,
+                                  uint64_t max_rows, uint64_t max_words, cudaStream_t s);
 
 // compaction: dense list of occupied slots that pass HAVING
 cudaError_t launch_compact(const DevFinal &f, uint32_t *block_counts, uint32_t n_blocks,

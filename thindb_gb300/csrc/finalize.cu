@@ -167,37 +167,42 @@ __device__ bool having_pass(const DevFinal &f, const unsigned long long *st) {
     return true;
 }
 
-// Encoded sort key: per ORDER BY value a 128-bit word pair (NULL = 0, a value
-// = its order-preserving image + 1, complemented for DESC), then the packed
-// key.  Smaller words = earlier row.
+// The two encoded words of ORDER BY entry `o` for a group: NULL = 0, a value
+// = its order-preserving image + 1, complemented for DESC.  Smaller words =
+// earlier row.
+__device__ __forceinline__ void order_words(const DevFinal &f, const DevOrder &o, uint64_t k0, uint64_t k1,
+                                            const unsigned long long *st, uint64_t &hi, uint64_t &lo) {
+    EmitVal v = o.target == TGPU_SORT_KEY ? emit_key(f, k0, k1, o.index) : emit_agg(f, st, o.index);
+    hi = 0;
+    lo = 0;
+    if (!v.null) {
+        if (v.is_f) {
+            double d = v.f;
+            uint64_t b = (d != d) ? 0x7FF8000000000000ULL : (d == 0.0 ? 0ULL : f64_bits(d));
+            lo = enc_f64_bits(b);
+        } else {
+            lo = v.lo;
+            hi = (uint64_t)v.hi ^ 0x8000000000000000ULL;
+        }
+        lo += 1;
+        if (lo == 0) hi += 1;
+    }
+    if (o.desc) {
+        hi = ~hi;
+        lo = ~lo;
+    }
+}
+
+// Encoded sort key: the ORDER BY word pairs, then the packed key (ties break
+// on the key ascending).  f.sort_words words.
 __device__ void encode_sort_key(const DevFinal &f, uint32_t gid, uint64_t *w) {
     uint64_t k0, k1;
     slot_key(f, gid, k0, k1);
     const unsigned long long *st = slot_states(f, gid);
     int n = 0;
     for (int i = 0; i < f.n_order; ++i) {
-        const DevOrder &o = f.order[i];
-        EmitVal v = o.target == TGPU_SORT_KEY ? emit_key(f, k0, k1, o.index) : emit_agg(f, st, o.index);
-        uint64_t hi = 0, lo = 0;
-        if (!v.null) {
-            if (v.is_f) {
-                double d = v.f;
-                uint64_t b = (d != d) ? 0x7FF8000000000000ULL : (d == 0.0 ? 0ULL : f64_bits(d));
-                lo = enc_f64_bits(b);
-                hi = 0;
-            } else {
-                lo = v.lo;
-                hi = (uint64_t)v.hi ^ 0x8000000000000000ULL;
-            }
-            lo += 1;
-            if (lo == 0) hi += 1;
-        }
-        if (o.desc) {
-            hi = ~hi;
-            lo = ~lo;
-        }
-        w[n++] = hi;
-        w[n++] = lo;
+        order_words(f, f.order[i], k0, k1, st, w[n], w[n + 1]);
+        n += 2;
     }
     w[n++] = k1;
     w[n++] = k0;
@@ -331,146 +336,195 @@ __global__ void __launch_bounds__(CPT_THREADS) compact_write_kernel(const __grid
 }
 
 // ----------------------------------------------------------------- top-k --
+//
+// k <= 32.  The key width is a compile-time class SW (topk_width: 4, 6, 8 or
+// 14 words) so the lists live in registers: the ORDER BY word pairs first,
+// zero padding, then the packed key in the last two words — the same order
+// as encode_sort_key's dense layout.
 
 constexpr int TOPK_THREADS = 256;
+constexpr int TOPK_WARPS = TOPK_THREADS / 32;
+constexpr uint32_t NO_ID = 0xFFFFFFFFu;
 
-// A warp's sorted list of up to k (<= 32) best entries, one per lane.
-struct WarpTop {
-    uint64_t key[MAX_SORT_WORDS];
-    uint32_t gid;
-    int count;  // warp-uniform
-};
-
-__device__ __forceinline__ void warp_top_init(WarpTop &t, int sw) {
-    for (int i = 0; i < MAX_SORT_WORDS; ++i) t.key[i] = ~0ULL;
-    t.gid = 0xFFFFFFFFu;
-    t.count = 0;
-    (void)sw;
+template <int SW>
+__device__ __forceinline__ bool lex_less(const uint64_t (&a)[SW], const uint64_t (&b)[SW]) {
+#pragma unroll
+    for (int i = 0; i < SW; ++i)
+        if (a[i] != b[i]) return a[i] < b[i];
+    return false;
 }
 
-// Offer each lane's candidate (valid flag) to the warp's list.
-__device__ void warp_top_offer(WarpTop &t, const uint64_t *cand, uint32_t cgid, bool valid, int k, int sw) {
-    const int lane = threadIdx.x & 31;
-    // once the list is full only candidates better than its worst entry matter
-    bool offer = valid;
-    if (t.count == k) {
-        uint64_t worst[MAX_SORT_WORDS];
+template <int SW>
+__device__ __forceinline__ void encode_top_key(const DevFinal &f, uint32_t gid, uint64_t (&w)[SW]) {
+    uint64_t k0, k1;
+    slot_key(f, gid, k0, k1);
+    const unsigned long long *st = slot_states(f, gid);
 #pragma unroll
-        for (int i = 0; i < MAX_SORT_WORDS; ++i)
-            worst[i] = (i < sw) ? (uint64_t)__shfl_sync(FULL, (long long)t.key[i], k - 1) : 0;
-        offer = valid && key_less(cand, worst, sw);
+    for (int i = 0; i < (SW - 2) / 2; ++i) {
+        uint64_t hi = 0, lo = 0;
+        if (i < f.n_order) order_words(f, f.order[i], k0, k1, st, hi, lo);
+        w[2 * i] = hi;
+        w[2 * i + 1] = lo;
     }
-    unsigned m = __ballot_sync(FULL, offer);
+    w[SW - 2] = k1;
+    w[SW - 1] = k0;
+}
+
+// A warp's sorted list of its best (up to k) entries, entry j in lane j.
+template <int SW>
+struct WarpList {
+    uint64_t key[SW];
+    uint64_t worst[SW];  // entry k-1 once the list is full (warp-uniform)
+    uint32_t gid;
+    int count;           // warp-uniform
+};
+
+template <int SW>
+__device__ __forceinline__ void wl_init(WarpList<SW> &t) {
+#pragma unroll
+    for (int i = 0; i < SW; ++i) t.key[i] = t.worst[i] = ~0ULL;
+    t.gid = NO_ID;
+    t.count = 0;
+}
+
+// Offer each lane's candidate (if valid).  Once the list is full only
+// candidates ahead of its k-th entry get past the first comparison, so the
+// serial insertions are few after the first k.
+template <int SW>
+__device__ __forceinline__ void wl_offer(WarpList<SW> &t, const uint64_t (&cand)[SW], uint32_t cgid, bool valid,
+                                         int k) {
+    const int lane = threadIdx.x & 31;
+    unsigned m = __ballot_sync(FULL, valid && (t.count < k || lex_less<SW>(cand, t.worst)));
     while (m) {
         const int src = __ffs(m) - 1;
         m &= m - 1;
-        uint64_t c[MAX_SORT_WORDS];
+        uint64_t c[SW];
 #pragma unroll
-        for (int i = 0; i < MAX_SORT_WORDS; ++i)
-            c[i] = (i < sw) ? (uint64_t)__shfl_sync(FULL, (long long)cand[i], src) : 0;
+        for (int i = 0; i < SW; ++i) c[i] = (uint64_t)__shfl_sync(FULL, (long long)cand[i], src);
         const uint32_t g = __shfl_sync(FULL, cgid, src);
-        // worst kept entry (lane k-1) when the list is full
-        if (t.count == k) {
-            uint64_t worst[MAX_SORT_WORDS];
+        if (t.count == k && !lex_less<SW>(c, t.worst)) continue;  // an earlier insertion raised the bar
+        const int pos = __popc(__ballot_sync(FULL, lane < t.count && lex_less<SW>(t.key, c)));
+        uint64_t up[SW];
 #pragma unroll
-            for (int i = 0; i < MAX_SORT_WORDS; ++i)
-                worst[i] = (i < sw) ? (uint64_t)__shfl_sync(FULL, (long long)t.key[i], k - 1) : 0;
-            if (!key_less(c, worst, sw)) continue;
-        }
-        const bool before = lane < t.count && key_less(t.key, c, sw);
-        const int pos = __popc(__ballot_sync(FULL, before));
-        // shift lanes >= pos down by one
-        uint64_t up[MAX_SORT_WORDS];
-#pragma unroll
-        for (int i = 0; i < MAX_SORT_WORDS; ++i)
-            up[i] = (i < sw) ? (uint64_t)__shfl_up_sync(FULL, (long long)t.key[i], 1) : 0;
-        uint32_t upg = __shfl_up_sync(FULL, t.gid, 1);
+        for (int i = 0; i < SW; ++i) up[i] = (uint64_t)__shfl_up_sync(FULL, (long long)t.key[i], 1);
+        const uint32_t upg = __shfl_up_sync(FULL, t.gid, 1);
         if (lane > pos && lane < k) {
 #pragma unroll
-            for (int i = 0; i < MAX_SORT_WORDS; ++i) t.key[i] = up[i];
+            for (int i = 0; i < SW; ++i) t.key[i] = up[i];
             t.gid = upg;
         }
         if (lane == pos) {
 #pragma unroll
-            for (int i = 0; i < MAX_SORT_WORDS; ++i) t.key[i] = c[i];
+            for (int i = 0; i < SW; ++i) t.key[i] = c[i];
             t.gid = g;
         }
-        if (t.count < k) t.count++;
+        if (t.count < k) ++t.count;
+        if (t.count == k) {
+#pragma unroll
+            for (int i = 0; i < SW; ++i) t.worst[i] = (uint64_t)__shfl_sync(FULL, (long long)t.key[i], k - 1);
+        }
     }
 }
 
-// Per-CTA top-k of the dense list; each warp scans a strided share, then
-// warp 0 merges the warps' lists.
+// Best k of the candidates i = first + warp*32 + lane (+ stride ...) < n, as
+// produced by get(i, key, gid) -> valid.  Every warp keeps its own list; warp
+// 0 merges them and writes k entries (NO_ID pads) to out_keys (if given) and
+// out_gids, and the kept count to *out_count (if given).
+template <int SW, class Get>
+__device__ __forceinline__ void block_topk(uint64_t n, uint64_t first, uint64_t stride, int k, Get get,
+                                           unsigned long long *out_keys, uint32_t *out_gids,
+                                           unsigned long long *out_count) {
+    __shared__ unsigned long long s_keys[TOPK_WARPS * 32 * SW];
+    __shared__ uint32_t s_ids[TOPK_WARPS * 32];
+    __shared__ int s_cnt[TOPK_WARPS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    WarpList<SW> t;
+    wl_init(t);
+    for (uint64_t base = first + (uint64_t)warp * 32; base < n; base += stride) {
+        const uint64_t i = base + lane;
+        uint64_t c[SW];
+        uint32_t g = NO_ID;
+        bool valid = false;
+        if (i < n) {
+            valid = get(i, c, g);
+        } else {
+#pragma unroll
+            for (int j = 0; j < SW; ++j) c[j] = 0;
+        }
+        wl_offer<SW>(t, c, g, valid, k);
+    }
+#pragma unroll
+    for (int i = 0; i < SW; ++i) s_keys[((size_t)warp * 32 + lane) * SW + i] = t.key[i];
+    s_ids[warp * 32 + lane] = t.gid;
+    if (lane == 0) s_cnt[warp] = t.count;
+    __syncthreads();
+    if (warp != 0) return;
+    WarpList<SW> m;
+    wl_init(m);
+    for (int w = 0; w < TOPK_WARPS; ++w) {
+        uint64_t c[SW];
+#pragma unroll
+        for (int i = 0; i < SW; ++i) c[i] = s_keys[((size_t)w * 32 + lane) * SW + i];
+        wl_offer<SW>(m, c, s_ids[w * 32 + lane], lane < s_cnt[w], k);
+    }
+    if (lane < k) {
+        if (out_keys) {
+#pragma unroll
+            for (int i = 0; i < SW; ++i) out_keys[(size_t)lane * SW + i] = m.key[i];
+        }
+        out_gids[lane] = lane < m.count ? m.gid : NO_ID;
+    }
+    if (out_count && lane == 0) *out_count = (unsigned long long)m.count;
+}
+
+// Per-CTA top-k of the dense group list: k candidates per CTA, at
+// cand_* + bid * 32.
+template <int SW>
 __device__ __forceinline__ void topk_partial_body(const DevFinal &f, const uint32_t *gids,
                                                   const unsigned long long *counts, int k,
                                                   unsigned long long *cand_keys, uint32_t *cand_gids, uint32_t bid,
                                                   uint32_t nblk) {
-    extern __shared__ unsigned long long tk_sh[];
-    const int sw = f.sort_words;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = TOPK_THREADS / 32;
     const uint64_t n = counts[1];
-    WarpTop t;
-    warp_top_init(t, sw);
-    const uint64_t stride = (uint64_t)nblk * TOPK_THREADS;
-    for (uint64_t base = (uint64_t)bid * TOPK_THREADS + warp * 32; base < n; base += stride) {
-        const uint64_t i = base + lane;
-        uint64_t c[MAX_SORT_WORDS];
-        uint32_t g = 0;
-        const bool valid = i < n;
-        if (valid) {
+    block_topk<SW>(
+        n, (uint64_t)bid * TOPK_THREADS, (uint64_t)nblk * TOPK_THREADS, k,
+        [&](uint64_t i, uint64_t(&c)[SW], uint32_t &g) {
             g = gids[i];
-            encode_sort_key(f, g, c);
-        }
-        warp_top_offer(t, c, g, valid, k, sw);
-    }
-    // park every warp's list in shared memory
-    unsigned long long *keys = tk_sh;                                  // nwarps*32*sw
-    uint32_t *ids = (uint32_t *)(keys + (size_t)nwarps * 32 * sw);     // nwarps*32
-    int *cnt = (int *)(ids + nwarps * 32);
-    for (int i = 0; i < sw; ++i) keys[((size_t)warp * 32 + lane) * sw + i] = t.key[i];
-    ids[warp * 32 + lane] = t.gid;
-    if (lane == 0) cnt[warp] = t.count;
-    __syncthreads();
-    if (warp == 0) {
-        WarpTop m;
-        warp_top_init(m, sw);
-        for (int w = 0; w < nwarps; ++w) {
-            uint64_t c[MAX_SORT_WORDS];
-            for (int i = 0; i < sw; ++i) c[i] = keys[((size_t)w * 32 + lane) * sw + i];
-            warp_top_offer(m, c, ids[w * 32 + lane], lane < cnt[w], k, sw);
-        }
-        for (int i = 0; i < sw; ++i) cand_keys[((size_t)bid * 32 + lane) * sw + i] = m.key[i];
-        cand_gids[bid * 32 + lane] = lane < m.count ? m.gid : 0xFFFFFFFFu;
-    }
+            encode_top_key<SW>(f, g, c);
+            return true;
+        },
+        cand_keys + (size_t)bid * 32 * SW, cand_gids + (size_t)bid * 32, nullptr);
 }
 
+// The best k of all CTAs' candidates -> sel_out, counts[3] = rows in sel_out.
+template <int SW>
+__device__ __forceinline__ void topk_final_body(const unsigned long long *cand_keys, const uint32_t *cand_gids,
+                                                uint32_t n_blocks, int k, uint32_t *sel_out,
+                                                unsigned long long *counts) {
+    block_topk<SW>(
+        (uint64_t)n_blocks * k, 0, TOPK_THREADS, k,
+        [&](uint64_t i, uint64_t(&c)[SW], uint32_t &g) {
+            const uint64_t e = (i / k) * 32 + (i % k);
+            g = cand_gids[e];
+#pragma unroll
+            for (int j = 0; j < SW; ++j) c[j] = cand_keys[e * SW + j];
+            return g != NO_ID;
+        },
+        nullptr, sel_out, counts + 3);
+}
+
+template <int SW>
 __global__ void __launch_bounds__(TOPK_THREADS) topk_partial_kernel(const __grid_constant__ DevFinal f, const uint32_t *gids,
                                                                     const unsigned long long *counts, int k,
                                                                     unsigned long long *cand_keys,
                                                                     uint32_t *cand_gids) {
-    topk_partial_body(f, gids, counts, k, cand_keys, cand_gids, blockIdx.x, gridDim.x);
+    topk_partial_body<SW>(f, gids, counts, k, cand_keys, cand_gids, blockIdx.x, gridDim.x);
 }
 
-__device__ __forceinline__ void topk_final_body(const DevFinal &f, const unsigned long long *cand_keys,
-                                                const uint32_t *cand_gids, uint32_t n_blocks, int k, uint32_t *sel_out,
-                                                unsigned long long *counts) {
-    const int sw = f.sort_words;
-    const int lane = threadIdx.x & 31;
-    WarpTop t;
-    warp_top_init(t, sw);
-    for (uint32_t b = 0; b < n_blocks; ++b) {
-        uint64_t c[MAX_SORT_WORDS];
-        for (int i = 0; i < sw; ++i) c[i] = cand_keys[((size_t)b * 32 + lane) * sw + i];
-        uint32_t g = cand_gids[b * 32 + lane];
-        warp_top_offer(t, c, g, g != 0xFFFFFFFFu, k, sw);
-    }
-    if (lane < t.count) sel_out[lane] = t.gid;
-    if (lane == 0) counts[3] = (unsigned long long)t.count;  // rows in `sel`
-}
-
-__global__ void topk_final_kernel(const __grid_constant__ DevFinal f, const unsigned long long *cand_keys, const uint32_t *cand_gids,
-                                  uint32_t n_blocks, int k, uint32_t *sel_out, unsigned long long *counts) {
-    topk_final_body(f, cand_keys, cand_gids, n_blocks, k, sel_out, counts);
+template <int SW>
+__global__ void __launch_bounds__(TOPK_THREADS) topk_final_kernel(const unsigned long long *cand_keys,
+                                                                  const uint32_t *cand_gids, uint32_t n_blocks, int k,
+                                                                  uint32_t *sel_out, unsigned long long *counts) {
+    topk_final_body<SW>(cand_keys, cand_gids, n_blocks, k, sel_out, counts);
 }
 
 // ------------------------------------------------------------ merge sort --
@@ -658,21 +712,26 @@ __global__ void __launch_bounds__(CPT_THREADS) compact_write_batch(const DevFina
     compact_write_body(f, occ_words(f.cap), b.block_counts, b.n_cpt_blocks, b.gids, b.counts, blockIdx.x);
 }
 
+// One launch per key-width class present in the batch: a query runs in the
+// launch of its own class (its candidate buffers are sized for that class).
+template <int SW>
 __global__ void __launch_bounds__(TOPK_THREADS) topk_partial_batch(const DevFinal *fs, const DevFinalBufs *bs) {
     const DevFinalBufs &b = bs[blockIdx.y];
-    if (b.rank != 1 || blockIdx.x >= b.n_cand_blocks) return;
-    topk_partial_body(fs[blockIdx.y], b.gids, b.counts, (int)b.k, b.cand_keys, b.cand_gids, blockIdx.x,
-                      b.n_cand_blocks);
+    const DevFinal &f = fs[blockIdx.y];
+    if (b.rank != 1 || topk_width(f.sort_words) != SW || blockIdx.x >= b.n_cand_blocks) return;
+    topk_partial_body<SW>(f, b.gids, b.counts, (int)b.k, b.cand_keys, b.cand_gids, blockIdx.x, b.n_cand_blocks);
 }
 
-__global__ void topk_final_batch(const DevFinal *fs, const DevFinalBufs *bs) {
+// do_all: this launch also sets the selection size of the all-groups queries.
+template <int SW>
+__global__ void __launch_bounds__(TOPK_THREADS) topk_final_batch(const DevFinal *fs, const DevFinalBufs *bs, int do_all) {
     const DevFinalBufs &b = bs[blockIdx.y];
     if (b.rank == 0) {
-        if (threadIdx.x == 0) b.counts[3] = b.counts[1];
+        if (do_all && threadIdx.x == 0) b.counts[3] = b.counts[1];
         return;
     }
-    if (b.rank != 1) return;
-    topk_final_body(fs[blockIdx.y], b.cand_keys, b.cand_gids, b.n_cand_blocks, (int)b.k, b.sel, b.counts);
+    if (b.rank != 1 || topk_width(fs[blockIdx.y].sort_words) != SW) return;
+    topk_final_body<SW>(b.cand_keys, b.cand_gids, b.n_cand_blocks, (int)b.k, b.sel, b.counts);
 }
 
 __global__ void gather_batch(const DevFinal *fs, const DevFinalBufs *bs) {
@@ -723,13 +782,23 @@ cudaError_t launch_compact(const DevFinal &f, uint32_t *block_counts, uint32_t n
     return cudaGetLastError();
 }
 
+template <int SW>
+static void launch_topk_w(const DevFinal &f, const uint32_t *gids, unsigned long long *counts, uint32_t k,
+                          unsigned long long *cand_keys, uint32_t *cand_gids, uint32_t n_cand_blocks,
+                          uint32_t *sel_out, cudaStream_t s) {
+    topk_partial_kernel<SW><<<n_cand_blocks, TOPK_THREADS, 0, s>>>(f, gids, counts, (int)k, cand_keys, cand_gids);
+    topk_final_kernel<SW><<<1, TOPK_THREADS, 0, s>>>(cand_keys, cand_gids, n_cand_blocks, (int)k, sel_out, counts);
+}
+
 cudaError_t launch_topk(const DevFinal &f, const uint32_t *gids, unsigned long long *counts, uint32_t k,
                         unsigned long long *cand_keys, uint32_t *cand_gids, uint32_t n_cand_blocks,
                         uint32_t *sel_out, cudaStream_t s) {
-    const int nwarps = TOPK_THREADS / 32;
-    size_t smem = (size_t)nwarps * 32 * f.sort_words * 8 + nwarps * 32 * 4 + nwarps * 4;
-    topk_partial_kernel<<<n_cand_blocks, TOPK_THREADS, smem, s>>>(f, gids, counts, (int)k, cand_keys, cand_gids);
-    topk_final_kernel<<<1, 32, 0, s>>>(f, cand_keys, cand_gids, n_cand_blocks, (int)k, sel_out, counts);
+    switch (topk_width(f.sort_words)) {
+        case 4: launch_topk_w<4>(f, gids, counts, k, cand_keys, cand_gids, n_cand_blocks, sel_out, s); break;
+        case 6: launch_topk_w<6>(f, gids, counts, k, cand_keys, cand_gids, n_cand_blocks, sel_out, s); break;
+        case 8: launch_topk_w<8>(f, gids, counts, k, cand_keys, cand_gids, n_cand_blocks, sel_out, s); break;
+        default: launch_topk_w<14>(f, gids, counts, k, cand_keys, cand_gids, n_cand_blocks, sel_out, s); break;
+    }
     return cudaGetLastError();
 }
 
@@ -780,18 +849,35 @@ cudaError_t launch_clear(unsigned long long *table, uint64_t cap, int32_t slot_w
 }
 
 cudaError_t launch_finalize_batch(const DevFinal *fs, const DevFinalBufs *bs, uint32_t n_queries,
-                                  uint32_t max_cpt_blocks, uint32_t max_cand_blocks, int max_sort_words,
-                                  bool any_topk, uint64_t max_rows, uint64_t max_words, cudaStream_t s) {
+                                  uint32_t max_cpt_blocks, uint32_t max_cand_blocks, uint32_t topk_widths,
+                                  uint64_t max_rows, uint64_t max_words, cudaStream_t s) {
     if (n_queries == 0) return cudaSuccess;
     dim3 gc(std::max<uint32_t>(1, max_cpt_blocks), n_queries);
     compact_count_batch<<<gc, CPT_THREADS, 0, s>>>(fs, bs);
     compact_write_batch<<<gc, CPT_THREADS, 0, s>>>(fs, bs);
-    if (any_topk) {
-        const int nwarps = TOPK_THREADS / 32;
-        size_t smem = (size_t)nwarps * 32 * max_sort_words * 8 + nwarps * 32 * 4 + nwarps * 4;
-        topk_partial_batch<<<dim3(std::max<uint32_t>(1, max_cand_blocks), n_queries), TOPK_THREADS, smem, s>>>(fs, bs);
+    const dim3 gp(std::max<uint32_t>(1, max_cand_blocks), n_queries), gf(1, n_queries);
+    int do_all = 1;
+    if (topk_widths & TOPK_W4) {
+        topk_partial_batch<4><<<gp, TOPK_THREADS, 0, s>>>(fs, bs);
+        topk_final_batch<4><<<gf, TOPK_THREADS, 0, s>>>(fs, bs, do_all);
+        do_all = 0;
     }
-    topk_final_batch<<<dim3(1, n_queries), 32, 0, s>>>(fs, bs);
+    if (topk_widths & TOPK_W6) {
+        topk_partial_batch<6><<<gp, TOPK_THREADS, 0, s>>>(fs, bs);
+        topk_final_batch<6><<<gf, TOPK_THREADS, 0, s>>>(fs, bs, do_all);
+        do_all = 0;
+    }
+    if (topk_widths & TOPK_W8) {
+        topk_partial_batch<8><<<gp, TOPK_THREADS, 0, s>>>(fs, bs);
+        topk_final_batch<8><<<gf, TOPK_THREADS, 0, s>>>(fs, bs, do_all);
+        do_all = 0;
+    }
+    if (topk_widths & TOPK_W14) {
+        topk_partial_batch<14><<<gp, TOPK_THREADS, 0, s>>>(fs, bs);
+        topk_final_batch<14><<<gf, TOPK_THREADS, 0, s>>>(fs, bs, do_all);
+        do_all = 0;
+    }
+    if (do_all) topk_final_batch<4><<<gf, 32, 0, s>>>(fs, bs, 1);
     unsigned gx = (unsigned)std::min<uint64_t>(std::max<uint64_t>(1, (max_rows + 255) / 256), 64);
     gather_batch<<<dim3(gx, n_queries), 256, 0, s>>>(fs, bs);
     pack_batch<<<dim3(1, n_queries), 256, 0, s>>>(bs);

@@ -583,6 +583,7 @@ __device__ __forceinline__ uint32_t filter_range(const DevQuery &q, uint64_t row
 template <int NA>
 struct GenericFold {
     using Row = RowVals<NA>;
+    static constexpr int LOOKAHEAD = 1;  // batches gathered before folding
     __device__ __forceinline__ static void load(const DevQuery &q, uint64_t r, bool me, Row &rv) {
         load_row<NA>(q, r, me, rv);
     }
@@ -601,6 +602,11 @@ template <int KM, int K0, int K1, int K2, int K3>
 struct FastFold {
     static constexpr int NA = (K0 != AK_NONE) + (K1 != AK_NONE) + (K2 != AK_NONE) + (K3 != AK_NONE);
     static constexpr int NV = NA > 0 ? NA : 1;
+    // batches whose gathers are all in flight before the first folds; the
+    // rows stay in registers (64 per thread at two CTAs per SM), so the depth
+    // shrinks as a row grows
+    static constexpr int ROW_REGS = (KM == 1 ? 2 : 4) + 2 * NV;
+    static constexpr int LOOKAHEAD = ROW_REGS <= 6 ? 4 : ROW_REGS <= 8 ? 2 : 1;
     __host__ __device__ static constexpr int kind(int a) { return a == 0 ? K0 : a == 1 ? K1 : a == 2 ? K2 : K3; }
     __host__ __device__ static constexpr bool is_f(int a) {
         return kind(a) == AK_SUM_F64 || kind(a) == AK_MIN_F || kind(a) == AK_MAX_F;
@@ -643,7 +649,7 @@ struct FastFold {
         }
     }
 
-    __device__ __noinline__ static void fold(const DevQuery &q, const ScanSmem &sm, const Row &in, unsigned active) {
+    __device__ __noinline__ static void fold(const DevQuery &q, const ScanSmem &sm, const Row in, unsigned active) {
         const int lane = threadIdx.x & 31;
         const bool me = (active >> lane) & 1u;
         uint64_t val[NV];
@@ -793,29 +799,28 @@ __device__ __forceinline__ void scan_chunk(const DevQuery &q, const ScanSmem &sm
     chunk_rows(q, c, row0, row_end);
     if (row0 >= row_end) return;
     if (q.n_preds == 0 || !q.gather) {
-        // every row (or every filtered row in place): 32 consecutive rows per batch
-        typename P::Row cur, nxt;
-        uint64_t r = row0 + lane;
-        bool pass = r < row_end && (q.n_preds == 0 || [&] {
-                        for (int i = 0; i < q.n_preds; ++i)
-                            if (!pred_holds(q, q.preds[i], r)) return false;
-                        return true;
-                    }());
-        P::load(q, r, pass, cur);
-        unsigned act = __ballot_sync(FULL, pass);
-        for (uint64_t b = row0; b < row_end; b += 32) {
-            const uint64_t rn = b + 32 + lane;
-            const bool pn = rn < row_end && (q.n_preds == 0 || [&] {
-                                for (int i = 0; i < q.n_preds; ++i)
-                                    if (!pred_holds(q, q.preds[i], rn)) return false;
-                                return true;
-                            }());
-            P::load(q, rn, pn, nxt);
-            const unsigned actn = __ballot_sync(FULL, pn);
-            selected += (lane == 0) ? __popc(act) : 0;
-            if (act) P::fold(q, sm, cur, act);
-            cur = nxt;
-            act = actn;
+        // every row (or every filtered row in place): 32 consecutive rows per
+        // batch, LOOKAHEAD batches loaded before any of them folds
+        constexpr int L = P::LOOKAHEAD;
+        for (uint64_t base = row0; base < row_end; base += 32 * L) {
+            typename P::Row rows[L];
+            unsigned act[L];
+#pragma unroll
+            for (int j = 0; j < L; ++j) {
+                const uint64_t r = base + 32 * j + lane;
+                const bool pass = r < row_end && (q.n_preds == 0 || [&] {
+                                      for (int i = 0; i < q.n_preds; ++i)
+                                          if (!pred_holds(q, q.preds[i], r)) return false;
+                                      return true;
+                                  }());
+                P::load(q, r, pass, rows[j]);
+                act[j] = __ballot_sync(FULL, pass);
+            }
+#pragma unroll
+            for (int j = 0; j < L; ++j) {
+                selected += (lane == 0) ? __popc(act[j]) : 0;
+                if (act[j]) P::fold(q, sm, rows[j], act[j]);
+            }
         }
         return;
     }
@@ -854,14 +859,21 @@ __device__ __forceinline__ void scan_chunk(const DevQuery &q, const ScanSmem &sm
     __syncwarp();
     selected += (lane == 0) ? n : 0;
     if (n == 0) return;
-    typename P::Row cur, nxt;
-    P::load(q, row0 + list[lane < n ? lane : 0], lane < n, cur);
-    for (uint32_t i = 0; i < n; i += 32) {
-        const uint32_t j = i + 32 + lane;
-        P::load(q, row0 + list[j < n ? j : 0], j < n, nxt);
-        const uint32_t left = n - i;
-        P::fold(q, sm, cur, left >= 32 ? FULL : ((1u << left) - 1));
-        cur = nxt;
+    constexpr int L = P::LOOKAHEAD;
+    for (uint32_t i = 0; i < n; i += 32 * L) {
+        typename P::Row rows[L];
+#pragma unroll
+        for (int j = 0; j < L; ++j) {
+            const uint32_t s = i + 32 * j + lane;
+            P::load(q, row0 + list[s < n ? s : 0], s < n, rows[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < L; ++j) {
+            const uint32_t b = i + 32 * j;
+            if (b >= n) break;
+            const uint32_t left = n - b;
+            P::fold(q, sm, rows[j], left >= 32 ? FULL : ((1u << left) - 1));
+        }
     }
 }
 
