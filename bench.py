@@ -127,39 +127,15 @@ class ClockSampler:
 # ----------------------------------------------------------------- inputs --
 
 def make_inputs(workload: str, n: int, pinned: bool):
-    """Host columns of the workload (pinned torch tensors when asked)."""
-    import torch
+    from thindb_gb300 import workloads
 
-    def buf(count, dtype):
-        return torch.empty(count, dtype=dtype, pin_memory=pinned)
-
-    if workload == "filtered":
-        k, a, d = buf(n, torch.int64), buf(n, torch.int64), buf(n, torch.int32)
-        datagen.filtered_into(n, 2, datagen.FILTERED_KEYS, k.data_ptr(), a.data_ptr(), d.data_ptr())
-        return [("k", abi.BIGINT, k, 0), ("amount", abi.DECIMAL64, a, 2), ("d", abi.DATE, d, 0)]
-    if workload == "plain":
-        k, v = buf(n, torch.int64), buf(n, torch.int32)
-        datagen.lib().tdg_plain(n, 1, k.data_ptr(), v.data_ptr(), 0)
-        return [("k", abi.BIGINT, k, 0), ("v", abi.INT, v, 0)]
-    r, u, us, lat = buf(n, torch.int16), buf(n, torch.int32), buf(n, torch.int64), buf(n, torch.float64)
-    datagen.lib().tdg_distinct(n, 3, datagen.DISTINCT_USERS, r.data_ptr(), u.data_ptr(), us.data_ptr(),
-                               lat.data_ptr(), 0)
-    return [("region", abi.SMALLINT, r, 0), ("url", abi.DICT32, u, 0), ("user_id", abi.BIGINT, us, 0),
-            ("latency_ms", abi.DOUBLE, lat, 0)]
+    return workloads.table_inputs(workload, n, pinned)
 
 
 def make_request(workload: str, flags: int = 0, stream: int = 0):
-    from thindb_gb300.engine import AggSpec, Pred, Request, SortSpec
+    from thindb_gb300 import workloads
 
-    if workload == "filtered":
-        return Request(["k"], [AggSpec("count", None, "c"), AggSpec("sum", "amount", "s"),
-                               AggSpec("avg", "amount", "a")], [SortSpec("s", True)], limit=10,
-                       where=[Pred("d", "between", datagen.FILTER_LO, datagen.FILTER_HI)], flags=flags, stream=stream)
-    if workload == "plain":
-        return Request(["k"], [AggSpec("count", None, "c"), AggSpec("sum", "v", "s"), AggSpec("min", "v", "mn"),
-                               AggSpec("max", "v", "mx")], flags=flags, stream=stream)
-    return Request(["region", "url"], [AggSpec("count", None, "c"), AggSpec("count_distinct", "user_id", "u"),
-                                       AggSpec("sum", "latency_ms", "lat")], flags=flags, stream=stream)
+    return workloads.workload_request(workload, flags, stream)
 
 
 def rows_of(result: dict) -> list:
@@ -171,9 +147,9 @@ def rows_of(result: dict) -> list:
 
 
 def columns_of(inputs, ndv=None):
-    from thindb_gb300.engine import Column
+    from thindb_gb300 import workloads
 
-    return [Column(nm, ty, t, scale=sc, ndv_hint=(ndv or {}).get(nm, 0)) for nm, ty, t, sc in inputs]
+    return workloads.columns(inputs, ndv)
 
 
 # ------------------------------------------------------------ CPU legs --
@@ -338,6 +314,8 @@ def gpu_arm(args, wl):
             "config": {"workload": wl["name"], "rows": n, "l2": "inputs larger than L2 (no flush)",
                        "selectivity": st.rows_selected / max(1, st.rows_scanned), "groups": st.groups,
                        "route": "shared-memory" if st.route == 1 else "global table",
+                       "scan": "survivor gather" if st.flags & abi.STAT_GATHER else "dense",
+                       "tuned": bool(st.flags & abi.STAT_TUNED),
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
@@ -366,10 +344,7 @@ def batched_arm(args):
 
     n = args.rows or datagen.FILTERED_ROWS
     torch.cuda.set_device(0)
-    inputs = make_inputs("filtered", n, pinned=True)
-    k10, k1k, k1m = (torch.empty(n, dtype=torch.int32, pin_memory=True) for _ in range(3))
-    datagen.lib().tdg_extra_keys(n, 2, k10.data_ptr(), k1k.data_ptr(), k1m.data_ptr(), 0)
-    inputs += [("k10", abi.INT, k10, 0), ("k1k", abi.INT, k1k, 0), ("k1m", abi.INT, k1m, 0)]
+    inputs = make_inputs("batched", n, pinned=True)
     stream = torch.cuda.Stream()
     table = Table(columns_of(inputs), compute_ndv=True, stream=stream.cuda_stream)
     nq = args.queries
@@ -448,10 +423,7 @@ def served_arm(args):
         inp = make_inputs(wl, n, pinned=True)
         tables.append(Table(columns_of(inp), compute_ndv=True, stream=stream.cuda_stream))
         del inp
-    inp = make_inputs("filtered", n_filt, pinned=True)
-    k10, k1k, k1m = (torch.empty(n_filt, dtype=torch.int32, pin_memory=True) for _ in range(3))
-    datagen.lib().tdg_extra_keys(n_filt, 2, k10.data_ptr(), k1k.data_ptr(), k1m.data_ptr(), 0)
-    inp += [("k10", abi.INT, k10, 0), ("k1k", abi.INT, k1k, 0), ("k1m", abi.INT, k1m, 0)]
+    inp = make_inputs("batched", n_filt, pinned=True)
     tables.append(Table(columns_of(inp), compute_ndv=True, stream=stream.cuda_stream))
     del inp
     resident = torch.cuda.memory_allocated()  # torch's own; the tables live in the engine's allocations

@@ -225,10 +225,14 @@ typedef struct tgpu_request {
 #define TGPU_FLAG_TIMING 0x1
 /* Force the global-table route even when the groups fit a CTA's shared memory. */
 #define TGPU_FLAG_FORCE_GLOBAL 0x2
-/* Load every needed column densely instead of gathering only survivors. */
+/* Load every needed column densely instead of gathering only survivors
+ * (the default unless the WHERE is estimated to keep under 4% of the rows). */
 #define TGPU_FLAG_DENSE_SCAN 0x4
 /* Disable the in-warp __match_any_sync pre-combine (tuning / tests). */
 #define TGPU_FLAG_NO_WARP_COMBINE 0x8
+/* Gather only the survivors' keys and inputs (late materialisation) whatever
+ * the estimated selectivity. */
+#define TGPU_FLAG_GATHER_SCAN 0x10
 
 /* ----------------------------------------------------------------- output -- */
 
@@ -267,12 +271,15 @@ typedef struct tgpu_query_stats {
     uint32_t route;              /* 1 = shared-memory (lowcard) route, 2 = global table */
     uint32_t retries;            /* group-table regrowths */
     uint32_t kernel_launches;    /* kernels the last execute launched */
-    uint32_t reserved;
+    uint32_t flags;              /* TGPU_STAT_* */
     double scan_ms;              /* filter + group + fold kernel (TGPU_FLAG_TIMING) */
     double finalize_ms;          /* compaction + ranking + output gather */
     double total_ms;             /* whole execute on the device */
     uint64_t device_bytes;       /* workspace bytes held by the query */
 } tgpu_query_stats;
+
+#define TGPU_STAT_TUNED 0x1     /* settings came from the tuning table */
+#define TGPU_STAT_GATHER 0x2    /* survivors gathered (late materialisation) */
 
 /* -------------------------------------------------------------- the API -- */
 
@@ -425,6 +432,43 @@ typedef struct tgpu_load_report {
 } tgpu_load_report;
 
 tgpu_status tgpu_server_run_load(tgpu_server *s, const tgpu_load_spec *spec, tgpu_load_report *out);
+
+/* ----------------------------------------------------------------- tuning -- */
+
+/* Measured engine settings per request shape.  thinDB fixes its engine knobs
+ * (scan tile rows, route block rows, bucket count) as defaults overridable from
+ * the environment (v2_group_topn_engine.zig:25-33, :521-626 paramsFromEnv);
+ * here an autotuner (thindb_gb300/autotune.py) measures them per shape class
+ * and installs the table with tgpu_tuning_set.  A request that sets
+ * chunk_rows, cache_slots, table_load_pct, a scan-mode flag or
+ * TGPU_FLAG_NO_TUNING keeps its own settings. */
+#define TGPU_FLAG_NO_TUNING 0x20
+
+typedef struct tgpu_shape {
+    int32_t key_words;    /* packed key words: 1 or 2 */
+    int32_t fold;         /* compiled fold signature, -1 = interpreter */
+    int32_t n_aggs;       /* aggregates requested */
+    int32_t distinct;     /* 1 if any COUNT(DISTINCT) */
+    int32_t filtered;     /* 1 if a WHERE is present */
+    int32_t sel_log2;     /* floor(log2(estimated kept fraction)); 0 without WHERE */
+    int32_t groups_log2;  /* ceil(log2(estimated groups)) */
+    int32_t batched;      /* 1 inside tgpu_batch_create */
+} tgpu_shape;
+
+typedef struct tgpu_tuning {
+    tgpu_shape shape;
+    int32_t chunk_rows;      /* 0 = built-in rule */
+    int32_t cache_slots;     /* 0 = built-in rule, -1 = no shared-memory table */
+    int32_t table_load_pct;  /* 0 = 50 */
+    int32_t flags;           /* TGPU_FLAG_DENSE_SCAN / _GATHER_SCAN / _NO_WARP_COMBINE */
+} tgpu_tuning;
+
+/* The shape class `req` falls in on `table` (plans the request; allocates nothing). */
+tgpu_status tgpu_request_shape(tgpu_table *table, const tgpu_request *req, int32_t batched, tgpu_shape *out);
+/* Replace the process-wide tuning table (n = 0 clears it). */
+tgpu_status tgpu_tuning_set(const tgpu_tuning *entries, uint32_t n);
+/* Copy up to `cap` entries out; returns the table size. */
+uint32_t tgpu_tuning_get(tgpu_tuning *entries, uint32_t cap);
 
 /* ------------------------------------------------- allocation-free call -- */
 

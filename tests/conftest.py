@@ -3,6 +3,10 @@ import sys
 
 import pytest
 
+# Tests choose their engine settings explicitly; the measured tuning table is
+# exercised by tests/test_gpu_tuning.py.
+os.environ.setdefault("THINDB_GPU_TUNING", "off")
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 for p in (ROOT, os.path.join(ROOT, "tests"), os.path.join(ROOT, "tests", "golden")):
     if p not in sys.path:

@@ -52,6 +52,8 @@ def test_struct_sizes_match_c_layout():
     assert C.sizeof(abi.OutputColumn) == 80
     assert C.sizeof(abi.QueryStats) == 104
     assert C.sizeof(abi.Batch) == 40
+    assert C.sizeof(abi.Shape) == 32
+    assert C.sizeof(abi.Tuning) == 48
 
 
 def test_no_device_fails_loudly():
@@ -68,3 +70,50 @@ def test_no_device_fails_loudly():
     with pytest.raises(engine.EngineError) as ei:
         engine.Table(cols)
     assert ei.value.status in (abi.ERR_NO_DEVICE, abi.ERR_CUDA)
+
+
+def test_tuning_table_round_trip_and_validation():
+    """tgpu_tuning_set / _get hold the table on the host (no device work)."""
+    lib = engine.lib()
+    saved = engine.tuning_entries()
+    try:
+        arr = (abi.Tuning * 2)()
+        arr[0].shape.key_words, arr[0].shape.fold, arr[0].shape.groups_log2 = 1, 3, 21
+        arr[0].chunk_rows, arr[0].cache_slots, arr[0].table_load_pct = 1024, -1, 25
+        arr[0].flags = abi.FLAG_GATHER_SCAN
+        arr[1].shape.batched, arr[1].chunk_rows = 1, 4096
+        assert lib.tgpu_tuning_set(arr, 2) == abi.OK
+        got = engine.tuning_entries()
+        assert len(got) == 2
+        assert got[0]["shape"]["groups_log2"] == 21 and got[0]["cache_slots"] == -1
+        assert got[1]["shape"]["batched"] == 1 and got[1]["chunk_rows"] == 4096
+        bad = (abi.Tuning * 1)()
+        bad[0].chunk_rows = 300  # not a multiple of 256
+        assert lib.tgpu_tuning_set(bad, 1) == abi.ERR_INVALID_ARGUMENT
+        assert len(engine.tuning_entries()) == 2  # a rejected table leaves the old one
+        engine.clear_tuning()
+        assert engine.tuning_entries() == []
+    finally:
+        arr = (abi.Tuning * max(1, len(saved)))()
+        lib.tgpu_tuning_set(arr, 0)
+        if saved:
+            import json
+            import tempfile
+
+            with tempfile.NamedTemporaryFile("w", suffix=".json", delete=False) as f:
+                json.dump({"entries": saved}, f)
+            engine.load_tuning(f.name)
+            os.unlink(f.name)
+
+
+def test_committed_tuning_table_parses():
+    """The measured table that ships with the package is well formed."""
+    import json
+
+    if not os.path.exists(engine.TUNING_PATH):
+        pytest.skip("no tuning table committed")
+    doc = json.load(open(engine.TUNING_PATH))
+    fields = {f for f, _ in abi.Shape._fields_}
+    for e in doc["entries"]:
+        assert set(e["shape"]) == fields
+        assert e["chunk_rows"] % 256 == 0 and e["table_load_pct"] in (0, 25, 50, 70)

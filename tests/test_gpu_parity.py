@@ -82,7 +82,8 @@ FILTER = [Pred("d", "between", datagen.FILTER_LO, datagen.FILTER_HI)]
 C2_AGGS = [AggSpec("count", None, "c"), AggSpec("sum", "amount", "s"), AggSpec("avg", "amount", "a")]
 
 
-@pytest.mark.parametrize("flags", [0, abi.FLAG_DENSE_SCAN, abi.FLAG_NO_WARP_COMBINE, abi.FLAG_FORCE_GLOBAL])
+@pytest.mark.parametrize("flags", [0, abi.FLAG_DENSE_SCAN, abi.FLAG_GATHER_SCAN, abi.FLAG_NO_WARP_COMBINE,
+                                   abi.FLAG_FORCE_GLOBAL])
 def test_filtered_top10(flags):
     cols = filtered_cols(2_000_000, 200_000)
     req = Request(["k"], C2_AGGS, [SortSpec("s", True)], limit=10, where=FILTER, flags=flags)

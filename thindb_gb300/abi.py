@@ -43,6 +43,10 @@ FLAG_TIMING = 0x1
 FLAG_FORCE_GLOBAL = 0x2
 FLAG_DENSE_SCAN = 0x4
 FLAG_NO_WARP_COMBINE = 0x8
+FLAG_GATHER_SCAN = 0x10
+FLAG_NO_TUNING = 0x20
+STAT_TUNED = 0x1
+STAT_GATHER = 0x2
 
 
 class ColumnDesc(C.Structure):
@@ -101,7 +105,7 @@ class QueryStats(C.Structure):
     _fields_ = [("rows_scanned", C.c_uint64), ("rows_selected", C.c_uint64), ("groups", C.c_uint64),
                 ("result_rows", C.c_uint64), ("table_capacity", C.c_uint64), ("distinct_capacity", C.c_uint64),
                 ("row_groups_total", C.c_uint32), ("row_groups_pruned", C.c_uint32), ("route", C.c_uint32),
-                ("retries", C.c_uint32), ("kernel_launches", C.c_uint32), ("reserved", C.c_uint32),
+                ("retries", C.c_uint32), ("kernel_launches", C.c_uint32), ("flags", C.c_uint32),
                 ("scan_ms", C.c_double), ("finalize_ms", C.c_double), ("total_ms", C.c_double),
                 ("device_bytes", C.c_uint64)]
 
@@ -180,3 +184,24 @@ SIGNATURES += [
 class BatchStats(C.Structure):
     _fields_ = [("n_queries", C.c_uint32), ("kernel_launches", C.c_uint32), ("graph", C.c_uint32),
                 ("rerun_queries", C.c_uint32), ("work_items", C.c_uint64), ("total_ms", C.c_double)]
+
+
+class Shape(C.Structure):
+    _fields_ = [("key_words", C.c_int32), ("fold", C.c_int32), ("n_aggs", C.c_int32), ("distinct", C.c_int32),
+                ("filtered", C.c_int32), ("sel_log2", C.c_int32), ("groups_log2", C.c_int32),
+                ("batched", C.c_int32)]
+
+    def as_dict(self):
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
+
+
+class Tuning(C.Structure):
+    _fields_ = [("shape", Shape), ("chunk_rows", C.c_int32), ("cache_slots", C.c_int32),
+                ("table_load_pct", C.c_int32), ("flags", C.c_int32)]
+
+
+SIGNATURES += [
+    ("tgpu_request_shape", C.c_int, [C.c_void_p, C.POINTER(Request), C.c_int32, C.POINTER(Shape)]),
+    ("tgpu_tuning_set", C.c_int, [C.POINTER(Tuning), C.c_uint32]),
+    ("tgpu_tuning_get", C.c_uint32, [C.POINTER(Tuning), C.c_uint32]),
+]

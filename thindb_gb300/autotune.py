@@ -1,0 +1,218 @@
+"""Autotuner: measures the engine's settings per request shape and writes the
+tuning table the library installs at load (thindb_gb300/tuning/gb300.json).
+
+thinDB fixes its engine knobs as defaults overridable from the environment
+(v2_group_topn_engine.zig:25-33: DOP, bucket count, scan tile row groups,
+route block rows, raw chunk rows; :521-626 paramsFromEnv).  This engine's
+knobs are
+
+    chunk_rows      rows per warp chunk (the scan tile)
+    cache_slots     shared-memory table slots per CTA, -1 = none (the
+                    pre-aggregation tier that takes the place of the bucket
+                    partition: hot keys fold on chip)
+    table_load_pct  global group-table load target (table sizing)
+    flags           scan mode: dense loads or survivor gathers; the in-warp
+                    pre-combine on or off
+
+For each shape class (tgpu_shape: key width, fold signature, aggregate count,
+distinct, selectivity class, group-count class, batched or not) a coordinate
+descent over the knobs keeps the setting with the lowest median device time
+whose results equal the built-in setting's (integers and keys bit for bit,
+FP64 sums within 1e-12 relative).  A batch is tuned as a whole (one setting
+for all of its queries), and every shape in it gets that setting.
+
+    python -m thindb_gb300.autotune [--out PATH] [--workloads plain,filtered,distinct,batched]
+"""
+from __future__ import annotations
+
+import argparse
+import dataclasses
+import json
+import statistics
+import sys
+import time
+
+import numpy as np
+
+from . import abi, datagen, workloads
+from .engine import QueryBatch, Request, Table, request_shape, try_build_group_topn
+
+KNOBS = {
+    "flags": [0, abi.FLAG_DENSE_SCAN, abi.FLAG_GATHER_SCAN, abi.FLAG_NO_WARP_COMBINE],
+    "chunk_rows": [0, 512, 1024, 2048, 4096],
+    "cache_slots": [0, -1, 256, 1024, 4096],
+    "table_load_pct": [0, 25, 70],
+}
+DEFAULT = {"flags": 0, "chunk_rows": 0, "cache_slots": 0, "table_load_pct": 0}
+GAIN = 0.97  # a setting must beat the current best by 3% to replace it
+
+
+def _with(req: Request, knobs: dict) -> Request:
+    return dataclasses.replace(req, chunk_rows=knobs["chunk_rows"], cache_slots=knobs["cache_slots"],
+                               table_load_pct=knobs["table_load_pct"],
+                               flags=req.flags | knobs["flags"] | abi.FLAG_TIMING | abi.FLAG_NO_TUNING)
+
+
+def _same(a: dict, b: dict) -> bool:
+    """Results equal: exact, except FP64 values within 1e-12 relative."""
+    if a.keys() != b.keys():
+        return False
+    for name in a:
+        va, oka = a[name]
+        vb, okb = b[name]
+        if (oka is None) != (okb is None) or (oka is not None and not np.array_equal(oka, okb)):
+            return False
+        if va.shape != vb.shape:
+            return False
+        if va.dtype.kind == "f":
+            if not np.allclose(va, vb, rtol=1e-12, atol=0.0, equal_nan=True):
+                return False
+        elif not np.array_equal(va, vb):
+            return False
+    return True
+
+
+def _sorted_result(res: dict) -> dict:
+    """A result in a canonical row order (all-groups results come in table order)."""
+    keys = [np.asarray(v).reshape(len(v), -1) for v, _ in res.values()]
+    if not keys or len(keys[0]) == 0:
+        return res
+    order = np.lexsort(tuple(k[:, j] for k in reversed(keys) for j in reversed(range(k.shape[1]))))
+    return {n: (np.asarray(v)[order], None if ok is None else np.asarray(ok)[order]) for n, (v, ok) in res.items()}
+
+
+def time_query(table: Table, req: Request, knobs: dict, reps: int):
+    """(median device ms, result) of `req` run with `knobs`; None if it fails."""
+    try:
+        q = try_build_group_topn(table, _with(req, knobs))
+    except Exception:
+        return None
+    if q is None:
+        return None
+    try:
+        times = []
+        res = None
+        for i in range(reps + 1):
+            q.execute()
+            q.synchronize()
+            if i:
+                times.append(q.stats().total_ms)
+            res = q.collect()
+        return statistics.median(times), _sorted_result(res)
+    except Exception:
+        return None
+    finally:
+        q.close()
+
+
+def time_batch(table: Table, reqs: list, knobs: dict, reps: int, stream: int):
+    try:
+        b = QueryBatch(table, [_with(r, knobs) for r in reqs], graph=True, stream=stream)
+    except Exception:
+        return None
+    try:
+        times = []
+        for i in range(reps + 1):
+            b.execute()
+            b.synchronize()
+            if i:
+                times.append(b.stats().total_ms)
+        res = [_sorted_result(b.collect(i)) for i in range(len(reqs))]
+        return statistics.median(times), res
+    except Exception:
+        return None
+    finally:
+        b.close()
+
+
+def descend(measure, same, log=print, rounds: int = 2):
+    """Coordinate descent over KNOBS from the built-in setting."""
+    base = measure(DEFAULT)
+    if base is None:
+        raise RuntimeError("the built-in setting failed")
+    best, (best_ms, ref) = dict(DEFAULT), base
+    default_ms = best_ms
+    log(f"  built-in: {best_ms:.3f} ms")
+    for _ in range(rounds):
+        improved = False
+        for knob, values in KNOBS.items():
+            for v in values:
+                if v == best[knob]:
+                    continue
+                cand = dict(best, **{knob: v})
+                r = measure(cand)
+                if r is None or not same(r[1], ref):
+                    log(f"  {cand}: rejected")
+                    continue
+                log(f"  {cand}: {r[0]:.3f} ms")
+                if r[0] < best_ms * GAIN:
+                    best, best_ms, improved = cand, r[0], True
+        if not improved:
+            break
+    return best, default_ms, best_ms
+
+
+def tune_workload(name: str, n: int, stream: int, reps: int, log=print) -> list:
+    """Tuning entries for one workload's shapes."""
+    inputs = workloads.table_inputs(name, n, pinned=True)
+    table = Table(workloads.columns(inputs), compute_ndv=True, stream=stream)
+    del inputs
+    entries = []
+    try:
+        if name == "batched":
+            reqs = workloads.batched_requests(256, seed=4)
+            for r in reqs:
+                r.stream = stream
+            best, d_ms, b_ms = descend(lambda k: time_batch(table, reqs, k, reps, stream),
+                                       lambda a, b: all(_same(x, y) for x, y in zip(a, b)), log)
+            shapes = {json.dumps(request_shape(table, r, batched=True), sort_keys=True) for r in reqs}
+            for sh in sorted(shapes):
+                entries.append({"shape": json.loads(sh), **best, "workload": "batched (256 queries, tuned as one)",
+                                "ms_builtin": d_ms, "ms_tuned": b_ms})
+        else:
+            req = workloads.workload_request(name, stream=stream)
+            best, d_ms, b_ms = descend(lambda k: time_query(table, req, k, reps), _same, log)
+            entries.append({"shape": request_shape(table, req), **best, "workload": name,
+                            "ms_builtin": d_ms, "ms_tuned": b_ms})
+    finally:
+        table.close()
+    return entries
+
+
+def main(argv=None) -> int:
+    import torch
+
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--out", default=None, help="tuning JSON to write (default: print only)")
+    ap.add_argument("--workloads", default="plain,filtered,distinct,batched")
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--scale", type=float, default=1.0, help="fraction of each workload's full row count")
+    args = ap.parse_args(argv)
+    sizes = {"plain": datagen.PLAIN_ROWS, "filtered": datagen.FILTERED_ROWS, "distinct": datagen.DISTINCT_ROWS,
+             "batched": datagen.FILTERED_ROWS}
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    t0 = time.time()
+    entries = []
+    for name in args.workloads.split(","):
+        n = max(1 << 16, int(sizes[name] * args.scale))
+        print(f"{name}: {n:,} rows", file=sys.stderr, flush=True)
+        entries += tune_workload(name, n, stream.cuda_stream, args.reps,
+                                 log=lambda m: print(m, file=sys.stderr, flush=True))
+    doc = {
+        "device": torch.cuda.get_device_name(0),
+        "generated_by": "python -m thindb_gb300.autotune " + " ".join(argv if argv is not None else sys.argv[1:]),
+        "seconds": round(time.time() - t0, 1),
+        "knobs": KNOBS,
+        "entries": entries,
+    }
+    text = json.dumps(doc, indent=1)
+    if args.out:
+        with open(args.out, "w") as f:
+            f.write(text + "\n")
+    print(text)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

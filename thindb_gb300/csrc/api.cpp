@@ -78,6 +78,8 @@ uint64_t next_pow2(uint64_t x) {
     while (p < x) p <<= 1;
     return p;
 }
+uint64_t ceil_div(uint64_t a, uint64_t b) { return (a + b - 1) / b; }
+uint64_t round_up(uint64_t a, uint64_t b) { return ceil_div(a, b) * b; }
 
 // ------------------------------------------------------------ device --
 
@@ -261,6 +263,7 @@ struct tgpu_query {
     int cache_req = 0;            // requested shared-memory slots (0 auto, -1 off)
     uint32_t chunk_req = 0;       // requested rows per warp chunk (0 auto)
     int load_pct = 50;            // group-table load target
+    bool tuned = false;           // settings taken from the tuning table
     // workspace
     Buffer table_buf, occ_buf;
     std::vector<Buffer> dset_bufs;
@@ -737,7 +740,13 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     df.cap = cap;
 
     dq.warp_combine = (q->flags & TGPU_FLAG_NO_WARP_COMBINE) ? 0 : 1;
-    dq.gather = (dq.n_preds > 0 && !(q->flags & TGPU_FLAG_DENSE_SCAN)) ? 1 : 0;
+    // late materialisation pays only when the survivors leave most 128-byte
+    // lines of the key/input columns untouched, i.e. at low selectivity
+    {
+        const bool sparse = q->sel_est * 25 < std::max<uint64_t>(1, q->rows_scanned);  // < 4% estimated
+        dq.gather = dq.n_preds > 0 && !(q->flags & TGPU_FLAG_DENSE_SCAN) &&
+                    ((q->flags & TGPU_FLAG_GATHER_SCAN) || sparse);
+    }
 
     // chunking: about eight chunks per warp of a two-CTA-per-SM grid
     {
@@ -1019,6 +1028,7 @@ tgpu_status finish(tgpu_query *q) {
     s.route = (uint32_t)q->route;
     s.retries = q->retries;
     s.kernel_launches = q->launches;
+    s.flags = (q->tuned ? TGPU_STAT_TUNED : 0) | (q->dq.gather ? TGPU_STAT_GATHER : 0);
     s.device_bytes = q->table_buf.bytes + q->occ_buf.bytes + q->scratch_bytes;
     for (auto &b : q->dset_bufs) s.device_bytes += b.bytes;
     if (q->flags & TGPU_FLAG_TIMING) {
@@ -1033,7 +1043,49 @@ tgpu_status finish(tgpu_query *q) {
     return TGPU_OK;
 }
 
+// ---------------------------------------------------------------- tuning --
+
+std::mutex g_tuning_mu;
+std::vector<tgpu_tuning> g_tuning;
+
+// The shape class of a planned query (the key of the tuning table).
+tgpu_shape shape_of(const tgpu_query *q, const tgpu_request *req, int batched) {
+    tgpu_shape s{};
+    s.key_words = q->dq.key_words;
+    s.fold = fast_fold_id(q->dq);
+    s.n_aggs = (int32_t)req->n_aggs;
+    s.distinct = q->dq.n_dsets > 0;
+    s.filtered = req->n_where > 0;
+    s.sel_log2 = 0;
+    if (req->n_where > 0 && q->rows_scanned > 0) {
+        const double f = (double)std::max<uint64_t>(1, q->sel_est) / (double)q->rows_scanned;
+        s.sel_log2 = std::max(-30, std::min(0, (int)std::floor(std::log2(f))));
+    }
+    s.groups_log2 = (int32_t)std::ceil(std::log2((double)std::max<uint64_t>(1, q->groups_est)));
+    s.batched = batched ? 1 : 0;
+    return s;
+}
+
+// Take the tuned settings of the query's shape unless the request chose its own.
+void apply_tuning(tgpu_query *q, const tgpu_request *req, int batched) {
+    const int own = TGPU_FLAG_DENSE_SCAN | TGPU_FLAG_GATHER_SCAN | TGPU_FLAG_NO_WARP_COMBINE | TGPU_FLAG_NO_TUNING;
+    if (req->chunk_rows || req->cache_slots || req->table_load_pct || (req->flags & own)) return;
+    const tgpu_shape s = shape_of(q, req, batched);
+    std::lock_guard<std::mutex> lk(g_tuning_mu);
+    for (const tgpu_tuning &t : g_tuning) {
+        if (std::memcmp(&t.shape, &s, sizeof(s)) != 0) continue;
+        q->chunk_req = (uint32_t)t.chunk_rows;
+        q->cache_req = t.cache_slots;
+        q->load_pct = t.table_load_pct ? t.table_load_pct : 50;
+        q->flags |= t.flags & (TGPU_FLAG_DENSE_SCAN | TGPU_FLAG_GATHER_SCAN | TGPU_FLAG_NO_WARP_COMBINE);
+        q->tuned = true;
+        return;
+    }
+}
+
 }  // namespace
+
+tgpu_status query_create(tgpu_table *table, const tgpu_request *req, int batched, tgpu_query **out);
 
 // ================================================================ C ABI ====
 
@@ -1163,6 +1215,12 @@ tgpu_status tgpu_table_info(const tgpu_table *t, int32_t column, uint64_t *n_row
 }
 
 tgpu_status tgpu_query_create(tgpu_table *table, const tgpu_request *req, tgpu_query **out) {
+    return query_create(table, req, 0, out);
+}
+
+}  // extern "C"
+
+tgpu_status query_create(tgpu_table *table, const tgpu_request *req, int batched, tgpu_query **out) {
     if (!table || !req || !out) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
     DeviceCtx *dev;
     tgpu_status st = device_ctx(&dev);
@@ -1185,6 +1243,7 @@ tgpu_status tgpu_query_create(tgpu_table *table, const tgpu_request *req, tgpu_q
     q->load_pct = req->table_load_pct ? req->table_load_pct : 50;
     st = plan_query(q.get(), table, req);
     if (st != TGPU_OK) return st;
+    apply_tuning(q.get(), req, batched);
     CU(cudaHostAlloc((void **)&q->h_cancel, sizeof(int), cudaHostAllocMapped));
     *q->h_cancel = 0;
     CU(cudaHostGetDevicePointer((void **)&q->d_cancel, q->h_cancel, 0));
@@ -1197,6 +1256,8 @@ tgpu_status tgpu_query_create(tgpu_table *table, const tgpu_request *req, tgpu_q
     *out = q.release();
     return TGPU_OK;
 }
+
+extern "C" {
 
 tgpu_status tgpu_query_output_schema(const tgpu_query *q, tgpu_output_column *cols, uint32_t cap, uint32_t *n) {
     if (!q) return fail(TGPU_ERR_INVALID_ARGUMENT, "null query");
@@ -1298,12 +1359,12 @@ struct tgpu_query_batch {
     std::vector<DevQuery> h_qs;
     std::vector<DevFinal> h_fs;
     std::vector<DevFinalBufs> h_bs;
-    std::vector<uint32_t> tile_start;
+    std::vector<uint2> items;               // {query, first chunk of a row group}, row group major
     void *dev = nullptr;                    // one allocation for every array below
     DevQuery *d_qs = nullptr;
     DevFinal *d_fs = nullptr;
     DevFinalBufs *d_bs = nullptr;
-    uint32_t *d_tile_start = nullptr;
+    uint2 *d_items = nullptr;               // own allocation
     unsigned int *d_ctrl = nullptr;         // [0] work counter, [1] status
     unsigned long long *d_counts = nullptr; // 8 per query
     unsigned int *d_qctrl = nullptr;        // 4 per query: tile counter, status
@@ -1333,6 +1394,7 @@ struct tgpu_query_batch {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         if (dev) cudaFree(dev);
+        if (d_items) cudaFree(d_items);
         if (h_counts) cudaFreeHost(h_counts);
         if (h_stage) cudaFreeHost(h_stage);
         if (h_cancel) cudaFreeHost(h_cancel);
@@ -1350,7 +1412,6 @@ tgpu_status batch_descriptors(tgpu_query_batch *b) {
     b->h_qs.resize(Q);
     b->h_fs.resize(Q);
     b->h_bs.resize(Q);
-    b->tile_start.assign(Q + 1, 0);
     b->max_aggs = 0;
     b->topk_widths = 0;
     b->smem = 0;
@@ -1385,6 +1446,15 @@ tgpu_status batch_descriptors(tgpu_query_batch *b) {
         q->d_counts = b->d_counts + 8 * (size_t)i;
         q->d_ctrl = b->d_qctrl + 4 * (size_t)i;
         DevQuery dq = q->dq;
+        // row-group aligned chunks: an item is the query's chunks of one row
+        // group, split evenly over the CTA's warps
+        dq.rg_list = q->d_rg_list;
+        dq.n_rg = (uint32_t)q->rg_list.size();
+        if (!dq.gather && !q->chunk_req)
+            dq.chunk_rows = (uint32_t)std::min<uint64_t>(4096, round_up(ceil_div(b->t->rg_rows, SCAN_WARPS), CHUNK_ALIGN));
+        dq.chunks_per_rg = (uint32_t)ceil_div(b->t->rg_rows, dq.chunk_rows);
+        dq.n_chunks = dq.n_rg * dq.chunks_per_rg;
+        dq.shared_scan = Q > 1;
         dq.tile_counter = q->d_ctrl;
         dq.status = q->d_ctrl + 1;
         dq.selected_rows = q->d_counts + 4;
@@ -1411,7 +1481,6 @@ tgpu_status batch_descriptors(tgpu_query_batch *b) {
         fb.pack_dst = fb.pack_rows ? b->d_stage + b->stage_off[i] : nullptr;
         fb.n_out = (uint32_t)q->schema.size();
         for (size_t c = 0; c < q->schema.size(); ++c) fb.out_bytes[c] = q->schema[c].elem_bytes;
-        b->tile_start[i + 1] = b->tile_start[i] + (dq.n_chunks + SCAN_WARPS - 1) / SCAN_WARPS;
         b->max_aggs = std::max(b->max_aggs, dq.n_aggs);
         if (fb.rank == 1) b->topk_widths |= topk_width_bit(q->df.sort_words);
         b->smem = std::max(b->smem, scan_smem_bytes(dq));
@@ -1422,17 +1491,32 @@ tgpu_status batch_descriptors(tgpu_query_batch *b) {
         b->any_distinct |= dq.n_dsets > 0;
         b->any_topk |= fb.rank == 1;
     }
+    if (!b->d_items) {
+        // row group major: every query that keeps row group g, then g + 1, ...
+        std::vector<size_t> pos(Q, 0);
+        for (uint32_t g = 0; g < b->t->n_rg; ++g)
+            for (uint32_t i = 0; i < Q; ++i) {
+                const std::vector<uint32_t> &rl = b->qs[i]->rg_list;
+                if (pos[i] < rl.size() && rl[pos[i]] == g) {
+                    b->items.push_back(make_uint2(i, (uint32_t)(pos[i] * b->h_qs[i].chunks_per_rg)));
+                    ++pos[i];
+                }
+            }
+        CU(cudaMalloc((void **)&b->d_items, sizeof(uint2) * std::max<size_t>(1, b->items.size())));
+        if (!b->items.empty())
+            CU(cudaMemcpyAsync(b->d_items, b->items.data(), sizeof(uint2) * b->items.size(), cudaMemcpyHostToDevice,
+                               b->stream));
+    }
     CU(cudaMemcpyAsync(b->d_qs, b->h_qs.data(), sizeof(DevQuery) * Q, cudaMemcpyHostToDevice, b->stream));
     CU(cudaMemcpyAsync(b->d_fs, b->h_fs.data(), sizeof(DevFinal) * Q, cudaMemcpyHostToDevice, b->stream));
     CU(cudaMemcpyAsync(b->d_bs, b->h_bs.data(), sizeof(DevFinalBufs) * Q, cudaMemcpyHostToDevice, b->stream));
-    CU(cudaMemcpyAsync(b->d_tile_start, b->tile_start.data(), 4 * (Q + 1), cudaMemcpyHostToDevice, b->stream));
     CU(cudaStreamSynchronize(b->stream));
     DeviceCtx *dev;
     tgpu_status st = device_ctx(&dev);
     if (st != TGPU_OK) return st;
     b->grid = batch_scan_grid(b->max_aggs, b->smem, dev->sms);
     b->descriptors_dirty = false;
-    b->stats.work_items = b->tile_start[Q];
+    b->stats.work_items = b->items.size();
     return TGPU_OK;
 }
 
@@ -1444,7 +1528,7 @@ tgpu_status batch_enqueue_work(tgpu_query_batch *b, bool capturing) {
     CU(cudaMemsetAsync(b->d_ctrl, 0, 8, s));
     CU(cudaMemsetAsync(b->d_counts, 0, 64 * (size_t)Q, s));
     CU(cudaMemsetAsync(b->d_qctrl, 0, 16 * (size_t)Q, s));
-    CU(launch_batch_scan(b->d_qs, b->d_tile_start, Q, b->max_aggs, b->smem, b->grid, b->d_ctrl,
+    CU(launch_batch_scan(b->d_qs, b->d_items, (uint32_t)b->items.size(), b->max_aggs, b->smem, b->grid,
                          (const volatile int *)b->d_cancel, b->d_ctrl + 1, s));
     CU(launch_finalize_batch(b->d_fs, b->d_bs, Q, b->max_cpt_blocks, b->max_cand_blocks, b->topk_widths,
                              b->max_rows, b->max_words, s));
@@ -1475,7 +1559,7 @@ tgpu_status tgpu_batch_create(tgpu_table *table, const tgpu_request *reqs, uint3
         tgpu_request r = reqs[i];
         r.stream = b->stream;
         tgpu_query *q = nullptr;
-        st = tgpu_query_create(table, &r, &q);
+        st = query_create(table, &r, 1, &q);
         if (st != TGPU_OK) return st;
         b->qs.push_back(q);
         if (q->rank == RANK_SORT) {
@@ -1490,13 +1574,12 @@ tgpu_status tgpu_batch_create(tgpu_table *table, const tgpu_request *reqs, uint3
         return o;
     };
     size_t o_qs = add(sizeof(DevQuery) * Q), o_fs = add(sizeof(DevFinal) * Q), o_bs = add(sizeof(DevFinalBufs) * Q),
-           o_ts = add(4 * (Q + 1)), o_ctrl = add(16), o_counts = add(64 * Q), o_qctrl = add(16 * Q);
+           o_ctrl = add(16), o_counts = add(64 * Q), o_qctrl = add(16 * Q);
     CU(cudaMalloc(&b->dev, off));
     char *base = (char *)b->dev;
     b->d_qs = (DevQuery *)(base + o_qs);
     b->d_fs = (DevFinal *)(base + o_fs);
     b->d_bs = (DevFinalBufs *)(base + o_bs);
-    b->d_tile_start = (uint32_t *)(base + o_ts);
     b->d_ctrl = (unsigned int *)(base + o_ctrl);
     b->d_counts = (unsigned long long *)(base + o_counts);
     b->d_qctrl = (unsigned int *)(base + o_qctrl);
@@ -1619,6 +1702,7 @@ tgpu_status tgpu_batch_synchronize(tgpu_query_batch *b) {
         q->stats.result_rows = c[2];
         q->stats.table_capacity = q->dq.cap;
         q->stats.route = (uint32_t)q->route;
+        q->stats.flags = (q->tuned ? TGPU_STAT_TUNED : 0) | (q->dq.gather ? TGPU_STAT_GATHER : 0);
     }
     return TGPU_OK;
 }
@@ -2161,6 +2245,45 @@ tgpu_status tgpu_server_run_load(tgpu_server *s, const tgpu_load_spec *spec, tgp
     for (double x : lat) sum += x;
     out->mean_ms = lat.empty() ? 0 : sum / lat.size();
     return TGPU_OK;
+}
+
+}  // extern "C"
+
+// ================================================================ tuning ==
+
+extern "C" {
+
+tgpu_status tgpu_request_shape(tgpu_table *table, const tgpu_request *req, int32_t batched, tgpu_shape *out) {
+    if (!table || !req || !out) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
+    std::unique_ptr<tgpu_query> q(new tgpu_query());
+    q->t = table;
+    q->flags = req->flags;
+    q->limit = req->limit;
+    q->offset = req->offset;
+    tgpu_status st = plan_query(q.get(), table, req);
+    if (st != TGPU_OK) return st;
+    *out = shape_of(q.get(), req, batched);
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_tuning_set(const tgpu_tuning *entries, uint32_t n) {
+    if (n && !entries) return fail(TGPU_ERR_INVALID_ARGUMENT, "null entries");
+    for (uint32_t i = 0; i < n; ++i) {
+        const tgpu_tuning &t = entries[i];
+        if (t.chunk_rows < 0 || t.chunk_rows % CHUNK_ALIGN != 0 || t.chunk_rows > 65536 ||
+            (t.cache_slots > 0 && (t.cache_slots & (t.cache_slots - 1))) || t.cache_slots < -1 ||
+            t.table_load_pct < 0 || t.table_load_pct > 90)
+            return fail(TGPU_ERR_INVALID_ARGUMENT, "tuning entry out of range");
+    }
+    std::lock_guard<std::mutex> lk(g_tuning_mu);
+    g_tuning.assign(entries, entries + n);
+    return TGPU_OK;
+}
+
+uint32_t tgpu_tuning_get(tgpu_tuning *entries, uint32_t cap) {
+    std::lock_guard<std::mutex> lk(g_tuning_mu);
+    for (uint32_t i = 0; entries && i < cap && i < g_tuning.size(); ++i) entries[i] = g_tuning[i];
+    return (uint32_t)g_tuning.size();
 }
 
 }  // extern "C"

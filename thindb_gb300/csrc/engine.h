@@ -98,7 +98,7 @@ struct DevQuery {
     uint32_t chunks_per_rg;
     uint32_t n_chunks;        // warp-sized units of work
     uint32_t chunk_rows;      // rows per chunk (multiple of 256)
-    uint32_t pad0;
+    uint32_t shared_scan;     // 1: other queries of a batch read the same rows (keep them in L2)
     // columns / predicates / key / aggregates
     DevCol cols[MAX_QCOLS];
     int32_t n_cols;
@@ -227,11 +227,11 @@ int scan_grid_size(const DevQuery &q, int device_sms);
 int fast_fold_id(const DevQuery &q);
 size_t scan_smem_bytes(const DevQuery &q);
 cudaError_t launch_scan(const DevQuery &q, int grid, cudaStream_t s);
-// many queries, one persistent kernel over (query, tile) work items
+// many queries, one persistent kernel over (query, row group) work items
 int batch_scan_grid(int max_aggs, size_t smem, int sms);
-cudaError_t launch_batch_scan(const DevQuery *qs, const uint32_t *tile_start, uint32_t n_queries, int max_aggs,
-                              size_t smem, int grid, unsigned int *work_counter, const volatile int *cancel,
-                              unsigned int *status, cudaStream_t s);
+// items[i] = {query, first chunk of one of its row groups}
+cudaError_t launch_batch_scan(const DevQuery *qs, const uint2 *items, uint32_t n_items, int max_aggs, size_t smem,
+                              int grid, const volatile int *cancel, unsigned int *status, cudaStream_t s);
 // compaction, top-k / all-groups selection, gather and clear for every query of a batch
 // topk_widths: TOPK_W* bits of the key-width classes of the batch's top-k queries
 cudaError_t launch_finalize_batch(const DevFinal *fs, const DevFinalBufs *bs, uint32_t n_queries,

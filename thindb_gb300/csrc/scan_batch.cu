@@ -6,37 +6,35 @@ namespace tgpu {
 
 namespace {
 
-// Many queries in one persistent kernel: work items are (query, tile of
-// SCAN_WARPS chunks) pairs, query-major.  CTA b takes items b, b + grid, ...;
-// all warps of a CTA work on one query's tile at a time, so the CTA's
-// shared-memory table belongs to that query until its next item moves on,
-// when the table is flushed.
+// Many queries in one persistent kernel.  A work item is (query, one row
+// group of that query's surviving row groups); the host lists the items row
+// group by row group, every query of a row group in turn, so the CTAs running
+// at any moment read the same few row groups and all but the first query of
+// each row group finds its columns in L2 (the table streams from HBM about
+// once per batch, not once per query).  CTA b takes items b, b + grid, ...;
+// its 16 warps split the item's chunks, and the CTA's shared-memory table
+// belongs to the item's query (flushed when the next item moves to another
+// query).
 template <int NA>
 __global__ void __launch_bounds__(SCAN_THREADS, NA <= 4 ? 2 : 1)
-    batch_scan_kernel(const DevQuery *__restrict__ qs, const uint32_t *__restrict__ tile_start, uint32_t n_queries,
-                      unsigned int *work_counter, const volatile int *cancel, unsigned int *batch_status) {
+    batch_scan_kernel(const DevQuery *__restrict__ qs, const uint2 *__restrict__ items, uint32_t n_items,
+                      const volatile int *cancel, unsigned int *batch_status) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t total = tile_start[n_queries];
-    (void)work_counter;
     int cur = -1;
-    uint32_t qi = 0;
     ScanSmem sm{};
     unsigned long long selected = 0;
     uint32_t k = 0;
     for (uint32_t item = blockIdx.x;; item += gridDim.x, ++k) {
-        bool stop = item >= total;
+        bool stop = item >= n_items;
         if (!stop && (k & 15) == 15 && cancel) {
             int c = 0;
             if (threadIdx.x == 0) c = *cancel;
             stop = __syncthreads_or(c) != 0;
             if (stop && threadIdx.x == 0) atomicOr(batch_status, ST_CANCELLED);
         }
-        int qn = -1;
-        if (!stop) {
-            while (qi + 1 < n_queries && tile_start[qi + 1] <= item) ++qi;  // items only grow
-            qn = (int)qi;
-        }
+        const uint2 it = stop ? make_uint2(0xFFFFFFFFu, 0u) : items[item];
+        const int qn = stop ? -1 : (int)it.x;
         if (qn != cur) {
             if (cur >= 0) {
                 const DevQuery &old = qs[cur];
@@ -52,10 +50,9 @@ __global__ void __launch_bounds__(SCAN_THREADS, NA <= 4 ? 2 : 1)
             cur = qn;
             __syncthreads();
         }
-        if (qn < 0) break;
         const DevQuery &q = qs[qn];
-        const uint32_t c = (item - tile_start[qn]) * SCAN_WARPS + warp;
-        if (c < q.n_chunks) scan_chunk_dispatch<NA>(q, sm, c, selected);
+        const uint32_t end = min(it.y + q.chunks_per_rg, q.n_chunks);
+        for (uint32_t c = it.y + warp; c < end; c += SCAN_WARPS) scan_chunk_dispatch<NA>(q, sm, c, selected);
     }
 }
 
@@ -77,17 +74,17 @@ int batch_scan_grid(int max_aggs, size_t smem, int sms) {
                                 : blocks_per_sm((const void *)batch_scan_kernel<16>, smem));
 }
 
-cudaError_t launch_batch_scan(const DevQuery *qs, const uint32_t *tile_start, uint32_t n_queries, int max_aggs,
-                              size_t smem, int grid, unsigned int *work_counter, const volatile int *cancel,
-                              unsigned int *status, cudaStream_t s) {
+cudaError_t launch_batch_scan(const DevQuery *qs, const uint2 *items, uint32_t n_items, int max_aggs, size_t smem,
+                              int grid, const volatile int *cancel, unsigned int *status, cudaStream_t s) {
+    if (n_items == 0) return cudaSuccess;
     if (max_aggs <= 4) {
         cudaError_t e = cudaFuncSetAttribute(batch_scan_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        batch_scan_kernel<4><<<grid, SCAN_THREADS, smem, s>>>(qs, tile_start, n_queries, work_counter, cancel, status);
+        batch_scan_kernel<4><<<grid, SCAN_THREADS, smem, s>>>(qs, items, n_items, cancel, status);
     } else {
         cudaError_t e = cudaFuncSetAttribute(batch_scan_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        batch_scan_kernel<16><<<grid, SCAN_THREADS, smem, s>>>(qs, tile_start, n_queries, work_counter, cancel, status);
+        batch_scan_kernel<16><<<grid, SCAN_THREADS, smem, s>>>(qs, items, n_items, cancel, status);
     }
     return cudaGetLastError();
 }

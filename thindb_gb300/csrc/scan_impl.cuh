@@ -61,15 +61,21 @@ __device__ __forceinline__ double col_f64(const DevCol &c, uint64_t r) {
     return __ldg((const double *)c.data + r);
 }
 
-// Streaming (evict-first) loads for the predicate columns: read once.
-__device__ __forceinline__ int64_t col_int_stream(const DevCol &c, uint64_t r) {
+// Predicate-column loads: streaming (evict-first) when the rows are read
+// once, default caching when other queries of a batch read them next.
+template <typename T>
+__device__ __forceinline__ T ld_pred(bool shared, const T *p) {
+    return shared ? __ldg(p) : __ldcs(p);
+}
+
+__device__ __forceinline__ int64_t col_int_stream(const DevCol &c, uint64_t r, bool shared) {
     switch (c.bytes) {
         case 1:
-            return c.type == TGPU_BOOLEAN ? (int64_t)__ldcs((const unsigned char *)c.data + r)
-                                          : (int64_t)(signed char)__ldcs((const signed char *)c.data + r);
-        case 2: return (int64_t)__ldcs((const short *)c.data + r);
-        case 4: return (int64_t)__ldcs((const int *)c.data + r);
-        default: return (int64_t)__ldcs((const long long *)c.data + r);
+            return c.type == TGPU_BOOLEAN ? (int64_t)ld_pred(shared, (const unsigned char *)c.data + r)
+                                          : (int64_t)ld_pred(shared, (const signed char *)c.data + r);
+        case 2: return (int64_t)ld_pred(shared, (const short *)c.data + r);
+        case 4: return (int64_t)ld_pred(shared, (const int *)c.data + r);
+        default: return (int64_t)ld_pred(shared, (const long long *)c.data + r);
     }
 }
 
@@ -104,7 +110,7 @@ __device__ __forceinline__ bool pred_holds(const DevQuery &q, const DevPred &p, 
     if (p.op == TGPU_PRED_IS_NULL) return !v;
     if (p.op == TGPU_PRED_IS_NOT_NULL) return v;
     if (!v) return false;
-    return p.is_float ? cmp_f(p.op, col_f64(c, r), p.flo, p.fhi) : cmp_int(p.op, col_int_stream(c, r), p.lo, p.hi);
+    return p.is_float ? cmp_f(p.op, col_f64(c, r), p.flo, p.fhi) : cmp_int(p.op, col_int_stream(c, r, q.shared_scan != 0), p.lo, p.hi);
 }
 
 // Packed key: parts LSB-first, a nullable part's slice is payload | valid-bit
@@ -555,14 +561,14 @@ __device__ __forceinline__ uint32_t filter_range(const DevQuery &q, uint64_t row
     const int lane = threadIdx.x & 31;
     const T *col = (const T *)q.fp_data;
     const int64_t lo = q.fp_lo, hi = q.fp_hi;
-    const bool neg = q.fp_negate != 0;
+    const bool neg = q.fp_negate != 0, shared = q.shared_scan != 0;
     uint32_t n = 0;
     for (uint64_t b = row0; b < row_end; b += 32 * FILTER_UNROLL) {
         T v[FILTER_UNROLL];
 #pragma unroll
         for (int u = 0; u < FILTER_UNROLL; ++u) {
             const uint64_t r = b + u * 32 + lane;
-            v[u] = r < row_end ? __ldcs(col + r) : T(0);
+            v[u] = r < row_end ? ld_pred(shared, col + r) : T(0);
         }
 #pragma unroll
         for (int u = 0; u < FILTER_UNROLL; ++u) {
@@ -575,6 +581,24 @@ __device__ __forceinline__ uint32_t filter_range(const DevQuery &q, uint64_t row
         }
     }
     return n;
+}
+
+// The whole WHERE for row r (the width-specialised range test when the plan
+// has one).
+__device__ __forceinline__ bool row_passes(const DevQuery &q, uint64_t r) {
+    int64_t x;
+    switch (q.fp_bytes) {
+        case 0: {
+            for (int i = 0; i < q.n_preds; ++i)
+                if (!pred_holds(q, q.preds[i], r)) return false;
+            return true;
+        }
+        case 1: x = ld_pred(q.shared_scan != 0, (const signed char *)q.fp_data + r); break;
+        case 2: x = ld_pred(q.shared_scan != 0, (const short *)q.fp_data + r); break;
+        case 4: x = ld_pred(q.shared_scan != 0, (const int *)q.fp_data + r); break;
+        default: x = ld_pred(q.shared_scan != 0, (const long long *)q.fp_data + r); break;
+    }
+    return (x >= q.fp_lo && x <= q.fp_hi) != (q.fp_negate != 0);
 }
 
 // ------------------------------------------------------ fold policies --
@@ -800,7 +824,11 @@ __device__ __forceinline__ void scan_chunk(const DevQuery &q, const ScanSmem &sm
     if (row0 >= row_end) return;
     if (q.n_preds == 0 || !q.gather) {
         // every row (or every filtered row in place): 32 consecutive rows per
-        // batch, LOOKAHEAD batches loaded before any of them folds
+        // batch, LOOKAHEAD batches loaded before any of them folds.  The key
+        // and input loads do not wait for the WHERE: at the selectivities
+        // that pick this mode the survivors touch nearly every line anyway,
+        // so loading all rows costs no extra DRAM bytes and keeps every load
+        // of the batch in flight at once.
         constexpr int L = P::LOOKAHEAD;
         for (uint64_t base = row0; base < row_end; base += 32 * L) {
             typename P::Row rows[L];
@@ -808,13 +836,12 @@ __device__ __forceinline__ void scan_chunk(const DevQuery &q, const ScanSmem &sm
 #pragma unroll
             for (int j = 0; j < L; ++j) {
                 const uint64_t r = base + 32 * j + lane;
-                const bool pass = r < row_end && (q.n_preds == 0 || [&] {
-                                      for (int i = 0; i < q.n_preds; ++i)
-                                          if (!pred_holds(q, q.preds[i], r)) return false;
-                                      return true;
-                                  }());
-                P::load(q, r, pass, rows[j]);
-                act[j] = __ballot_sync(FULL, pass);
+                P::load(q, r, r < row_end, rows[j]);
+            }
+#pragma unroll
+            for (int j = 0; j < L; ++j) {
+                const uint64_t r = base + 32 * j + lane;
+                act[j] = __ballot_sync(FULL, r < row_end && row_passes(q, r));
             }
 #pragma unroll
             for (int j = 0; j < L; ++j) {

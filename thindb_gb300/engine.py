@@ -41,7 +41,48 @@ def lib() -> C.CDLL:
             fn.restype = res
             fn.argtypes = args
         _LIB = L
+        # the measured settings for this GPU (THINDB_GPU_TUNING=off: built-in
+        # rules only; =<path>: another table)
+        choice = os.environ.get("THINDB_GPU_TUNING", "")
+        if choice != "off":
+            path = choice or TUNING_PATH
+            if os.path.exists(path):
+                load_tuning(path)
     return _LIB
+
+
+TUNING_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning", "gb300.json")
+
+
+def load_tuning(path: str = TUNING_PATH) -> int:
+    """Install the tuning table a JSON file written by thindb_gb300.autotune holds;
+    returns the number of entries."""
+    import json
+    with open(path) as f:
+        doc = json.load(f)
+    entries = doc.get("entries", [])
+    arr = (abi.Tuning * max(1, len(entries)))()
+    for i, e in enumerate(entries):
+        for k, v in e["shape"].items():
+            setattr(arr[i].shape, k, int(v))
+        arr[i].chunk_rows = int(e.get("chunk_rows", 0))
+        arr[i].cache_slots = int(e.get("cache_slots", 0))
+        arr[i].table_load_pct = int(e.get("table_load_pct", 0))
+        arr[i].flags = int(e.get("flags", 0))
+    _check(lib().tgpu_tuning_set(arr, len(entries)))
+    return len(entries)
+
+
+def clear_tuning() -> None:
+    _check(lib().tgpu_tuning_set(None, 0))
+
+
+def tuning_entries() -> list:
+    n = lib().tgpu_tuning_get(None, 0)
+    arr = (abi.Tuning * max(1, n))()
+    lib().tgpu_tuning_get(arr, n)
+    return [{"shape": arr[i].shape.as_dict(), "chunk_rows": arr[i].chunk_rows, "cache_slots": arr[i].cache_slots,
+             "table_load_pct": arr[i].table_load_pct, "flags": arr[i].flags} for i in range(n)]
 
 
 class EngineError(RuntimeError):
@@ -407,6 +448,14 @@ class Query:
 def _schema(cols) -> list:
     return [OutCol(c.name.decode(), c.type, bool(c.nullable), c.elem_bytes, c.decimal_precision, c.decimal_scale)
             for c in cols]
+
+
+def request_shape(table: Table, req: Request, batched: bool = False) -> dict:
+    """The shape class (tuning-table key) of `req` on `table`."""
+    creq, _keep = build_request(table, req)
+    out = abi.Shape()
+    _check(lib().tgpu_request_shape(table.handle, C.byref(creq), 1 if batched else 0, C.byref(out)))
+    return out.as_dict()
 
 
 def try_build_group_topn(table: Table, req: Request) -> Optional[Query]:
