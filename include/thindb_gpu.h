@@ -225,8 +225,9 @@ typedef struct tgpu_request {
 #define TGPU_FLAG_TIMING 0x1
 /* Force the global-table route even when the groups fit a CTA's shared memory. */
 #define TGPU_FLAG_FORCE_GLOBAL 0x2
-/* Load every needed column densely instead of gathering only survivors
- * (the default unless the WHERE is estimated to keep under 4% of the rows). */
+/* Fold rows in place (every needed column loaded densely) instead of
+ * compacting the WHERE's survivors and gathering their keys and inputs (the
+ * default unless the WHERE is estimated to keep 60% of the rows or more). */
 #define TGPU_FLAG_DENSE_SCAN 0x4
 /* Disable the in-warp __match_any_sync pre-combine (tuning / tests). */
 #define TGPU_FLAG_NO_WARP_COMBINE 0x8

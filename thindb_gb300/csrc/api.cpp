@@ -567,7 +567,9 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
                 int width = (wide ? 2 : 1) + (nullable ? 1 : 0);
                 if (next + width - 1 > MAX_AGGS) return fail(TGPU_DECLINE, "aggregate state count");
                 next += width;
-                if (sum) g.kind = is_float_t(in_type) ? AK_SUM_F64 : (wide ? AK_SUM_I128 : AK_SUM_I64);
+                // a group of a table under 2^32 rows folds fewer than 2^32 values: carry-free words
+                const int wide_kind = t->n_rows < (1ULL << 32) ? AK_SUM_I128 : AK_SUM_I128C;
+                if (sum) g.kind = is_float_t(in_type) ? AK_SUM_F64 : (wide ? wide_kind : AK_SUM_I64);
                 else {
                     bool mn = a.func == TGPU_AGG_MIN;
                     g.kind = is_float_t(in_type) ? (mn ? AK_MIN_F : AK_MAX_F) : (mn ? AK_MIN_I : AK_MAX_I);
@@ -740,12 +742,13 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     df.cap = cap;
 
     dq.warp_combine = (q->flags & TGPU_FLAG_NO_WARP_COMBINE) ? 0 : 1;
-    // late materialisation pays only when the survivors leave most 128-byte
-    // lines of the key/input columns untouched, i.e. at low selectivity
+    // survivors are compacted and folded 32 at a time (gather) unless the
+    // WHERE is estimated to keep most rows: folding in place runs a fold per
+    // 32 scanned rows, however few of them survive
     {
-        const bool sparse = q->sel_est * 25 < std::max<uint64_t>(1, q->rows_scanned);  // < 4% estimated
+        const bool dense_enough = q->sel_est * 10 >= std::max<uint64_t>(1, q->rows_scanned) * 6;  // >= 60%
         dq.gather = dq.n_preds > 0 && !(q->flags & TGPU_FLAG_DENSE_SCAN) &&
-                    ((q->flags & TGPU_FLAG_GATHER_SCAN) || sparse);
+                    ((q->flags & TGPU_FLAG_GATHER_SCAN) || !dense_enough);
     }
 
     // chunking: about eight chunks per warp of a two-CTA-per-SM grid

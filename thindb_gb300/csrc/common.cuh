@@ -15,6 +15,17 @@ __host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
     return z ^ (z >> 31);
 }
 
+// Carry-free exact sums of 64-bit integers: w0 accumulates the unsigned low
+// 32-bit halves, w1 the signed high halves, so every update is a plain
+// add (an atomic whose result nobody waits for).  The sum is w1 * 2^32 + w0,
+// exact while fewer than 2^32 values are added (|w1| < 2^63, w0 < 2^64).
+__host__ __device__ __forceinline__ uint64_t split_lo(int64_t v) { return (uint64_t)(uint32_t)(uint64_t)v; }
+__host__ __device__ __forceinline__ uint64_t split_hi(int64_t v) { return (uint64_t)(v >> 32); }
+__host__ __device__ __forceinline__ void i128_of_split(uint64_t w0, uint64_t w1, uint64_t &lo, int64_t &hi) {
+    lo = w0 + (w1 << 32);
+    hi = ((int64_t)w1 >> 32) + (lo < w0 ? 1 : 0);
+}
+
 __host__ __device__ __forceinline__ uint64_t hash_key(uint64_t lo, uint64_t hi) {
     // hashU128 (group_table.zig:52-55): mix64(lo ^ mix64(hi))
     return mix64(lo ^ mix64(hi));

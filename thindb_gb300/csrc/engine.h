@@ -45,13 +45,17 @@ enum AggKind : int32_t {
     AK_COUNT_ROWS = 0,   // COUNT(*) / non-nullable COUNT(col): word 0
     AK_COUNT_VALID = 1,  // nullable COUNT(col): own word
     AK_SUM_I64 = 2,      // SUM/AVG over 8/16/32-bit ints: wrapping u64 word
-    AK_SUM_I128 = 3,     // SUM/AVG over 64-bit ints / DECIMAL64: lo, hi words
+    AK_SUM_I128 = 3,     // SUM/AVG over 64-bit ints / DECIMAL64: two carry-free words,
+                         // sum of low 32-bit halves (u64) and of high halves (i64);
+                         // exact while a group folds < 2^32 values (i128_of_split)
     AK_SUM_F64 = 4,      // SUM/AVG over FLOAT/DOUBLE: f64 word
     AK_MIN_I = 5,        // ~enc_i64 word, folded by atomicMax
     AK_MAX_I = 6,        // enc_i64 word
     AK_MIN_F = 7,        // ~enc_f64 word
     AK_MAX_F = 8,        // enc_f64 word
-    AK_DISTINCT = 9      // count word + a (group, value) set
+    AK_DISTINCT = 9,     // count word + a (group, value) set
+    AK_SUM_I128C = 10    // as AK_SUM_I128 for tables of 2^32 rows or more: i128 lo, hi
+                         // words, the carry taken from the low word's atomicAdd
 };
 
 struct DevCol {

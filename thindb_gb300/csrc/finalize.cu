@@ -68,8 +68,12 @@ __device__ EmitVal emit_agg(const DevFinal &f, const unsigned long long *st, int
                 v.lo = st[o.word];
                 v.hi = (int64_t)v.lo < 0 ? -1 : 0;
             } else {
-                v.lo = st[o.word];
-                v.hi = (int64_t)st[o.word + 1];
+                if (o.kind == AK_SUM_I128) {
+                    i128_of_split(st[o.word], st[o.word + 1], v.lo, v.hi);
+                } else {
+                    v.lo = st[o.word];
+                    v.hi = (int64_t)st[o.word + 1];
+                }
                 if (o.out_type == TGPU_BIGINT) v.hi = (int64_t)v.lo < 0 ? -1 : 0;  // wraps to BIGINT
             }
             return v;
@@ -80,7 +84,9 @@ __device__ EmitVal emit_agg(const DevFinal &f, const unsigned long long *st, int
                 v.f = bits_f64(st[o.word]) / (double)den;
             } else {
                 uint64_t lo = st[o.word];
-                int64_t hi = o.kind == AK_SUM_I128 ? (int64_t)st[o.word + 1] : ((int64_t)lo < 0 ? -1 : 0);
+                int64_t hi = (int64_t)lo < 0 ? -1 : 0;
+                if (o.kind == AK_SUM_I128) i128_of_split(st[o.word], st[o.word + 1], lo, hi);
+                else if (o.kind == AK_SUM_I128C) hi = (int64_t)st[o.word + 1];
                 v.f = i128_to_f64(lo, hi) / (double)den / POW10[o.scale];
             }
             return v;

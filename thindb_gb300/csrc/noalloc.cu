@@ -142,7 +142,8 @@ tgpu_status tgpu_group_by_i64_noalloc(const int64_t *keys, const int64_t *values
     q.n_parts = 1;
     q.key_words = 1;
     q.aggs[0] = DevAgg{AK_COUNT_ROWS, -1, 0, -1, 0, 0, 1, 0};
-    q.aggs[1] = DevAgg{AK_SUM_I128, 1, 1, -1, 0, 0, 1, 1};
+    const int32_t sum_kind = n_rows < (1ULL << 32) ? AK_SUM_I128 : AK_SUM_I128C;  // carry-free below 2^32 rows
+    q.aggs[1] = DevAgg{sum_kind, 1, 1, -1, 0, 0, 1, 1};
     q.aggs[2] = DevAgg{AK_MIN_I, 1, 3, -1, 0, 0, 1, 1};
     q.aggs[3] = DevAgg{AK_MAX_I, 1, 4, -1, 0, 0, 1, 1};
     q.n_aggs = 4;
@@ -178,7 +179,7 @@ tgpu_status tgpu_group_by_i64_noalloc(const int64_t *keys, const int64_t *values
     f.parts[0] = q.parts[0];
     f.part_types[0] = TGPU_BIGINT;
     f.outs[0] = DevOut{TGPU_AGG_COUNT, AK_COUNT_ROWS, 0, -1, TGPU_BIGINT, 0, 0, 0};
-    f.outs[1] = DevOut{TGPU_AGG_SUM, AK_SUM_I128, 1, -1, TGPU_BIGINT, TGPU_BIGINT, 0, 0};
+    f.outs[1] = DevOut{TGPU_AGG_SUM, sum_kind, 1, -1, TGPU_BIGINT, TGPU_BIGINT, 0, 0};
     f.outs[2] = DevOut{TGPU_AGG_MIN, AK_MIN_I, 3, -1, TGPU_BIGINT, TGPU_BIGINT, 0, 0};
     f.outs[3] = DevOut{TGPU_AGG_MAX, AK_MAX_I, 4, -1, TGPU_BIGINT, TGPU_BIGINT, 0, 0};
 

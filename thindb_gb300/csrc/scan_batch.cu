@@ -50,6 +50,7 @@ __global__ void __launch_bounds__(SCAN_THREADS, NA <= 4 ? 2 : 1)
             cur = qn;
             __syncthreads();
         }
+        if (qn < 0) break;  // a CTA that got no item at all (cur == qn == -1)
         const DevQuery &q = qs[qn];
         const uint32_t end = min(it.y + q.chunks_per_rg, q.n_chunks);
         for (uint32_t c = it.y + warp; c < end; c += SCAN_WARPS) scan_chunk_dispatch<NA>(q, sm, c, selected);
@@ -77,6 +78,7 @@ int batch_scan_grid(int max_aggs, size_t smem, int sms) {
 cudaError_t launch_batch_scan(const DevQuery *qs, const uint2 *items, uint32_t n_items, int max_aggs, size_t smem,
                               int grid, const volatile int *cancel, unsigned int *status, cudaStream_t s) {
     if (n_items == 0) return cudaSuccess;
+    if ((uint32_t)grid > n_items) grid = (int)n_items;
     if (max_aggs <= 4) {
         cudaError_t e = cudaFuncSetAttribute(batch_scan_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;

@@ -79,6 +79,11 @@ __device__ __forceinline__ int64_t col_int_stream(const DevCol &c, uint64_t r, b
     }
 }
 
+__device__ __forceinline__ double col_f64_stream(const DevCol &c, uint64_t r, bool shared) {
+    if (c.bytes == 4) return (double)ld_pred(shared, (const float *)c.data + r);
+    return ld_pred(shared, (const double *)c.data + r);
+}
+
 __device__ __forceinline__ bool cmp_int(int op, int64_t x, int64_t lo, int64_t hi) {
     switch (op) {
         case TGPU_PRED_BETWEEN: return x >= lo && x <= hi;
@@ -257,7 +262,11 @@ __device__ __forceinline__ void apply_states(const DevQuery &q, unsigned long lo
             case AK_SUM_I64:
                 if (acc.lo[a]) atomicAdd(w, (unsigned long long)acc.lo[a]);
                 break;
-            case AK_SUM_I128: {
+            case AK_SUM_I128:
+                if (acc.lo[a]) atomicAdd(w, (unsigned long long)acc.lo[a]);
+                if (acc.hi[a]) atomicAdd(w + 1, (unsigned long long)acc.hi[a]);
+                break;
+            case AK_SUM_I128C: {
                 unsigned long long lo = acc.lo[a], hi = acc.hi[a];
                 if (lo) {
                     unsigned long long old = atomicAdd(w, lo);
@@ -291,7 +300,8 @@ __device__ __forceinline__ void acc_init(const DevQuery &q, Acc<NA> &acc, const 
         acc.vc[a] = 1;
         switch (kind) {
             case AK_SUM_I64: acc.lo[a] = v; break;
-            case AK_SUM_I128: acc.lo[a] = v; acc.hi[a] = ((int64_t)v < 0) ? ~0ULL : 0ULL; break;
+            case AK_SUM_I128: acc.lo[a] = split_lo((int64_t)v); acc.hi[a] = split_hi((int64_t)v); break;
+            case AK_SUM_I128C: acc.lo[a] = v; acc.hi[a] = ((int64_t)v < 0) ? ~0ULL : 0ULL; break;
             case AK_SUM_F64: acc.lo[a] = v; break;
             case AK_MAX_I: acc.lo[a] = enc_i64((int64_t)v); break;
             case AK_MIN_I: acc.lo[a] = ~enc_i64((int64_t)v); break;
@@ -313,7 +323,11 @@ __device__ __forceinline__ void acc_add(const DevQuery &q, Acc<NA> &acc, const u
         acc.vc[a] += 1;
         switch (kind) {
             case AK_SUM_I64: acc.lo[a] += v; break;
-            case AK_SUM_I128: {
+            case AK_SUM_I128:
+                acc.lo[a] += split_lo((int64_t)v);
+                acc.hi[a] += split_hi((int64_t)v);
+                break;
+            case AK_SUM_I128C: {
                 uint64_t lo = acc.lo[a] + v;
                 acc.hi[a] += (((int64_t)v < 0) ? ~0ULL : 0ULL) + (lo < acc.lo[a] ? 1ULL : 0ULL);
                 acc.lo[a] = lo;
@@ -400,7 +414,11 @@ __device__ void cache_flush(const DevQuery &q, const ScanSmem &sm) {
                 case AK_COUNT_VALID: case AK_SUM_I64:
                     if (st[g.word]) atomicAdd(w, st[g.word]);
                     break;
-                case AK_SUM_I128: {
+                case AK_SUM_I128:
+                    if (st[g.word]) atomicAdd(w, st[g.word]);
+                    if (st[g.word + 1]) atomicAdd(w + 1, st[g.word + 1]);
+                    break;
+                case AK_SUM_I128C: {
                     unsigned long long lo = st[g.word], hi = st[g.word + 1];
                     if (lo) {
                         unsigned long long old = atomicAdd(w, lo);
@@ -601,6 +619,17 @@ __device__ __forceinline__ bool row_passes(const DevQuery &q, uint64_t r) {
     return (x >= q.fp_lo && x <= q.fp_hi) != (q.fp_negate != 0);
 }
 
+// Pull a gathered row's global-table slot toward L2 as soon as its key is
+// known, so the fold's probe of batch j + 1 .. j + LOOKAHEAD - 1 overlaps the
+// fold of batch j instead of waiting on DRAM.  Not for the resident route,
+// whose groups all live in shared memory.
+__device__ __forceinline__ void prefetch_slot(const DevQuery &q, uint64_t k0, uint64_t k1, bool me) {
+    if (!me || (q.cache_slots && q.cache_probe == q.cache_slots)) return;
+    const uint64_t h = hash_key(k0, k1) & (q.cap - 1);
+    const unsigned long long *p = q.table + h * (uint64_t)q.slot_words;
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // ------------------------------------------------------ fold policies --
 
 // The interpreter: any plan, aggregate kinds read from the plan at run time.
@@ -613,6 +642,9 @@ struct GenericFold {
     }
     __device__ __forceinline__ static void fold(const DevQuery &q, const ScanSmem &sm, const Row &rv, unsigned act) {
         fold_batch<NA>(q, sm, rv, act);
+    }
+    __device__ __forceinline__ static void prefetch(const DevQuery &q, const Row &rv, bool me) {
+        prefetch_slot(q, rv.k0, rv.k1, me);
     }
 };
 
@@ -648,14 +680,16 @@ struct FastFold {
 #pragma unroll
         for (int a = 0; a < NV; ++a) rv.val[a] = 0;
         if (!me) return;
+        // gathered columns are read once unless other queries of a batch follow
+        const bool shared = q.shared_scan != 0;
         if (KM == 1) {
             const DevKeyPart &kp = q.parts[0];
-            uint64_t raw = (uint64_t)col_int(q.cols[kp.col], r);
+            uint64_t raw = (uint64_t)col_int_stream(q.cols[kp.col], r, shared);
             rv.k0 = kp.payload < 64 ? (raw & ((1ULL << kp.payload) - 1)) : raw;
         } else {
             for (int i = 0; i < q.n_parts; ++i) {
                 const DevKeyPart &kp = q.parts[i];
-                uint64_t raw = (uint64_t)col_int(q.cols[kp.col], r);
+                uint64_t raw = (uint64_t)col_int_stream(q.cols[kp.col], r, shared);
                 if (kp.payload < 64) raw &= (1ULL << kp.payload) - 1;
                 const int off = kp.offset;
                 if (off < 64) {
@@ -669,8 +703,12 @@ struct FastFold {
 #pragma unroll
         for (int a = 0; a < NA; ++a) {
             const DevCol &c = q.cols[q.faggs[a].col];
-            rv.val[a] = is_f(a) ? f64_bits(col_f64(c, r)) : (uint64_t)col_int(c, r);
+            rv.val[a] = is_f(a) ? f64_bits(col_f64_stream(c, r, shared)) : (uint64_t)col_int_stream(c, r, shared);
         }
+    }
+
+    __device__ __forceinline__ static void prefetch(const DevQuery &q, const Row &rv, bool me) {
+        prefetch_slot(q, rv.k0, rv.k1, me);
     }
 
     __device__ __noinline__ static void fold(const DevQuery &q, const ScanSmem &sm, const Row in, unsigned active) {
@@ -708,7 +746,7 @@ struct FastFold {
             const uint64_t v = val[a];
             switch (kind(a)) {
                 case AK_SUM_I64: case AK_SUM_F64: lo[a] = v; break;
-                case AK_SUM_I128: lo[a] = v; hi[a] = ((int64_t)v < 0) ? ~0ULL : 0ULL; break;
+                case AK_SUM_I128: lo[a] = split_lo((int64_t)v); hi[a] = split_hi((int64_t)v); break;
                 case AK_MAX_I: lo[a] = enc_i64((int64_t)v); break;
                 case AK_MIN_I: lo[a] = ~enc_i64((int64_t)v); break;
                 case AK_MAX_F: lo[a] = enc_f64_bits(v); break;
@@ -731,12 +769,10 @@ struct FastFold {
                         const uint64_t v = x[a];
                         switch (kind(a)) {
                             case AK_SUM_I64: lo[a] += v; break;
-                            case AK_SUM_I128: {
-                                const uint64_t l = lo[a] + v;
-                                hi[a] += (((int64_t)v < 0) ? ~0ULL : 0ULL) + (l < lo[a] ? 1ULL : 0ULL);
-                                lo[a] = l;
+                            case AK_SUM_I128:
+                                lo[a] += split_lo((int64_t)v);
+                                hi[a] += split_hi((int64_t)v);
                                 break;
-                            }
                             case AK_SUM_F64: lo[a] = f64_bits(bits_f64(lo[a]) + bits_f64(v)); break;
                             case AK_MAX_I: lo[a] = max(lo[a], (uint64_t)enc_i64((int64_t)v)); break;
                             case AK_MIN_I: lo[a] = max(lo[a], ~enc_i64((int64_t)v)); break;
@@ -781,15 +817,10 @@ struct FastFold {
                         case AK_SUM_I64:
                             if (lo[a]) atomicAdd(w, (unsigned long long)lo[a]);
                             break;
-                        case AK_SUM_I128: {
-                            unsigned long long l = lo[a], h = hi[a];
-                            if (l) {
-                                const unsigned long long old = atomicAdd(w, l);
-                                h += (old + l < old) ? 1ULL : 0ULL;
-                            }
-                            if (h) atomicAdd(w + 1, h);
+                        case AK_SUM_I128:
+                            if (lo[a]) atomicAdd(w, (unsigned long long)lo[a]);
+                            if (hi[a]) atomicAdd(w + 1, (unsigned long long)hi[a]);
                             break;
-                        }
                         case AK_SUM_F64: atomicAdd((double *)w, bits_f64(lo[a])); break;
                         case AK_MIN_I: case AK_MAX_I: case AK_MIN_F: case AK_MAX_F:
                             atomicMax(w, (unsigned long long)lo[a]);
@@ -894,6 +925,8 @@ __device__ __forceinline__ void scan_chunk(const DevQuery &q, const ScanSmem &sm
             const uint32_t s = i + 32 * j + lane;
             P::load(q, row0 + list[s < n ? s : 0], s < n, rows[j]);
         }
+#pragma unroll
+        for (int j = 0; j < L; ++j) P::prefetch(q, rows[j], i + 32 * j + lane < n);
 #pragma unroll
         for (int j = 0; j < L; ++j) {
             const uint32_t b = i + 32 * j;
