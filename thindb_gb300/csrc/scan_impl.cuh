@@ -204,11 +204,19 @@ __device__ uint64_t global_slot(const DevQuery &q, uint64_t k0, uint64_t k1) {
 
 // Insert (gid, value bits) into a distinct set; true when the pair is new.
 // Entries are {value, gid | epoch << 32}; an entry from an older epoch is free.
-__device__ bool distinct_insert(const DevQuery &q, int d, uint32_t gid, uint64_t bits) {
+// Home slot of (group, value) in distinct set d.  It hashes the group's
+// packed key (hk = hash_key of it) rather than its gid: key and gid are one
+// to one within a query, and the key is known as soon as the row is loaded,
+// so the entry can be prefetched before the group probe returns the gid.
+__device__ __forceinline__ uint64_t distinct_home(const DevQuery &q, int d, uint64_t hk, uint64_t bits) {
+    return mix64(bits ^ hk) & (q.dset_cap[d] - 1);
+}
+
+__device__ bool distinct_insert(const DevQuery &q, int d, uint32_t gid, uint64_t bits, uint64_t hk) {
     unsigned long long *set = q.dset[d];
     const uint64_t mask = q.dset_cap[d] - 1;
     const uint64_t tag = (uint64_t)gid | ((uint64_t)q.epoch << 32);
-    uint64_t h = mix64(bits ^ mix64((uint64_t)gid)) & mask;
+    uint64_t h = distinct_home(q, d, hk, bits);
     for (unsigned p = 0; p < MAX_PROBE; ++p) {
         unsigned long long *sp = set + 2 * h;
         ulonglong2 cur = ld128(sp);  // a hint; every decision below is confirmed atomically
@@ -553,7 +561,7 @@ __device__ __noinline__ void fold_batch(const DevQuery &q, const ScanSmem &sm, c
                 const DevAgg &g = q.aggs[a];
                 if (g.kind != AK_DISTINCT || !((ok >> a) & 1u)) continue;
                 uint64_t bits = g.is_float_in ? canon_f64_bits(bits_f64(val[a])) : val[a];
-                if (distinct_insert(q, g.dset, gid, bits)) atomicAdd(gst + g.word, 1ULL);
+                if (distinct_insert(q, g.dset, gid, bits, hash_key(k0, k1))) atomicAdd(gst + g.word, 1ULL);
             }
         }
     }
@@ -623,11 +631,13 @@ __device__ __forceinline__ bool row_passes(const DevQuery &q, uint64_t r) {
 // known, so the fold's probe of batch j + 1 .. j + LOOKAHEAD - 1 overlaps the
 // fold of batch j instead of waiting on DRAM.  Not for the resident route,
 // whose groups all live in shared memory.
-__device__ __forceinline__ void prefetch_slot(const DevQuery &q, uint64_t k0, uint64_t k1, bool me) {
-    if (!me || (q.cache_slots && q.cache_probe == q.cache_slots)) return;
-    const uint64_t h = hash_key(k0, k1) & (q.cap - 1);
-    const unsigned long long *p = q.table + h * (uint64_t)q.slot_words;
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+__device__ __forceinline__ uint64_t prefetch_slot(const DevQuery &q, uint64_t k0, uint64_t k1, bool me) {
+    const uint64_t hk = hash_key(k0, k1);
+    if (me && !(q.cache_slots && q.cache_probe == q.cache_slots))
+        prefetch_l2(q.table + (hk & (q.cap - 1)) * (uint64_t)q.slot_words);
+    return hk;
 }
 
 // ------------------------------------------------------ fold policies --
@@ -644,7 +654,7 @@ struct GenericFold {
         fold_batch<NA>(q, sm, rv, act);
     }
     __device__ __forceinline__ static void prefetch(const DevQuery &q, const Row &rv, bool me) {
-        prefetch_slot(q, rv.k0, rv.k1, me);
+        (void)prefetch_slot(q, rv.k0, rv.k1, me);
     }
 };
 
@@ -708,7 +718,15 @@ struct FastFold {
     }
 
     __device__ __forceinline__ static void prefetch(const DevQuery &q, const Row &rv, bool me) {
-        prefetch_slot(q, rv.k0, rv.k1, me);
+        const uint64_t hk = prefetch_slot(q, rv.k0, rv.k1, me);
+        if (DISTINCT && me) {
+#pragma unroll
+            for (int a = 0; a < NA; ++a)
+                if (kind(a) == AK_DISTINCT) {
+                    const int d = q.faggs[a].dset;
+                    prefetch_l2(q.dset[d] + 2 * distinct_home(q, d, hk, rv.val[a]));
+                }
+        }
     }
 
     __device__ __noinline__ static void fold(const DevQuery &q, const ScanSmem &sm, const Row in, unsigned active) {
@@ -834,10 +852,11 @@ struct FastFold {
             gid = __shfl_sync(FULL, gid, leader_lane);
             if (me && gid != NO_GID) {
                 unsigned long long *gst = q.table + (uint64_t)gid * q.slot_words + q.key_words;
+                const uint64_t hk = hash_key(k0, k1);
 #pragma unroll
                 for (int a = 0; a < NV; ++a) {
                     if (a >= NA || kind(a) != AK_DISTINCT) continue;
-                    if (distinct_insert(q, q.faggs[a].dset, gid, val[a])) atomicAdd(gst + q.faggs[a].word, 1ULL);
+                    if (distinct_insert(q, q.faggs[a].dset, gid, val[a], hk)) atomicAdd(gst + q.faggs[a].word, 1ULL);
                 }
             }
         }
@@ -874,6 +893,8 @@ __device__ __forceinline__ void scan_chunk(const DevQuery &q, const ScanSmem &sm
                 const uint64_t r = base + 32 * j + lane;
                 act[j] = __ballot_sync(FULL, r < row_end && row_passes(q, r));
             }
+#pragma unroll
+            for (int j = 0; j < L; ++j) P::prefetch(q, rows[j], (act[j] >> lane) & 1u);
 #pragma unroll
             for (int j = 0; j < L; ++j) {
                 selected += (lane == 0) ? __popc(act[j]) : 0;
