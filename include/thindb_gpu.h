@@ -234,6 +234,12 @@ typedef struct tgpu_request {
 /* Gather only the survivors' keys and inputs (late materialisation) whatever
  * the estimated selectivity. */
 #define TGPU_FLAG_GATHER_SCAN 0x10
+/* Run the staged scan (every column through a shared-memory ring of bulk
+ * asynchronous copies) whenever the plan qualifies (compiled fold, NOT NULL
+ * columns, a single range WHERE or none); by default it runs for a WHERE or
+ * a COUNT(DISTINCT) over 4M rows or more.  TGPU_FLAG_NO_STAGED never. */
+#define TGPU_FLAG_STAGED_SCAN 0x40
+#define TGPU_FLAG_NO_STAGED 0x80
 
 /* ----------------------------------------------------------------- output -- */
 
@@ -281,6 +287,7 @@ typedef struct tgpu_query_stats {
 
 #define TGPU_STAT_TUNED 0x1     /* settings came from the tuning table */
 #define TGPU_STAT_GATHER 0x2    /* survivors gathered (late materialisation) */
+#define TGPU_STAT_STAGED 0x4    /* the staged (bulk-copy ring) scan ran */
 
 /* -------------------------------------------------------------- the API -- */
 
@@ -461,7 +468,7 @@ typedef struct tgpu_tuning {
     int32_t chunk_rows;      /* 0 = built-in rule */
     int32_t cache_slots;     /* 0 = built-in rule, -1 = no shared-memory table */
     int32_t table_load_pct;  /* 0 = 50 */
-    int32_t flags;           /* TGPU_FLAG_DENSE_SCAN / _GATHER_SCAN / _NO_WARP_COMBINE */
+    int32_t flags;           /* scan-mode flags: DENSE / GATHER / STAGED / NO_STAGED / NO_WARP_COMBINE */
 } tgpu_tuning;
 
 /* The shape class `req` falls in on `table` (plans the request; allocates nothing). */

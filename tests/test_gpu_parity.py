@@ -240,3 +240,75 @@ def test_device_resident_columns():
     got, _ = run_gpu(dev, req, location="device")
     want = oracle.run(oracle.HostTable(host), req)
     compare_results(got, want, 1, True)
+
+
+# ------------------------------------------------------------- staged scan --
+# The staged scan (tiles of every column through a shared-memory ring of bulk
+# copies) runs by default only from 4M rows; these force it on small tables
+# whose last tile is partial (the plain-copy tail) and compare with the oracle.
+
+STAGED = abi.FLAG_STAGED_SCAN
+
+
+def _assert_staged(st):
+    assert st.flags & abi.STAT_STAGED, "the staged scan did not run"
+
+
+def test_staged_filtered_top10_and_all_groups():
+    cols = filtered_cols(2_000_000, 200_000)  # 2,000,000 = 1953 tiles of 1024 + 128 rows
+    _, st = run_both(cols, Request(["k"], C2_AGGS, [SortSpec("s", True)], limit=10, where=FILTER, flags=STAGED))
+    _assert_staged(st)
+    _, st = run_both(cols, Request(["k"], C2_AGGS, where=FILTER, flags=STAGED))
+    _assert_staged(st)
+    _, st = run_both(cols, Request(["k"], C2_AGGS, where=FILTER, flags=STAGED | abi.FLAG_FORCE_GLOBAL |
+                                   abi.FLAG_NO_WARP_COMBINE))
+    _assert_staged(st)
+
+
+@pytest.mark.parametrize("flags", [STAGED, STAGED | abi.FLAG_FORCE_GLOBAL])
+def test_staged_plain_lowcard(flags):
+    cols = plain_cols((1 << 20) + 333)
+    req = Request(["k"], [AggSpec("count", None, "c"), AggSpec("sum", "v", "s"), AggSpec("min", "v", "mn"),
+                          AggSpec("max", "v", "mx")], flags=flags)
+    _, st = run_both(cols, req)
+    _assert_staged(st)
+    assert st.groups == 1024
+
+
+def test_staged_distinct_composite():
+    cols = distinct_cols(1_000_000, 50_000)
+    req = Request(["region", "url"], [AggSpec("count", None, "c"), AggSpec("count_distinct", "user_id", "u"),
+                                      AggSpec("sum", "latency_ms", "lat")], flags=STAGED)
+    _, st = run_both(cols, req)
+    _assert_staged(st)
+
+
+def test_staged_zone_map_pruning_and_rerun():
+    n = (1 << 20) + 1000
+    d = np.sort(np.random.default_rng(1).integers(0, 1000, n)).astype(np.int32)
+    k = (np.arange(n) % 777).astype(np.int64)
+    cols = [Column("k", abi.BIGINT, k), Column("d", abi.DATE, d)]
+    req = Request(["k"], [AggSpec("count", None, "c"), AggSpec("max", "d", "md")],
+                  where=[Pred("d", "between", 300, 320)], flags=STAGED)
+    got, st = run_both(cols, req)
+    _assert_staged(st)
+    assert st.row_groups_pruned > 0
+    t = Table(cols)
+    q = try_build_group_topn(t, req)
+    first = to_rows(q.collect())
+    for _ in range(2):
+        q.execute()
+        assert to_rows(q.collect()) == first
+    q.close()
+    t.close()
+
+
+def test_staged_declines_to_plain_scan_for_nullable_inputs():
+    """A nullable input column is not staged: the query runs the regular scan."""
+    n = 300_000
+    rng = np.random.default_rng(3)
+    v = rng.integers(-1000, 1000, n).astype(np.int64)
+    ok = rng.random(n) > 0.2
+    cols = [Column("k", abi.BIGINT, (np.arange(n) % 100).astype(np.int64)), Column("v", abi.BIGINT, v, validity=ok)]
+    _, st = run_both(cols, Request(["k"], [AggSpec("sum", "v", "s")], flags=STAGED))
+    assert not st.flags & abi.STAT_STAGED

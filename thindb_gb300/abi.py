@@ -45,8 +45,11 @@ FLAG_DENSE_SCAN = 0x4
 FLAG_NO_WARP_COMBINE = 0x8
 FLAG_GATHER_SCAN = 0x10
 FLAG_NO_TUNING = 0x20
+FLAG_STAGED_SCAN = 0x40
+FLAG_NO_STAGED = 0x80
 STAT_TUNED = 0x1
 STAT_GATHER = 0x2
+STAT_STAGED = 0x4
 
 
 class ColumnDesc(C.Structure):

@@ -11,8 +11,9 @@ knobs are
                     pre-aggregation tier that takes the place of the bucket
                     partition: hot keys fold on chip)
     table_load_pct  global group-table load target (table sizing)
-    flags           scan mode: dense loads or survivor gathers; the in-warp
-                    pre-combine on or off
+    flags           scan mode: the staged scan (column tiles through a
+                    shared-memory ring of bulk copies), dense loads or survivor
+                    gathers; the in-warp pre-combine on or off
 
 For each shape class (tgpu_shape: key width, fold signature, aggregate count,
 distinct, selectivity class, group-count class, batched or not) a coordinate
@@ -38,7 +39,8 @@ from . import abi, datagen, workloads
 from .engine import QueryBatch, Request, Table, request_shape, try_build_group_topn
 
 KNOBS = {
-    "flags": [0, abi.FLAG_DENSE_SCAN, abi.FLAG_GATHER_SCAN, abi.FLAG_NO_WARP_COMBINE],
+    "flags": [0, abi.FLAG_STAGED_SCAN, abi.FLAG_NO_STAGED, abi.FLAG_DENSE_SCAN | abi.FLAG_NO_STAGED,
+              abi.FLAG_GATHER_SCAN | abi.FLAG_NO_STAGED, abi.FLAG_NO_WARP_COMBINE],
     "chunk_rows": [0, 512, 1024, 2048, 4096],
     "cache_slots": [0, -1, 256, 1024, 4096],
     "table_load_pct": [0, 25, 70],

@@ -264,6 +264,9 @@ struct tgpu_query {
     uint32_t chunk_req = 0;       // requested rows per warp chunk (0 auto)
     int load_pct = 50;            // group-table load target
     bool tuned = false;           // settings taken from the tuning table
+    bool staged = false;          // the staged (bulk-copy ring) scan runs this query
+    StagePlan sp{};
+    int stage_grid = 0;
     // workspace
     Buffer table_buf, occ_buf;
     std::vector<Buffer> dset_bufs;
@@ -923,6 +926,26 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
         dq.chunks_per_rg = 0;
         dq.n_chunks = (uint32_t)((t->n_rows + dq.chunk_rows - 1) / dq.chunk_rows);
     }
+
+    // the staged scan (tiles of every column through a shared-memory ring of
+    // bulk copies) for a compiled fold over NOT NULL columns, by default when
+    // a range WHERE or a COUNT(DISTINCT) leaves the warps waiting on memory
+    q->staged = false;
+    const bool want_staged = !(q->flags & TGPU_FLAG_NO_STAGED) &&
+                             ((q->flags & TGPU_FLAG_STAGED_SCAN) ||
+                              ((dq.n_preds > 0 || dq.n_dsets > 0) && q->rows_scanned >= (4ULL << 20)));
+    if (want_staged && t->rg_rows % STAGE_TILE == 0) {
+        DevQuery probe = dq;
+        const uint64_t tiles = (uint64_t)dq.n_rg * (t->rg_rows / STAGE_TILE);
+        DeviceCtx *dev;
+        if (tiles > 0 && stage_plan(probe, tiles, &q->sp) && device_ctx(&dev) == TGPU_OK) {
+            dq.cache_slots = probe.cache_slots;
+            dq.cache_probe = probe.cache_probe;
+            if (q->route == 1 && !(dq.cache_slots && dq.cache_probe == dq.cache_slots)) q->route = 2;
+            q->stage_grid = (int)std::min<uint64_t>((uint64_t)dev->sms, tiles);
+            q->staged = true;
+        }
+    }
     return TGPU_OK;
 }
 
@@ -951,7 +974,10 @@ tgpu_status enqueue(tgpu_query *q) {
     CU(cudaMemsetAsync(q->d_counts, 0, 8 * 8, s));
     const bool timing = (q->flags & TGPU_FLAG_TIMING) != 0;
     if (timing) CU(cudaEventRecord(q->ev[0], s));
-    if (dq.n_chunks > 0) {
+    if (q->staged) {
+        CU(launch_staged_scan(dq, q->sp, q->stage_grid, s));
+        q->launches++;
+    } else if (dq.n_chunks > 0) {
         CU(launch_scan(dq, q->grid, s));
         q->launches++;
     }
@@ -1004,6 +1030,12 @@ tgpu_status finish(tgpu_query *q) {
             q->result_rows = 0;
             return fail(TGPU_ERR_CANCELLED, "query cancelled");
         }
+        if (status & (ST_WAIT_TIMEOUT | ST_BAD_INDEX)) {
+            q->synced = true;
+            q->result_rows = 0;
+            return fail(TGPU_ERR_INTERNAL, status & ST_WAIT_TIMEOUT ? "a staged column copy never completed"
+                                                                     : "a device bounds check failed");
+        }
         if (status & (ST_TABLE_FULL | ST_DISTINCT_FULL)) {
             if (++q->retries > 4) return fail(TGPU_ERR_INTERNAL, "group table kept overflowing");
             if (status & ST_TABLE_FULL) q->groups_est = std::max<uint64_t>(q->groups_est * 4, 1024);
@@ -1031,7 +1063,8 @@ tgpu_status finish(tgpu_query *q) {
     s.route = (uint32_t)q->route;
     s.retries = q->retries;
     s.kernel_launches = q->launches;
-    s.flags = (q->tuned ? TGPU_STAT_TUNED : 0) | (q->dq.gather ? TGPU_STAT_GATHER : 0);
+    s.flags = (q->tuned ? TGPU_STAT_TUNED : 0) | (q->dq.gather && !q->staged ? TGPU_STAT_GATHER : 0) |
+              (q->staged ? TGPU_STAT_STAGED : 0);
     s.device_bytes = q->table_buf.bytes + q->occ_buf.bytes + q->scratch_bytes;
     for (auto &b : q->dset_bufs) s.device_bytes += b.bytes;
     if (q->flags & TGPU_FLAG_TIMING) {
@@ -1071,7 +1104,9 @@ tgpu_shape shape_of(const tgpu_query *q, const tgpu_request *req, int batched) {
 
 // Take the tuned settings of the query's shape unless the request chose its own.
 void apply_tuning(tgpu_query *q, const tgpu_request *req, int batched) {
-    const int own = TGPU_FLAG_DENSE_SCAN | TGPU_FLAG_GATHER_SCAN | TGPU_FLAG_NO_WARP_COMBINE | TGPU_FLAG_NO_TUNING;
+    const int modes = TGPU_FLAG_DENSE_SCAN | TGPU_FLAG_GATHER_SCAN | TGPU_FLAG_NO_WARP_COMBINE |
+                      TGPU_FLAG_STAGED_SCAN | TGPU_FLAG_NO_STAGED;
+    const int own = modes | TGPU_FLAG_NO_TUNING;
     if (req->chunk_rows || req->cache_slots || req->table_load_pct || (req->flags & own)) return;
     const tgpu_shape s = shape_of(q, req, batched);
     std::lock_guard<std::mutex> lk(g_tuning_mu);
@@ -1080,7 +1115,7 @@ void apply_tuning(tgpu_query *q, const tgpu_request *req, int batched) {
         q->chunk_req = (uint32_t)t.chunk_rows;
         q->cache_req = t.cache_slots;
         q->load_pct = t.table_load_pct ? t.table_load_pct : 50;
-        q->flags |= t.flags & (TGPU_FLAG_DENSE_SCAN | TGPU_FLAG_GATHER_SCAN | TGPU_FLAG_NO_WARP_COMBINE);
+        q->flags |= t.flags & modes;
         q->tuned = true;
         return;
     }

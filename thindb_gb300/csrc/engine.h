@@ -38,6 +38,7 @@ constexpr unsigned ST_TABLE_FULL = 1u;      // a probe ran past MAX_PROBE: regro
 constexpr unsigned ST_DISTINCT_FULL = 2u;   // a distinct set probe ran past MAX_PROBE
 constexpr unsigned ST_CANCELLED = 4u;       // the host cancel flag was seen
 constexpr unsigned ST_BAD_INDEX = 8u;       // a bounds check caught an index (never expected)
+constexpr unsigned ST_WAIT_TIMEOUT = 16u;   // a bounded wait on an asynchronous copy gave up
 constexpr unsigned MAX_PROBE = 4096;
 
 // Aggregate fold kinds (one state word each unless noted).
@@ -220,6 +221,31 @@ struct DevFinalBufs {
     uint32_t n_out;
     uint32_t out_bytes[MAX_GROUP_KEYS + MAX_AGGS];
 };
+
+// The staged scan (scan_staged.cu): tiles of tile_rows rows of every staged
+// column, brought into an S-deep shared-memory ring by bulk asynchronous
+// copies.  Tile t covers rows [row0, row0 + tile_rows) of surviving row group
+// t / tiles_per_rg.
+constexpr int STAGE_THREADS = 512;
+constexpr uint32_t STAGE_TILE = 1024;
+constexpr uint32_t STAGE_FOLD_AT = 512;                    // queued rows that start a fold round
+constexpr uint32_t STAGE_QCAP = STAGE_FOLD_AT + STAGE_TILE;  // fold-queue rows
+struct StagePlan {
+    uint32_t n_tiles;
+    uint32_t tiles_per_rg;
+    uint32_t stages;             // ring depth S
+    uint32_t stage_bytes;        // bytes of one tile of every staged column
+    uint32_t n_cols;             // staged columns
+    uint32_t row_bytes;          // bytes of one fold-queue entry
+    int32_t col[MAX_QCOLS];      // query column of staged column i
+    uint32_t off[MAX_QCOLS];     // its byte offset inside a stage
+    int32_t slot[MAX_QCOLS];     // staged index of query column c, -1 = not staged
+    uint32_t cache_off, queue_off, ring_off, smem_bytes;
+};
+// Plan the staged scan for q (its cache_slots may shrink to fit); false if
+// the query does not qualify.
+bool stage_plan(DevQuery &q, uint64_t tile_count, StagePlan *sp);
+cudaError_t launch_staged_scan(const DevQuery &q, const StagePlan &sp, int grid, cudaStream_t s);
 
 // Message returned by tgpu_last_error_message() on this thread (api.cpp).
 void set_error(const char *msg);

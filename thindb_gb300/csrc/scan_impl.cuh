@@ -668,6 +668,7 @@ template <int KM, int K0, int K1, int K2, int K3>
 struct FastFold {
     static constexpr int NA = (K0 != AK_NONE) + (K1 != AK_NONE) + (K2 != AK_NONE) + (K3 != AK_NONE);
     static constexpr int NV = NA > 0 ? NA : 1;
+    static constexpr int KM_ = KM, NA_ = NA;
     // batches whose gathers are all in flight before the first folds; the
     // rows stay in registers (64 per thread at two CTAs per SM), so the depth
     // shrinks as a row grows
