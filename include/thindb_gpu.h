@@ -235,11 +235,15 @@ typedef struct tgpu_request {
  * the estimated selectivity. */
 #define TGPU_FLAG_GATHER_SCAN 0x10
 /* Run the staged scan (every column through a shared-memory ring of bulk
- * asynchronous copies) whenever the plan qualifies (compiled fold, NOT NULL
- * columns, a single range WHERE or none); by default it runs for a WHERE or
- * a COUNT(DISTINCT) over 4M rows or more.  TGPU_FLAG_NO_STAGED never. */
+ * asynchronous copies) when the plan qualifies (compiled fold, NOT NULL
+ * columns, a single range WHERE or none).  TGPU_FLAG_NO_STAGED: never. */
 #define TGPU_FLAG_STAGED_SCAN 0x40
 #define TGPU_FLAG_NO_STAGED 0x80
+/* Prefetch control: no L2 prefetch of group-table slots; no bulk L2
+ * prefetch of each warp's next chunk; also prefetch distinct-set entries. */
+#define TGPU_FLAG_NO_PREFETCH 0x100
+#define TGPU_FLAG_NO_CHUNK_PREFETCH 0x200
+#define TGPU_FLAG_DISTINCT_PREFETCH 0x400
 
 /* ----------------------------------------------------------------- output -- */
 
@@ -468,7 +472,7 @@ typedef struct tgpu_tuning {
     int32_t chunk_rows;      /* 0 = built-in rule */
     int32_t cache_slots;     /* 0 = built-in rule, -1 = no shared-memory table */
     int32_t table_load_pct;  /* 0 = 50 */
-    int32_t flags;           /* scan-mode flags: DENSE / GATHER / STAGED / NO_STAGED / NO_WARP_COMBINE */
+    int32_t flags;           /* scan-mode and prefetch TGPU_FLAG_* bits */
 } tgpu_tuning;
 
 /* The shape class `req` falls in on `table` (plans the request; allocates nothing). */

@@ -293,12 +293,14 @@ def test_staged_zone_map_pruning_and_rerun():
     got, st = run_both(cols, req)
     _assert_staged(st)
     assert st.row_groups_pruned > 0
+    # without ORDER BY the rows come in group-slot order, and which of two
+    # colliding keys claims a slot first varies: compare as sets
     t = Table(cols)
     q = try_build_group_topn(t, req)
-    first = to_rows(q.collect())
+    first = sorted(to_rows(q.collect()))
     for _ in range(2):
         q.execute()
-        assert to_rows(q.collect()) == first
+        assert sorted(to_rows(q.collect())) == first
     q.close()
     t.close()
 

@@ -47,6 +47,9 @@ FLAG_GATHER_SCAN = 0x10
 FLAG_NO_TUNING = 0x20
 FLAG_STAGED_SCAN = 0x40
 FLAG_NO_STAGED = 0x80
+FLAG_NO_PREFETCH = 0x100
+FLAG_NO_CHUNK_PREFETCH = 0x200
+FLAG_DISTINCT_PREFETCH = 0x400
 STAT_TUNED = 0x1
 STAT_GATHER = 0x2
 STAT_STAGED = 0x4

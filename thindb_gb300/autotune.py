@@ -13,7 +13,8 @@ knobs are
     table_load_pct  global group-table load target (table sizing)
     flags           scan mode: the staged scan (column tiles through a
                     shared-memory ring of bulk copies), dense loads or survivor
-                    gathers; the in-warp pre-combine on or off
+                    gathers; the in-warp pre-combine on or off; which L2
+                    prefetches run (table slots, next chunks, distinct entries)
 
 For each shape class (tgpu_shape: key width, fold signature, aggregate count,
 distinct, selectivity class, group-count class, batched or not) a coordinate
@@ -39,8 +40,9 @@ from . import abi, datagen, workloads
 from .engine import QueryBatch, Request, Table, request_shape, try_build_group_topn
 
 KNOBS = {
-    "flags": [0, abi.FLAG_STAGED_SCAN, abi.FLAG_NO_STAGED, abi.FLAG_DENSE_SCAN | abi.FLAG_NO_STAGED,
-              abi.FLAG_GATHER_SCAN | abi.FLAG_NO_STAGED, abi.FLAG_NO_WARP_COMBINE],
+    "flags": [0, abi.FLAG_STAGED_SCAN, abi.FLAG_DENSE_SCAN, abi.FLAG_GATHER_SCAN, abi.FLAG_NO_WARP_COMBINE,
+              abi.FLAG_NO_PREFETCH, abi.FLAG_NO_CHUNK_PREFETCH, abi.FLAG_NO_PREFETCH | abi.FLAG_NO_CHUNK_PREFETCH,
+              abi.FLAG_DISTINCT_PREFETCH],
     "chunk_rows": [0, 512, 1024, 2048, 4096],
     "cache_slots": [0, -1, 256, 1024, 4096],
     "table_load_pct": [0, 25, 70],

@@ -927,13 +927,29 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
         dq.n_chunks = (uint32_t)((t->n_rows + dq.chunk_rows - 1) / dq.chunk_rows);
     }
 
+    // prefetching: group-table slots (and distinct entries on request) as
+    // soon as a gathered row's key is known; each warp's next chunk of every
+    // scanned column into L2 with one bulk prefetch per column
+    dq.prefetch = ((q->flags & TGPU_FLAG_NO_PREFETCH) ? 0 : PF_SLOT) |
+                  ((q->flags & TGPU_FLAG_NO_CHUNK_PREFETCH) ? 0 : PF_NEXT) |
+                  ((q->flags & TGPU_FLAG_DISTINCT_PREFETCH) ? PF_DISTINCT : 0);
+    dq.n_pf = 0;
+    {
+        auto add_pf = [&](int c) {
+            if (c < 0 || dq.n_pf >= 8 || ((uintptr_t)dq.cols[c].data & 15)) return;
+            for (int i = 0; i < dq.n_pf; ++i)
+                if (dq.pf_cols[i] == c) return;
+            dq.pf_cols[dq.n_pf++] = c;
+        };
+        for (int i = 0; i < dq.n_preds; ++i) add_pf(dq.preds[i].col);
+        for (int i = 0; i < dq.n_parts; ++i) add_pf(dq.parts[i].col);
+        for (int a = 0; a < dq.n_aggs; ++a) add_pf(dq.aggs[a].col);
+    }
+
     // the staged scan (tiles of every column through a shared-memory ring of
-    // bulk copies) for a compiled fold over NOT NULL columns, by default when
-    // a range WHERE or a COUNT(DISTINCT) leaves the warps waiting on memory
+    // bulk copies) for a compiled fold over NOT NULL columns, on request
     q->staged = false;
-    const bool want_staged = !(q->flags & TGPU_FLAG_NO_STAGED) &&
-                             ((q->flags & TGPU_FLAG_STAGED_SCAN) ||
-                              ((dq.n_preds > 0 || dq.n_dsets > 0) && q->rows_scanned >= (4ULL << 20)));
+    const bool want_staged = !(q->flags & TGPU_FLAG_NO_STAGED) && (q->flags & TGPU_FLAG_STAGED_SCAN);
     if (want_staged && t->rg_rows % STAGE_TILE == 0) {
         DevQuery probe = dq;
         const uint64_t tiles = (uint64_t)dq.n_rg * (t->rg_rows / STAGE_TILE);
@@ -1105,7 +1121,8 @@ tgpu_shape shape_of(const tgpu_query *q, const tgpu_request *req, int batched) {
 // Take the tuned settings of the query's shape unless the request chose its own.
 void apply_tuning(tgpu_query *q, const tgpu_request *req, int batched) {
     const int modes = TGPU_FLAG_DENSE_SCAN | TGPU_FLAG_GATHER_SCAN | TGPU_FLAG_NO_WARP_COMBINE |
-                      TGPU_FLAG_STAGED_SCAN | TGPU_FLAG_NO_STAGED;
+                      TGPU_FLAG_STAGED_SCAN | TGPU_FLAG_NO_STAGED | TGPU_FLAG_NO_PREFETCH |
+                      TGPU_FLAG_NO_CHUNK_PREFETCH | TGPU_FLAG_DISTINCT_PREFETCH;
     const int own = modes | TGPU_FLAG_NO_TUNING;
     if (req->chunk_rows || req->cache_slots || req->table_load_pct || (req->flags & own)) return;
     const tgpu_shape s = shape_of(q, req, batched);

@@ -41,6 +41,11 @@ constexpr unsigned ST_BAD_INDEX = 8u;       // a bounds check caught an index (n
 constexpr unsigned ST_WAIT_TIMEOUT = 16u;   // a bounded wait on an asynchronous copy gave up
 constexpr unsigned MAX_PROBE = 4096;
 
+// DevQuery::prefetch bits
+constexpr int PF_SLOT = 1;      // a gathered row's group-table slot, as soon as its key is loaded
+constexpr int PF_NEXT = 2;      // the warp's next chunk of every scanned column (bulk L2 prefetch)
+constexpr int PF_DISTINCT = 4;  // a gathered row's distinct-set entries
+
 // Aggregate fold kinds (one state word each unless noted).
 enum AggKind : int32_t {
     AK_COUNT_ROWS = 0,   // COUNT(*) / non-nullable COUNT(col): word 0
@@ -144,6 +149,11 @@ struct DevQuery {
     int32_t cache_probe;      // probe limit (cache_slots when the table holds every group)
     int32_t warp_combine;     // __match_any_sync pre-combine on/off
     int32_t gather;           // 1 = compact survivors, then gather; 0 = process rows in place
+    // prefetching: PF_* bits, and the columns whose next chunk a warp pulls
+    // into L2 with one bulk prefetch per column before scanning its chunk
+    int32_t prefetch;
+    int32_t n_pf;
+    int32_t pf_cols[8];
     // control
     unsigned int *tile_counter;
     unsigned int *status;

@@ -27,6 +27,7 @@ __global__ void __launch_bounds__(SCAN_THREADS, MINB) scan_group_kernel(const __
                 break;
             }
         }
+        prefetch_chunk(q, c + nw);  // this warp's next chunk
         scan_chunk<P>(q, sm, c, selected);
     }
     if (q.cache_slots) {

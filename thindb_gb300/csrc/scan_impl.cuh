@@ -635,7 +635,7 @@ __device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefe
 
 __device__ __forceinline__ uint64_t prefetch_slot(const DevQuery &q, uint64_t k0, uint64_t k1, bool me) {
     const uint64_t hk = hash_key(k0, k1);
-    if (me && !(q.cache_slots && q.cache_probe == q.cache_slots))
+    if (me && (q.prefetch & PF_SLOT) && !(q.cache_slots && q.cache_probe == q.cache_slots))
         prefetch_l2(q.table + (hk & (q.cap - 1)) * (uint64_t)q.slot_words);
     return hk;
 }
@@ -720,7 +720,7 @@ struct FastFold {
 
     __device__ __forceinline__ static void prefetch(const DevQuery &q, const Row &rv, bool me) {
         const uint64_t hk = prefetch_slot(q, rv.k0, rv.k1, me);
-        if (DISTINCT && me) {
+        if (DISTINCT && me && (q.prefetch & PF_DISTINCT)) {
 #pragma unroll
             for (int a = 0; a < NA; ++a)
                 if (kind(a) == AK_DISTINCT) {
@@ -863,6 +863,24 @@ struct FastFold {
         }
     }
 };
+
+// Lanes 0 .. n_pf - 1 pull chunk c of one scanned column each into L2 (one
+// bulk prefetch: 16-byte aligned start, size rounded down to 16 bytes), so
+// the warp's filter and gathers of that chunk find it there.
+__device__ __forceinline__ void prefetch_chunk(const DevQuery &q, uint32_t c) {
+    const int lane = threadIdx.x & 31;
+    if (!(q.prefetch & PF_NEXT) || lane >= q.n_pf || c >= q.n_chunks) return;
+    uint64_t row0, row_end;
+    chunk_rows(q, c, row0, row_end);
+    if (row0 >= row_end) return;
+    const DevCol &col = q.cols[q.pf_cols[lane]];
+    // [begin, end) of the chunk's bytes, shrunk to whole 16-byte blocks
+    const uintptr_t begin = (uintptr_t)col.data + row0 * (uint64_t)col.bytes;
+    const uintptr_t end = (uintptr_t)col.data + row_end * (uint64_t)col.bytes;
+    const uintptr_t b16 = (begin + 15) & ~(uintptr_t)15, e16 = end & ~(uintptr_t)15;
+    if (e16 <= b16) return;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(b16), "r"((uint32_t)(e16 - b16)) : "memory");
+}
 
 // One warp folds chunk c: filter + compaction, then batches of 32 survivors
 // (each batch's gathers issued before the previous batch folds).
