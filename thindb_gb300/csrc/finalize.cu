@@ -446,18 +446,27 @@ __device__ __forceinline__ void block_topk(uint64_t n, uint64_t first, uint64_t 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     WarpList<SW> t;
     wl_init(t);
-    for (uint64_t base = first + (uint64_t)warp * 32; base < n; base += stride) {
-        const uint64_t i = base + lane;
-        uint64_t c[SW];
-        uint32_t g = NO_ID;
-        bool valid = false;
-        if (i < n) {
-            valid = get(i, c, g);
-        } else {
+    // U batches of 32 candidates are loaded (their gathers all in flight)
+    // before any is offered
+    constexpr int U = SW <= 6 ? 4 : 2;
+    for (uint64_t base = first + (uint64_t)warp * 32; base < n; base += stride * U) {
+        uint64_t c[U][SW];
+        uint32_t g[U];
+        bool valid[U];
 #pragma unroll
-            for (int j = 0; j < SW; ++j) c[j] = 0;
+        for (int u = 0; u < U; ++u) {
+            const uint64_t i = base + stride * u + lane;
+            g[u] = NO_ID;
+            valid[u] = false;
+            if (i < n) {
+                valid[u] = get(i, c[u], g[u]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < SW; ++j) c[u][j] = 0;
+            }
         }
-        wl_offer<SW>(t, c, g, valid, k);
+#pragma unroll
+        for (int u = 0; u < U; ++u) wl_offer<SW>(t, c[u], g[u], valid[u], k);
     }
 #pragma unroll
     for (int i = 0; i < SW; ++i) s_keys[((size_t)warp * 32 + lane) * SW + i] = t.key[i];
