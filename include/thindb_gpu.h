@@ -473,6 +473,9 @@ typedef struct tgpu_tuning {
     int32_t cache_slots;     /* 0 = built-in rule, -1 = no shared-memory table */
     int32_t table_load_pct;  /* 0 = 50 */
     int32_t flags;           /* scan-mode and prefetch TGPU_FLAG_* bits */
+    int32_t groups_shift;    /* size the group table for (estimated groups >> groups_shift),
+                              * 0..8; an estimate found too small regrows the table x4 */
+    int32_t reserved;
 } tgpu_tuning;
 
 /* The shape class `req` falls in on `table` (plans the request; allocates nothing). */

@@ -53,7 +53,7 @@ def test_struct_sizes_match_c_layout():
     assert C.sizeof(abi.QueryStats) == 104
     assert C.sizeof(abi.Batch) == 40
     assert C.sizeof(abi.Shape) == 32
-    assert C.sizeof(abi.Tuning) == 48
+    assert C.sizeof(abi.Tuning) == 56
 
 
 def test_no_device_fails_loudly():

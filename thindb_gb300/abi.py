@@ -203,7 +203,8 @@ class Shape(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("shape", Shape), ("chunk_rows", C.c_int32), ("cache_slots", C.c_int32),
-                ("table_load_pct", C.c_int32), ("flags", C.c_int32)]
+                ("table_load_pct", C.c_int32), ("flags", C.c_int32), ("groups_shift", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 SIGNATURES += [

@@ -11,6 +11,9 @@ knobs are
                     pre-aggregation tier that takes the place of the bucket
                     partition: hot keys fold on chip)
     table_load_pct  global group-table load target (table sizing)
+    groups_shift    size the group table for (estimated groups >> shift): the
+                    estimate from NDV sketches and selectivity can be far above
+                    the real count (a table that proves too small regrows)
     flags           scan mode: the staged scan (column tiles through a
                     shared-memory ring of bulk copies), dense loads or survivor
                     gathers; the in-warp pre-combine on or off; which L2
@@ -38,6 +41,7 @@ import numpy as np
 
 from . import abi, datagen, workloads
 from .engine import QueryBatch, Request, Table, request_shape, try_build_group_topn
+from .engine import lib as engine_lib
 
 KNOBS = {
     "flags": [0, abi.FLAG_STAGED_SCAN, abi.FLAG_DENSE_SCAN, abi.FLAG_GATHER_SCAN, abi.FLAG_NO_WARP_COMBINE,
@@ -46,15 +50,25 @@ KNOBS = {
     "chunk_rows": [0, 512, 1024, 2048, 4096],
     "cache_slots": [0, -1, 256, 1024, 4096],
     "table_load_pct": [0, 25, 70],
+    "groups_shift": [0, 2, 3, 4],
 }
-DEFAULT = {"flags": 0, "chunk_rows": 0, "cache_slots": 0, "table_load_pct": 0}
+DEFAULT = {"flags": 0, "chunk_rows": 0, "cache_slots": 0, "table_load_pct": 0, "groups_shift": 0}
 GAIN = 0.97  # a setting must beat the current best by 3% to replace it
 
 
-def _with(req: Request, knobs: dict) -> Request:
-    return dataclasses.replace(req, chunk_rows=knobs["chunk_rows"], cache_slots=knobs["cache_slots"],
-                               table_load_pct=knobs["table_load_pct"],
-                               flags=req.flags | knobs["flags"] | abi.FLAG_TIMING | abi.FLAG_NO_TUNING)
+def _install(shapes: list, knobs: dict) -> None:
+    """Make `knobs` the tuning-table entry of every shape in `shapes` (only)."""
+    arr = (abi.Tuning * max(1, len(shapes)))()
+    for i, sh in enumerate(shapes):
+        for k, v in sh.items():
+            setattr(arr[i].shape, k, int(v))
+        for k, v in knobs.items():
+            setattr(arr[i], k, int(v))
+    engine_lib().tgpu_tuning_set(arr, len(shapes))
+
+
+def _timed(req: Request) -> Request:
+    return dataclasses.replace(req, flags=req.flags | abi.FLAG_TIMING)
 
 
 def _same(a: dict, b: dict) -> bool:
@@ -86,9 +100,11 @@ def _sorted_result(res: dict) -> dict:
 
 
 def time_query(table: Table, req: Request, knobs: dict, reps: int):
-    """(median device ms, result) of `req` run with `knobs`; None if it fails."""
+    """(median device ms, result) of `req` run with `knobs` as its shape's
+    tuning entry; None if it fails."""
+    _install([request_shape(table, req)], knobs)
     try:
-        q = try_build_group_topn(table, _with(req, knobs))
+        q = try_build_group_topn(table, _timed(req))
     except Exception:
         return None
     if q is None:
@@ -110,8 +126,10 @@ def time_query(table: Table, req: Request, knobs: dict, reps: int):
 
 
 def time_batch(table: Table, reqs: list, knobs: dict, reps: int, stream: int):
+    shapes = {json.dumps(request_shape(table, r, batched=True), sort_keys=True) for r in reqs}
+    _install([json.loads(x) for x in sorted(shapes)], knobs)
     try:
-        b = QueryBatch(table, [_with(r, knobs) for r in reqs], graph=True, stream=stream)
+        b = QueryBatch(table, [_timed(r) for r in reqs], graph=True, stream=stream)
     except Exception:
         return None
     try:

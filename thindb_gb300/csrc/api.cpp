@@ -1133,6 +1133,8 @@ void apply_tuning(tgpu_query *q, const tgpu_request *req, int batched) {
         q->cache_req = t.cache_slots;
         q->load_pct = t.table_load_pct ? t.table_load_pct : 50;
         q->flags |= t.flags & modes;
+        if (t.groups_shift > 0 && !req->expected_groups)
+            q->groups_est = std::max<uint64_t>(64, q->groups_est >> t.groups_shift);
         q->tuned = true;
         return;
     }
@@ -2327,7 +2329,7 @@ tgpu_status tgpu_tuning_set(const tgpu_tuning *entries, uint32_t n) {
         const tgpu_tuning &t = entries[i];
         if (t.chunk_rows < 0 || t.chunk_rows % CHUNK_ALIGN != 0 || t.chunk_rows > 65536 ||
             (t.cache_slots > 0 && (t.cache_slots & (t.cache_slots - 1))) || t.cache_slots < -1 ||
-            t.table_load_pct < 0 || t.table_load_pct > 90)
+            t.table_load_pct < 0 || t.table_load_pct > 90 || t.groups_shift < 0 || t.groups_shift > 8)
             return fail(TGPU_ERR_INVALID_ARGUMENT, "tuning entry out of range");
     }
     std::lock_guard<std::mutex> lk(g_tuning_mu);

@@ -69,6 +69,7 @@ def load_tuning(path: str = TUNING_PATH) -> int:
         arr[i].cache_slots = int(e.get("cache_slots", 0))
         arr[i].table_load_pct = int(e.get("table_load_pct", 0))
         arr[i].flags = int(e.get("flags", 0))
+        arr[i].groups_shift = int(e.get("groups_shift", 0))
     _check(lib().tgpu_tuning_set(arr, len(entries)))
     return len(entries)
 
@@ -82,7 +83,8 @@ def tuning_entries() -> list:
     arr = (abi.Tuning * max(1, n))()
     lib().tgpu_tuning_get(arr, n)
     return [{"shape": arr[i].shape.as_dict(), "chunk_rows": arr[i].chunk_rows, "cache_slots": arr[i].cache_slots,
-             "table_load_pct": arr[i].table_load_pct, "flags": arr[i].flags} for i in range(n)]
+             "table_load_pct": arr[i].table_load_pct, "flags": arr[i].flags, "groups_shift": arr[i].groups_shift}
+            for i in range(n)]
 
 
 class EngineError(RuntimeError):
