@@ -124,6 +124,8 @@ struct Buffer {
 void trim_all();
 
 struct Pool {
+    explicit Pool(bool zero_) : zero(zero_) {}
+    const bool zero;  // hands out zeroed buffers (group tables, bitmaps, sets)
     std::mutex mu;
     std::vector<Buffer> free_;
     tgpu_status take(size_t bytes, cudaStream_t s, Buffer *out) {
@@ -137,7 +139,7 @@ struct Pool {
             if (best >= 0) {
                 *out = free_[best];
                 free_.erase(free_.begin() + best);
-                if (out->dirty) {
+                if (out->dirty && zero) {
                     CU(cudaMemsetAsync(out->p, 0, out->bytes, s));
                     out->dirty = false;
                     out->epoch = 0;
@@ -158,7 +160,7 @@ struct Pool {
                 return fail(TGPU_ERR_MEMORY_BUDGET, "device allocation of " + std::to_string(bytes) + " bytes failed");
             }
         }
-        CU(cudaMemsetAsync(b.p, 0, bytes, s));
+        if (zero) CU(cudaMemsetAsync(b.p, 0, bytes, s));
         *out = b;
         return TGPU_OK;
     }
@@ -176,13 +178,77 @@ struct Pool {
 
 // Zero-clean buffers (group tables, occupancy bitmaps) and epoch-tagged
 // distinct sets never mix: a set's stale entries are not zero.
-Pool g_pool;
-Pool g_set_pool;
+Pool g_pool(true);
+Pool g_set_pool(true);
+// Per-query and per-batch scratch (counters, candidate lists, outputs,
+// descriptors): reused as is, so creating a query calls no cudaMalloc and
+// destroying one no cudaFree (both of which would stall the whole device).
+Pool g_scratch_pool(false);
 
 void trim_all() {
     g_pool.trim();
     g_set_pool.trim();
+    g_scratch_pool.trim();
 }
+
+// Small pinned, device-mapped host blocks (a query's counters and cancel
+// flag): carved from 64 KiB cudaHostAlloc chunks and recycled, so creating a
+// query allocates no pinned memory.
+struct HostSlab {
+    static constexpr size_t BLOCK = 128, CHUNK = 64 * 1024;
+    std::mutex mu;
+    std::vector<char *> free_;
+    tgpu_status take(char **out) {
+        std::lock_guard<std::mutex> lk(mu);
+        if (free_.empty()) {
+            char *c = nullptr;
+            CU(cudaHostAlloc((void **)&c, CHUNK, cudaHostAllocMapped));
+            for (size_t o = 0; o < CHUNK; o += BLOCK) free_.push_back(c + o);
+        }
+        *out = free_.back();
+        free_.pop_back();
+        std::memset(*out, 0, BLOCK);
+        return TGPU_OK;
+    }
+    void give(char *p) {
+        if (!p) return;
+        std::lock_guard<std::mutex> lk(mu);
+        free_.push_back(p);
+    }
+};
+HostSlab g_slab;
+
+// Larger pinned, device-mapped host buffers (a batch's packed results and
+// counters), best fit from a free list.
+struct PinnedPool {
+    std::mutex mu;
+    std::vector<std::pair<char *, size_t>> free_;
+    tgpu_status take(size_t bytes, char **out, size_t *got) {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            int best = -1;
+            for (size_t i = 0; i < free_.size(); ++i)
+                if (free_[i].second >= bytes && free_[i].second <= 2 * bytes + 65536 &&
+                    (best < 0 || free_[i].second < free_[best].second))
+                    best = (int)i;
+            if (best >= 0) {
+                *out = free_[best].first;
+                *got = free_[best].second;
+                free_.erase(free_.begin() + best);
+                return TGPU_OK;
+            }
+        }
+        CU(cudaHostAlloc((void **)out, bytes, cudaHostAllocMapped));
+        *got = bytes;
+        return TGPU_OK;
+    }
+    void give(char *p, size_t bytes) {
+        if (!p) return;
+        std::lock_guard<std::mutex> lk(mu);
+        free_.emplace_back(p, bytes);
+    }
+};
+PinnedPool g_pinned;
 
 // ----------------------------------------------------------------- table --
 
@@ -271,7 +337,8 @@ struct tgpu_query {
     Buffer table_buf, occ_buf;
     std::vector<Buffer> dset_bufs;
     std::vector<uint64_t> dset_need;   // distinct entries estimated per set
-    void *scratch = nullptr;           // per-query small buffers (one allocation)
+    Buffer scratch_buf;                // per-query small buffers (one pooled allocation)
+    void *scratch = nullptr;
     size_t scratch_bytes = 0;
     uint32_t *d_rg_list = nullptr;
     unsigned int *d_ctrl = nullptr;            // [0] tile counter, [1] status
@@ -290,7 +357,8 @@ struct tgpu_query {
     void **d_out_ptrs = nullptr;
     uint8_t **d_valid_ptrs = nullptr;
     std::vector<uint32_t> rg_list;
-    // host pinned
+    // host pinned (one slab block: counts at 0, cancel flag at 96)
+    char *h_block = nullptr;
     int *h_cancel = nullptr;
     int *d_cancel = nullptr;
     unsigned long long *h_counts = nullptr;   // [0..4] counts + selected, [5] status
@@ -308,9 +376,8 @@ struct tgpu_query {
     ~tgpu_query() {
         if (stream) cudaStreamSynchronize(stream);
         release_workspace();
-        if (scratch) cudaFree(scratch);
-        if (h_cancel) cudaFreeHost(h_cancel);
-        if (h_counts) cudaFreeHost(h_counts);
+        g_scratch_pool.give(scratch_buf);
+        g_slab.give(h_block);
         for (auto e : ev)
             if (e) cudaEventDestroy(e);
     }
@@ -868,10 +935,11 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
         dq.dset_cap[d] = dcap[d];
     }
     if (scratch > q->scratch_bytes) {
-        if (q->scratch) CU(cudaFree(q->scratch));
-        q->scratch = nullptr;
-        CU(cudaMalloc(&q->scratch, scratch));
-        q->scratch_bytes = scratch;
+        g_scratch_pool.give(q->scratch_buf);
+        q->scratch_buf = Buffer();
+        if ((st = g_scratch_pool.take(scratch, q->stream, &q->scratch_buf)) != TGPU_OK) return st;
+        q->scratch = q->scratch_buf.p;
+        q->scratch_bytes = q->scratch_buf.bytes;
     }
     char *base = (char *)q->scratch;
     q->d_ctrl = (unsigned int *)(base + o_ctrl);
@@ -900,8 +968,8 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     CU(cudaMemcpyAsync(q->d_valid_ptrs, q->d_outvalid.data(), q->schema.size() * 8, cudaMemcpyHostToDevice, q->stream));
     if (!q->rg_list.empty())
         CU(cudaMemcpyAsync(q->d_rg_list, q->rg_list.data(), 4 * q->rg_list.size(), cudaMemcpyHostToDevice, q->stream));
-    // the host vectors above are read by the copies: finish them before returning
-    CU(cudaStreamSynchronize(q->stream));
+    // (pageable sources: each copy has staged its bytes when it returns, so
+    // the vectors may change afterwards; no synchronisation needed)
 
     dq.table = (unsigned long long *)q->table_buf.p;
     dq.occ = (uint32_t *)q->occ_buf.p;
@@ -989,6 +1057,8 @@ tgpu_status enqueue(tgpu_query *q) {
     CU(cudaMemsetAsync(q->d_ctrl, 0, 16, s));
     CU(cudaMemsetAsync(q->d_counts, 0, 8 * 8, s));
     const bool timing = (q->flags & TGPU_FLAG_TIMING) != 0;
+    if (timing && !q->ev[0])
+        for (auto &e : q->ev) CU(cudaEventCreate(&e));
     if (timing) CU(cudaEventRecord(q->ev[0], s));
     if (q->staged) {
         CU(launch_staged_scan(dq, q->sp, q->stage_grid, s));
@@ -1301,12 +1371,11 @@ tgpu_status query_create(tgpu_table *table, const tgpu_request *req, int batched
     st = plan_query(q.get(), table, req);
     if (st != TGPU_OK) return st;
     apply_tuning(q.get(), req, batched);
-    CU(cudaHostAlloc((void **)&q->h_cancel, sizeof(int), cudaHostAllocMapped));
-    *q->h_cancel = 0;
+    st = g_slab.take(&q->h_block);
+    if (st != TGPU_OK) return st;
+    q->h_counts = (unsigned long long *)q->h_block;
+    q->h_cancel = (int *)(q->h_block + 96);
     CU(cudaHostGetDevicePointer((void **)&q->d_cancel, q->h_cancel, 0));
-    CU(cudaHostAlloc((void **)&q->h_counts, 8 * 8, cudaHostAllocDefault));
-    std::memset(q->h_counts, 0, 64);
-    for (auto &e : q->ev) CU(cudaEventCreate(&e));
     st = size_workspace(q.get(), next_pow2(std::max<uint64_t>(64, q->groups_est * 100 / q->load_pct)));
     if (st != TGPU_OK) return st;
     q->grid = scan_grid_size(q->dq, dev->sms);
@@ -1417,15 +1486,19 @@ struct tgpu_query_batch {
     std::vector<DevFinal> h_fs;
     std::vector<DevFinalBufs> h_bs;
     std::vector<uint2> items;               // {query, first chunk of a row group}, row group major
-    void *dev = nullptr;                    // one allocation for every array below
+    Buffer dev_buf;                         // one pooled allocation for every array below
+    void *dev = nullptr;
     DevQuery *d_qs = nullptr;
     DevFinal *d_fs = nullptr;
     DevFinalBufs *d_bs = nullptr;
-    uint2 *d_items = nullptr;               // own allocation
+    Buffer items_buf;                       // pooled
+    uint2 *d_items = nullptr;
     unsigned int *d_ctrl = nullptr;         // [0] work counter, [1] status
     unsigned long long *d_counts = nullptr; // 8 per query
     unsigned int *d_qctrl = nullptr;        // 4 per query: tile counter, status
     unsigned long long *h_counts = nullptr; // pinned: 8 per query, then Q statuses + batch status
+    size_t counts_bytes = 0;
+    char *h_block = nullptr;                // slab block holding the cancel flag
     int *h_cancel = nullptr, *d_cancel = nullptr;
     uint8_t *h_stage = nullptr, *d_stage = nullptr;  // mapped pinned: packed result rows
     size_t stage_bytes = 0;
@@ -1450,11 +1523,11 @@ struct tgpu_query_batch {
         for (auto *q : qs) delete q;
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
-        if (dev) cudaFree(dev);
-        if (d_items) cudaFree(d_items);
-        if (h_counts) cudaFreeHost(h_counts);
-        if (h_stage) cudaFreeHost(h_stage);
-        if (h_cancel) cudaFreeHost(h_cancel);
+        g_scratch_pool.give(dev_buf);
+        g_scratch_pool.give(items_buf);
+        g_pinned.give((char *)h_counts, counts_bytes);
+        g_pinned.give((char *)h_stage, stage_bytes);
+        g_slab.give(h_block);
         for (auto e : ev)
             if (e) cudaEventDestroy(e);
     }
@@ -1492,10 +1565,14 @@ tgpu_status batch_descriptors(tgpu_query_batch *b) {
         stage += (bytes + 15) & ~(size_t)15;
     }
     if (stage > b->stage_bytes) {
-        if (b->h_stage) CU(cudaFreeHost(b->h_stage));
+        g_pinned.give((char *)b->h_stage, b->stage_bytes);
         b->h_stage = nullptr;
-        CU(cudaHostAlloc((void **)&b->h_stage, stage, cudaHostAllocMapped));
+        b->stage_bytes = 0;
+        size_t got = 0;
+        tgpu_status pst = g_pinned.take(stage, (char **)&b->h_stage, &got);
+        if (pst != TGPU_OK) return pst;
         CU(cudaHostGetDevicePointer((void **)&b->d_stage, b->h_stage, 0));
+        stage = got;
         b->stage_bytes = stage;
     }
     for (uint32_t i = 0; i < Q; ++i) {
@@ -1559,7 +1636,10 @@ tgpu_status batch_descriptors(tgpu_query_batch *b) {
                     ++pos[i];
                 }
             }
-        CU(cudaMalloc((void **)&b->d_items, sizeof(uint2) * std::max<size_t>(1, b->items.size())));
+        tgpu_status ist = g_scratch_pool.take(sizeof(uint2) * std::max<size_t>(1, b->items.size()), b->stream,
+                                              &b->items_buf);
+        if (ist != TGPU_OK) return ist;
+        b->d_items = (uint2 *)b->items_buf.p;
         if (!b->items.empty())
             CU(cudaMemcpyAsync(b->d_items, b->items.data(), sizeof(uint2) * b->items.size(), cudaMemcpyHostToDevice,
                                b->stream));
@@ -1632,7 +1712,9 @@ tgpu_status tgpu_batch_create(tgpu_table *table, const tgpu_request *reqs, uint3
     };
     size_t o_qs = add(sizeof(DevQuery) * Q), o_fs = add(sizeof(DevFinal) * Q), o_bs = add(sizeof(DevFinalBufs) * Q),
            o_ctrl = add(16), o_counts = add(64 * Q), o_qctrl = add(16 * Q);
-    CU(cudaMalloc(&b->dev, off));
+    st = g_scratch_pool.take(off, b->stream, &b->dev_buf);
+    if (st != TGPU_OK) return st;
+    b->dev = b->dev_buf.p;
     char *base = (char *)b->dev;
     b->d_qs = (DevQuery *)(base + o_qs);
     b->d_fs = (DevFinal *)(base + o_fs);
@@ -1640,10 +1722,12 @@ tgpu_status tgpu_batch_create(tgpu_table *table, const tgpu_request *reqs, uint3
     b->d_ctrl = (unsigned int *)(base + o_ctrl);
     b->d_counts = (unsigned long long *)(base + o_counts);
     b->d_qctrl = (unsigned int *)(base + o_qctrl);
-    CU(cudaHostAlloc((void **)&b->h_counts, 8 * (11 * Q + 2), cudaHostAllocDefault));
+    st = g_pinned.take(8 * (11 * Q + 2), (char **)&b->h_counts, &b->counts_bytes);
+    if (st != TGPU_OK) return st;
     std::memset(b->h_counts, 0, 8 * (11 * Q + 2));
-    CU(cudaHostAlloc((void **)&b->h_cancel, sizeof(int), cudaHostAllocMapped));
-    *b->h_cancel = 0;
+    st = g_slab.take(&b->h_block);
+    if (st != TGPU_OK) return st;
+    b->h_cancel = (int *)b->h_block;
     CU(cudaHostGetDevicePointer((void **)&b->d_cancel, b->h_cancel, 0));
     for (auto &e : b->ev) CU(cudaEventCreate(&e));
     for (auto *q : b->qs)

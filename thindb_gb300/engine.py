@@ -383,10 +383,10 @@ class Query:
         valid = []
         for c in self.schema:
             if c.type == abi.DECIMAL128:
-                vals.append(np.zeros((capacity, 2), dtype=np.int64))
+                vals.append(np.empty((capacity, 2), dtype=np.int64))
             else:
-                vals.append(np.zeros(capacity, dtype=NP_DTYPES[c.type]))
-            valid.append(np.zeros((capacity + 7) // 8, dtype=np.uint8))
+                vals.append(np.empty(capacity, dtype=NP_DTYPES[c.type]))
+            valid.append(np.empty((capacity + 7) // 8, dtype=np.uint8))
         b = abi.Batch()
         b.n_columns = len(self.schema)
         vp = (C.c_void_p * len(vals))(*[v.ctypes.data for v in vals])
@@ -407,6 +407,9 @@ class Query:
     def collect(self, capacity: int = 1 << 20) -> dict:
         """Drain the query: {column name: (values, validity or None)} in result order."""
         parts: list[Batch] = []
+        rows = self._result_rows()
+        if rows is not None:
+            capacity = max(1, min(capacity, rows))
         while True:
             b = self.next(capacity)
             if b is None:
@@ -426,6 +429,13 @@ class Query:
                 ok = np.zeros(0, dtype=bool) if c.nullable else None
             out[c.name] = (v, ok)
         return out
+
+    def _result_rows(self) -> Optional[int]:
+        """Rows the current execution emits (a zero-row next runs or waits for
+        it), so collect sizes its buffers to the result."""
+        if self.next(0) is None:
+            return 0
+        return int(self.stats().result_rows)
 
     def cancel(self) -> None:
         _check(lib().tgpu_query_cancel(self.handle))
@@ -488,6 +498,9 @@ class _BatchMember(Query):
 
     def _next_c(self, b, done) -> None:
         _check(lib().tgpu_batch_next(self.batch.handle, self.index, C.byref(b), C.byref(done)))
+
+    def _result_rows(self) -> Optional[int]:
+        return None
 
     def close(self) -> None:
         pass
@@ -560,6 +573,9 @@ class _ServerResult(Query):
 
     def _next_c(self, b, done) -> None:
         _check(lib().tgpu_server_next(self.server.handle, self.ticket, C.byref(b), C.byref(done)))
+
+    def _result_rows(self) -> Optional[int]:
+        return None
 
     def close(self) -> None:
         pass
