@@ -244,6 +244,11 @@ typedef struct tgpu_request {
 #define TGPU_FLAG_NO_PREFETCH 0x100
 #define TGPU_FLAG_NO_CHUNK_PREFETCH 0x200
 #define TGPU_FLAG_DISTINCT_PREFETCH 0x400
+/* COUNT(DISTINCT) through hash partitions of (group, value) pairs, each
+ * deduplicated in one CTA's shared memory (the default for one distinct
+ * aggregate over 8M rows or more outside batches), or never. */
+#define TGPU_FLAG_DISTINCT_PARTITION 0x800
+#define TGPU_FLAG_NO_DISTINCT_PARTITION 0x1000
 
 /* ----------------------------------------------------------------- output -- */
 
@@ -292,6 +297,7 @@ typedef struct tgpu_query_stats {
 #define TGPU_STAT_TUNED 0x1     /* settings came from the tuning table */
 #define TGPU_STAT_GATHER 0x2    /* survivors gathered (late materialisation) */
 #define TGPU_STAT_STAGED 0x4    /* the staged (bulk-copy ring) scan ran */
+#define TGPU_STAT_DISTINCT_PARTITION 0x8  /* COUNT(DISTINCT) went through partitions */
 
 /* -------------------------------------------------------------- the API -- */
 

@@ -314,3 +314,49 @@ def test_staged_declines_to_plain_scan_for_nullable_inputs():
     cols = [Column("k", abi.BIGINT, (np.arange(n) % 100).astype(np.int64)), Column("v", abi.BIGINT, v, validity=ok)]
     _, st = run_both(cols, Request(["k"], [AggSpec("sum", "v", "s")], flags=STAGED))
     assert not st.flags & abi.STAT_STAGED
+
+
+# ------------------------------------------------ partitioned COUNT(DISTINCT) --
+# (group, value) pairs go to hash partitions, each deduplicated by one CTA in
+# shared memory; the default from 8M rows, forced here on small tables.
+
+DPART = abi.FLAG_DISTINCT_PARTITION
+
+
+def test_distinct_partitioned_composite():
+    cols = distinct_cols(1_000_000, 50_000)
+    req = Request(["region", "url"], [AggSpec("count", None, "c"), AggSpec("count_distinct", "user_id", "u"),
+                                      AggSpec("sum", "latency_ms", "lat")], flags=DPART)
+    _, st = run_both(cols, req)
+    assert st.flags & abi.STAT_DISTINCT_PARTITION
+    assert st.groups > 100_000
+
+
+def test_distinct_partitioned_region_top_and_reruns():
+    cols = distinct_cols(600_000, 20_000)
+    req = Request(["region"], [AggSpec("count_distinct", "user_id", "u"), AggSpec("count", None, "c")],
+                  [SortSpec("u", True)], limit=10, flags=DPART)
+    got, st = run_both(cols, req)
+    assert st.flags & abi.STAT_DISTINCT_PARTITION
+    t = Table(cols)
+    q = try_build_group_topn(t, req)
+    first = to_rows(q.collect())
+    for _ in range(3):
+        q.execute()
+        assert to_rows(q.collect()) == first
+    q.close()
+    t.close()
+
+
+def test_distinct_partitioned_nullable_and_float_values():
+    """Interpreter fold (nullable / DOUBLE distinct values) through partitions."""
+    n = 400_000
+    rng = np.random.default_rng(21)
+    k = rng.integers(0, 3000, n).astype(np.int64)
+    v = rng.integers(0, 500, n).astype(np.float64) / 4.0
+    v[rng.random(n) < 0.01] = -0.0
+    ok = rng.random(n) > 0.1
+    cols = [Column("k", abi.BIGINT, k), Column("v", abi.DOUBLE, v, validity=ok)]
+    req = Request(["k"], [AggSpec("count_distinct", "v", "d"), AggSpec("count", None, "c")], flags=DPART)
+    _, st = run_both(cols, req)
+    assert st.flags & abi.STAT_DISTINCT_PARTITION

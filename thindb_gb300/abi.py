@@ -50,9 +50,12 @@ FLAG_NO_STAGED = 0x80
 FLAG_NO_PREFETCH = 0x100
 FLAG_NO_CHUNK_PREFETCH = 0x200
 FLAG_DISTINCT_PREFETCH = 0x400
+FLAG_DISTINCT_PARTITION = 0x800
+FLAG_NO_DISTINCT_PARTITION = 0x1000
 STAT_TUNED = 0x1
 STAT_GATHER = 0x2
 STAT_STAGED = 0x4
+STAT_DISTINCT_PARTITION = 0x8
 
 
 class ColumnDesc(C.Structure):

@@ -331,6 +331,10 @@ struct tgpu_query {
     int load_pct = 50;            // group-table load target
     bool tuned = false;           // settings taken from the tuning table
     bool staged = false;          // the staged (bulk-copy ring) scan runs this query
+    bool batched = false;         // created for a batch (runs inside the batched kernel)
+    int dpart_extra = 0;          // partition bits added after overflows
+    Buffer dpart_cursor_buf, dpart_pairs_buf;
+    int dpart_word = -1;          // the distinct aggregate's state word
     StagePlan sp{};
     int stage_grid = 0;
     // workspace
@@ -386,6 +390,9 @@ struct tgpu_query {
         g_pool.give(table_buf);
         g_pool.give(occ_buf);
         table_buf = occ_buf = Buffer();
+        g_scratch_pool.give(dpart_cursor_buf);
+        g_scratch_pool.give(dpart_pairs_buf);
+        dpart_cursor_buf = dpart_pairs_buf = Buffer();
         for (auto &b : dset_bufs) g_set_pool.give(b);
         dset_bufs.clear();
     }
@@ -872,9 +879,30 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     const uint64_t slots = cap + 1;
     const size_t table_bytes = slots * (size_t)dq.slot_words * 8;
     const size_t occ_bytes = ((slots + 31) / 32) * 4;
+    // COUNT(DISTINCT): partitioned (pairs to hash partitions, deduplicated
+    // per partition in shared memory) for one distinct aggregate over many
+    // rows, else a global (group, value) set
+    dq.dpart_bits = 0;
+    dq.dpart_cap = 0;
+    q->dpart_word = -1;
+    size_t dpart_bytes = 0;
+    if (dq.n_dsets == 1 && !q->batched && !(q->flags & TGPU_FLAG_NO_DISTINCT_PARTITION) &&
+        ((q->flags & TGPU_FLAG_DISTINCT_PARTITION) || q->sel_est >= (8ULL << 20))) {
+        // about three quarters of a partition's capacity expected
+        const uint64_t per = DPART_CAP * 3 / 4;
+        int bits = 1;
+        while (bits < 18 && ((uint64_t)1 << bits) * per < q->sel_est) ++bits;
+        bits = std::min(20, bits + q->dpart_extra);
+        dq.dpart_bits = bits;
+        dq.dpart_cap = DPART_CAP;
+        for (int a = 0; a < dq.n_aggs; ++a)
+            if (dq.aggs[a].kind == AK_DISTINCT) q->dpart_word = dq.aggs[a].word;
+        dpart_bytes = ((size_t)4 << bits) + ((size_t)DPART_CAP * 16 << bits);
+    }
     std::vector<uint64_t> dcap;
     size_t dset_bytes = 0;
     for (uint64_t need : q->dset_need) {
+        if (dq.dpart_bits) break;
         uint64_t c = next_pow2(std::max<uint64_t>(64, need * 2));
         dcap.push_back(c);
         dset_bytes += c * 16;
@@ -918,7 +946,7 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     size_t o_ptrs = add(q->schema.size() * 8), o_vptrs = add(q->schema.size() * 8);
     (void)row_bytes;
 
-    const size_t total = table_bytes + occ_bytes + dset_bytes + scratch;
+    const size_t total = table_bytes + occ_bytes + dset_bytes + dpart_bytes + scratch;
     if (q->budget && total > q->budget)
         return fail(TGPU_ERR_MEMORY_BUDGET, "query needs " + std::to_string(total) + " device bytes, budget " +
                                                 std::to_string(q->budget));
@@ -933,6 +961,17 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
         q->dset_bufs.push_back(b);
         dq.dset[d] = (unsigned long long *)b.p;
         dq.dset_cap[d] = dcap[d];
+    }
+    if (dq.dpart_bits) {
+        if ((st = g_scratch_pool.take((size_t)4 << dq.dpart_bits, q->stream, &q->dpart_cursor_buf)) != TGPU_OK)
+            return st;
+        if ((st = g_scratch_pool.take((size_t)DPART_CAP * 16 << dq.dpart_bits, q->stream, &q->dpart_pairs_buf)) !=
+            TGPU_OK)
+            return st;
+        dq.dpart_cursor = (uint32_t *)q->dpart_cursor_buf.p;
+        dq.dpart_buf = (ulonglong2 *)q->dpart_pairs_buf.p;
+        dq.dset[0] = nullptr;
+        dq.dset_cap[0] = 0;
     }
     if (scratch > q->scratch_bytes) {
         g_scratch_pool.give(q->scratch_buf);
@@ -1060,11 +1099,16 @@ tgpu_status enqueue(tgpu_query *q) {
     if (timing && !q->ev[0])
         for (auto &e : q->ev) CU(cudaEventCreate(&e));
     if (timing) CU(cudaEventRecord(q->ev[0], s));
+    if (dq.dpart_bits) CU(cudaMemsetAsync(dq.dpart_cursor, 0, (size_t)4 << dq.dpart_bits, s));
     if (q->staged) {
         CU(launch_staged_scan(dq, q->sp, q->stage_grid, s));
         q->launches++;
     } else if (dq.n_chunks > 0) {
         CU(launch_scan(dq, q->grid, s));
+        q->launches++;
+    }
+    if (dq.dpart_bits) {
+        CU(launch_distinct_partitions(dq, q->dpart_word, s));
         q->launches++;
     }
     if (timing) CU(cudaEventRecord(q->ev[1], s));
@@ -1125,8 +1169,10 @@ tgpu_status finish(tgpu_query *q) {
         if (status & (ST_TABLE_FULL | ST_DISTINCT_FULL)) {
             if (++q->retries > 4) return fail(TGPU_ERR_INTERNAL, "group table kept overflowing");
             if (status & ST_TABLE_FULL) q->groups_est = std::max<uint64_t>(q->groups_est * 4, 1024);
-            if (status & ST_DISTINCT_FULL)
+            if (status & ST_DISTINCT_FULL) {
                 for (auto &n : q->dset_need) n *= 4;
+                if (q->dq.dpart_bits) q->dpart_extra += 2;
+            }
             tgpu_status st = size_workspace(q, next_pow2(q->groups_est * 100 / q->load_pct));
             if (st != TGPU_OK) return st;
             st = enqueue(q);
@@ -1143,14 +1189,15 @@ tgpu_status finish(tgpu_query *q) {
     s.groups = q->h_counts[0];
     s.result_rows = q->h_counts[2];
     s.table_capacity = q->dq.cap;
-    s.distinct_capacity = q->dq.n_dsets ? q->dq.dset_cap[0] : 0;
+    s.distinct_capacity = q->dq.dpart_bits ? ((uint64_t)q->dq.dpart_cap << q->dq.dpart_bits)
+                                           : (q->dq.n_dsets ? q->dq.dset_cap[0] : 0);
     s.row_groups_total = q->rg_total;
     s.row_groups_pruned = q->rg_pruned;
     s.route = (uint32_t)q->route;
     s.retries = q->retries;
     s.kernel_launches = q->launches;
     s.flags = (q->tuned ? TGPU_STAT_TUNED : 0) | (q->dq.gather && !q->staged ? TGPU_STAT_GATHER : 0) |
-              (q->staged ? TGPU_STAT_STAGED : 0);
+              (q->staged ? TGPU_STAT_STAGED : 0) | (q->dq.dpart_bits ? TGPU_STAT_DISTINCT_PARTITION : 0);
     s.device_bytes = q->table_buf.bytes + q->occ_buf.bytes + q->scratch_bytes;
     for (auto &b : q->dset_bufs) s.device_bytes += b.bytes;
     if (q->flags & TGPU_FLAG_TIMING) {
@@ -1192,7 +1239,8 @@ tgpu_shape shape_of(const tgpu_query *q, const tgpu_request *req, int batched) {
 void apply_tuning(tgpu_query *q, const tgpu_request *req, int batched) {
     const int modes = TGPU_FLAG_DENSE_SCAN | TGPU_FLAG_GATHER_SCAN | TGPU_FLAG_NO_WARP_COMBINE |
                       TGPU_FLAG_STAGED_SCAN | TGPU_FLAG_NO_STAGED | TGPU_FLAG_NO_PREFETCH |
-                      TGPU_FLAG_NO_CHUNK_PREFETCH | TGPU_FLAG_DISTINCT_PREFETCH;
+                      TGPU_FLAG_NO_CHUNK_PREFETCH | TGPU_FLAG_DISTINCT_PREFETCH | TGPU_FLAG_DISTINCT_PARTITION |
+                      TGPU_FLAG_NO_DISTINCT_PARTITION;
     const int own = modes | TGPU_FLAG_NO_TUNING;
     if (req->chunk_rows || req->cache_slots || req->table_load_pct || (req->flags & own)) return;
     const tgpu_shape s = shape_of(q, req, batched);
@@ -1354,6 +1402,7 @@ tgpu_status query_create(tgpu_table *table, const tgpu_request *req, int batched
     if (st != TGPU_OK) return st;
     std::unique_ptr<tgpu_query> q(new tgpu_query());
     q->t = table;
+    q->batched = batched != 0;
     q->stream = req->stream ? (cudaStream_t)req->stream : dev->stream;
     q->flags = req->flags;
     q->limit = req->limit;

@@ -149,6 +149,13 @@ struct DevQuery {
     int32_t cache_probe;      // probe limit (cache_slots when the table holds every group)
     int32_t warp_combine;     // __match_any_sync pre-combine on/off
     int32_t gather;           // 1 = compact survivors, then gather; 0 = process rows in place
+    // partitioned COUNT(DISTINCT) (one distinct aggregate): the scan appends
+    // (value, gid) pairs to 2^dpart_bits hash partitions of dpart_cap
+    // entries; dpart_bits == 0: inserts go straight to the distinct set
+    int32_t dpart_bits;
+    uint32_t dpart_cap;
+    uint32_t *dpart_cursor;          // per partition
+    ulonglong2 *dpart_buf;           // partition p at [p * dpart_cap, (p + 1) * dpart_cap)
     // prefetching: PF_* bits, and the columns whose next chunk a warp pulls
     // into L2 with one bulk prefetch per column before scanning its chunk
     int32_t prefetch;
@@ -256,6 +263,14 @@ struct StagePlan {
 // the query does not qualify.
 bool stage_plan(DevQuery &q, uint64_t tile_count, StagePlan *sp);
 cudaError_t launch_staged_scan(const DevQuery &q, const StagePlan &sp, int grid, cudaStream_t s);
+
+// Partitioned COUNT(DISTINCT): pairs per partition (one CTA deduplicates a
+// partition in shared memory) and the partition's index-table slots.
+constexpr uint32_t DPART_CAP = 8192;
+constexpr uint32_t DPART_SLOTS = 16384;
+// Deduplicate every partition's pairs and add each new pair to its group's
+// distinct count (table word `word` of slot gid).
+cudaError_t launch_distinct_partitions(const DevQuery &q, int word, cudaStream_t s);
 
 // Message returned by tgpu_last_error_message() on this thread (api.cpp).
 void set_error(const char *msg);

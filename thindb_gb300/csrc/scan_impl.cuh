@@ -242,6 +242,20 @@ __device__ bool distinct_insert(const DevQuery &q, int d, uint32_t gid, uint64_t
     return false;
 }
 
+// Partition of a (gid, value) pair in the partitioned COUNT(DISTINCT), and
+// the pair's slot in that partition's shared-memory index table: top and low
+// bits of one hash.
+__device__ __forceinline__ uint64_t dpart_hash(uint32_t gid, uint64_t bits) { return mix64(bits ^ mix64(gid)); }
+
+// Append (value, gid) to its partition; a full partition sets
+// ST_DISTINCT_FULL (the host reruns with four times the partitions).
+__device__ __forceinline__ void dpart_append(const DevQuery &q, uint32_t gid, uint64_t bits) {
+    const uint64_t p = dpart_hash(gid, bits) >> (64 - q.dpart_bits);
+    const uint32_t pos = atomicAdd(q.dpart_cursor + p, 1u);
+    if (pos < q.dpart_cap) q.dpart_buf[p * q.dpart_cap + pos] = make_ulonglong2(bits, gid);
+    else atomicOr(q.status, ST_DISTINCT_FULL);
+}
+
 // ------------------------------------------------------- fold of states --
 
 template <int NA>
@@ -561,7 +575,8 @@ __device__ __noinline__ void fold_batch(const DevQuery &q, const ScanSmem &sm, c
                 const DevAgg &g = q.aggs[a];
                 if (g.kind != AK_DISTINCT || !((ok >> a) & 1u)) continue;
                 uint64_t bits = g.is_float_in ? canon_f64_bits(bits_f64(val[a])) : val[a];
-                if (distinct_insert(q, g.dset, gid, bits, hash_key(k0, k1))) atomicAdd(gst + g.word, 1ULL);
+                if (q.dpart_bits) dpart_append(q, gid, bits);
+                else if (distinct_insert(q, g.dset, gid, bits, hash_key(k0, k1))) atomicAdd(gst + g.word, 1ULL);
             }
         }
     }
@@ -720,7 +735,7 @@ struct FastFold {
 
     __device__ __forceinline__ static void prefetch(const DevQuery &q, const Row &rv, bool me) {
         const uint64_t hk = prefetch_slot(q, rv.k0, rv.k1, me);
-        if (DISTINCT && me && (q.prefetch & PF_DISTINCT)) {
+        if (DISTINCT && me && (q.prefetch & PF_DISTINCT) && !q.dpart_bits) {
 #pragma unroll
             for (int a = 0; a < NA; ++a)
                 if (kind(a) == AK_DISTINCT) {
@@ -857,7 +872,9 @@ struct FastFold {
 #pragma unroll
                 for (int a = 0; a < NV; ++a) {
                     if (a >= NA || kind(a) != AK_DISTINCT) continue;
-                    if (distinct_insert(q, q.faggs[a].dset, gid, val[a], hk)) atomicAdd(gst + q.faggs[a].word, 1ULL);
+                    if (q.dpart_bits) dpart_append(q, gid, val[a]);
+                    else if (distinct_insert(q, q.faggs[a].dset, gid, val[a], hk))
+                        atomicAdd(gst + q.faggs[a].word, 1ULL);
                 }
             }
         }
