@@ -46,7 +46,7 @@ from .engine import lib as engine_lib
 KNOBS = {
     "flags": [0, abi.FLAG_STAGED_SCAN, abi.FLAG_DENSE_SCAN, abi.FLAG_GATHER_SCAN, abi.FLAG_NO_WARP_COMBINE,
               abi.FLAG_NO_PREFETCH, abi.FLAG_NO_CHUNK_PREFETCH, abi.FLAG_NO_PREFETCH | abi.FLAG_NO_CHUNK_PREFETCH,
-              abi.FLAG_DISTINCT_PREFETCH],
+              abi.FLAG_DISTINCT_PREFETCH, abi.FLAG_NO_DISTINCT_PARTITION],
     "chunk_rows": [0, 512, 1024, 2048, 4096],
     "cache_slots": [0, -1, 256, 1024, 4096],
     "table_load_pct": [0, 25, 70],
