@@ -403,9 +403,11 @@ typedef struct tgpu_server tgpu_server;
 typedef struct tgpu_server_options {
     uint64_t memory_budget_bytes;  /* 0 = 120 GB */
     uint32_t max_batch;            /* requests per wave, 0 = 256 */
-    uint32_t max_inflight;         /* waves on the device at once, 0 = 4 */
+    uint32_t max_inflight;         /* waves on the device at once, 0 = 8 */
     int32_t mode;                  /* TGPU_SERVE_* */
-    int32_t reserved;
+    int32_t batch_min;             /* continuous mode: waiting requests on one table that
+                                    * make a wave one batched kernel (0 = 64); fewer run as
+                                    * separate executions overlapping on the wave streams */
 } tgpu_server_options;
 
 typedef struct tgpu_server_stats {

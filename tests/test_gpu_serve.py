@@ -41,10 +41,13 @@ def alone(tables, ti, req):
     return rows
 
 
-@pytest.mark.parametrize("mode", ["continuous", "plain"])
+@pytest.mark.parametrize("mode", ["continuous-batched", "continuous", "plain"])
 def test_results_same_alone_and_in_the_mix(tables, mode):
+    """continuous: overlapping single executions; continuous-batched: every
+    wave of same-table requests as one batched kernel (batch_min 1)."""
     mix = workloads.served_mix(36, seed=8)
-    srv = Server(tables, mode=mode, max_batch=16, max_inflight=3)
+    srv = Server(tables, mode="plain" if mode == "plain" else "continuous", max_batch=16, max_inflight=3,
+                 batch_min=1 if mode == "continuous-batched" else 0)
     tickets = [srv.submit(ti, rq) for ti, rq in mix]  # all in flight together
     for (ti, rq), tk in zip(mix, tickets):
         got = to_rows(srv.result(tk))
@@ -54,7 +57,7 @@ def test_results_same_alone_and_in_the_mix(tables, mode):
         srv.release(tk)
     st = srv.stats()
     assert st.completed == len(mix) and st.failed == 0
-    if mode == "continuous":
+    if mode == "continuous-batched":
         assert st.waves < len(mix)  # requests shared waves
     srv.close()
 

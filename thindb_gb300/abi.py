@@ -155,7 +155,7 @@ SERVE_CONTINUOUS, SERVE_PLAIN = 0, 1
 
 class ServerOptions(C.Structure):
     _fields_ = [("memory_budget_bytes", C.c_uint64), ("max_batch", C.c_uint32), ("max_inflight", C.c_uint32),
-                ("mode", C.c_int32), ("reserved", C.c_int32)]
+                ("mode", C.c_int32), ("batch_min", C.c_int32)]
 
 
 class ServerStats(C.Structure):

@@ -2133,8 +2133,16 @@ struct tgpu_server {
                 break;
             }
         if (slot < 0) return false;
-        const uint32_t max_batch = opt.mode == TGPU_SERVE_PLAIN ? 1 : (opt.max_batch ? opt.max_batch : 256);
+        uint32_t max_batch = opt.mode == TGPU_SERVE_PLAIN ? 1 : (opt.max_batch ? opt.max_batch : 256);
         table = pending.front()->table;
+        if (max_batch > 1) {
+            // a short backlog runs as separate executions overlapping on the
+            // wave streams; a long one on one table as one batched kernel
+            const uint32_t batch_min = opt.batch_min > 0 ? (uint32_t)opt.batch_min : 64;
+            uint32_t same = 0;
+            for (Ticket *tk : pending) same += tk->table == table ? 1 : 0;
+            if (same < batch_min) max_batch = 1;
+        }
         bytes = 0;
         for (auto it = pending.begin(); it != pending.end() && out.size() < max_batch;) {
             Ticket *tk = *it;
@@ -2269,7 +2277,7 @@ tgpu_status tgpu_server_create(tgpu_table *const *tables, uint32_t n, const tgpu
     s->tables.assign(tables, tables + n);
     if (opts) s->opt = *opts;
     if (!s->opt.memory_budget_bytes) s->opt.memory_budget_bytes = 120ULL << 30;
-    if (!s->opt.max_inflight) s->opt.max_inflight = 4;
+    if (!s->opt.max_inflight) s->opt.max_inflight = 8;
     if (s->opt.mode == TGPU_SERVE_PLAIN) s->opt.max_inflight = 1;
     s->device = dev->id;
     for (uint32_t i = 0; i < s->opt.max_inflight; ++i) {

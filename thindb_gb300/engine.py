@@ -585,13 +585,14 @@ class Server:
     """Continuous-batching request loop over resident tables (native dispatcher)."""
 
     def __init__(self, tables: Sequence[Table], mode: str = "continuous", memory_budget: int = 0,
-                 max_batch: int = 0, max_inflight: int = 0):
+                 max_batch: int = 0, max_inflight: int = 0, batch_min: int = 0):
         self.tables = list(tables)
         arr = (C.c_void_p * len(self.tables))(*[t.handle.value for t in self.tables])
         o = abi.ServerOptions()
         o.memory_budget_bytes = memory_budget
         o.max_batch = max_batch
         o.max_inflight = max_inflight
+        o.batch_min = batch_min
         o.mode = abi.SERVE_PLAIN if mode == "plain" else abi.SERVE_CONTINUOUS
         h = C.c_void_p()
         _check(lib().tgpu_server_create(arr, len(self.tables), C.byref(o), C.byref(h)))
