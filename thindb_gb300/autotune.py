@@ -42,6 +42,7 @@ import numpy as np
 from . import abi, datagen, workloads
 from .engine import QueryBatch, Request, Table, request_shape, try_build_group_topn
 from .engine import lib as engine_lib
+from .engine import tuning_entries as engine_tuning_entries
 
 KNOBS = {
     "flags": [0, abi.FLAG_STAGED_SCAN, abi.FLAG_DENSE_SCAN, abi.FLAG_GATHER_SCAN, abi.FLAG_NO_WARP_COMBINE,
@@ -147,14 +148,21 @@ def time_batch(table: Table, reqs: list, knobs: dict, reps: int, stream: int):
         b.close()
 
 
-def descend(measure, same, log=print, rounds: int = 2):
-    """Coordinate descent over KNOBS from the built-in setting."""
+def descend(measure, same, log=print, rounds: int = 3, starts=()):
+    """Coordinate descent over KNOBS from the best of the built-in setting and
+    `starts` (e.g. the installed table's entry for the shape)."""
     base = measure(DEFAULT)
     if base is None:
         raise RuntimeError("the built-in setting failed")
     best, (best_ms, ref) = dict(DEFAULT), base
     default_ms = best_ms
     log(f"  built-in: {best_ms:.3f} ms")
+    for st in starts:
+        r = measure(st)
+        if r is not None and same(r[1], ref):
+            log(f"  start {st}: {r[0]:.3f} ms")
+            if r[0] < best_ms:
+                best, best_ms = dict(st), r[0]
     for _ in range(rounds):
         improved = False
         for knob, values in KNOBS.items():
@@ -174,7 +182,15 @@ def descend(measure, same, log=print, rounds: int = 2):
     return best, default_ms, best_ms
 
 
-def tune_workload(name: str, n: int, stream: int, reps: int, log=print) -> list:
+def _incumbent(shape: dict, table: list) -> list:
+    """The installed table's setting for `shape`, as a starting point."""
+    for e in table:
+        if e["shape"] == shape:
+            return [{k: int(e.get(k, 0)) for k in DEFAULT}]
+    return []
+
+
+def tune_workload(name: str, n: int, stream: int, reps: int, log=print, previous=()) -> list:
     """Tuning entries for one workload's shapes."""
     inputs = workloads.table_inputs(name, n, pinned=True)
     table = Table(workloads.columns(inputs), compute_ndv=True, stream=stream)
@@ -185,15 +201,17 @@ def tune_workload(name: str, n: int, stream: int, reps: int, log=print) -> list:
             reqs = workloads.batched_requests(256, seed=4)
             for r in reqs:
                 r.stream = stream
-            best, d_ms, b_ms = descend(lambda k: time_batch(table, reqs, k, reps, stream),
-                                       lambda a, b: all(_same(x, y) for x, y in zip(a, b)), log)
             shapes = {json.dumps(request_shape(table, r, batched=True), sort_keys=True) for r in reqs}
+            starts = _incumbent(json.loads(sorted(shapes)[0]), previous)
+            best, d_ms, b_ms = descend(lambda k: time_batch(table, reqs, k, reps, stream),
+                                       lambda a, b: all(_same(x, y) for x, y in zip(a, b)), log, starts=starts)
             for sh in sorted(shapes):
                 entries.append({"shape": json.loads(sh), **best, "workload": "batched (256 queries, tuned as one)",
                                 "ms_builtin": d_ms, "ms_tuned": b_ms})
         else:
             req = workloads.workload_request(name, stream=stream)
-            best, d_ms, b_ms = descend(lambda k: time_query(table, req, k, reps), _same, log)
+            starts = _incumbent(request_shape(table, req), previous)
+            best, d_ms, b_ms = descend(lambda k: time_query(table, req, k, reps), _same, log, starts=starts)
             entries.append({"shape": request_shape(table, req), **best, "workload": name,
                             "ms_builtin": d_ms, "ms_tuned": b_ms})
     finally:
@@ -215,12 +233,13 @@ def main(argv=None) -> int:
     torch.cuda.set_device(0)
     stream = torch.cuda.Stream()
     t0 = time.time()
+    previous = engine_tuning_entries()  # the installed table: warm starts
     entries = []
     for name in args.workloads.split(","):
         n = max(1 << 16, int(sizes[name] * args.scale))
         print(f"{name}: {n:,} rows", file=sys.stderr, flush=True)
         entries += tune_workload(name, n, stream.cuda_stream, args.reps,
-                                 log=lambda m: print(m, file=sys.stderr, flush=True))
+                                 log=lambda m: print(m, file=sys.stderr, flush=True), previous=previous)
     doc = {
         "device": torch.cuda.get_device_name(0),
         "generated_by": "python -m thindb_gb300.autotune " + " ".join(argv if argv is not None else sys.argv[1:]),
