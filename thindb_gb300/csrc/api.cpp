@@ -1112,16 +1112,19 @@ tgpu_status enqueue(tgpu_query *q) {
         q->launches++;
     }
     if (timing) CU(cudaEventRecord(q->ev[1], s));
-    CU(launch_compact(df, q->d_block_counts, q->n_cpt_blocks, q->d_gids, q->d_counts, s));
-    q->launches += 2;
+    if (q->rank != RANK_TOPK) {
+        CU(launch_compact(df, q->d_block_counts, q->n_cpt_blocks, q->d_gids, q->d_counts, s));
+        q->launches += 2;
+    }
     const uint32_t *sel = q->d_gids;
     uint64_t gather_offset = 0, gather_rows = q->out_rows_max;
     if (q->rank == RANK_NONE) {
         CU(launch_sel_all(q->d_counts, s));
         q->launches++;
     } else if (q->rank == RANK_TOPK) {
-        CU(launch_topk(df, q->d_gids, q->d_counts, q->k, q->d_cand_keys, q->d_cand_gids, q->n_cand_blocks, q->d_sel, s));
-        q->launches += 2;
+        CU(launch_topk_scan(df, q->d_counts, q->k, q->d_cand_keys, q->d_cand_gids, q->n_cand_blocks, q->d_sel,
+                            q->d_ctrl + 2, s));
+        q->launches += 1;
         sel = q->d_sel;
         gather_offset = q->offset;
         gather_rows = q->limit;

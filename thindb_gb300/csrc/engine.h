@@ -288,6 +288,11 @@ int batch_scan_grid(int max_aggs, size_t smem, int sms);
 cudaError_t launch_batch_scan(const DevQuery *qs, const uint2 *items, uint32_t n_items, int max_aggs, size_t smem,
                               int grid, const volatile int *cancel, unsigned int *status, cudaStream_t s);
 // compaction, top-k / all-groups selection, gather and clear for every query of a batch
+// single-query top-k straight from the occupancy bitmap (counts[0] groups,
+// [1] kept, [3] selected); `done` is a zeroed counter
+cudaError_t launch_topk_scan(const DevFinal &f, unsigned long long *counts, uint32_t k, unsigned long long *cand_keys,
+                             uint32_t *cand_gids, uint32_t n_cand_blocks, uint32_t *sel_out, unsigned int *done,
+                             cudaStream_t s);
 // topk_widths: TOPK_W* bits of the key-width classes of the batch's top-k queries
 cudaError_t launch_finalize_batch(const DevFinal *fs, const DevFinalBufs *bs, uint32_t n_queries,
                                   uint32_t max_cpt_blocks, uint32_t max_cand_blocks, uint32_t topk_widths,

@@ -436,13 +436,46 @@ __device__ __forceinline__ void wl_offer(WarpList<SW> &t, const uint64_t (&cand)
 // produced by get(i, key, gid) -> valid.  Every warp keeps its own list; warp
 // 0 merges them and writes k entries (NO_ID pads) to out_keys (if given) and
 // out_gids, and the kept count to *out_count (if given).
+// Every warp's list -> the CTA's best k, written by warp 0 to out_keys (if
+// given) and out_gids (k entries, NO_ID pads), the count to *out_count (if
+// given).  All threads return after the merge.
+template <int SW>
+__device__ __forceinline__ void block_merge(const WarpList<SW> &t, int k, unsigned long long *out_keys,
+                                            uint32_t *out_gids, unsigned long long *out_count) {
+    __shared__ unsigned long long s_keys[TOPK_WARPS * 32 * SW];
+    __shared__ uint32_t s_ids[TOPK_WARPS * 32];
+    __shared__ int s_cnt[TOPK_WARPS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < SW; ++i) s_keys[((size_t)warp * 32 + lane) * SW + i] = t.key[i];
+    s_ids[warp * 32 + lane] = t.gid;
+    if (lane == 0) s_cnt[warp] = t.count;
+    __syncthreads();
+    if (warp == 0) {
+        WarpList<SW> m;
+        wl_init(m);
+        for (int w = 0; w < TOPK_WARPS; ++w) {
+            uint64_t c[SW];
+#pragma unroll
+            for (int i = 0; i < SW; ++i) c[i] = s_keys[((size_t)w * 32 + lane) * SW + i];
+            wl_offer<SW>(m, c, s_ids[w * 32 + lane], lane < s_cnt[w], k);
+        }
+        if (lane < k) {
+            if (out_keys) {
+#pragma unroll
+                for (int i = 0; i < SW; ++i) out_keys[(size_t)lane * SW + i] = m.key[i];
+            }
+            out_gids[lane] = lane < m.count ? m.gid : NO_ID;
+        }
+        if (out_count && lane == 0) *out_count = (unsigned long long)m.count;
+    }
+    __syncthreads();
+}
+
 template <int SW, class Get>
 __device__ __forceinline__ void block_topk(uint64_t n, uint64_t first, uint64_t stride, int k, Get get,
                                            unsigned long long *out_keys, uint32_t *out_gids,
                                            unsigned long long *out_count) {
-    __shared__ unsigned long long s_keys[TOPK_WARPS * 32 * SW];
-    __shared__ uint32_t s_ids[TOPK_WARPS * 32];
-    __shared__ int s_cnt[TOPK_WARPS];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     WarpList<SW> t;
     wl_init(t);
@@ -468,28 +501,7 @@ __device__ __forceinline__ void block_topk(uint64_t n, uint64_t first, uint64_t 
 #pragma unroll
         for (int u = 0; u < U; ++u) wl_offer<SW>(t, c[u], g[u], valid[u], k);
     }
-#pragma unroll
-    for (int i = 0; i < SW; ++i) s_keys[((size_t)warp * 32 + lane) * SW + i] = t.key[i];
-    s_ids[warp * 32 + lane] = t.gid;
-    if (lane == 0) s_cnt[warp] = t.count;
-    __syncthreads();
-    if (warp != 0) return;
-    WarpList<SW> m;
-    wl_init(m);
-    for (int w = 0; w < TOPK_WARPS; ++w) {
-        uint64_t c[SW];
-#pragma unroll
-        for (int i = 0; i < SW; ++i) c[i] = s_keys[((size_t)w * 32 + lane) * SW + i];
-        wl_offer<SW>(m, c, s_ids[w * 32 + lane], lane < s_cnt[w], k);
-    }
-    if (lane < k) {
-        if (out_keys) {
-#pragma unroll
-            for (int i = 0; i < SW; ++i) out_keys[(size_t)lane * SW + i] = m.key[i];
-        }
-        out_gids[lane] = lane < m.count ? m.gid : NO_ID;
-    }
-    if (out_count && lane == 0) *out_count = (unsigned long long)m.count;
+    block_merge<SW>(t, k, out_keys, out_gids, out_count);
 }
 
 // Per-CTA top-k of the dense group list: k candidates per CTA, at
@@ -540,6 +552,84 @@ __global__ void __launch_bounds__(TOPK_THREADS) topk_final_kernel(const unsigned
                                                                   const uint32_t *cand_gids, uint32_t n_blocks, int k,
                                                                   uint32_t *sel_out, unsigned long long *counts) {
     topk_final_body<SW>(cand_keys, cand_gids, n_blocks, k, sel_out, counts);
+}
+
+// Single-query top-k in one launch: CTA b walks bitmap words b*256 + ...,
+// counts the groups and the HAVING survivors, offers each survivor's
+// encoded key to its warp's list, merges them into the CTA's k candidates,
+// and the last CTA to finish (a counter bumped after a threadfence; nobody
+// waits) merges every CTA's candidates into sel_out / counts[3].
+template <int SW>
+__global__ void __launch_bounds__(TOPK_THREADS) topk_scan_kernel(const __grid_constant__ DevFinal f, uint64_t n_words,
+                                                                 int k, unsigned long long *cand_keys,
+                                                                 uint32_t *cand_gids, uint32_t *sel_out,
+                                                                 unsigned long long *counts, unsigned int *done) {
+    __shared__ unsigned long long s_sum[2][TOPK_WARPS];
+    __shared__ int s_last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    WarpList<SW> t;
+    wl_init(t);
+    unsigned long long groups = 0, kept = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * TOPK_THREADS;
+    for (uint64_t base = (uint64_t)blockIdx.x * TOPK_THREADS + (uint64_t)warp * 32; base < n_words; base += stride) {
+        const uint64_t w = base + lane;
+        uint32_t bits = w < n_words ? f.occ[w] : 0u;
+        groups += (unsigned)__popc(bits);
+        while (__any_sync(FULL, bits != 0)) {
+            uint64_t c[SW];
+            uint32_t g = NO_ID;
+            bool valid = false;
+            if (bits) {
+                const int b = __ffs(bits) - 1;
+                bits &= bits - 1;
+                g = (uint32_t)(w * 32 + b);
+                valid = f.n_having == 0 || having_pass(f, slot_states(f, g));
+            }
+            if (valid) {
+                encode_top_key<SW>(f, g, c);
+                ++kept;
+            } else {
+#pragma unroll
+                for (int j = 0; j < SW; ++j) c[j] = 0;
+            }
+            wl_offer<SW>(t, c, g, valid, k);
+        }
+    }
+    for (int o = 16; o; o >>= 1) {
+        groups += __shfl_down_sync(FULL, groups, o);
+        kept += __shfl_down_sync(FULL, kept, o);
+    }
+    if (lane == 0) {
+        s_sum[0][warp] = groups;
+        s_sum[1][warp] = kept;
+    }
+    block_merge<SW>(t, k, cand_keys + (size_t)blockIdx.x * 32 * SW, cand_gids + (size_t)blockIdx.x * 32, nullptr);
+    if (threadIdx.x == 0) {
+        unsigned long long gsum = 0, ksum = 0;
+        for (int i = 0; i < TOPK_WARPS; ++i) {
+            gsum += s_sum[0][i];
+            ksum += s_sum[1][i];
+        }
+        if (gsum) atomicAdd(&counts[0], gsum);
+        if (ksum) atomicAdd(&counts[1], ksum);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const uint32_t nb = gridDim.x;
+    block_topk<SW>(
+        (uint64_t)nb * k, 0, TOPK_THREADS, k,
+        [&](uint64_t i, uint64_t(&c)[SW], uint32_t &g) {
+            const uint64_t e = (i / k) * 32 + (i % k);
+            g = __ldcg(cand_gids + e);
+#pragma unroll
+            for (int j = 0; j < SW; ++j) c[j] = __ldcg(cand_keys + e * SW + j);
+            return g != NO_ID;
+        },
+        nullptr, sel_out, counts + 3);
 }
 
 // ------------------------------------------------------------ merge sort --
@@ -813,6 +903,26 @@ cudaError_t launch_topk(const DevFinal &f, const uint32_t *gids, unsigned long l
         case 6: launch_topk_w<6>(f, gids, counts, k, cand_keys, cand_gids, n_cand_blocks, sel_out, s); break;
         case 8: launch_topk_w<8>(f, gids, counts, k, cand_keys, cand_gids, n_cand_blocks, sel_out, s); break;
         default: launch_topk_w<14>(f, gids, counts, k, cand_keys, cand_gids, n_cand_blocks, sel_out, s); break;
+    }
+    return cudaGetLastError();
+}
+
+template <int SW>
+static void launch_topk_scan_w(const DevFinal &f, uint32_t k, unsigned long long *cand_keys, uint32_t *cand_gids,
+                               uint32_t n_blocks, uint32_t *sel_out, unsigned long long *counts, unsigned int *done,
+                               cudaStream_t s) {
+    topk_scan_kernel<SW><<<n_blocks, TOPK_THREADS, 0, s>>>(f, occ_words(f.cap), (int)k, cand_keys, cand_gids, sel_out,
+                                                           counts, done);
+}
+
+cudaError_t launch_topk_scan(const DevFinal &f, unsigned long long *counts, uint32_t k, unsigned long long *cand_keys,
+                             uint32_t *cand_gids, uint32_t n_cand_blocks, uint32_t *sel_out, unsigned int *done,
+                             cudaStream_t s) {
+    switch (topk_width(f.sort_words)) {
+        case 4: launch_topk_scan_w<4>(f, k, cand_keys, cand_gids, n_cand_blocks, sel_out, counts, done, s); break;
+        case 6: launch_topk_scan_w<6>(f, k, cand_keys, cand_gids, n_cand_blocks, sel_out, counts, done, s); break;
+        case 8: launch_topk_scan_w<8>(f, k, cand_keys, cand_gids, n_cand_blocks, sel_out, counts, done, s); break;
+        default: launch_topk_scan_w<14>(f, k, cand_keys, cand_gids, n_cand_blocks, sel_out, counts, done, s); break;
     }
     return cudaGetLastError();
 }
