@@ -225,9 +225,8 @@ typedef struct tgpu_request {
 #define TGPU_FLAG_TIMING 0x1
 /* Force the global-table route even when the groups fit a CTA's shared memory. */
 #define TGPU_FLAG_FORCE_GLOBAL 0x2
-/* Fold rows in place (every needed column loaded densely) instead of
- * compacting the WHERE's survivors and gathering their keys and inputs (the
- * default unless the WHERE is estimated to keep 60% of the rows or more). */
+/* Fold rows in place (every needed column loaded densely, a fold per 32
+ * scanned rows) instead of the queue or gather modes. */
 #define TGPU_FLAG_DENSE_SCAN 0x4
 /* Disable the in-warp __match_any_sync pre-combine (tuning / tests). */
 #define TGPU_FLAG_NO_WARP_COMBINE 0x8
@@ -249,6 +248,11 @@ typedef struct tgpu_request {
  * aggregate over 8M rows or more outside batches), or never. */
 #define TGPU_FLAG_DISTINCT_PARTITION 0x800
 #define TGPU_FLAG_NO_DISTINCT_PARTITION 0x1000
+/* Queue mode for a WHERE: every row's key and inputs loaded densely, the
+ * survivors compacted into a per-warp shared-memory ring and folded in full
+ * batches (the default for a compiled fold unless the WHERE is estimated to
+ * keep under 4% of the rows, when survivors are gathered instead). */
+#define TGPU_FLAG_QUEUE_SCAN 0x2000
 
 /* ----------------------------------------------------------------- output -- */
 
@@ -298,6 +302,7 @@ typedef struct tgpu_query_stats {
 #define TGPU_STAT_GATHER 0x2    /* survivors gathered (late materialisation) */
 #define TGPU_STAT_STAGED 0x4    /* the staged (bulk-copy ring) scan ran */
 #define TGPU_STAT_DISTINCT_PARTITION 0x8  /* COUNT(DISTINCT) went through partitions */
+#define TGPU_STAT_QUEUE 0x10    /* queue mode (dense loads, per-warp survivor ring) */
 
 /* -------------------------------------------------------------- the API -- */
 

@@ -360,3 +360,32 @@ def test_distinct_partitioned_nullable_and_float_values():
     req = Request(["k"], [AggSpec("count_distinct", "v", "d"), AggSpec("count", None, "c")], flags=DPART)
     _, st = run_both(cols, req)
     assert st.flags & abi.STAT_DISTINCT_PARTITION
+
+
+# -------------------------------------------------------------- queue mode --
+# Dense coalesced loads, survivors compacted into a per-warp shared-memory
+# ring, full-batch folds: the default for a compiled fold under a WHERE that
+# keeps 4% of the rows or more; forced here on other selectivities too.
+
+@pytest.mark.parametrize("flags", [abi.FLAG_QUEUE_SCAN, abi.FLAG_QUEUE_SCAN | abi.FLAG_FORCE_GLOBAL,
+                                   abi.FLAG_QUEUE_SCAN | abi.FLAG_NO_WARP_COMBINE])
+def test_queue_mode_filtered(flags):
+    cols = filtered_cols(2_000_000, 200_000)
+    _, st = run_both(cols, Request(["k"], C2_AGGS, [SortSpec("s", True)], limit=10, where=FILTER, flags=flags))
+    assert st.flags & abi.STAT_QUEUE
+    _, st = run_both(cols, Request(["k"], C2_AGGS, where=FILTER, flags=flags))
+    assert st.flags & abi.STAT_QUEUE
+
+
+def test_queue_mode_sparse_and_pruned():
+    cols = filtered_cols(1_500_000, 100_000)
+    narrow = [Pred("d", "between", datagen.FILTER_LO, datagen.FILTER_LO)]  # one day, ~0.3%
+    _, st = run_both(cols, Request(["k"], C2_AGGS, where=narrow, flags=abi.FLAG_QUEUE_SCAN))
+    assert st.flags & abi.STAT_QUEUE
+    n = (1 << 20) + 77
+    d = np.sort(np.random.default_rng(4).integers(0, 1000, n)).astype(np.int32)
+    k = (np.arange(n) % 911).astype(np.int64)
+    cols = [Column("k", abi.BIGINT, k), Column("d", abi.DATE, d)]
+    _, st = run_both(cols, Request(["k"], [AggSpec("count", None, "c"), AggSpec("max", "d", "md")],
+                                   where=[Pred("d", "between", 300, 320)], flags=abi.FLAG_QUEUE_SCAN))
+    assert st.flags & abi.STAT_QUEUE and st.row_groups_pruned > 0

@@ -45,7 +45,8 @@ from .engine import lib as engine_lib
 from .engine import tuning_entries as engine_tuning_entries
 
 KNOBS = {
-    "flags": [0, abi.FLAG_STAGED_SCAN, abi.FLAG_DENSE_SCAN, abi.FLAG_GATHER_SCAN, abi.FLAG_NO_WARP_COMBINE,
+    "flags": [0, abi.FLAG_STAGED_SCAN, abi.FLAG_DENSE_SCAN, abi.FLAG_GATHER_SCAN, abi.FLAG_QUEUE_SCAN,
+              abi.FLAG_NO_WARP_COMBINE,
               abi.FLAG_NO_PREFETCH, abi.FLAG_NO_CHUNK_PREFETCH, abi.FLAG_NO_PREFETCH | abi.FLAG_NO_CHUNK_PREFETCH,
               abi.FLAG_DISTINCT_PREFETCH, abi.FLAG_NO_DISTINCT_PARTITION],
     "chunk_rows": [0, 512, 1024, 2048, 4096],

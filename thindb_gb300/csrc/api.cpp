@@ -822,10 +822,19 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     // survivors are compacted and folded 32 at a time (gather) unless the
     // WHERE is estimated to keep most rows: folding in place runs a fold per
     // 32 scanned rows, however few of them survive
+    // queue mode (dense coalesced loads, survivors compacted into a per-warp
+    // shared-memory ring, full-batch folds) for a compiled fold unless the
+    // WHERE keeps so few rows that gathering them reads far fewer lines
     {
-        const bool dense_enough = q->sel_est * 10 >= std::max<uint64_t>(1, q->rows_scanned) * 6;  // >= 60%
-        dq.gather = dq.n_preds > 0 && !(q->flags & TGPU_FLAG_DENSE_SCAN) &&
-                    ((q->flags & TGPU_FLAG_GATHER_SCAN) || !dense_enough);
+        const uint64_t rows = std::max<uint64_t>(1, q->rows_scanned);
+        const bool dense_enough = q->sel_est * 10 >= rows * 6;  // >= 60%
+        const bool sparse = q->sel_est * 25 < rows;              // < 4%
+        dq.gather = 0;
+        if (dq.n_preds > 0 && !(q->flags & TGPU_FLAG_DENSE_SCAN)) {
+            if (q->flags & TGPU_FLAG_GATHER_SCAN) dq.gather = 1;
+            else if (dq.fast_id >= 0 && ((q->flags & TGPU_FLAG_QUEUE_SCAN) || !sparse)) dq.gather = 2;
+            else if (!dense_enough) dq.gather = 1;
+        }
     }
 
     // chunking: about eight chunks per warp of a two-CTA-per-SM grid
@@ -838,11 +847,13 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
         if (!chunk) {
             chunk = std::max<uint64_t>(1, q->rows_scanned / (warps * 8));
             chunk = std::max<uint64_t>(CHUNK_ALIGN, chunk / CHUNK_ALIGN * CHUNK_ALIGN);
-            chunk = std::min<uint64_t>(chunk, dq.gather ? 1024 : 4096);
+            chunk = std::min<uint64_t>(chunk, dq.gather == 1 ? 1024 : 4096);
         }
         dq.chunk_rows = (uint32_t)chunk;
     }
-    const size_t list_bytes = dq.gather ? (size_t)SCAN_WARPS * dq.chunk_rows * 2 : 0;
+    const size_t list_bytes =
+        dq.gather == 1 ? (size_t)SCAN_WARPS * dq.chunk_rows * 2
+        : dq.gather == 2 ? (size_t)SCAN_WARPS * WQ_RING_ROWS * (16 + 8 * (size_t)std::max(1, dq.n_faggs)) + 16 : 0;
 
     // route: the shared-memory table holds every group (lowcard), keeps the
     // first-seen (hottest) keys of a larger key space (global route), or is off
@@ -1199,7 +1210,8 @@ tgpu_status finish(tgpu_query *q) {
     s.route = (uint32_t)q->route;
     s.retries = q->retries;
     s.kernel_launches = q->launches;
-    s.flags = (q->tuned ? TGPU_STAT_TUNED : 0) | (q->dq.gather && !q->staged ? TGPU_STAT_GATHER : 0) |
+    s.flags = (q->tuned ? TGPU_STAT_TUNED : 0) | (q->dq.gather == 1 && !q->staged ? TGPU_STAT_GATHER : 0) |
+              (q->dq.gather == 2 && !q->staged ? TGPU_STAT_QUEUE : 0) |
               (q->staged ? TGPU_STAT_STAGED : 0) | (q->dq.dpart_bits ? TGPU_STAT_DISTINCT_PARTITION : 0);
     s.device_bytes = q->table_buf.bytes + q->occ_buf.bytes + q->scratch_bytes;
     for (auto &b : q->dset_bufs) s.device_bytes += b.bytes;
@@ -1243,7 +1255,7 @@ void apply_tuning(tgpu_query *q, const tgpu_request *req, int batched) {
     const int modes = TGPU_FLAG_DENSE_SCAN | TGPU_FLAG_GATHER_SCAN | TGPU_FLAG_NO_WARP_COMBINE |
                       TGPU_FLAG_STAGED_SCAN | TGPU_FLAG_NO_STAGED | TGPU_FLAG_NO_PREFETCH |
                       TGPU_FLAG_NO_CHUNK_PREFETCH | TGPU_FLAG_DISTINCT_PREFETCH | TGPU_FLAG_DISTINCT_PARTITION |
-                      TGPU_FLAG_NO_DISTINCT_PARTITION;
+                      TGPU_FLAG_NO_DISTINCT_PARTITION | TGPU_FLAG_QUEUE_SCAN;
     const int own = modes | TGPU_FLAG_NO_TUNING;
     if (req->chunk_rows || req->cache_slots || req->table_load_pct || (req->flags & own)) return;
     const tgpu_shape s = shape_of(q, req, batched);
@@ -1632,6 +1644,7 @@ tgpu_status batch_descriptors(tgpu_query_batch *b) {
         q->d_counts = b->d_counts + 8 * (size_t)i;
         q->d_ctrl = b->d_qctrl + 4 * (size_t)i;
         DevQuery dq = q->dq;
+        if (dq.gather == 2) dq.gather = 1;  // the batched kernel gathers survivors per chunk
         // row-group aligned chunks: an item is the query's chunks of one row
         // group, split evenly over the CTA's warps
         dq.rg_list = q->d_rg_list;
@@ -1895,7 +1908,7 @@ tgpu_status tgpu_batch_synchronize(tgpu_query_batch *b) {
         q->stats.result_rows = c[2];
         q->stats.table_capacity = q->dq.cap;
         q->stats.route = (uint32_t)q->route;
-        q->stats.flags = (q->tuned ? TGPU_STAT_TUNED : 0) | (q->dq.gather ? TGPU_STAT_GATHER : 0);
+        q->stats.flags = (q->tuned ? TGPU_STAT_TUNED : 0) | (q->dq.gather ? TGPU_STAT_GATHER : 0);  // batched: gather
     }
     return TGPU_OK;
 }

@@ -32,6 +32,7 @@ __host__ __device__ constexpr uint32_t topk_width_bit(int sw) {
 constexpr int SCAN_THREADS = 512;
 constexpr int SCAN_WARPS = SCAN_THREADS / 32;
 constexpr int CHUNK_ALIGN = 256;
+constexpr int WQ_RING_ROWS = 64;  // queue mode: fold rows per warp ring (scan_impl.cuh WQ_ROWS)
 
 // Status bits the kernels OR into the query's device status word.
 constexpr unsigned ST_TABLE_FULL = 1u;      // a probe ran past MAX_PROBE: regrow and rerun

@@ -8,7 +8,7 @@ namespace {
 
 // ---------------------------------------------------------------- kernel --
 
-template <class P, int MINB>
+template <class P, int MINB, bool QUEUE>
 __global__ void __launch_bounds__(SCAN_THREADS, MINB) scan_group_kernel(const __grid_constant__ DevQuery q) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const ScanSmem sm = carve(q, smem_raw);
@@ -17,6 +17,7 @@ __global__ void __launch_bounds__(SCAN_THREADS, MINB) scan_group_kernel(const __
     __syncthreads();
     unsigned long long selected = 0;
     const uint32_t nw = gridDim.x * SCAN_WARPS;
+    WarpQueue<P> wq{(typename P::Row *)sm.wlist + (size_t)warp * WQ_ROWS, 0u, 0u};
     uint32_t k = 0;
     for (uint32_t c = blockIdx.x * SCAN_WARPS + warp; c < q.n_chunks; c += nw, ++k) {
         if ((k & 31) == 31 && q.cancel) {  // poll the host-mapped cancel flag now and then
@@ -28,8 +29,10 @@ __global__ void __launch_bounds__(SCAN_THREADS, MINB) scan_group_kernel(const __
             }
         }
         prefetch_chunk(q, c + nw);  // this warp's next chunk
-        scan_chunk<P>(q, sm, c, selected);
+        if constexpr (QUEUE) scan_chunk_queue<P>(q, sm, c, selected, wq);
+        else scan_chunk<P>(q, sm, c, selected);
     }
+    if constexpr (QUEUE) wq_flush<P>(q, sm, wq);
     if (q.cache_slots) {
         __syncthreads();
         cache_flush(q, sm);
@@ -43,9 +46,9 @@ struct ScanKernel {
     const void *fn;
 };
 
-template <class P, int MINB>
+template <class P, int MINB, bool QUEUE = false>
 static ScanKernel kernel_of() {
-    return ScanKernel{(const void *)scan_group_kernel<P, MINB>};
+    return ScanKernel{(const void *)scan_group_kernel<P, MINB, QUEUE>};
 }
 
 int fold_id_of(const DevQuery &q) {
@@ -60,9 +63,11 @@ int fold_id_of(const DevQuery &q) {
 }
 
 ScanKernel pick_kernel(const DevQuery &q) {
+    const bool queue = q.gather == 2;
     switch (fold_id_of(q)) {
-#define TGPU_PICK(I, KM, A, B, C2, D) \
-    case I: return kernel_of<FastFold<KM, A, B, C2, D>, 2>();
+#define TGPU_PICK(I, KM, A, B, C2, D)                                                       \
+    case I:                                                                                  \
+        return queue ? kernel_of<FastFold<KM, A, B, C2, D>, 2, true>() : kernel_of<FastFold<KM, A, B, C2, D>, 2>();
         TGPU_FAST_FOLDS(TGPU_PICK)
 #undef TGPU_PICK
         default: break;
@@ -76,8 +81,10 @@ ScanKernel pick_kernel(const DevQuery &q) {
 int fast_fold_id(const DevQuery &q) { return fold_id_of(q); }
 
 size_t scan_smem_bytes(const DevQuery &q) {
-    size_t list = q.gather ? (size_t)SCAN_WARPS * q.chunk_rows * 2 : 0;
-    return (size_t)q.cache_slots * (8 + 8 * (size_t)q.state_words + 4) + list + 16;
+    size_t list = 0;
+    if (q.gather == 1) list = (size_t)SCAN_WARPS * q.chunk_rows * 2;
+    if (q.gather == 2) list = (size_t)SCAN_WARPS * WQ_ROWS * (16 + 8 * (size_t)(q.n_faggs > 0 ? q.n_faggs : 1));
+    return (size_t)q.cache_slots * (8 + 8 * (size_t)q.state_words + 4) + 16 + list + 16;
 }
 
 static int blocks_per_sm(const void *kernel, size_t smem) {

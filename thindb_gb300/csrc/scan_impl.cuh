@@ -373,7 +373,8 @@ struct ScanSmem {
     unsigned long long *ckeys;   // cache_slots
     unsigned long long *cstate;  // cache_slots * state_words
     uint32_t *cgid;              // cache_slots
-    uint16_t *wlist;             // SCAN_WARPS * chunk_rows survivor offsets (gather mode)
+    uint16_t *wlist;             // gather mode: SCAN_WARPS * chunk_rows survivor offsets;
+                                 // queue mode: SCAN_WARPS rings of WQ_ROWS fold rows (16-byte aligned)
 };
 
 __device__ __forceinline__ ScanSmem carve(const DevQuery &q, unsigned char *base) {
@@ -382,7 +383,7 @@ __device__ __forceinline__ ScanSmem carve(const DevQuery &q, unsigned char *base
     s.ckeys = (unsigned long long *)base;
     s.cstate = s.ckeys + C;
     s.cgid = (uint32_t *)(s.cstate + (size_t)C * q.state_words);
-    s.wlist = (uint16_t *)(s.cgid + C);
+    s.wlist = (uint16_t *)(((uintptr_t)(s.cgid + C) + 15) & ~(uintptr_t)15);
     return s;
 }
 
@@ -661,6 +662,8 @@ __device__ __forceinline__ uint64_t prefetch_slot(const DevQuery &q, uint64_t k0
 template <int NA>
 struct GenericFold {
     using Row = RowVals<NA>;
+    static constexpr bool QUEUE_OK = false;  // rows too wide for the warp queue
+    static constexpr int QLOOKAHEAD = 1;
     static constexpr int LOOKAHEAD = 1;  // batches gathered before folding
     __device__ __forceinline__ static void load(const DevQuery &q, uint64_t r, bool me, Row &rv) {
         load_row<NA>(q, r, me, rv);
@@ -684,6 +687,8 @@ struct FastFold {
     static constexpr int NA = (K0 != AK_NONE) + (K1 != AK_NONE) + (K2 != AK_NONE) + (K3 != AK_NONE);
     static constexpr int NV = NA > 0 ? NA : 1;
     static constexpr int KM_ = KM, NA_ = NA;
+    static constexpr bool QUEUE_OK = true;
+    static constexpr int QLOOKAHEAD = 2;  // queue mode: 32-row steps loaded before any is compacted
     // batches whose gathers are all in flight before the first folds; the
     // rows stay in registers (64 per thread at two CTAs per SM), so the depth
     // shrinks as a row grows
@@ -990,6 +995,86 @@ __device__ __forceinline__ void scan_chunk(const DevQuery &q, const ScanSmem &sm
             if (b >= n) break;
             const uint32_t left = n - b;
             P::fold(q, sm, rows[j], left >= 32 ? FULL : ((1u << left) - 1));
+        }
+    }
+}
+
+// ------------------------------------------------------------ queue mode --
+// (q.gather == 2) Every row's key and inputs are loaded densely — coalesced,
+// with the predicate's, LOOKAHEAD steps of 32 rows in flight — and the
+// WHERE's survivors are appended to the warp's ring of WQ_ROWS fold rows in
+// shared memory; every time the ring holds 32 rows the warp folds them as
+// one full batch.  The ring persists across the warp's chunks (a row carries
+// its key and inputs, not a chunk offset), so only the warp's last batch is
+// partial.  At the selectivities that pick this mode the survivors touch
+// nearly every line of the key and input columns, so loading them densely
+// costs no extra DRAM bytes and removes the filter -> gather dependency.
+
+constexpr uint32_t WQ_ROWS = WQ_RING_ROWS;
+
+template <class P>
+struct WarpQueue {
+    typename P::Row *ring;  // this warp's WQ_ROWS rows
+    uint32_t head, count;   // warp-uniform; count < 32 between steps
+};
+
+template <class P>
+__device__ __forceinline__ void wq_fold_full(const DevQuery &q, const ScanSmem &sm, WarpQueue<P> &wq) {
+    const int lane = threadIdx.x & 31;
+    while (wq.count >= 32) {
+        __syncwarp();
+        const typename P::Row rv = wq.ring[(wq.head + lane) & (WQ_ROWS - 1)];
+        __syncwarp();
+        P::fold(q, sm, rv, FULL);
+        wq.head = (wq.head + 32) & (WQ_ROWS - 1);
+        wq.count -= 32;
+    }
+}
+
+template <class P>
+__device__ __forceinline__ void wq_flush(const DevQuery &q, const ScanSmem &sm, WarpQueue<P> &wq) {
+    const int lane = threadIdx.x & 31;
+    if (wq.count == 0) return;
+    __syncwarp();
+    const typename P::Row rv = wq.ring[(wq.head + lane) & (WQ_ROWS - 1)];
+    __syncwarp();
+    P::fold(q, sm, rv, (1u << wq.count) - 1);
+    wq.head = 0;
+    wq.count = 0;
+}
+
+template <class P>
+__device__ __forceinline__ void scan_chunk_queue(const DevQuery &q, const ScanSmem &sm, uint32_t c,
+                                                 unsigned long long &selected, WarpQueue<P> &wq) {
+    const int lane = threadIdx.x & 31;
+    uint64_t row0, row_end;
+    chunk_rows(q, c, row0, row_end);
+    if (row0 >= row_end) return;
+    constexpr int L = P::QLOOKAHEAD;
+    for (uint64_t base = row0; base < row_end; base += 32 * L) {
+        typename P::Row rows[L];
+        bool pass[L];
+#pragma unroll
+        for (int j = 0; j < L; ++j) {
+            const uint64_t r = base + 32 * j + lane;
+            P::load(q, r, r < row_end, rows[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < L; ++j) {
+            const uint64_t r = base + 32 * j + lane;
+            pass[j] = r < row_end && row_passes(q, r);
+        }
+#pragma unroll
+        for (int j = 0; j < L; ++j) {
+            const unsigned m = __ballot_sync(FULL, pass[j]);
+            if (m == 0) continue;
+            selected += (lane == 0) ? __popc(m) : 0;
+            if (pass[j]) {
+                wq.ring[(wq.head + wq.count + __popc(m & ((1u << lane) - 1))) & (WQ_ROWS - 1)] = rows[j];
+                P::prefetch(q, rows[j], true);
+            }
+            wq.count += __popc(m);
+            wq_fold_full<P>(q, sm, wq);
         }
     }
 }
