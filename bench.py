@@ -314,7 +314,8 @@ def gpu_arm(args, wl):
             "config": {"workload": wl["name"], "rows": n, "l2": "inputs larger than L2 (no flush)",
                        "selectivity": st.rows_selected / max(1, st.rows_scanned), "groups": st.groups,
                        "route": "shared-memory" if st.route == 1 else "global table",
-                       "scan": "survivor gather" if st.flags & abi.STAT_GATHER else "dense",
+                       "scan": ("staged" if st.flags & abi.STAT_STAGED else "queue" if st.flags & abi.STAT_QUEUE
+                                else "survivor gather" if st.flags & abi.STAT_GATHER else "in place"),
                        "tuned": bool(st.flags & abi.STAT_TUNED),
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
