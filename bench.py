@@ -266,12 +266,10 @@ def gpu_arm(args, wl):
     clk = clocks.stop()
     st = q.stats()
     res = q.collect()
-    ms_per_step = total_ms / args.steps
-    if dist:
-        tt = torch.tensor([ms_per_step], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_per_step = float(tt.item())
-    value = n * world / (ms_per_step / 1e3)
+    from thindb_gb300 import replicas
+
+    ms_per_step = replicas.slowest_ms(total_ms / args.steps, dist, device="cuda")
+    value = replicas.job_rows_per_s(n, world, ms_per_step)
     q.close()
 
     # end to end through the C ABI from pinned host buffers
