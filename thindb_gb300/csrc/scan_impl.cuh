@@ -750,7 +750,7 @@ struct FastFold {
         }
     }
 
-    __device__ __forceinline__ static void fold(const DevQuery &q, const ScanSmem &sm, const Row &in, unsigned active) {
+    __device__ __noinline__ static void fold(const DevQuery &q, const ScanSmem &sm, const Row in, unsigned active) {
         const int lane = threadIdx.x & 31;
         const bool me = (active >> lane) & 1u;
         uint64_t val[NV];
@@ -1094,17 +1094,6 @@ __device__ __forceinline__ void scan_chunk_queue(const DevQuery &q, const ScanSm
     X(10, 2, AK_DISTINCT, AK_SUM_F64, AK_NONE, AK_NONE)                \
     X(11, 2, AK_NONE, AK_NONE, AK_NONE, AK_NONE)
 
-// P with its fold out of line: the batched kernel dispatches over every
-// compiled fold in one kernel, where twelve inlined folds would crowd the
-// instruction cache.
-template <class P>
-struct OutOfLine : P {
-    __device__ __noinline__ static void fold(const DevQuery &q, const ScanSmem &sm, const typename P::Row in,
-                                             unsigned active) {
-        P::fold(q, sm, in, active);
-    }
-};
-
 // The same work as scan_chunk<P> for the fold the plan's fast_id names.
 template <int NA>
 __device__ __forceinline__ void scan_chunk_dispatch(const DevQuery &q, const ScanSmem &sm, uint32_t c,
@@ -1114,7 +1103,7 @@ __device__ __forceinline__ void scan_chunk_dispatch(const DevQuery &q, const Sca
     } else {
         switch (q.fast_id) {
 #define TGPU_CASE(I, KM, A, B, C2, D) \
-    case I: scan_chunk<OutOfLine<FastFold<KM, A, B, C2, D>>>(q, sm, c, selected); break;
+    case I: scan_chunk<FastFold<KM, A, B, C2, D>>(q, sm, c, selected); break;
             TGPU_FAST_FOLDS(TGPU_CASE)
 #undef TGPU_CASE
             default: scan_chunk<GenericFold<NA>>(q, sm, c, selected); break;
