@@ -248,10 +248,9 @@ typedef struct tgpu_request {
  * aggregate over 8M rows or more outside batches), or never. */
 #define TGPU_FLAG_DISTINCT_PARTITION 0x800
 #define TGPU_FLAG_NO_DISTINCT_PARTITION 0x1000
-/* Queue mode for a WHERE: every row's key and inputs loaded densely, the
- * survivors compacted into a per-warp shared-memory ring and folded in full
- * batches (the default for a compiled fold unless the WHERE is estimated to
- * keep under 4% of the rows, when survivors are gathered instead). */
+/* Queue mode for a WHERE (compiled folds): every row's key and inputs loaded
+ * densely, the survivors compacted into a per-warp shared-memory ring and
+ * folded in full batches. */
 #define TGPU_FLAG_QUEUE_SCAN 0x2000
 
 /* ----------------------------------------------------------------- output -- */

@@ -822,17 +822,17 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     // survivors are compacted and folded 32 at a time (gather) unless the
     // WHERE is estimated to keep most rows: folding in place runs a fold per
     // 32 scanned rows, however few of them survive
-    // queue mode (dense coalesced loads, survivors compacted into a per-warp
-    // shared-memory ring, full-batch folds) for a compiled fold unless the
-    // WHERE keeps so few rows that gathering them reads far fewer lines
+    // survivor gather for a WHERE (queue mode — dense coalesced loads,
+    // survivors compacted into a per-warp shared-memory ring, full-batch
+    // folds — on request: with the out-of-line fold its spills around each
+    // call cost more than the gathers it saves)
     {
         const uint64_t rows = std::max<uint64_t>(1, q->rows_scanned);
         const bool dense_enough = q->sel_est * 10 >= rows * 6;  // >= 60%
-        const bool sparse = q->sel_est * 25 < rows;              // < 4%
         dq.gather = 0;
         if (dq.n_preds > 0 && !(q->flags & TGPU_FLAG_DENSE_SCAN)) {
             if (q->flags & TGPU_FLAG_GATHER_SCAN) dq.gather = 1;
-            else if (dq.fast_id >= 0 && ((q->flags & TGPU_FLAG_QUEUE_SCAN) || !sparse)) dq.gather = 2;
+            else if (dq.fast_id >= 0 && (q->flags & TGPU_FLAG_QUEUE_SCAN)) dq.gather = 2;
             else if (!dense_enough) dq.gather = 1;
         }
     }
