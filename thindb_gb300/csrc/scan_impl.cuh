@@ -498,7 +498,7 @@ __device__ __forceinline__ void load_row(const DevQuery &q, uint64_t row, bool m
 // Fold up to 32 gathered rows (bit i of `active` = lane i holds one).  One
 // out-of-line copy keeps the instruction footprint small.
 template <int NA>
-__device__ __noinline__ void fold_batch(const DevQuery &q, const ScanSmem &sm, const RowVals<NA> &in, unsigned active) {
+__device__ __noinline__ void fold_batch(const DevQuery &q, const ScanSmem sm, const RowVals<NA> &in, unsigned active) {
     const int lane = threadIdx.x & 31;
     const bool me = (active >> lane) & 1u;
     uint64_t val[NA];
@@ -750,7 +750,7 @@ struct FastFold {
         }
     }
 
-    __device__ __noinline__ static void fold(const DevQuery &q, const ScanSmem &sm, const Row in, unsigned active) {
+    __device__ __noinline__ static void fold(const DevQuery &q, const ScanSmem sm, const Row in, unsigned active) {
         const int lane = threadIdx.x & 31;
         const bool me = (active >> lane) & 1u;
         uint64_t val[NV];
