@@ -266,37 +266,12 @@ struct Acc {
     uint32_t rows;     // rows folded (COUNT(*))
 };
 
-// 64-bit state updates.  Global memory has native 64-bit atomics.  In shared
-// memory only 32-bit atomics are native (wider ones loop on compare-and-swap,
-// retrying under the contention hot keys bring), so an add is two 32-bit
-// adds, the high half taking the carry the low half's old value shows (the
-// final word is exact: every wrap of the low half is seen by exactly one
-// adder), and a max first compares with the current value (a running max
-// rarely changes, so the atomic is rarely needed).
-__device__ __forceinline__ void state_add(unsigned long long *w, unsigned long long x, bool shared) {
-    if (!shared) {
-        atomicAdd(w, x);
-        return;
-    }
-    unsigned *h = (unsigned *)w;
-    const unsigned xl = (unsigned)x, xh = (unsigned)(x >> 32);
-    const unsigned old = xl ? atomicAdd(h, xl) : 0u;
-    const unsigned up = xh + ((unsigned)(old + xl) < old ? 1u : 0u);
-    if (up) atomicAdd(h + 1, up);
-}
-
-__device__ __forceinline__ void state_max(unsigned long long *w, unsigned long long x, bool shared) {
-    if (shared && x <= *(volatile unsigned long long *)w) return;
-    atomicMax(w, x);
-}
-
-// Apply a combined contribution to a slot's state words (the CTA's shared
-// table when `shared`, else the global table).  Aggregates that share a
+// Apply a combined contribution to a slot's state words (shared or global:
+// the atomics resolve to the address space of `st`).  Aggregates that share a
 // state word (SUM and AVG of one column) fold it once (g.owner).
 template <int NA>
-__device__ __forceinline__ void apply_states(const DevQuery &q, unsigned long long *st, const Acc<NA> &acc,
-                                             bool shared) {
-    state_add(st, (unsigned long long)acc.rows, shared);
+__device__ __forceinline__ void apply_states(const DevQuery &q, unsigned long long *st, const Acc<NA> &acc) {
+    atomicAdd(st, (unsigned long long)acc.rows);
 #pragma unroll 1
     for (int a = 0; a < NA; ++a) {
         if (a >= q.n_aggs) break;
@@ -305,13 +280,13 @@ __device__ __forceinline__ void apply_states(const DevQuery &q, unsigned long lo
         if (vc == 0 || !g.owner) continue;
         unsigned long long *w = st + g.word;
         switch (g.kind) {
-            case AK_COUNT_VALID: state_add(w, (unsigned long long)vc, shared); break;
+            case AK_COUNT_VALID: atomicAdd(w, (unsigned long long)vc); break;
             case AK_SUM_I64:
-                if (acc.lo[a]) state_add(w, (unsigned long long)acc.lo[a], shared);
+                if (acc.lo[a]) atomicAdd(w, (unsigned long long)acc.lo[a]);
                 break;
             case AK_SUM_I128:
-                if (acc.lo[a]) state_add(w, (unsigned long long)acc.lo[a], shared);
-                if (acc.hi[a]) state_add(w + 1, (unsigned long long)acc.hi[a], shared);
+                if (acc.lo[a]) atomicAdd(w, (unsigned long long)acc.lo[a]);
+                if (acc.hi[a]) atomicAdd(w + 1, (unsigned long long)acc.hi[a]);
                 break;
             case AK_SUM_I128C: {
                 unsigned long long lo = acc.lo[a], hi = acc.hi[a];
@@ -324,11 +299,11 @@ __device__ __forceinline__ void apply_states(const DevQuery &q, unsigned long lo
             }
             case AK_SUM_F64: atomicAdd((double *)w, __longlong_as_double((long long)acc.lo[a])); break;
             case AK_MIN_I: case AK_MAX_I: case AK_MIN_F: case AK_MAX_F:
-                state_max(w, (unsigned long long)acc.lo[a], shared);
+                atomicMax(w, (unsigned long long)acc.lo[a]);
                 break;
             default: break;
         }
-        if (g.vword >= 0) state_add(st + g.vword, (unsigned long long)vc, shared);
+        if (g.vword >= 0) atomicAdd(st + g.vword, (unsigned long long)vc);
     }
 }
 
@@ -581,13 +556,13 @@ __device__ __noinline__ void fold_batch(const DevQuery &q, const ScanSmem sm, co
                     gid = *((volatile uint32_t *)sm.cgid + e);
                     if (gid == NO_GID) gid = (uint32_t)global_slot(q, k0, 0);
                 }
-                apply_states<NA>(q, sm.cstate + (size_t)e * q.state_words, acc, true);
+                apply_states<NA>(q, sm.cstate + (size_t)e * q.state_words, acc);
                 done = true;
             }
         }
         if (!done) {
             gid = (uint32_t)global_slot(q, k0, k1);
-            if (gid != NO_GID) apply_states<NA>(q, q.table + (uint64_t)gid * q.slot_words + q.key_words, acc, false);
+            if (gid != NO_GID) apply_states<NA>(q, q.table + (uint64_t)gid * q.slot_words + q.key_words, acc);
         }
     }
 
@@ -853,7 +828,6 @@ struct FastFold {
         uint32_t gid = NO_GID;
         if (leader) {
             unsigned long long *st = nullptr;
-            bool in_smem = false;
             if (q.cache_slots && q.key_words == 1 && k0 != 0) {
                 bool claimed;
                 const int e = cache_find(q, sm, k0, claimed);
@@ -866,7 +840,6 @@ struct FastFold {
                         if (gid == NO_GID) gid = (uint32_t)global_slot(q, k0, 0);
                     }
                     st = sm.cstate + (size_t)e * q.state_words;
-                    in_smem = true;
                 }
             }
             if (!st) {
@@ -874,22 +847,22 @@ struct FastFold {
                 if (gid != NO_GID) st = q.table + (uint64_t)gid * q.slot_words + q.key_words;
             }
             if (st) {
-                state_add(st, (unsigned long long)rows, in_smem);
+                atomicAdd(st, (unsigned long long)rows);
 #pragma unroll
                 for (int a = 0; a < NV; ++a) {
                     if (a >= NA) continue;
                     unsigned long long *w = st + q.faggs[a].word;
                     switch (kind(a)) {
                         case AK_SUM_I64:
-                            if (lo[a]) state_add(w, (unsigned long long)lo[a], in_smem);
+                            if (lo[a]) atomicAdd(w, (unsigned long long)lo[a]);
                             break;
                         case AK_SUM_I128:
-                            if (lo[a]) state_add(w, (unsigned long long)lo[a], in_smem);
-                            if (hi[a]) state_add(w + 1, (unsigned long long)hi[a], in_smem);
+                            if (lo[a]) atomicAdd(w, (unsigned long long)lo[a]);
+                            if (hi[a]) atomicAdd(w + 1, (unsigned long long)hi[a]);
                             break;
                         case AK_SUM_F64: atomicAdd((double *)w, bits_f64(lo[a])); break;
                         case AK_MIN_I: case AK_MAX_I: case AK_MIN_F: case AK_MAX_F:
-                            state_max(w, (unsigned long long)lo[a], in_smem);
+                            atomicMax(w, (unsigned long long)lo[a]);
                             break;
                         default: break;
                     }
