@@ -19,7 +19,7 @@ namespace {
 constexpr int DP_THREADS = 512;
 constexpr uint32_t DP_EMPTY = 0xFFFFFFFFu;
 
-__global__ void __launch_bounds__(DP_THREADS, 1)
+__global__ void __launch_bounds__(DP_THREADS, 2)
     distinct_partition_kernel(const ulonglong2 *__restrict__ buf, const uint32_t *__restrict__ cursor, uint32_t cap,
                               unsigned long long *table, int32_t slot_words, int32_t key_words, int32_t word,
                               unsigned int *status) {
@@ -30,7 +30,20 @@ __global__ void __launch_bounds__(DP_THREADS, 1)
     const uint32_t n = min(cursor[p], cap);  // a larger count set ST_DISTINCT_FULL already
     if (n == 0) return;
     const ulonglong2 *src = buf + (size_t)p * cap;
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) pairs[i] = src[i];
+    // four 16-byte loads in flight per thread before the stores
+    for (uint32_t i0 = threadIdx.x; i0 < n; i0 += 4 * blockDim.x) {
+        ulonglong2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t i = i0 + u * blockDim.x;
+            if (i < n) v[u] = __ldcs(src + i);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t i = i0 + u * blockDim.x;
+            if (i < n) pairs[i] = v[u];
+        }
+    }
     for (uint32_t i = threadIdx.x; i < DPART_SLOTS; i += blockDim.x) slots[i] = DP_EMPTY;
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {

@@ -267,8 +267,8 @@ cudaError_t launch_staged_scan(const DevQuery &q, const StagePlan &sp, int grid,
 
 // Partitioned COUNT(DISTINCT): pairs per partition (one CTA deduplicates a
 // partition in shared memory) and the partition's index-table slots.
-constexpr uint32_t DPART_CAP = 8192;
-constexpr uint32_t DPART_SLOTS = 16384;
+constexpr uint32_t DPART_CAP = 4096;     // 64 KB of pairs + 32 KB of slots: two CTAs per SM
+constexpr uint32_t DPART_SLOTS = 8192;
 // Deduplicate every partition's pairs and add each new pair to its group's
 // distinct count (table word `word` of slot gid).
 cudaError_t launch_distinct_partitions(const DevQuery &q, int word, cudaStream_t s);
