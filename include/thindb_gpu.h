@@ -245,7 +245,7 @@ typedef struct tgpu_request {
 #define TGPU_FLAG_DISTINCT_PREFETCH 0x400
 /* COUNT(DISTINCT) through hash partitions of (group, value) pairs, each
  * deduplicated in one CTA's shared memory (the default for one distinct
- * aggregate over 8M rows or more outside batches), or never. */
+ * aggregate over 2M rows or more outside batches), or never. */
 #define TGPU_FLAG_DISTINCT_PARTITION 0x800
 #define TGPU_FLAG_NO_DISTINCT_PARTITION 0x1000
 /* Queue mode for a WHERE (compiled folds): every row's key and inputs loaded

@@ -898,7 +898,7 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     q->dpart_word = -1;
     size_t dpart_bytes = 0;
     if (dq.n_dsets == 1 && !q->batched && !(q->flags & TGPU_FLAG_NO_DISTINCT_PARTITION) &&
-        ((q->flags & TGPU_FLAG_DISTINCT_PARTITION) || q->sel_est >= (8ULL << 20))) {
+        ((q->flags & TGPU_FLAG_DISTINCT_PARTITION) || q->sel_est >= (2ULL << 20))) {
         // about three quarters of a partition's capacity expected
         const uint64_t per = DPART_CAP * 3 / 4;
         int bits = 1;
