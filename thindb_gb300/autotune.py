@@ -191,6 +191,39 @@ def _incumbent(shape: dict, table: list) -> list:
     return []
 
 
+def tune_served(scale: float, stream: int, reps: int, log=print, previous=(), max_shapes: int = 12) -> list:
+    """Entries for the served mix's shapes (single executions: the continuous
+    server runs short backlogs as separate queries): the most frequent shapes,
+    each tuned on its first request."""
+    sizes = {"plain": datagen.PLAIN_ROWS, "filtered": datagen.FILTERED_ROWS, "distinct": datagen.DISTINCT_ROWS,
+             "batched": datagen.FILTERED_ROWS}
+    tables = []
+    for wl in workloads.SERVED_TABLES:
+        inputs = workloads.table_inputs(wl, max(1 << 16, int(sizes[wl] * scale)), pinned=True)
+        tables.append(Table(workloads.columns(inputs), compute_ndv=True, stream=stream))
+        del inputs
+    entries = []
+    try:
+        by_shape = {}
+        for ti, req in workloads.served_mix(96, seed=5):
+            req.stream = stream
+            key = json.dumps(request_shape(tables[ti], req), sort_keys=True)
+            by_shape.setdefault(key, []).append((ti, req))
+        ranked = sorted(by_shape.items(), key=lambda kv: -len(kv[1]))[:max_shapes]
+        for key, reqs in ranked:
+            ti, req = reqs[0]
+            shape = json.loads(key)
+            log(f"served shape {shape} ({len(reqs)} of 96 requests)")
+            best, d_ms, b_ms = descend(lambda k: time_query(tables[ti], req, k, reps), _same, log,
+                                       starts=_incumbent(shape, previous))
+            entries.append({"shape": shape, **best, "workload": f"served ({len(reqs)} of 96 requests)",
+                            "ms_builtin": d_ms, "ms_tuned": b_ms})
+    finally:
+        for t in tables:
+            t.close()
+    return entries
+
+
 def tune_workload(name: str, n: int, stream: int, reps: int, log=print, previous=()) -> list:
     """Tuning entries for one workload's shapes."""
     inputs = workloads.table_inputs(name, n, pinned=True)
@@ -225,7 +258,7 @@ def main(argv=None) -> int:
 
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--out", default=None, help="tuning JSON to write (default: print only)")
-    ap.add_argument("--workloads", default="plain,filtered,distinct,batched")
+    ap.add_argument("--workloads", default="plain,filtered,distinct,batched,served")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of each workload's full row count")
     args = ap.parse_args(argv)
@@ -236,11 +269,18 @@ def main(argv=None) -> int:
     t0 = time.time()
     previous = engine_tuning_entries()  # the installed table: warm starts
     entries = []
+    log = lambda m: print(m, file=sys.stderr, flush=True)  # noqa: E731
     for name in args.workloads.split(","):
-        n = max(1 << 16, int(sizes[name] * args.scale))
-        print(f"{name}: {n:,} rows", file=sys.stderr, flush=True)
-        entries += tune_workload(name, n, stream.cuda_stream, args.reps,
-                                 log=lambda m: print(m, file=sys.stderr, flush=True), previous=previous)
+        if name == "served":
+            log("served: the four served tables")
+            new = tune_served(args.scale, stream.cuda_stream, args.reps, log=log, previous=previous)
+        else:
+            n = max(1 << 16, int(sizes[name] * args.scale))
+            log(f"{name}: {n:,} rows")
+            new = tune_workload(name, n, stream.cuda_stream, args.reps, log=log, previous=previous)
+        # a shape tuned by an earlier workload keeps that entry
+        seen = {json.dumps(e["shape"], sort_keys=True) for e in entries}
+        entries += [e for e in new if json.dumps(e["shape"], sort_keys=True) not in seen]
     doc = {
         "device": torch.cuda.get_device_name(0),
         "generated_by": "python -m thindb_gb300.autotune " + " ".join(argv if argv is not None else sys.argv[1:]),
