@@ -410,8 +410,8 @@ typedef struct tgpu_server_options {
     uint32_t max_inflight;         /* waves on the device at once, 0 = 8 */
     int32_t mode;                  /* TGPU_SERVE_* */
     int32_t batch_min;             /* continuous mode: waiting requests on one table that
-                                    * make a wave one batched kernel (0 = 64); fewer run as
-                                    * separate executions overlapping on the wave streams */
+                                    * make a wave one batched kernel (0 = never: every request
+                                    * runs as its own execution, overlapping on the wave streams) */
 } tgpu_server_options;
 
 typedef struct tgpu_server_stats {

@@ -2152,12 +2152,12 @@ struct tgpu_server {
         uint32_t max_batch = opt.mode == TGPU_SERVE_PLAIN ? 1 : (opt.max_batch ? opt.max_batch : 256);
         table = pending.front()->table;
         if (max_batch > 1) {
-            // a short backlog runs as separate executions overlapping on the
-            // wave streams; a long one on one table as one batched kernel
-            const uint32_t batch_min = opt.batch_min > 0 ? (uint32_t)opt.batch_min : 64;
+            // separate executions overlapping on the wave streams, unless the
+            // options ask for batched kernels from a backlog of batch_min
+            // requests on one table
             uint32_t same = 0;
             for (Ticket *tk : pending) same += tk->table == table ? 1 : 0;
-            if (same < batch_min) max_batch = 1;
+            if (opt.batch_min <= 0 || same < (uint32_t)opt.batch_min) max_batch = 1;
         }
         bytes = 0;
         for (auto it = pending.begin(); it != pending.end() && out.size() < max_batch;) {
