@@ -472,7 +472,7 @@ def main():
     ap.add_argument("--rows", type=int, default=0, help="rows of the workload (default: its full size)")
     ap.add_argument("--queries", type=int, default=256, help="queries of the batched workload")
     ap.add_argument("--rates", default="500,750,1000,1250,2500,5000",
-                    help="offered loads of the served workload (q/s): the BASELINE rates and points between")
+                    help="offered loads of the served workload (q/s): the configured rates and points between")
     ap.add_argument("--duration", type=float, default=4.0, help="seconds of arrivals per served rate")
     args = ap.parse_args()
     if args.workload == "served":

@@ -294,7 +294,7 @@ def main(argv=None) -> int:
                 entries[index[k]] = e
     doc = {
         "device": torch.cuda.get_device_name(0),
-        "generated_by": "python -m thindb_gb300.autotune " + " ".join(argv if argv is not None else sys.argv[1:]),
+        "generated_by": f"python -m thindb_gb300.autotune --workloads {args.workloads} --reps {args.reps}",
         "seconds": round(time.time() - t0, 1),
         "knobs": KNOBS,
         "entries": entries,
