@@ -149,12 +149,13 @@ def time_batch(table: Table, reqs: list, knobs: dict, reps: int, stream: int):
         b.close()
 
 
-GRID = [(c, k) for c in (512, 1024, 2048, 4096) for k in (0, -1, 256, 1024)]
+GRID = [(c, k, f) for c in (512, 1024, 2048, 4096) for k in (0, -1, 256, 1024)
+        for f in (0, abi.FLAG_NO_PREFETCH | abi.FLAG_NO_CHUNK_PREFETCH)]
 
 
 def descend(measure, same, log=print, rounds: int = 3, starts=()):
-    """A joint grid over rows per chunk x shared-table slots (the two knobs
-    interact through shared memory), then coordinate descent over KNOBS from
+    """A joint grid over rows per chunk x shared-table slots x prefetching
+    (the knobs interact), then coordinate descent over KNOBS from
     the best of that, the built-in setting and `starts` (e.g. the installed
     table's entry for the shape)."""
     base = measure(DEFAULT)
@@ -163,7 +164,7 @@ def descend(measure, same, log=print, rounds: int = 3, starts=()):
     best, (best_ms, ref) = dict(DEFAULT), base
     default_ms = best_ms
     log(f"  built-in: {best_ms:.3f} ms")
-    for st in list(starts) + [dict(DEFAULT, chunk_rows=c, cache_slots=k) for c, k in GRID]:
+    for st in list(starts) + [dict(DEFAULT, chunk_rows=c, cache_slots=k, flags=f) for c, k, f in GRID]:
         r = measure(st)
         if r is not None and same(r[1], ref):
             log(f"  start {st}: {r[0]:.3f} ms")

@@ -10,7 +10,7 @@
 //      (inside the row groups that survived the zone maps): no tile claims and
 //      no block barriers in the main loop.
 //   2. The fused WHERE is evaluated 32 rows per step with coalesced streaming
-//      loads, eight steps in flight; a warp ballot gives the survivors, whose
+//      loads, sixteen steps in flight; a warp ballot gives the survivors, whose
 //      chunk offsets are compacted into the warp's shared-memory list
 //      (position = popc of the ballot below the lane).
 //   3. Survivors are folded 32 at a time: their key parts and aggregate inputs
@@ -38,7 +38,7 @@ namespace {
 
 constexpr unsigned FULL = 0xFFFFFFFFu;
 constexpr uint32_t NO_GID = 0xFFFFFFFFu;
-constexpr int FILTER_UNROLL = 8;  // 32-row filter steps in flight per warp
+constexpr int FILTER_UNROLL = 16;  // 32-row filter steps in flight per warp
 
 __device__ __forceinline__ bool col_valid(const DevCol &c, uint64_t r) {
     return c.valid == nullptr || ((__ldg(c.valid + (r >> 5)) >> (r & 31)) & 1u);
