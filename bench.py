@@ -132,10 +132,17 @@ def make_inputs(workload: str, n: int, pinned: bool):
     return workloads.table_inputs(workload, n, pinned)
 
 
+KNOBS = {}  # explicit engine settings (--chunk-rows / --cache-slots / --table-load / --flags)
+
+
 def make_request(workload: str, flags: int = 0, stream: int = 0):
     from thindb_gb300 import workloads
 
-    return workloads.workload_request(workload, flags, stream)
+    req = workloads.workload_request(workload, flags | KNOBS.get("flags", 0), stream)
+    for k in ("chunk_rows", "cache_slots", "table_load_pct"):
+        if k in KNOBS:
+            setattr(req, k, KNOBS[k])
+    return req
 
 
 def rows_of(result: dict) -> list:
@@ -474,7 +481,15 @@ def main():
     ap.add_argument("--rates", default="500,750,1000,1250,2500,5000",
                     help="offered loads of the served workload (q/s): the configured rates and points between")
     ap.add_argument("--duration", type=float, default=4.0, help="seconds of arrivals per served rate")
+    ap.add_argument("--chunk-rows", type=int, default=None, help="pin rows per warp chunk (profiling a small case)")
+    ap.add_argument("--cache-slots", type=int, default=None, help="pin shared-memory table slots (-1 none)")
+    ap.add_argument("--table-load", type=int, default=None, help="pin the group-table load target (%%)")
+    ap.add_argument("--flags", type=int, default=None, help="extra TGPU_FLAG_* bits for the request")
     args = ap.parse_args()
+    for name, key in (("chunk_rows", "chunk_rows"), ("cache_slots", "cache_slots"), ("table_load", "table_load_pct"),
+                      ("flags", "flags")):
+        if getattr(args, name) is not None:
+            KNOBS[key] = getattr(args, name)
     if args.workload == "served":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the served mode has no CPU reference arm; "
