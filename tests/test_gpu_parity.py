@@ -389,13 +389,3 @@ def test_queue_mode_sparse_and_pruned():
     _, st = run_both(cols, Request(["k"], [AggSpec("count", None, "c"), AggSpec("max", "d", "md")],
                                    where=[Pred("d", "between", 300, 320)], flags=abi.FLAG_QUEUE_SCAN))
     assert st.flags & abi.STAT_QUEUE and st.row_groups_pruned > 0
-
-
-def test_vector_filter_tail_rows():
-    """The 16-byte predicate loads stop at the last whole group; the last
-    rows % 4 rows go through 4-byte loads (1,000,003 rows: 3 left over)."""
-    cols = filtered_cols(1_000_003, 100_000)
-    for flags in (0, abi.FLAG_GATHER_SCAN):
-        _, st = run_both(cols, Request(["k"], C2_AGGS, [SortSpec("s", True)], limit=10, where=FILTER, flags=flags))
-        assert st.flags & abi.STAT_GATHER
-        _, st = run_both(cols, Request(["k"], C2_AGGS, where=FILTER, flags=flags, chunk_rows=768))

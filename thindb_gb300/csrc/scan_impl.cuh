@@ -656,52 +656,6 @@ __device__ __forceinline__ uint64_t prefetch_slot(const DevQuery &q, uint64_t k0
     return hk;
 }
 
-// The fast WHERE on a 4-byte column with 16-byte loads: lane l tests rows
-// 4l .. 4l + 3 of each 128-row step, VEC_UNROLL steps in flight (1,024 rows
-// per round trip).  Needs row0 and the column base on 16-byte boundaries;
-// only whole 16-byte groups inside [row0, row_end) are loaded, the last
-// rows % 4 rows with 4-byte loads.
-constexpr int VEC_UNROLL = 6;
-
-__device__ __forceinline__ uint32_t filter_range_v4(const DevQuery &q, uint64_t row0, uint64_t row_end,
-                                                    uint16_t *list) {
-    const int lane = threadIdx.x & 31;
-    const int *base = (const int *)q.fp_data + row0;
-    const int4 *col = (const int4 *)base;
-    const int64_t lo = q.fp_lo, hi = q.fp_hi;
-    const bool neg = q.fp_negate != 0, shared = q.shared_scan != 0;
-    const uint32_t rows = (uint32_t)(row_end - row0);
-    const uint32_t vecs = rows / 4;  // whole 16-byte groups
-    uint32_t n = 0;
-    for (uint32_t b = 0; b < vecs; b += 32 * VEC_UNROLL) {
-        int4 v[VEC_UNROLL];
-#pragma unroll
-        for (int u = 0; u < VEC_UNROLL; ++u) {
-            const uint32_t g = b + u * 32 + lane;
-            v[u] = g < vecs ? ld_pred(shared, col + g) : make_int4(0, 0, 0, 0);
-        }
-#pragma unroll
-        for (int u = 0; u < VEC_UNROLL; ++u) {
-            const uint32_t g = b + u * 32 + lane;
-            const int x[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const bool pass = g < vecs && (((int64_t)x[j] >= lo && (int64_t)x[j] <= hi) != neg);
-                const unsigned m = __ballot_sync(FULL, pass);
-                if (pass) list[n + __popc(m & ((1u << lane) - 1))] = (uint16_t)(4 * g + j);
-                n += __popc(m);
-            }
-        }
-    }
-    const uint32_t r = 4 * vecs + lane;  // the last rows % 4 rows
-    const bool pass = r < rows && (((int64_t)ld_pred(shared, base + (r < rows ? r : 0)) >= lo &&
-                                    (int64_t)ld_pred(shared, base + (r < rows ? r : 0)) <= hi) != neg);
-    const unsigned m = __ballot_sync(FULL, pass);
-    if (pass) list[n + __popc(m & ((1u << lane) - 1))] = (uint16_t)r;
-    n += __popc(m);
-    return n;
-}
-
 // ------------------------------------------------------ fold policies --
 
 // The interpreter: any plan, aggregate kinds read from the plan at run time.
@@ -996,10 +950,7 @@ __device__ __forceinline__ void scan_chunk(const DevQuery &q, const ScanSmem &sm
     switch (q.fp_bytes) {
         case 1: n = filter_range<signed char>(q, row0, row_end, list); break;
         case 2: n = filter_range<short>(q, row0, row_end, list); break;
-        case 4:
-            n = ((row0 & 3) == 0 && ((uintptr_t)q.fp_data & 15) == 0) ? filter_range_v4(q, row0, row_end, list)
-                                                                      : filter_range<int>(q, row0, row_end, list);
-            break;
+        case 4: n = filter_range<int>(q, row0, row_end, list); break;
         case 8: n = filter_range<long long>(q, row0, row_end, list); break;
         default: break;
     }
