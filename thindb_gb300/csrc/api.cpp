@@ -925,7 +925,7 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
         tgpu_status st = device_ctx(&dev);
         if (st != TGPU_OK) return st;
         const uint64_t want = (std::min<uint64_t>(q->groups_est, cap + 1) + 2047) / 2048;
-        q->n_cand_blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)dev->sms * 8));
+        q->n_cand_blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)dev->sms * 2));
     }
     size_t row_bytes = 0;
     for (auto &oc : q->schema) row_bytes += oc.elem_bytes + 1;
