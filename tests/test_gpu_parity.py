@@ -389,3 +389,11 @@ def test_queue_mode_sparse_and_pruned():
     _, st = run_both(cols, Request(["k"], [AggSpec("count", None, "c"), AggSpec("max", "d", "md")],
                                    where=[Pred("d", "between", 300, 320)], flags=abi.FLAG_QUEUE_SCAN))
     assert st.flags & abi.STAT_QUEUE and st.row_groups_pruned > 0
+
+
+def test_odd_row_count_chunks():
+    """A table whose row count and chunk size leave ragged last chunks."""
+    cols = filtered_cols(1_000_003, 100_000)
+    for flags in (0, abi.FLAG_GATHER_SCAN, abi.FLAG_DENSE_SCAN):
+        run_both(cols, Request(["k"], C2_AGGS, [SortSpec("s", True)], limit=10, where=FILTER, flags=flags))
+        run_both(cols, Request(["k"], C2_AGGS, where=FILTER, flags=flags, chunk_rows=768))
