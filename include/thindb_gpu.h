@@ -121,7 +121,8 @@ typedef struct tgpu_table_desc {
     uint32_t row_group_rows;    /* 0 = 65536 */
     uint64_t n_rows;
     int32_t location;           /* tgpu_location */
-    int32_t compute_ndv;        /* 1 = run the HLL pass for columns without ndv_hint */
+    int32_t compute_ndv;        /* 1 = run the HLL pass for columns without ndv_hint, and let
+                                   plans sketch a composite group key once (kept with the table) */
     void *stream;               /* cudaStream_t for the copies / stats, NULL = library stream */
 } tgpu_table_desc;
 

@@ -318,7 +318,7 @@ def test_staged_declines_to_plain_scan_for_nullable_inputs():
 
 # ------------------------------------------------ partitioned COUNT(DISTINCT) --
 # (group, value) pairs go to hash partitions, each deduplicated by one CTA in
-# shared memory; the default from 8M rows, forced here on small tables.
+# shared memory; the default from 2M rows, forced here on small tables.
 
 DPART = abi.FLAG_DISTINCT_PARTITION
 
@@ -362,10 +362,60 @@ def test_distinct_partitioned_nullable_and_float_values():
     assert st.flags & abi.STAT_DISTINCT_PARTITION
 
 
+def test_distinct_partitioned_staged():
+    """Staged scan rows reserve their pair places in the fold."""
+    cols = distinct_cols(1_000_000, 50_000)
+    req = Request(["region", "url"], [AggSpec("count", None, "c"), AggSpec("count_distinct", "user_id", "u"),
+                                      AggSpec("sum", "latency_ms", "lat")], flags=DPART | abi.FLAG_STAGED_SCAN)
+    _, st = run_both(cols, req)
+    assert st.flags & abi.STAT_DISTINCT_PARTITION and st.flags & abi.STAT_STAGED
+
+
+@pytest.mark.parametrize("flags", [abi.FLAG_QUEUE_SCAN, abi.FLAG_DENSE_SCAN, abi.FLAG_GATHER_SCAN])
+def test_distinct_partitioned_scan_modes(flags):
+    """Every scan mode under a WHERE feeds the partitions."""
+    cols = distinct_cols(1_000_000, 50_000)
+    req = Request(["region", "url"], [AggSpec("count", None, "c"), AggSpec("count_distinct", "user_id", "u"),
+                                      AggSpec("sum", "latency_ms", "lat")],
+                  where=[Pred("region", "between", 3, 40)], flags=DPART | flags)
+    _, st = run_both(cols, req)
+    assert st.flags & abi.STAT_DISTINCT_PARTITION
+
+
+def test_distinct_partition_overflow_on_repeated_pairs():
+    """One (group, value) pair repeated past a partition's capacity (all its
+    copies hash to one partition): the rerun deduplicates in the global set."""
+    n = 300_000
+    rng = np.random.default_rng(23)
+    k = (rng.random(n) < 0.5).astype(np.int64)
+    v = np.where(rng.random(n) < 0.9, 7, rng.integers(0, 1000, n)).astype(np.int64)
+    cols = [Column("k", abi.BIGINT, k), Column("v", abi.BIGINT, v)]
+    req = Request(["k"], [AggSpec("count_distinct", "v", "d"), AggSpec("count", None, "c")], [SortSpec("k")],
+                  flags=DPART)
+    _, st = run_both(cols, req)
+    assert not st.flags & abi.STAT_DISTINCT_PARTITION
+    assert st.retries >= 1
+
+
+def test_distinct_partition_overflow_on_underestimated_where():
+    """A WHERE estimated to keep a few rows keeps 90%: the partitions
+    overflow and the rerun sizes them for the rows that passed."""
+    n = 300_000
+    rng = np.random.default_rng(24)
+    x = np.where(rng.random(n) < 0.9, 500_000, rng.integers(0, 1_000_000, n)).astype(np.int32)
+    k = rng.integers(0, 2000, n).astype(np.int64)
+    u = rng.integers(0, 100_000, n).astype(np.int64)
+    cols = [Column("x", abi.INT, x), Column("k", abi.BIGINT, k), Column("u", abi.BIGINT, u)]
+    req = Request(["k"], [AggSpec("count_distinct", "u", "d"), AggSpec("count", None, "c")],
+                  where=[Pred("x", "between", 500_000, 500_000)], flags=DPART)
+    _, st = run_both(cols, req)
+    assert st.flags & abi.STAT_DISTINCT_PARTITION
+    assert st.retries >= 1
+
+
 # -------------------------------------------------------------- queue mode --
 # Dense coalesced loads, survivors compacted into a per-warp shared-memory
-# ring, full-batch folds: the default for a compiled fold under a WHERE that
-# keeps 4% of the rows or more; forced here on other selectivities too.
+# ring, full-batch folds: opt-in (TGPU_FLAG_QUEUE_SCAN), forced here.
 
 @pytest.mark.parametrize("flags", [abi.FLAG_QUEUE_SCAN, abi.FLAG_QUEUE_SCAN | abi.FLAG_FORCE_GLOBAL,
                                    abi.FLAG_QUEUE_SCAN | abi.FLAG_NO_WARP_COMBINE])

@@ -40,7 +40,7 @@ import time
 import numpy as np
 
 from . import abi, datagen, workloads
-from .engine import QueryBatch, Request, Table, request_shape, try_build_group_topn
+from .engine import EngineError, QueryBatch, Request, Table, request_shape, try_build_group_topn
 from .engine import lib as engine_lib
 from .engine import tuning_entries as engine_tuning_entries
 
@@ -101,13 +101,21 @@ def _sorted_result(res: dict) -> dict:
     return {n: (np.asarray(v)[order], None if ok is None else np.asarray(ok)[order]) for n, (v, ok) in res.items()}
 
 
+def _fatal(e: Exception) -> bool:
+    """A CUDA error can leave the context unusable: tuning stops there
+    instead of rejecting every later candidate."""
+    return isinstance(e, EngineError) and e.status in (abi.ERR_CUDA, abi.ERR_NO_DEVICE)
+
+
 def time_query(table: Table, req: Request, knobs: dict, reps: int):
     """(median device ms, result) of `req` run with `knobs` as its shape's
     tuning entry; None if it fails."""
     _install([request_shape(table, req)], knobs)
     try:
         q = try_build_group_topn(table, _timed(req))
-    except Exception:
+    except Exception as e:
+        if _fatal(e):
+            raise
         return None
     if q is None:
         return None
@@ -121,7 +129,9 @@ def time_query(table: Table, req: Request, knobs: dict, reps: int):
                 times.append(q.stats().total_ms)
             res = q.collect()
         return statistics.median(times), _sorted_result(res)
-    except Exception:
+    except Exception as e:
+        if _fatal(e):
+            raise
         return None
     finally:
         q.close()
@@ -132,7 +142,9 @@ def time_batch(table: Table, reqs: list, knobs: dict, reps: int, stream: int):
     _install([json.loads(x) for x in sorted(shapes)], knobs)
     try:
         b = QueryBatch(table, [_timed(r) for r in reqs], graph=True, stream=stream)
-    except Exception:
+    except Exception as e:
+        if _fatal(e):
+            raise
         return None
     try:
         times = []
@@ -143,7 +155,9 @@ def time_batch(table: Table, reqs: list, knobs: dict, reps: int, stream: int):
                 times.append(b.stats().total_ms)
         res = [_sorted_result(b.collect(i)) for i in range(len(reqs))]
         return statistics.median(times), res
-    except Exception:
+    except Exception as e:
+        if _fatal(e):
+            raise
         return None
     finally:
         b.close()
@@ -267,6 +281,8 @@ def main(argv=None) -> int:
     ap.add_argument("--workloads", default="plain,filtered,distinct,batched,served")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of each workload's full row count")
+    ap.add_argument("--merge", default=None,
+                    help="tuning JSON whose entries to keep, except the shapes this run tunes again")
     args = ap.parse_args(argv)
     sizes = {"plain": datagen.PLAIN_ROWS, "filtered": datagen.FILTERED_ROWS, "distinct": datagen.DISTINCT_ROWS,
              "batched": datagen.FILTERED_ROWS}
@@ -293,10 +309,21 @@ def main(argv=None) -> int:
                 entries.append(e)
             elif e["ms_tuned"] < entries[index[k]]["ms_tuned"]:
                 entries[index[k]] = e
+    command = f"python -m thindb_gb300.autotune --workloads {args.workloads} --reps {args.reps}"
+    seconds = round(time.time() - t0, 1)
+    if args.merge:
+        with open(args.merge) as f:
+            old = json.load(f)
+        tuned = {json.dumps(e["shape"], sort_keys=True) for e in entries}
+        kept = [e for e in old["entries"] if json.dumps(e["shape"], sort_keys=True) not in tuned]
+        entries = kept + entries
+        before = old["generated_by"] if isinstance(old["generated_by"], list) else [old["generated_by"]]
+        command = before + [command + " --merge <this file>"]
+        seconds = round(old.get("seconds", 0) + seconds, 1)
     doc = {
         "device": torch.cuda.get_device_name(0),
-        "generated_by": f"python -m thindb_gb300.autotune --workloads {args.workloads} --reps {args.reps}",
-        "seconds": round(time.time() - t0, 1),
+        "generated_by": command,
+        "seconds": seconds,
         "knobs": KNOBS,
         "entries": entries,
     }

@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <random>
@@ -275,6 +276,9 @@ struct tgpu_table {
     uint32_t rg_rows = 65536;
     uint32_t n_rg = 0;
     std::vector<Column> cols;
+    bool sketches = false;  // registered with compute_ndv: plans may sketch composite keys
+    mutable std::mutex key_mu;
+    mutable std::map<std::vector<int32_t>, uint64_t> key_ndv;  // composite-key NDV per group-column list
     ~tgpu_table() {
         for (auto &c : cols) {
             if (c.owned) cudaFree(c.d_data);
@@ -300,6 +304,50 @@ double hll_estimate(const std::vector<uint32_t> &regs) {
 }
 
 }  // namespace
+
+// Distinct composite keys of the group columns over all of t's rows: a
+// HyperLogLog sketch computed on the device once per column list and kept
+// with the table (thinDB sizes its group tables from NDV estimates,
+// silo_group_core.zig expectedTotalGroups :11398).
+tgpu_status composite_ndv(const tgpu_table *t, const int32_t *cols, uint32_t n, uint64_t *out) {
+    const std::vector<int32_t> key(cols, cols + n);
+    {
+        std::lock_guard<std::mutex> lk(t->key_mu);
+        auto it = t->key_ndv.find(key);
+        if (it != t->key_ndv.end()) {
+            *out = it->second;
+            return TGPU_OK;
+        }
+    }
+    DeviceCtx *dev;
+    tgpu_status st = device_ctx(&dev);
+    if (st != TGPU_OK) return st;
+    const cudaStream_t s = dev->stream;
+    KeySketchCols k{};
+    k.n = (int32_t)n;
+    for (uint32_t i = 0; i < n; ++i) {
+        const Column &c = t->cols[cols[i]];
+        k.data[i] = c.d_data;
+        k.valid[i] = c.d_valid;
+        k.type[i] = c.type;
+    }
+    std::vector<uint32_t> regs(1u << HLL_P);
+    uint32_t *d_regs = nullptr;
+    CU(cudaMallocAsync((void **)&d_regs, regs.size() * 4, s));
+    cudaError_t e = cudaMemsetAsync(d_regs, 0, regs.size() * 4, s);
+    if (e == cudaSuccess) e = launch_key_hll(k, t->n_rows, d_regs, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(regs.data(), d_regs, regs.size() * 4, cudaMemcpyDeviceToHost, s);
+    const cudaError_t f = cudaFreeAsync(d_regs, s);
+    if (e == cudaSuccess) e = f;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    CU(e);
+    const uint64_t nd = (uint64_t)std::llround(hll_estimate(regs));
+    std::lock_guard<std::mutex> lk(t->key_mu);
+    t->key_ndv[key] = nd;
+    *out = nd;
+    return TGPU_OK;
+}
+
 
 // ----------------------------------------------------------------- query --
 
@@ -332,7 +380,8 @@ struct tgpu_query {
     bool tuned = false;           // settings taken from the tuning table
     bool staged = false;          // the staged (bulk-copy ring) scan runs this query
     bool batched = false;         // created for a batch (runs inside the batched kernel)
-    int dpart_extra = 0;          // partition bits added after overflows
+    uint64_t dpart_rows = 0;      // rows that passed when the partitions overflowed
+    bool dpart_off = false;       // repeated pairs overflowed a partition: global set
     Buffer dpart_cursor_buf, dpart_pairs_buf;
     int dpart_word = -1;          // the distinct aggregate's state word
     StagePlan sp{};
@@ -785,6 +834,14 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
         uint64_t nd = std::max<uint64_t>(1, c.ndv) + (c.nullable ? 1 : 0);
         groups = (groups > (1ULL << 40) / nd) ? (1ULL << 40) : groups * nd;
     }
+    if (req->n_group_cols >= 2 && t->sketches && !req->expected_groups && groups > COMPOSITE_SKETCH_MIN) {
+        // correlated parts: the product overestimates; the key's own sketch
+        // (+1/16 for the sketch's error) bounds it
+        uint64_t nd = 0;
+        tgpu_status st = composite_ndv(t, req->group_cols, req->n_group_cols, &nd);
+        if (st != TGPU_OK) return st;
+        if (nd) groups = std::min<uint64_t>(groups, nd + nd / 16 + 64);
+    }
     groups = std::min<uint64_t>(groups, std::max<uint64_t>(1, sel_rows));
     if (req->expected_groups) groups = req->expected_groups;
     q->groups_est = groups;
@@ -853,7 +910,7 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     }
     const size_t list_bytes =
         dq.gather == 1 ? (size_t)SCAN_WARPS * dq.chunk_rows * 2
-        : dq.gather == 2 ? (size_t)SCAN_WARPS * WQ_RING_ROWS * (16 + 8 * (size_t)std::max(1, dq.n_faggs)) + 16 : 0;
+        : dq.gather == 2 ? (size_t)SCAN_WARPS * WQ_RING_ROWS * (24 + 8 * (size_t)std::max(1, dq.n_faggs)) + 16 : 0;
 
     // route: the shared-memory table holds every group (lowcard), keeps the
     // first-seen (hottest) keys of a larger key space (global route), or is off
@@ -897,13 +954,12 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     dq.dpart_cap = 0;
     q->dpart_word = -1;
     size_t dpart_bytes = 0;
-    if (dq.n_dsets == 1 && !q->batched && !(q->flags & TGPU_FLAG_NO_DISTINCT_PARTITION) &&
+    if (dq.n_dsets == 1 && !q->batched && !q->dpart_off && !(q->flags & TGPU_FLAG_NO_DISTINCT_PARTITION) &&
         ((q->flags & TGPU_FLAG_DISTINCT_PARTITION) || q->sel_est >= (2ULL << 20))) {
         // about three quarters of a partition's capacity expected
-        const uint64_t per = DPART_CAP * 3 / 4;
+        const uint64_t per = DPART_CAP * 3 / 4, rows = std::max(q->sel_est, q->dpart_rows);
         int bits = 1;
-        while (bits < 18 && ((uint64_t)1 << bits) * per < q->sel_est) ++bits;
-        bits = std::min(20, bits + q->dpart_extra);
+        while (bits < DPART_MAX_BITS && ((uint64_t)1 << bits) * per < rows) ++bits;
         dq.dpart_bits = bits;
         dq.dpart_cap = DPART_CAP;
         for (int a = 0; a < dq.n_aggs; ++a)
@@ -1184,8 +1240,21 @@ tgpu_status finish(tgpu_query *q) {
             if (++q->retries > 4) return fail(TGPU_ERR_INTERNAL, "group table kept overflowing");
             if (status & ST_TABLE_FULL) q->groups_est = std::max<uint64_t>(q->groups_est * 4, 1024);
             if (status & ST_DISTINCT_FULL) {
-                for (auto &n : q->dset_need) n *= 4;
-                if (q->dq.dpart_bits) q->dpart_extra += 2;
+                if (q->dq.dpart_bits) {
+                    // Partitions hold three quarters of their capacity on
+                    // average, so with a uniform hash only more passing rows
+                    // than planned overflow one: size for the rows that
+                    // passed.  Otherwise one (group, value) pair repeated
+                    // beyond a partition's capacity filled it (all its
+                    // copies hash alike): deduplicate in the global set.
+                    const uint64_t selected = q->h_counts[4];
+                    const uint64_t room = ((uint64_t)DPART_CAP * 3 / 4) << q->dq.dpart_bits;
+                    const uint64_t most = ((uint64_t)DPART_CAP * 3 / 4) << DPART_MAX_BITS;
+                    if (selected > room && selected <= most) q->dpart_rows = selected;
+                    else q->dpart_off = true;
+                } else {
+                    for (auto &n : q->dset_need) n *= 4;
+                }
             }
             tgpu_status st = size_workspace(q, next_pow2(q->groups_est * 100 / q->load_pct));
             if (st != TGPU_OK) return st;
@@ -1301,6 +1370,7 @@ tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out) {
     std::unique_ptr<tgpu_table> t(new tgpu_table());
     t->n_rows = desc->n_rows;
     t->rg_rows = desc->row_group_rows ? desc->row_group_rows : 65536u;
+    t->sketches = desc->compute_ndv != 0;
     t->n_rg = (uint32_t)((t->n_rows + t->rg_rows - 1) / t->rg_rows);
     const uint64_t n = t->n_rows;
     const uint64_t vwords = (n + 31) / 32 + 1;

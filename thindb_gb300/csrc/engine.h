@@ -10,6 +10,8 @@
 namespace tgpu {
 
 constexpr int MAX_GROUP_KEYS = 8;   // thinDB MAX_GROUP_KEYS (v2_shape_group_topn.zig:50)
+// Composite keys whose parts' NDV product exceeds this get their own sketch.
+constexpr uint64_t COMPOSITE_SKETCH_MIN = 1ULL << 16;
 constexpr int MAX_AGGS = 16;        // thinDB MAX_AGGS (v2_shape_group_topn.zig:54)
 constexpr int MAX_STATE_WORDS = 17; // the row count + 16 numeric slots
 constexpr int MAX_DISTINCT = 8;     // thinDB MAX_DISTINCT_AGG_SLOTS (v2_shape_group_topn.zig:62)
@@ -269,6 +271,7 @@ cudaError_t launch_staged_scan(const DevQuery &q, const StagePlan &sp, int grid,
 // partition in shared memory) and the partition's index-table slots.
 constexpr uint32_t DPART_CAP = 4096;     // 64 KB of pairs + 32 KB of slots: two CTAs per SM
 constexpr uint32_t DPART_SLOTS = 8192;
+constexpr int DPART_MAX_BITS = 20;      // 2^20 partitions: 64 GB of pairs for 3.2G rows
 // Deduplicate every partition's pairs and add each new pair to its group's
 // distinct count (table word `word` of slot gid).
 cudaError_t launch_distinct_partitions(const DevQuery &q, int word, cudaStream_t s);
@@ -328,6 +331,14 @@ cudaError_t launch_zone_maps(const void *data, const uint32_t *valid, int32_t ty
                              double *fmax, uint32_t *nulls, cudaStream_t s);
 cudaError_t launch_hll(const void *data, const uint32_t *valid, int32_t type, uint64_t n_rows, uint32_t *regs,
                        cudaStream_t s);
+// Columns of a composite key for its HyperLogLog sketch.
+struct KeySketchCols {
+    const void *data[MAX_GROUP_KEYS];
+    const uint32_t *valid[MAX_GROUP_KEYS];
+    int32_t type[MAX_GROUP_KEYS];
+    int32_t n;
+};
+cudaError_t launch_key_hll(const KeySketchCols &k, uint64_t n_rows, uint32_t *regs, cudaStream_t s);
 constexpr int HLL_P = 14;
 
 }  // namespace tgpu

@@ -349,6 +349,9 @@ __global__ void __launch_bounds__(CPT_THREADS) compact_write_kernel(const __grid
 // as encode_sort_key's dense layout.
 
 constexpr int TOPK_THREADS = 256;
+constexpr int TOPK_UNROLL = 4;  // occupied slots per lane per round of the bitmap walk
+
+__device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
 constexpr int TOPK_WARPS = TOPK_THREADS / 32;
 constexpr uint32_t NO_ID = 0xFFFFFFFFu;
 
@@ -432,16 +435,17 @@ __device__ __forceinline__ void wl_offer(WarpList<SW> &t, const uint64_t (&cand)
     }
 }
 
-// Best k of the candidates i = first + warp*32 + lane (+ stride ...) < n, as
-// produced by get(i, key, gid) -> valid.  Every warp keeps its own list; warp
-// 0 merges them and writes k entries (NO_ID pads) to out_keys (if given) and
-// out_gids, and the kept count to *out_count (if given).
-// Every warp's list -> the CTA's best k, written by warp 0 to out_keys (if
-// given) and out_gids (k entries, NO_ID pads), the count to *out_count (if
-// given).  All threads return after the merge.
+// Every warp's list -> the CTA's best k, written to out_keys (if given) and
+// out_gids (k entries, NO_ID pads), the count to *out_count (if given).  All
+// threads return after the merge.
 template <int SW>
 __device__ __forceinline__ void block_merge(const WarpList<SW> &t, int k, unsigned long long *out_keys,
                                             uint32_t *out_gids, unsigned long long *out_count) {
+    // Merge by rank: every thread owns one warp-list entry and counts the
+    // valid entries ordered before it (ties, which distinct packed keys rule
+    // out, fall back to the entry index), so the entry of rank r < k lands at
+    // position r.  All threads at once, instead of one warp inserting the
+    // lists one entry at a time.
     __shared__ unsigned long long s_keys[TOPK_WARPS * 32 * SW];
     __shared__ uint32_t s_ids[TOPK_WARPS * 32];
     __shared__ int s_cnt[TOPK_WARPS];
@@ -451,27 +455,46 @@ __device__ __forceinline__ void block_merge(const WarpList<SW> &t, int k, unsign
     s_ids[warp * 32 + lane] = t.gid;
     if (lane == 0) s_cnt[warp] = t.count;
     __syncthreads();
-    if (warp == 0) {
-        WarpList<SW> m;
-        wl_init(m);
+    int total = 0;
+    for (int w = 0; w < TOPK_WARPS; ++w) total += s_cnt[w];
+    if (lane < t.count) {
+        const int me = warp * 32 + lane;
+        int rank = 0;
         for (int w = 0; w < TOPK_WARPS; ++w) {
-            uint64_t c[SW];
+            const int n = s_cnt[w];
+            for (int j = 0; j < n; ++j) {
+                const unsigned long long *o = s_keys + ((size_t)w * 32 + j) * SW;
+                int cmp = 0;  // -1: o orders before mine, 1: after
 #pragma unroll
-            for (int i = 0; i < SW; ++i) c[i] = s_keys[((size_t)w * 32 + lane) * SW + i];
-            wl_offer<SW>(m, c, s_ids[w * 32 + lane], lane < s_cnt[w], k);
+                for (int i = 0; i < SW; ++i)
+                    if (cmp == 0 && o[i] != t.key[i]) cmp = o[i] < t.key[i] ? -1 : 1;
+                rank += (cmp < 0 || (cmp == 0 && w * 32 + j < me)) ? 1 : 0;
+            }
         }
-        if (lane < k) {
+        if (rank < k) {
             if (out_keys) {
 #pragma unroll
-                for (int i = 0; i < SW; ++i) out_keys[(size_t)lane * SW + i] = m.key[i];
+                for (int i = 0; i < SW; ++i) out_keys[(size_t)rank * SW + i] = t.key[i];
             }
-            out_gids[lane] = lane < m.count ? m.gid : NO_ID;
+            out_gids[rank] = t.gid;
         }
-        if (out_count && lane == 0) *out_count = (unsigned long long)m.count;
     }
+    const int kept = total < k ? total : k;
+    if ((int)threadIdx.x >= kept && (int)threadIdx.x < k) {
+        if (out_keys) {
+#pragma unroll
+            for (int i = 0; i < SW; ++i) out_keys[(size_t)threadIdx.x * SW + i] = 0;
+        }
+        out_gids[threadIdx.x] = NO_ID;
+    }
+    if (out_count && threadIdx.x == 0) *out_count = (unsigned long long)kept;
     __syncthreads();
 }
 
+// Best k of the candidates i = first + warp*32 + lane (+ stride ...) < n, as
+// produced by get(i, key, gid) -> valid.  Every warp keeps its own list, then
+// block_merge writes the CTA's k entries (NO_ID pads) to out_keys (if given)
+// and out_gids, and the kept count to *out_count (if given).
 template <int SW, class Get>
 __device__ __forceinline__ void block_topk(uint64_t n, uint64_t first, uint64_t stride, int k, Get get,
                                            unsigned long long *out_keys, uint32_t *out_gids,
@@ -576,23 +599,35 @@ __global__ void __launch_bounds__(TOPK_THREADS) topk_scan_kernel(const __grid_co
         uint32_t bits = w < n_words ? f.occ[w] : 0u;
         groups += (unsigned)__popc(bits);
         while (__any_sync(FULL, bits != 0)) {
-            uint64_t c[SW];
-            uint32_t g = NO_ID;
-            bool valid = false;
-            if (bits) {
-                const int b = __ffs(bits) - 1;
-                bits &= bits - 1;
-                g = (uint32_t)(w * 32 + b);
-                valid = f.n_having == 0 || having_pass(f, slot_states(f, g));
-            }
-            if (valid) {
-                encode_top_key<SW>(f, g, c);
-                ++kept;
-            } else {
+            // up to TOPK_UNROLL occupied slots of this lane's word per round:
+            // their slot lines are requested together (into L1), so a round
+            // waits on one memory latency instead of one per slot
+            uint32_t g[TOPK_UNROLL];
 #pragma unroll
-                for (int j = 0; j < SW; ++j) c[j] = 0;
+            for (int u = 0; u < TOPK_UNROLL; ++u) {
+                g[u] = NO_ID;
+                if (bits) {
+                    const int b = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    g[u] = (uint32_t)(w * 32 + b);
+                    const unsigned long long *slot = f.table + (uint64_t)g[u] * f.slot_words;
+                    prefetch_l1(slot);
+                    prefetch_l1(slot + f.slot_words - 1);
+                }
             }
-            wl_offer<SW>(t, c, g, valid, k);
+#pragma unroll
+            for (int u = 0; u < TOPK_UNROLL; ++u) {
+                uint64_t c[SW];
+                const bool valid = g[u] != NO_ID && (f.n_having == 0 || having_pass(f, slot_states(f, g[u])));
+                if (valid) {
+                    encode_top_key<SW>(f, g[u], c);
+                    ++kept;
+                } else {
+#pragma unroll
+                    for (int j = 0; j < SW; ++j) c[j] = 0;
+                }
+                wl_offer<SW>(t, c, g[u], valid, k);
+            }
         }
     }
     for (int o = 16; o; o >>= 1) {

@@ -18,6 +18,8 @@ __global__ void __launch_bounds__(SCAN_THREADS, MINB) scan_group_kernel(const __
     unsigned long long selected = 0;
     const uint32_t nw = gridDim.x * SCAN_WARPS;
     WarpQueue<P> wq{(typename P::Row *)sm.wlist + (size_t)warp * WQ_ROWS, 0u, 0u};
+    if constexpr (QUEUE)
+        static_assert(sizeof(typename P::Row) <= 24 + 8 * P::NV, "queue ring rows sized in scan_smem_bytes");
     uint32_t k = 0;
     for (uint32_t c = blockIdx.x * SCAN_WARPS + warp; c < q.n_chunks; c += nw, ++k) {
         if ((k & 31) == 31 && q.cancel) {  // poll the host-mapped cancel flag now and then
@@ -83,7 +85,9 @@ int fast_fold_id(const DevQuery &q) { return fold_id_of(q); }
 size_t scan_smem_bytes(const DevQuery &q) {
     size_t list = 0;
     if (q.gather == 1) list = (size_t)SCAN_WARPS * q.chunk_rows * 2;
-    if (q.gather == 2) list = (size_t)SCAN_WARPS * WQ_ROWS * (16 + 8 * (size_t)(q.n_faggs > 0 ? q.n_faggs : 1));
+    // a fold row: two key words, one word per input, and a COUNT(DISTINCT)
+    // row's reserved pair place (8 bytes, counted for every fold)
+    if (q.gather == 2) list = (size_t)SCAN_WARPS * WQ_ROWS * (24 + 8 * (size_t)(q.n_faggs > 0 ? q.n_faggs : 1));
     return (size_t)q.cache_slots * (8 + 8 * (size_t)q.state_words + 4) + 16 + list + 16;
 }
 

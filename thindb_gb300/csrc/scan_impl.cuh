@@ -38,6 +38,16 @@ namespace {
 
 constexpr unsigned FULL = 0xFFFFFFFFu;
 constexpr uint32_t NO_GID = 0xFFFFFFFFu;
+
+// Pick<c, A, B>::type is A when c holds, else B.
+template <bool C, typename A, typename B>
+struct Pick {
+    using type = A;
+};
+template <typename A, typename B>
+struct Pick<false, A, B> {
+    using type = B;
+};
 constexpr int FILTER_UNROLL = 16;  // 32-row filter steps in flight per warp
 
 __device__ __forceinline__ bool col_valid(const DevCol &c, uint64_t r) {
@@ -242,18 +252,31 @@ __device__ bool distinct_insert(const DevQuery &q, int d, uint32_t gid, uint64_t
     return false;
 }
 
-// Partition of a (gid, value) pair in the partitioned COUNT(DISTINCT), and
-// the pair's slot in that partition's shared-memory index table: top and low
-// bits of one hash.
-__device__ __forceinline__ uint64_t dpart_hash(uint32_t gid, uint64_t bits) { return mix64(bits ^ mix64(gid)); }
+// Partition of a (group, value) pair in the partitioned COUNT(DISTINCT): top
+// bits of a hash of the value and the group key's hash (hash_key), so that a
+// row can reserve its pair's place before its group id is known.
+__device__ __forceinline__ uint32_t dpart_of(const DevQuery &q, uint64_t hk, uint64_t bits) {
+    return (uint32_t)(mix64(bits ^ hk) >> (64 - q.dpart_bits));
+}
 
-// Append (value, gid) to its partition; a full partition sets
-// ST_DISTINCT_FULL (the host reruns with four times the partitions).
-__device__ __forceinline__ void dpart_append(const DevQuery &q, uint32_t gid, uint64_t bits) {
-    const uint64_t p = dpart_hash(gid, bits) >> (64 - q.dpart_bits);
-    const uint32_t pos = atomicAdd(q.dpart_cursor + p, 1u);
-    if (pos < q.dpart_cap) q.dpart_buf[p * q.dpart_cap + pos] = make_ulonglong2(bits, gid);
+// A reserved place: partition and position (DPOS_NONE = none reserved yet).
+constexpr uint32_t DPOS_NONE = 0xFFFFFFFFu;
+
+// Store (value, gid) at the place reserved for it.  Every reserved place is
+// stored, a pair whose group found no slot (gid NO_GID: the table is full and
+// the host reruns) too: the partition kernel skips it.  A full partition sets
+// ST_DISTINCT_FULL (the host resizes or deduplicates in the global set).
+__device__ __forceinline__ void dpart_store(const DevQuery &q, uint32_t p, uint32_t pos, uint32_t gid,
+                                            uint64_t bits) {
+    if (p >> q.dpart_bits) atomicOr(q.status, ST_BAD_INDEX);  // not a partition: report, never write
+    else if (pos < q.dpart_cap) q.dpart_buf[(uint64_t)p * q.dpart_cap + pos] = make_ulonglong2(bits, gid);
     else atomicOr(q.status, ST_DISTINCT_FULL);
+}
+
+// Reserve a place and store (value, gid) in one go.
+__device__ __forceinline__ void dpart_append(const DevQuery &q, uint64_t hk, uint32_t gid, uint64_t bits) {
+    const uint32_t p = dpart_of(q, hk, bits);
+    dpart_store(q, p, atomicAdd(q.dpart_cursor + p, 1u), gid, bits);
 }
 
 // ------------------------------------------------------- fold of states --
@@ -576,7 +599,7 @@ __device__ __noinline__ void fold_batch(const DevQuery &q, const ScanSmem sm, co
                 const DevAgg &g = q.aggs[a];
                 if (g.kind != AK_DISTINCT || !((ok >> a) & 1u)) continue;
                 uint64_t bits = g.is_float_in ? canon_f64_bits(bits_f64(val[a])) : val[a];
-                if (q.dpart_bits) dpart_append(q, gid, bits);
+                if (q.dpart_bits) dpart_append(q, hash_key(k0, k1), gid, bits);
                 else if (distinct_insert(q, g.dset, gid, bits, hash_key(k0, k1))) atomicAdd(gst + g.word, 1ULL);
             }
         }
@@ -674,6 +697,7 @@ struct GenericFold {
     __device__ __forceinline__ static void prefetch(const DevQuery &q, const Row &rv, bool me) {
         (void)prefetch_slot(q, rv.k0, rv.k1, me);
     }
+    __device__ __forceinline__ static void reserve(const DevQuery &, Row &, bool) {}
 };
 
 // A plan whose NOT NULL inputs fold with the compile-time kinds K0..K3 (the
@@ -700,16 +724,22 @@ struct FastFold {
     }
     static constexpr bool DISTINCT = K0 == AK_DISTINCT || K1 == AK_DISTINCT || K2 == AK_DISTINCT || K3 == AK_DISTINCT;
 
-    struct Row {
+    // a COUNT(DISTINCT) row also carries its pair's reserved place
+    struct PlainRow {
         uint64_t k0, k1;
         uint64_t val[NV];
     };
+    struct DistinctRow : PlainRow {
+        uint32_t dp = 0, dpos = DPOS_NONE;  // a row built by any caller starts unreserved
+    };
+    using Row = typename Pick<DISTINCT, DistinctRow, PlainRow>::type;
 
     __device__ __forceinline__ static void load(const DevQuery &q, uint64_t r, bool me, Row &rv) {
         rv.k0 = 0;
         rv.k1 = 0;
 #pragma unroll
         for (int a = 0; a < NV; ++a) rv.val[a] = 0;
+        if constexpr (DISTINCT) rv.dpos = DPOS_NONE;
         if (!me) return;
         // gathered columns are read once unless other queries of a batch follow
         const bool shared = q.shared_scan != 0;
@@ -746,6 +776,22 @@ struct FastFold {
                 if (kind(a) == AK_DISTINCT) {
                     const int d = q.faggs[a].dset;
                     prefetch_l2(q.dset[d] + 2 * distinct_home(q, d, hk, rv.val[a]));
+                }
+        }
+    }
+
+    // Partitioned COUNT(DISTINCT): reserve each row's pair place as soon as
+    // the row is loaded (the partition needs the key, not the group id), so
+    // the cursor atomics of all batches in flight overlap the folds' probes.
+    // Every lane that reserves is active in the batch's fold, which stores.
+    __device__ __forceinline__ static void reserve(const DevQuery &q, Row &rv, bool me) {
+        if constexpr (DISTINCT) {
+            if (!me || !q.dpart_bits) return;
+#pragma unroll
+            for (int a = 0; a < NA; ++a)
+                if (kind(a) == AK_DISTINCT) {
+                    rv.dp = dpart_of(q, hash_key(rv.k0, rv.k1), rv.val[a]);
+                    rv.dpos = atomicAdd(q.dpart_cursor + rv.dp, 1u);
                 }
         }
     }
@@ -869,17 +915,23 @@ struct FastFold {
                 }
             }
         }
-        if (DISTINCT) {
+        if constexpr (DISTINCT) {
             gid = __shfl_sync(FULL, gid, leader_lane);
-            if (me && gid != NO_GID) {
-                unsigned long long *gst = q.table + (uint64_t)gid * q.slot_words + q.key_words;
+            if (me) {
                 const uint64_t hk = hash_key(k0, k1);
 #pragma unroll
                 for (int a = 0; a < NV; ++a) {
                     if (a >= NA || kind(a) != AK_DISTINCT) continue;
-                    if (q.dpart_bits) dpart_append(q, gid, val[a]);
-                    else if (distinct_insert(q, q.faggs[a].dset, gid, val[a], hk))
-                        atomicAdd(gst + q.faggs[a].word, 1ULL);
+                    if (q.dpart_bits) {
+                        uint32_t p = in.dp, pos = in.dpos;
+                        if (pos == DPOS_NONE) {  // callers that do not reserve ahead
+                            p = dpart_of(q, hk, val[a]);
+                            pos = atomicAdd(q.dpart_cursor + p, 1u);
+                        }
+                        dpart_store(q, p, pos, gid, val[a]);
+                    } else if (gid != NO_GID && distinct_insert(q, q.faggs[a].dset, gid, val[a], hk)) {
+                        atomicAdd(q.table + (uint64_t)gid * q.slot_words + q.key_words + q.faggs[a].word, 1ULL);
+                    }
                 }
             }
         }
@@ -937,6 +989,8 @@ __device__ __forceinline__ void scan_chunk(const DevQuery &q, const ScanSmem &sm
 #pragma unroll
             for (int j = 0; j < L; ++j) P::prefetch(q, rows[j], (act[j] >> lane) & 1u);
 #pragma unroll
+            for (int j = 0; j < L; ++j) P::reserve(q, rows[j], (act[j] >> lane) & 1u);
+#pragma unroll
             for (int j = 0; j < L; ++j) {
                 selected += (lane == 0) ? __popc(act[j]) : 0;
                 if (act[j]) P::fold(q, sm, rows[j], act[j]);
@@ -989,6 +1043,8 @@ __device__ __forceinline__ void scan_chunk(const DevQuery &q, const ScanSmem &sm
         }
 #pragma unroll
         for (int j = 0; j < L; ++j) P::prefetch(q, rows[j], i + 32 * j + lane < n);
+#pragma unroll
+        for (int j = 0; j < L; ++j) P::reserve(q, rows[j], i + 32 * j + lane < n);
 #pragma unroll
         for (int j = 0; j < L; ++j) {
             const uint32_t b = i + 32 * j;

@@ -24,6 +24,7 @@
 // A partial last tile (the table's last rows) is copied with plain loads.
 #include <algorithm>
 
+#include "bulk.cuh"
 #include "scan_impl.cuh"
 
 namespace tgpu {
@@ -31,52 +32,6 @@ namespace tgpu {
 namespace {
 
 constexpr int STAGE_WARPS = STAGE_THREADS / 32;
-constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s of SM clock before a stage counts as lost
-
-__device__ __forceinline__ uint32_t s_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(s_addr(bar)) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_tx(uint64_t *bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(s_addr(bar)), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
-    uint32_t done;
-    asm volatile(
-        "{\n"
-        ".reg .pred p;\n"
-        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        "selp.u32 %0, 1, 0, p;\n"
-        "}\n"
-        : "=r"(done)
-        : "r"(s_addr(bar)), "r"(parity)
-        : "memory");
-    return done != 0;
-}
-
-// Bounded wait for phase `parity` of `bar` to complete.
-__device__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    if (mbar_test(bar, parity)) return true;
-    const long long t0 = clock64();
-    for (uint32_t i = 1;; ++i) {
-        if (mbar_test(bar, parity)) return true;
-        if ((i & 63) == 0) {
-            if (clock64() - t0 > WAIT_CYCLES) return false;
-            __nanosleep(32);
-        }
-    }
-}
-
-__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(s_addr(dst)),
-        "l"(src), "r"(bytes), "r"(s_addr(bar))
-        : "memory");
-}
 
 // First row and row count of tile t (0 rows: past the table's end).
 __device__ __forceinline__ void tile_rows(const DevQuery &q, const StagePlan &sp, uint32_t t, uint64_t &row0,
@@ -137,6 +92,7 @@ __device__ __forceinline__ double st_f64(const DevCol &c, const unsigned char *p
 template <class P>
 __device__ __forceinline__ void stage_row(const DevQuery &q, const StagePlan &sp, const unsigned char *stage,
                                           uint32_t r, typename P::Row &rv) {
+    rv = typename P::Row{};  // zero keys and inputs; a COUNT(DISTINCT) row unreserved
     rv.k0 = 0;
     rv.k1 = 0;
 #pragma unroll
@@ -202,6 +158,7 @@ __global__ void __launch_bounds__(STAGE_THREADS, 1)
     using Row = typename P::Row;
     uint64_t *bars = (uint64_t *)smem;
     const ScanSmem sm = carve(q, smem + sp.cache_off);
+    static_assert(sizeof(Row) <= 24 + 8 * P::NV, "fold-queue rows sized in stage_plan");
     Row *queue = (Row *)(smem + sp.queue_off);
     unsigned char *ring = smem + sp.ring_off;
     __shared__ uint32_t queue_n;
@@ -214,7 +171,7 @@ __global__ void __launch_bounds__(STAGE_THREADS, 1)
 
     if (threadIdx.x == 0) {
         for (uint32_t s = 0; s < S; ++s) mbar_init(&bars[s]);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        mbar_init_fence();
         queue_n = 0;
         stop = 0;
     }
@@ -273,7 +230,7 @@ __global__ void __launch_bounds__(STAGE_THREADS, 1)
         __syncthreads();
         // the stage is consumed: refill it with tile i + S
         if (threadIdx.x == 0 && issued < my_n) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            fence_proxy_async_smem();
             issue_tile(q, sp, blockIdx.x + issued * G, ring + (size_t)(issued % S) * sp.stage_bytes,
                        &bars[issued % S]);
             ++issued;
@@ -344,7 +301,9 @@ bool stage_plan(DevQuery &q, uint64_t tile_count, StagePlan *sp) {
     if (!ok || p.n_cols == 0) return false;
     p.n_tiles = (uint32_t)tile_count;
     p.tiles_per_rg = q.rg_rows / STAGE_TILE;
-    p.row_bytes = 16 + 8 * (uint32_t)(q.n_faggs > 0 ? q.n_faggs : 1);
+    // two key words, one word per input, a COUNT(DISTINCT) row's reserved
+    // pair place (FastFold::Row; 8 bytes, counted for every fold)
+    p.row_bytes = 24 + 8 * (uint32_t)(q.n_faggs > 0 ? q.n_faggs : 1);
     // shared memory: barriers | hot-key cache | fold queue | ring of stages
     const uint32_t budget = 220 * 1024;
     const uint32_t queue_bytes = STAGE_QCAP * p.row_bytes;

@@ -123,6 +123,34 @@ __global__ void hll_kernel(const void *data, const uint32_t *valid, int32_t type
         if (sreg[i]) atomicMax(&regs[i], sreg[i]);
 }
 
+// HyperLogLog of composite keys: each row's parts' value bits chained
+// through mix64 (a NULL part hashes as a marker), registers as above.  The
+// product of the parts' NDVs overestimates the groups of correlated parts
+// (a url belongs to one region), and the group table sized from it would
+// spread the groups over many times the memory they need.
+__global__ void key_hll_kernel(const __grid_constant__ KeySketchCols k, uint64_t n_rows, uint32_t *regs) {
+    extern __shared__ uint32_t sreg[];
+    for (int i = threadIdx.x; i < HLL_M; i += blockDim.x) sreg[i] = 0;
+    __syncthreads();
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t h = 0x6A09E667F3BCC909ULL;
+        for (int i = 0; i < k.n; ++i) {
+            const bool is_f = k.type[i] == TGPU_FLOAT || k.type[i] == TGPU_DOUBLE;
+            uint64_t bits = 0x8000000000000001ULL;  // NULL
+            if (valid_at(k.valid[i], r))
+                bits = is_f ? canon_f64_bits(f_at(k.data[i], k.type[i], r)) : (uint64_t)int_at(k.data[i], k.type[i], r);
+            h = mix64(h ^ bits);
+        }
+        uint32_t idx = (uint32_t)(h >> (64 - HLL_P));
+        uint64_t w = (h << HLL_P) | (1ULL << (HLL_P - 1));
+        uint32_t rank = (uint32_t)__clzll((long long)w) + 1;
+        if (rank > sreg[idx]) atomicMax(&sreg[idx], rank);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < HLL_M; i += blockDim.x)
+        if (sreg[i]) atomicMax(&regs[i], sreg[i]);
+}
+
 }  // namespace
 
 cudaError_t launch_zone_maps(const void *data, const uint32_t *valid, int32_t type, uint64_t n_rows,
@@ -141,6 +169,16 @@ cudaError_t launch_hll(const void *data, const uint32_t *valid, int32_t type, ui
     cudaError_t e = cudaFuncSetAttribute(hll_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     hll_kernel<<<grid, 512, smem, s>>>(data, valid, type, n_rows, regs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_key_hll(const KeySketchCols &k, uint64_t n_rows, uint32_t *regs, cudaStream_t s) {
+    if (n_rows == 0) return cudaSuccess;
+    int grid = (int)std::min<uint64_t>((n_rows + 1023) / 1024, 1024);
+    size_t smem = HLL_M * sizeof(uint32_t);
+    cudaError_t e = cudaFuncSetAttribute(key_hll_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    key_hll_kernel<<<grid, 512, smem, s>>>(k, n_rows, regs);
     return cudaGetLastError();
 }
 
