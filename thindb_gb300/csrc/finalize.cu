@@ -349,9 +349,6 @@ __global__ void __launch_bounds__(CPT_THREADS) compact_write_kernel(const __grid
 // as encode_sort_key's dense layout.
 
 constexpr int TOPK_THREADS = 256;
-constexpr int TOPK_UNROLL = 4;  // occupied slots per lane per round of the bitmap walk
-
-__device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
 constexpr int TOPK_WARPS = TOPK_THREADS / 32;
 constexpr uint32_t NO_ID = 0xFFFFFFFFu;
 
@@ -599,35 +596,23 @@ __global__ void __launch_bounds__(TOPK_THREADS) topk_scan_kernel(const __grid_co
         uint32_t bits = w < n_words ? f.occ[w] : 0u;
         groups += (unsigned)__popc(bits);
         while (__any_sync(FULL, bits != 0)) {
-            // up to TOPK_UNROLL occupied slots of this lane's word per round:
-            // their slot lines are requested together (into L1), so a round
-            // waits on one memory latency instead of one per slot
-            uint32_t g[TOPK_UNROLL];
-#pragma unroll
-            for (int u = 0; u < TOPK_UNROLL; ++u) {
-                g[u] = NO_ID;
-                if (bits) {
-                    const int b = __ffs(bits) - 1;
-                    bits &= bits - 1;
-                    g[u] = (uint32_t)(w * 32 + b);
-                    const unsigned long long *slot = f.table + (uint64_t)g[u] * f.slot_words;
-                    prefetch_l1(slot);
-                    prefetch_l1(slot + f.slot_words - 1);
-                }
+            uint64_t c[SW];
+            uint32_t g = NO_ID;
+            bool valid = false;
+            if (bits) {
+                const int b = __ffs(bits) - 1;
+                bits &= bits - 1;
+                g = (uint32_t)(w * 32 + b);
+                valid = f.n_having == 0 || having_pass(f, slot_states(f, g));
             }
+            if (valid) {
+                encode_top_key<SW>(f, g, c);
+                ++kept;
+            } else {
 #pragma unroll
-            for (int u = 0; u < TOPK_UNROLL; ++u) {
-                uint64_t c[SW];
-                const bool valid = g[u] != NO_ID && (f.n_having == 0 || having_pass(f, slot_states(f, g[u])));
-                if (valid) {
-                    encode_top_key<SW>(f, g[u], c);
-                    ++kept;
-                } else {
-#pragma unroll
-                    for (int j = 0; j < SW; ++j) c[j] = 0;
-                }
-                wl_offer<SW>(t, c, g[u], valid, k);
+                for (int j = 0; j < SW; ++j) c[j] = 0;
             }
+            wl_offer<SW>(t, c, g, valid, k);
         }
     }
     for (int o = 16; o; o >>= 1) {
