@@ -349,6 +349,7 @@ __global__ void __launch_bounds__(CPT_THREADS) compact_write_kernel(const __grid
 // as encode_sort_key's dense layout.
 
 constexpr int TOPK_THREADS = 256;
+constexpr int TOPK_LIST = 32 * 32;  // occupied slots of one warp's 32 bitmap words at most
 constexpr int TOPK_WARPS = TOPK_THREADS / 32;
 constexpr uint32_t NO_ID = 0xFFFFFFFFu;
 
@@ -550,7 +551,9 @@ __device__ __forceinline__ void topk_final_body(const unsigned long long *cand_k
     block_topk<SW>(
         (uint64_t)n_blocks * k, 0, TOPK_THREADS, k,
         [&](uint64_t i, uint64_t(&c)[SW], uint32_t &g) {
-            const uint64_t e = (i / k) * 32 + (i % k);
+            // every CTA's best first, then every CTA's second, ...: the
+            // lists' heads set a high bar early, so few later entries insert
+            const uint64_t e = (i % n_blocks) * 32 + (i / n_blocks);
             g = cand_gids[e];
 #pragma unroll
             for (int j = 0; j < SW; ++j) c[j] = cand_keys[e * SW + j];
@@ -586,34 +589,55 @@ __global__ void __launch_bounds__(TOPK_THREADS) topk_scan_kernel(const __grid_co
                                                                  unsigned long long *counts, unsigned int *done) {
     __shared__ unsigned long long s_sum[2][TOPK_WARPS];
     __shared__ int s_last;
+    extern __shared__ uint32_t s_lists[];  // TOPK_WARPS lists of up to 32 x 32 occupied slots
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t *list = s_lists + (size_t)warp * TOPK_LIST;
     WarpList<SW> t;
     wl_init(t);
     unsigned long long groups = 0, kept = 0;
     const uint64_t stride = (uint64_t)gridDim.x * TOPK_THREADS;
+    // U batches of 32 listed slots are loaded (all in flight) before any is offered
+    constexpr int U = SW <= 6 ? 4 : 2;
     for (uint64_t base = (uint64_t)blockIdx.x * TOPK_THREADS + (uint64_t)warp * 32; base < n_words; base += stride) {
+        // 32 bitmap words -> the warp's dense list of occupied slots, so the
+        // candidates below keep every lane busy whatever the words' counts
         const uint64_t w = base + lane;
         uint32_t bits = w < n_words ? f.occ[w] : 0u;
-        groups += (unsigned)__popc(bits);
-        while (__any_sync(FULL, bits != 0)) {
-            uint64_t c[SW];
-            uint32_t g = NO_ID;
-            bool valid = false;
-            if (bits) {
-                const int b = __ffs(bits) - 1;
-                bits &= bits - 1;
-                g = (uint32_t)(w * 32 + b);
-                valid = f.n_having == 0 || having_pass(f, slot_states(f, g));
-            }
-            if (valid) {
-                encode_top_key<SW>(f, g, c);
-                ++kept;
-            } else {
+        const int nb = __popc(bits);
+        int end = nb;
 #pragma unroll
-                for (int j = 0; j < SW; ++j) c[j] = 0;
-            }
-            wl_offer<SW>(t, c, g, valid, k);
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL, end, o);
+            if (lane >= o) end += y;
         }
+        const int total = __shfl_sync(FULL, end, 31);
+        groups += (unsigned)nb;
+        for (int at = end - nb; bits; ++at) {
+            list[at] = (uint32_t)(w * 32 + (__ffs(bits) - 1));
+            bits &= bits - 1;
+        }
+        __syncwarp();
+        for (int i0 = 0; i0 < total; i0 += 32 * U) {
+            uint64_t c[U][SW];
+            uint32_t g[U];
+            bool valid[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int i = i0 + u * 32 + lane;
+                g[u] = i < total ? list[i] : NO_ID;
+                valid[u] = g[u] != NO_ID && (f.n_having == 0 || having_pass(f, slot_states(f, g[u])));
+                if (valid[u]) {
+                    encode_top_key<SW>(f, g[u], c[u]);
+                    ++kept;
+                } else {
+#pragma unroll
+                    for (int j = 0; j < SW; ++j) c[u][j] = 0;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) wl_offer<SW>(t, c[u], g[u], valid[u], k);
+        }
+        __syncwarp();
     }
     for (int o = 16; o; o >>= 1) {
         groups += __shfl_down_sync(FULL, groups, o);
@@ -643,7 +667,9 @@ __global__ void __launch_bounds__(TOPK_THREADS) topk_scan_kernel(const __grid_co
     block_topk<SW>(
         (uint64_t)nb * k, 0, TOPK_THREADS, k,
         [&](uint64_t i, uint64_t(&c)[SW], uint32_t &g) {
-            const uint64_t e = (i / k) * 32 + (i % k);
+            // every CTA's best first, then every CTA's second, ...: the
+            // lists' heads set a high bar early, so few later entries insert
+            const uint64_t e = (i % nb) * 32 + (i / nb);
             g = __ldcg(cand_gids + e);
 #pragma unroll
             for (int j = 0; j < SW; ++j) c[j] = __ldcg(cand_keys + e * SW + j);
@@ -928,23 +954,27 @@ cudaError_t launch_topk(const DevFinal &f, const uint32_t *gids, unsigned long l
 }
 
 template <int SW>
-static void launch_topk_scan_w(const DevFinal &f, uint32_t k, unsigned long long *cand_keys, uint32_t *cand_gids,
+static cudaError_t launch_topk_scan_w(const DevFinal &f, uint32_t k, unsigned long long *cand_keys, uint32_t *cand_gids,
                                uint32_t n_blocks, uint32_t *sel_out, unsigned long long *counts, unsigned int *done,
                                cudaStream_t s) {
-    topk_scan_kernel<SW><<<n_blocks, TOPK_THREADS, 0, s>>>(f, occ_words(f.cap), (int)k, cand_keys, cand_gids, sel_out,
-                                                           counts, done);
+    const size_t smem = (size_t)TOPK_WARPS * TOPK_LIST * sizeof(uint32_t);
+    const cudaError_t e =
+        cudaFuncSetAttribute(topk_scan_kernel<SW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    topk_scan_kernel<SW><<<n_blocks, TOPK_THREADS, smem, s>>>(f, occ_words(f.cap), (int)k, cand_keys, cand_gids,
+                                                              sel_out, counts, done);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_topk_scan(const DevFinal &f, unsigned long long *counts, uint32_t k, unsigned long long *cand_keys,
                              uint32_t *cand_gids, uint32_t n_cand_blocks, uint32_t *sel_out, unsigned int *done,
                              cudaStream_t s) {
     switch (topk_width(f.sort_words)) {
-        case 4: launch_topk_scan_w<4>(f, k, cand_keys, cand_gids, n_cand_blocks, sel_out, counts, done, s); break;
-        case 6: launch_topk_scan_w<6>(f, k, cand_keys, cand_gids, n_cand_blocks, sel_out, counts, done, s); break;
-        case 8: launch_topk_scan_w<8>(f, k, cand_keys, cand_gids, n_cand_blocks, sel_out, counts, done, s); break;
-        default: launch_topk_scan_w<14>(f, k, cand_keys, cand_gids, n_cand_blocks, sel_out, counts, done, s); break;
+        case 4: return launch_topk_scan_w<4>(f, k, cand_keys, cand_gids, n_cand_blocks, sel_out, counts, done, s);
+        case 6: return launch_topk_scan_w<6>(f, k, cand_keys, cand_gids, n_cand_blocks, sel_out, counts, done, s);
+        case 8: return launch_topk_scan_w<8>(f, k, cand_keys, cand_gids, n_cand_blocks, sel_out, counts, done, s);
+        default: return launch_topk_scan_w<14>(f, k, cand_keys, cand_gids, n_cand_blocks, sel_out, counts, done, s);
     }
-    return cudaGetLastError();
 }
 
 cudaError_t launch_sort(const DevFinal &f, const uint32_t *gids, unsigned long long *counts, uint64_t max_n,
