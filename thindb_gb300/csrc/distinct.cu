@@ -107,7 +107,9 @@ __global__ void __launch_bounds__(DP_THREADS, 1)
             if (!done) atomicOr(status, ST_BAD_INDEX);  // cannot happen: n <= cap < DPART_SLOTS
             // a pair stored with no group (NO_GID: the table filled up, the
             // host reruns) is deduplicated like any other and counted nowhere
-            if (fresh && gid <= max_gid) atomicAdd(table + (uint64_t)gid * slot_words + key_words + word, 1ULL);
+            if (fresh && gid <= max_gid)
+                asm volatile("red.global.add.u64 [%0], 1;" ::"l"(table + (uint64_t)gid * slot_words + key_words + word)
+                             : "memory");
         }
         __syncthreads();  // stage s and the slots are free again
         if (threadIdx.x == 0 && issued < my_n) {

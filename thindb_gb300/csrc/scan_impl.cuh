@@ -292,9 +292,30 @@ struct Acc {
 // Apply a combined contribution to a slot's state words (shared or global:
 // the atomics resolve to the address space of `st`).  Aggregates that share a
 // state word (SUM and AVG of one column) fold it once (g.owner).
+// Fire-and-forget updates of a group's state words.  The folds reach a
+// state through a pointer that may lead into the shared-memory table or the
+// global one (and arrives as a parameter of an out-of-line fold), so the
+// compiler sees a generic address; for a global state it then emits an
+// atomic that returns the old value, a full round trip whose destination
+// register the warp waits on, where red.global returns nothing.  Shared
+// states keep the generic atomics (measured faster there than red.shared).
+__device__ __forceinline__ void red_add(unsigned long long *p, unsigned long long v, bool smem) {
+    if (smem) atomicAdd(p, v);
+    else asm volatile("red.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void red_max(unsigned long long *p, unsigned long long v, bool smem) {
+    if (smem) atomicMax(p, v);
+    else asm volatile("red.global.max.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void red_add_f64(unsigned long long *p, double v, bool smem) {
+    if (smem) atomicAdd((double *)p, v);
+    else asm volatile("red.global.add.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+
 template <int NA>
-__device__ __forceinline__ void apply_states(const DevQuery &q, unsigned long long *st, const Acc<NA> &acc) {
-    atomicAdd(st, (unsigned long long)acc.rows);
+__device__ __forceinline__ void apply_states(const DevQuery &q, unsigned long long *st, bool smem,
+                                             const Acc<NA> &acc) {
+    red_add(st, (unsigned long long)acc.rows, smem);
 #pragma unroll 1
     for (int a = 0; a < NA; ++a) {
         if (a >= q.n_aggs) break;
@@ -303,13 +324,13 @@ __device__ __forceinline__ void apply_states(const DevQuery &q, unsigned long lo
         if (vc == 0 || !g.owner) continue;
         unsigned long long *w = st + g.word;
         switch (g.kind) {
-            case AK_COUNT_VALID: atomicAdd(w, (unsigned long long)vc); break;
+            case AK_COUNT_VALID: red_add(w, (unsigned long long)vc, smem); break;
             case AK_SUM_I64:
-                if (acc.lo[a]) atomicAdd(w, (unsigned long long)acc.lo[a]);
+                if (acc.lo[a]) red_add(w, (unsigned long long)acc.lo[a], smem);
                 break;
             case AK_SUM_I128:
-                if (acc.lo[a]) atomicAdd(w, (unsigned long long)acc.lo[a]);
-                if (acc.hi[a]) atomicAdd(w + 1, (unsigned long long)acc.hi[a]);
+                if (acc.lo[a]) red_add(w, (unsigned long long)acc.lo[a], smem);
+                if (acc.hi[a]) red_add(w + 1, (unsigned long long)acc.hi[a], smem);
                 break;
             case AK_SUM_I128C: {
                 unsigned long long lo = acc.lo[a], hi = acc.hi[a];
@@ -317,16 +338,16 @@ __device__ __forceinline__ void apply_states(const DevQuery &q, unsigned long lo
                     unsigned long long old = atomicAdd(w, lo);
                     hi += (old + lo < old) ? 1ULL : 0ULL;
                 }
-                if (hi) atomicAdd(w + 1, hi);
+                if (hi) red_add(w + 1, hi, smem);
                 break;
             }
-            case AK_SUM_F64: atomicAdd((double *)w, __longlong_as_double((long long)acc.lo[a])); break;
+            case AK_SUM_F64: red_add_f64(w, __longlong_as_double((long long)acc.lo[a]), smem); break;
             case AK_MIN_I: case AK_MAX_I: case AK_MIN_F: case AK_MAX_F:
-                atomicMax(w, (unsigned long long)acc.lo[a]);
+                red_max(w, (unsigned long long)acc.lo[a], smem);
                 break;
             default: break;
         }
-        if (g.vword >= 0) atomicAdd(st + g.vword, (unsigned long long)vc);
+        if (g.vword >= 0) red_add(st + g.vword, (unsigned long long)vc, smem);
     }
 }
 
@@ -579,13 +600,13 @@ __device__ __noinline__ void fold_batch(const DevQuery &q, const ScanSmem sm, co
                     gid = *((volatile uint32_t *)sm.cgid + e);
                     if (gid == NO_GID) gid = (uint32_t)global_slot(q, k0, 0);
                 }
-                apply_states<NA>(q, sm.cstate + (size_t)e * q.state_words, acc);
+                apply_states<NA>(q, sm.cstate + (size_t)e * q.state_words, true, acc);
                 done = true;
             }
         }
         if (!done) {
             gid = (uint32_t)global_slot(q, k0, k1);
-            if (gid != NO_GID) apply_states<NA>(q, q.table + (uint64_t)gid * q.slot_words + q.key_words, acc);
+            if (gid != NO_GID) apply_states<NA>(q, q.table + (uint64_t)gid * q.slot_words + q.key_words, false, acc);
         }
     }
 
@@ -600,7 +621,7 @@ __device__ __noinline__ void fold_batch(const DevQuery &q, const ScanSmem sm, co
                 if (g.kind != AK_DISTINCT || !((ok >> a) & 1u)) continue;
                 uint64_t bits = g.is_float_in ? canon_f64_bits(bits_f64(val[a])) : val[a];
                 if (q.dpart_bits) dpart_append(q, hash_key(k0, k1), gid, bits);
-                else if (distinct_insert(q, g.dset, gid, bits, hash_key(k0, k1))) atomicAdd(gst + g.word, 1ULL);
+                else if (distinct_insert(q, g.dset, gid, bits, hash_key(k0, k1))) red_add(gst + g.word, 1ULL, false);
             }
         }
     }
@@ -796,6 +817,32 @@ struct FastFold {
         }
     }
 
+    // The folded contribution of one group to its state words.
+    template <bool SMEM>
+    __device__ __forceinline__ static void apply(const DevQuery &q, unsigned long long *st, uint32_t rows,
+                                                 const uint64_t (&lo)[NV], const uint64_t (&hi)[NV]) {
+        red_add(st, (unsigned long long)rows, SMEM);
+#pragma unroll
+        for (int a = 0; a < NV; ++a) {
+            if (a >= NA) continue;
+            unsigned long long *w = st + q.faggs[a].word;
+            switch (kind(a)) {
+                case AK_SUM_I64:
+                    if (lo[a]) red_add(w, (unsigned long long)lo[a], SMEM);
+                    break;
+                case AK_SUM_I128:
+                    if (lo[a]) red_add(w, (unsigned long long)lo[a], SMEM);
+                    if (hi[a]) red_add(w + 1, (unsigned long long)hi[a], SMEM);
+                    break;
+                case AK_SUM_F64: red_add_f64(w, bits_f64(lo[a]), SMEM); break;
+                case AK_MIN_I: case AK_MAX_I: case AK_MIN_F: case AK_MAX_F:
+                    red_max(w, (unsigned long long)lo[a], SMEM);
+                    break;
+                default: break;
+            }
+        }
+    }
+
     __device__ __noinline__ static void fold(const DevQuery &q, const ScanSmem sm, const Row in, unsigned active) {
         const int lane = threadIdx.x & 31;
         const bool me = (active >> lane) & 1u;
@@ -874,6 +921,7 @@ struct FastFold {
         uint32_t gid = NO_GID;
         if (leader) {
             unsigned long long *st = nullptr;
+            bool st_smem = false;
             if (q.cache_slots && q.key_words == 1 && k0 != 0) {
                 bool claimed;
                 const int e = cache_find(q, sm, k0, claimed);
@@ -886,6 +934,7 @@ struct FastFold {
                         if (gid == NO_GID) gid = (uint32_t)global_slot(q, k0, 0);
                     }
                     st = sm.cstate + (size_t)e * q.state_words;
+                    st_smem = true;
                 }
             }
             if (!st) {
@@ -893,26 +942,9 @@ struct FastFold {
                 if (gid != NO_GID) st = q.table + (uint64_t)gid * q.slot_words + q.key_words;
             }
             if (st) {
-                atomicAdd(st, (unsigned long long)rows);
-#pragma unroll
-                for (int a = 0; a < NV; ++a) {
-                    if (a >= NA) continue;
-                    unsigned long long *w = st + q.faggs[a].word;
-                    switch (kind(a)) {
-                        case AK_SUM_I64:
-                            if (lo[a]) atomicAdd(w, (unsigned long long)lo[a]);
-                            break;
-                        case AK_SUM_I128:
-                            if (lo[a]) atomicAdd(w, (unsigned long long)lo[a]);
-                            if (hi[a]) atomicAdd(w + 1, (unsigned long long)hi[a]);
-                            break;
-                        case AK_SUM_F64: atomicAdd((double *)w, bits_f64(lo[a])); break;
-                        case AK_MIN_I: case AK_MAX_I: case AK_MIN_F: case AK_MAX_F:
-                            atomicMax(w, (unsigned long long)lo[a]);
-                            break;
-                        default: break;
-                    }
-                }
+                // one copy of the updates per state space, chosen once
+                if (st_smem) apply<true>(q, st, rows, lo, hi);
+                else apply<false>(q, st, rows, lo, hi);
             }
         }
         if constexpr (DISTINCT) {
@@ -930,7 +962,7 @@ struct FastFold {
                         }
                         dpart_store(q, p, pos, gid, val[a]);
                     } else if (gid != NO_GID && distinct_insert(q, q.faggs[a].dset, gid, val[a], hk)) {
-                        atomicAdd(q.table + (uint64_t)gid * q.slot_words + q.key_words + q.faggs[a].word, 1ULL);
+                        red_add(q.table + (uint64_t)gid * q.slot_words + q.key_words + q.faggs[a].word, 1ULL, false);
                     }
                 }
             }
