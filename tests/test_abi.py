@@ -117,3 +117,25 @@ def test_committed_tuning_table_parses():
     for e in doc["entries"]:
         assert set(e["shape"]) == fields
         assert e["chunk_rows"] % 256 == 0 and e["table_load_pct"] in (0, 25, 50, 70)
+
+
+def test_tuning_merge_keeps_untouched_shapes():
+    """--merge: a shape tuned again takes its new entry, other shapes keep
+    theirs, and the provenance lists both runs."""
+    from thindb_gb300.autotune import merge_tables
+
+    def entry(groups_log2, chunk):
+        shape = {f: 0 for f, _ in abi.Shape._fields_}
+        shape["groups_log2"] = groups_log2
+        return {"shape": shape, "chunk_rows": chunk}
+
+    old = {"generated_by": "python -m thindb_gb300.autotune --workloads plain --reps 3", "seconds": 10.0,
+           "entries": [entry(10, 512), entry(20, 1024)]}
+    entries, by, seconds = merge_tables(old, [entry(20, 4096), entry(22, 2048)],
+                                        "python -m thindb_gb300.autotune --workloads distinct --reps 3", 5.0)
+    assert [(e["shape"]["groups_log2"], e["chunk_rows"]) for e in entries] == [(10, 512), (20, 4096), (22, 2048)]
+    assert by == [old["generated_by"], "python -m thindb_gb300.autotune --workloads distinct --reps 3 --merge <this file>"]
+    assert seconds == 15.0
+    # a second merge appends to the list
+    _, by2, _ = merge_tables({"generated_by": by, "seconds": seconds, "entries": entries}, [], "cmd", 1.0)
+    assert by2[:2] == by and by2[2] == "cmd --merge <this file>"

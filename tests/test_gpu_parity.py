@@ -120,6 +120,19 @@ def test_distinct_composite():
     assert st.groups > 100_000
 
 
+def test_composite_key_sized_by_its_own_sketch():
+    """url codes belong to one region: the product of the parts' NDVs (64 x
+    50,000) overestimates the groups 8x; the composite key's own sketch
+    sizes the table near the real count."""
+    cols = distinct_cols(1_000_000, 50_000)
+    req = Request(["region", "url"], [AggSpec("count", None, "c"), AggSpec("sum", "latency_ms", "lat")])
+    _, st = run_both(cols, req)
+    assert st.groups > 300_000
+    assert st.table_capacity <= 4 * st.groups  # product-sized: next_pow2(2 x 1.25M rows) = 4M
+    _, st0 = run_gpu(cols, req, compute_ndv=False)  # no sketches: the column domains bound it
+    assert st0.groups == st.groups
+
+
 def test_distinct_rerun_epochs():
     """The distinct set is reused across executions (epoch tags): results repeat."""
     cols = distinct_cols(300_000, 20_000)

@@ -273,6 +273,16 @@ def tune_workload(name: str, n: int, stream: int, reps: int, log=print, previous
     return entries
 
 
+def merge_tables(old: dict, entries: list, command: str, seconds: float):
+    """(entries, generated_by, seconds) of a tuning table `old` updated with
+    freshly tuned `entries`: a shape tuned again takes the new entry, every
+    other shape keeps its old one; the provenance lists both commands."""
+    tuned = {json.dumps(e["shape"], sort_keys=True) for e in entries}
+    kept = [e for e in old["entries"] if json.dumps(e["shape"], sort_keys=True) not in tuned]
+    before = old["generated_by"] if isinstance(old["generated_by"], list) else [old["generated_by"]]
+    return kept + entries, before + [command + " --merge <this file>"], round(old.get("seconds", 0) + seconds, 1)
+
+
 def main(argv=None) -> int:
     import torch
 
@@ -313,13 +323,7 @@ def main(argv=None) -> int:
     seconds = round(time.time() - t0, 1)
     if args.merge:
         with open(args.merge) as f:
-            old = json.load(f)
-        tuned = {json.dumps(e["shape"], sort_keys=True) for e in entries}
-        kept = [e for e in old["entries"] if json.dumps(e["shape"], sort_keys=True) not in tuned]
-        entries = kept + entries
-        before = old["generated_by"] if isinstance(old["generated_by"], list) else [old["generated_by"]]
-        command = before + [command + " --merge <this file>"]
-        seconds = round(old.get("seconds", 0) + seconds, 1)
+            entries, command, seconds = merge_tables(json.load(f), entries, command, seconds)
     doc = {
         "device": torch.cuda.get_device_name(0),
         "generated_by": command,

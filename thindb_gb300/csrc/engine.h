@@ -269,7 +269,7 @@ cudaError_t launch_staged_scan(const DevQuery &q, const StagePlan &sp, int grid,
 
 // Partitioned COUNT(DISTINCT): pairs per partition (one CTA deduplicates a
 // partition in shared memory) and the partition's index-table slots.
-constexpr uint32_t DPART_CAP = 4096;     // 64 KB of pairs + 32 KB of slots: two CTAs per SM
+constexpr uint32_t DPART_CAP = 4096;     // 64 KB of pairs per ring stage; three stages + 32 KB of slots per SM
 constexpr uint32_t DPART_SLOTS = 8192;
 constexpr int DPART_MAX_BITS = 20;      // 2^20 partitions: 64 GB of pairs for 3.2G rows
 // Deduplicate every partition's pairs and add each new pair to its group's
