@@ -19,6 +19,7 @@
 // equality compares the full pair, so the count is exact), barrier, refill
 // the stage with partition i + S.
 #include <algorithm>
+#include <mutex>
 
 #include "bulk.cuh"
 #include "common.cuh"
@@ -131,9 +132,11 @@ struct DpLaunch {
 };
 
 DpLaunch dp_launch_shape(uint32_t cap) {
+    static std::mutex mu;
     static DpLaunch cached[64];  // per device ordinal
     int dev = 0;
     cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
     DpLaunch &d = cached[dev & 63];
     if (!d.sms) {
         int optin = 0, sms = 0;
