@@ -139,12 +139,17 @@ struct Plan {
     std::vector<AggPlan> aggs;
     int n_slots = 0;
     int n_distinct = 0;
+    bool global = false;  // no GROUP BY: v2_global_aggregate.zig, one output row
 };
 
 // validateShape restated (v2_shape_group_topn.zig:2051-2370) for the shapes
 // this engine runs; strings (hashed keys) and wide decimals decline.
 int build_plan(const Table &t, const tgpu_request *req, Plan &p) {
-    if (req->n_group_cols == 0 || req->n_group_cols > MAX_GROUP_KEYS) return fail(TGPU_DECLINE, "group key count");
+    if (req->n_group_cols > MAX_GROUP_KEYS) return fail(TGPU_DECLINE, "group key count");
+    // No GROUP BY: the global aggregate (v2_global_aggregate.zig tryBuild
+    // :1188-1191), which declines HAVING.
+    p.global = req->n_group_cols == 0;
+    if (p.global && req->n_having) return fail(TGPU_DECLINE, "HAVING on a global aggregate");
     if (req->n_aggs == 0 || req->n_aggs > MAX_AGGS) return fail(TGPU_DECLINE, "aggregate count");
     int off = 0;
     for (uint32_t i = 0; i < req->n_group_cols; ++i) {
@@ -472,7 +477,7 @@ uint64_t agg_denom(const Group &g, const AggPlan &a) {  // aggDenom, :1407-1411
     return g.count;
 }
 
-Value agg_value(const Group &g, const AggPlan &a) {
+Value agg_value(const Group &g, const AggPlan &a, bool global) {
     Value v;
     switch (a.func) {
         case TGPU_AGG_COUNT:  // countValue, :1400-1404
@@ -484,7 +489,10 @@ Value agg_value(const Group &g, const AggPlan &a) {
         default: break;
     }
     uint64_t den = agg_denom(g, a);
-    if (a.nullable && den == 0) { v.null = true; return v; }  // aggIsNull, :1413-1424
+    // aggIsNull, :1413-1424 (a group's non-nullable input always has rows);
+    // the global aggregate's emitRow: NULL over zero non-NULL inputs
+    // (v2_global_aggregate.zig:1853-1855)
+    if (den == 0) { v.null = true; return v; }
     switch (a.func) {
         case TGPU_AGG_SUM:
             if (a.fl) { v.is_f = true; v.f = slot_f64(g.slots, a.state); }
@@ -499,7 +507,8 @@ Value agg_value(const Group &g, const AggPlan &a) {
             if (a.fl) v.f = slot_f64(g.slots, a.state) / (double)den;  // avgFloatValue, :1467-1470
             else {
                 i128 s = a.wide ? wide_value(g.slots, a.state) : (i128)g.slots[a.state - 1];
-                v.f = (double)s / (double)den / POW10[a.scale];  // avgValue, :1438-1446
+                v.f = global ? (double)s / ((double)den * POW10[a.scale])  // emitRow, v2_global_aggregate.zig:1872-1877
+                             : (double)s / (double)den / POW10[a.scale];   // avgValue, :1438-1446
             }
             return v;
         default:  // MIN / MAX
@@ -639,6 +648,9 @@ int run(const Table &t, const tgpu_request *req, int threads, Result &res) {
     }
     res.groups = groups.size();
     res.selected = selected;
+    // a global aggregate answers one row even when no row passed: COUNTs 0,
+    // the other aggregates NULL (v2_global_aggregate.zig emitRow :1839-1905)
+    if (p.global && groups.empty()) groups.push_back(Group{0, 0, {}});
 
     // HAVING (applyHaving, v2_shape_group_topn.zig:2586)
     std::vector<uint32_t> keep;
@@ -646,13 +658,13 @@ int run(const Table &t, const tgpu_request *req, int threads, Result &res) {
     for (uint32_t g = 0; g < groups.size(); ++g) {
         bool ok = true;
         for (uint32_t h = 0; h < req->n_having && ok; ++h)
-            ok = having_ok(agg_value(groups[g], p.aggs[req->having[h].agg]), req->having[h]);
+            ok = having_ok(agg_value(groups[g], p.aggs[req->having[h].agg], p.global), req->having[h]);
         if (ok) keep.push_back(g);
     }
     // ORDER BY, then the packed key (rowOrderBefore, :1327-1335)
     if (req->n_order > 0) {
         auto order_val = [&](const Group &g, const tgpu_sort_spec &s) {
-            return s.target == TGPU_SORT_KEY ? key_value(g, p.parts[s.index]) : agg_value(g, p.aggs[s.index]);
+            return s.target == TGPU_SORT_KEY ? key_value(g, p.parts[s.index]) : agg_value(g, p.aggs[s.index], p.global);
         };
         std::sort(keep.begin(), keep.end(), [&](uint32_t x, uint32_t y) {
             const Group &a = groups[x], &b = groups[y];
@@ -693,7 +705,7 @@ int run(const Table &t, const tgpu_request *req, int threads, Result &res) {
         const char *nm = req->aggs[i].as;
         std::snprintf(oc.name, sizeof(oc.name), "%s", nm ? nm : "");
         oc.type = p.aggs[i].out_type;
-        oc.nullable = p.aggs[i].nullable && p.aggs[i].func != TGPU_AGG_COUNT && !p.aggs[i].distinct;
+        oc.nullable = (p.aggs[i].nullable || p.global) && p.aggs[i].func != TGPU_AGG_COUNT && !p.aggs[i].distinct;
         if (oc.type == TGPU_DECIMAL128) { oc.decimal_precision = 38; oc.decimal_scale = (uint8_t)p.aggs[i].scale; }
         if (oc.type == TGPU_DECIMAL64) {
             oc.decimal_precision = t.cols[p.aggs[i].col].decimal_precision;
@@ -711,7 +723,7 @@ int run(const Table &t, const tgpu_request *req, int threads, Result &res) {
         }
         for (size_t i = 0; i < p.aggs.size(); ++i) {
             size_t c = p.parts.size() + i;
-            Value v = agg_value(g, p.aggs[i]);
+            Value v = agg_value(g, p.aggs[i], p.global);
             int ty = p.aggs[i].out_type;
             if (v.null) {
                 std::vector<uint8_t> z(elem_bytes(ty), 0);

@@ -110,6 +110,7 @@ WRAP_FILLER_ROWS = 70_000
 WRAP_G1 = 8553255926290448384
 WRAP_G2 = -8446744073709551616
 WRAP_G3 = 3
+WRAP_TOTAL = 106_511_852_580_896_771  # aggregate_test.zig:1302: every non-NULL v, wrapped to BIGINT
 
 
 def bigint_wrap() -> Case:
@@ -128,7 +129,10 @@ def bigint_wrap() -> Case:
     c = Case("bigint_wrap", cols, 4096)
     assert wrap64(3 * 9_000_000_000_000_000_000) == WRAP_G1
     assert wrap64(2 * 5_000_000_000_000_000_000) == WRAP_G2
+    assert wrap64(3 * 9_000_000_000_000_000_000 + 2 * 5_000_000_000_000_000_000 + 1 + 2) == WRAP_TOTAL
     s = [AggSpec("sum", "v", "s")]
+    # SELECT SUM(v) FROM w: the global aggregate (aggregate_test.zig:1392-1398)
+    c.queries.append(Query("global_sum", Request([], s), ordered=True, expected=[[WRAP_TOTAL]]))
     c.queries.append(Query("by_g", Request(["g"], s, [SortSpec("g")]), ordered=True,
                            expected=[[1, WRAP_G1], [2, WRAP_G2], [3, WRAP_G3], [4, 0]]))
     c.queries.append(Query("by_g_top2", Request(["g"], s, [SortSpec("s", True)], limit=2), ordered=True,

@@ -80,3 +80,26 @@ def test_batch_declines_sorted_pages_and_cancels(table_and_cols):
     with pytest.raises(QueryCancelled):
         b.execute()
     b.close()
+
+
+def test_batch_with_global_aggregates(table_and_cols):
+    """Queries without GROUP BY ride in a batch too; one keeps no row and
+    still answers its single row (COUNT 0, the rest NULL)."""
+    from thindb_gb300.engine import Pred
+
+    t, cols = table_and_cols
+    aggs = [AggSpec("count", None, "c"), AggSpec("sum", "amount", "s"), AggSpec("max", "amount", "m")]
+    reqs = [Request([], aggs), Request([], aggs, where=[Pred("k1m", "between", 10, 5000)]),
+            Request([], aggs, where=[Pred("d", ">", 10_000_000)]),
+            Request(["k10"], aggs, [SortSpec("s", True)], limit=3)]
+    b = QueryBatch(t, reqs, graph=True)
+    host = oracle.HostTable(cols)
+    for rep in range(2):
+        b.execute()
+        b.synchronize()
+        for i, r in enumerate(reqs):
+            got = b.collect(i)
+            compare_results(got, oracle.run(host, r), len(r.group_cols), True)
+            if not r.group_cols:
+                assert len(got["c"][0]) == 1
+    b.close()

@@ -426,6 +426,56 @@ def test_distinct_partition_overflow_on_underestimated_where():
     assert st.retries >= 1
 
 
+# -------------------------------------------------------- global aggregate --
+# No GROUP BY (thinDB's v2_global_aggregate.zig): one row, folded in each
+# CTA's shared-memory table under the packed key 1; over no rows the row
+# still comes back with COUNTs 0 and the rest NULL.
+
+GLOBAL_AGGS = [AggSpec("count", None, "c"), AggSpec("sum", "amount", "s"), AggSpec("avg", "amount", "a"),
+               AggSpec("min", "amount", "mn"), AggSpec("max", "d", "md")]
+
+
+@pytest.mark.parametrize("where", [None, FILTER, [Pred("d", ">", 10_000_000)]], ids=["all", "filtered", "empty"])
+def test_global_aggregate(where):
+    cols = filtered_cols(2_000_000, 200_000)
+    got, st = run_both(cols, Request([], GLOBAL_AGGS, where=where), ordered=True)
+    assert len(got["c"][0]) == 1
+    assert st.groups == (0 if where and where[0].op == ">" else 1)
+
+
+def test_global_aggregate_nullable_float_and_distinct():
+    n = 600_000
+    rng = np.random.default_rng(31)
+    v = rng.normal(size=n)
+    ok = rng.random(n) > 0.2
+    u = rng.integers(0, 50_000, n).astype(np.int64)
+    w = rng.integers(-1000, 1000, n).astype(np.int32)
+    cols = [Column("v", abi.DOUBLE, v, validity=ok), Column("u", abi.BIGINT, u), Column("w", abi.INT, w)]
+    aggs = [AggSpec("count", "v", "cv"), AggSpec("sum", "v", "sv"), AggSpec("avg", "v", "av"),
+            AggSpec("min", "w", "mn"), AggSpec("count_distinct", "u", "du"), AggSpec("sum", "w", "sw")]
+    run_both(cols, Request([], aggs), ordered=True)
+    run_both(cols, Request([], aggs, flags=DPART), ordered=True)
+    # every v NULL where the WHERE keeps rows: SUM/AVG NULL, COUNT(v) 0
+    run_both(cols, Request([], aggs, where=[Pred("w", "between", 5, 5)]), ordered=True)
+
+
+def test_global_aggregate_pages():
+    cols = filtered_cols(300_000, 10_000)
+    for kw in ({"limit": 0}, {"offset": 1}, {"limit": 1}, {"limit": 5, "offset": 0}):
+        got, _ = run_both(cols, Request([], GLOBAL_AGGS, **kw), ordered=True)
+        assert len(got["c"][0]) == (0 if kw.get("limit") == 0 or kw.get("offset") else 1)
+    got, _ = run_both(cols, Request([], GLOBAL_AGGS, [SortSpec("s", True)], where=[Pred("d", ">", 10_000_000)]),
+                      ordered=True)
+    assert len(got["c"][0]) == 1
+
+
+def test_global_aggregate_declines_having():
+    cols = filtered_cols(10_000, 100)
+    t = Table(cols)
+    assert try_build_group_topn(t, Request([], GLOBAL_AGGS, having=[HavingSpec("c", ">", 0)])) is None
+    t.close()
+
+
 # -------------------------------------------------------------- queue mode --
 # Dense coalesced loads, survivors compacted into a per-warp shared-memory
 # ring, full-batch folds: opt-in (TGPU_FLAG_QUEUE_SCAN), forced here.

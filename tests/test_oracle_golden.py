@@ -30,3 +30,35 @@ def test_golden_fixture_is_current():
                 assert e["rows"] == len(q.expected)
                 if "digest" in e:
                     assert e["digest"] == rows_digest(q.expected)
+
+
+def test_oracle_global_aggregate_over_no_rows():
+    """No GROUP BY and a WHERE that keeps nothing: still one row, COUNTs 0 and
+    the other aggregates NULL (v2_global_aggregate.zig emitRow :1839-1905)."""
+    import numpy as np
+
+    from thindb_gb300 import abi
+    from thindb_gb300.engine import AggSpec, Column, Pred, Request
+
+    x = np.arange(1000, dtype=np.int32)
+    cols = [Column("x", abi.INT, x), Column("d", abi.DECIMAL64, x.astype(np.int64) * 7, scale=2)]
+    aggs = [AggSpec("count", None, "c"), AggSpec("count", "x", "cx"), AggSpec("sum", "x", "s"),
+            AggSpec("avg", "d", "a"), AggSpec("min", "x", "mn"), AggSpec("max", "x", "mx"),
+            AggSpec("count_distinct", "x", "u")]
+    host = oracle.HostTable(cols, 256)
+    res = oracle.run(host, Request([], aggs, where=[Pred("x", ">", 5000)]))
+    assert res["__groups__"] == 0 and res["__selected__"] == 0
+    for name in ("c", "cx", "u"):
+        vals, ok = res[name]
+        assert list(vals) == [0] and (ok is None or list(ok) == [True])
+    for name in ("s", "a", "mn", "mx"):
+        vals, ok = res[name]
+        assert len(vals) == 1 and list(ok) == [False]
+    # with rows: one group; the DECIMAL AVG divides the sum by count x 10^scale
+    res = oracle.run(host, Request([], aggs, where=[Pred("x", "<", 10)]))
+    assert res["__groups__"] == 1
+    assert res["a"][0][0] == float(sum(range(10)) * 7) / (10 * 100.0)
+    assert res["s"][0][0] == 45 and res["mx"][0][0] == 9 and res["u"][0][0] == 10
+    # OFFSET past the row, or LIMIT 0: nothing
+    assert oracle.run(host, Request([], aggs, limit=0))["c"][0].size == 0
+    assert oracle.run(host, Request([], aggs, offset=1))["c"][0].size == 0

@@ -421,6 +421,8 @@ struct tgpu_query {
     // state
     bool executed = false, synced = false;
     uint64_t returned = 0, result_rows = 0;
+    bool global_agg = false;   // no GROUP BY: exactly one row before OFFSET/LIMIT
+    bool synth_empty = false;  // that row, with no rows passing, is written on the host
     uint32_t retries = 0;
     uint32_t launches = 0;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
@@ -556,8 +558,11 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
     std::memset(&df, 0, sizeof(df));
     std::vector<int> map(t->cols.size(), -1);
 
-    if (req->n_group_cols == 0 || req->n_group_cols > (uint32_t)MAX_GROUP_KEYS)
-        return fail(TGPU_DECLINE, "group key count");
+    // no GROUP BY: thinDB's global aggregate (v2_global_aggregate.zig), one
+    // row; it declines HAVING (:1191)
+    if (req->n_group_cols > (uint32_t)MAX_GROUP_KEYS) return fail(TGPU_DECLINE, "group key count");
+    q->global_agg = req->n_group_cols == 0;
+    if (q->global_agg && req->n_having) return fail(TGPU_DECLINE, "HAVING on a global aggregate");
     if (req->n_aggs == 0 || req->n_aggs > (uint32_t)MAX_AGGS) return fail(TGPU_DECLINE, "aggregate count");
     if (req->n_where > (uint32_t)MAX_PREDS) return fail(TGPU_DECLINE, "too many WHERE conjuncts");
     if (req->n_order > (uint32_t)MAX_ORDER) return fail(TGPU_DECLINE, "too many ORDER BY keys");
@@ -640,6 +645,10 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
     }
     if (off > 128) return fail(TGPU_DECLINE, "packed key wider than 128 bits (hashed keys)");
     dq.key_words = off > 64 ? 2 : 1;
+    // a global aggregate's one group takes the packed key 1, not the empty
+    // marker 0, so it lives in each CTA's shared-memory table
+    dq.key_or = q->global_agg ? 1 : 0;
+    df.global_avg = q->global_agg ? 1 : 0;
 
     // aggregates and state words (word 0 = the group's row count).  `next`
     // counts slots exactly as thinDB does (its 16-slot limit decides
@@ -750,7 +759,10 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
         tgpu_output_column oc{};
         std::snprintf(oc.name, sizeof(oc.name), "%s", a.as ? a.as : "");
         oc.type = out_type;
-        oc.nullable = o.nullable;
+        // a global aggregate over no rows still emits its row: SUM, AVG, MIN
+        // and MAX are NULL there (v2_global_aggregate.zig:1853-1855)
+        oc.nullable = o.nullable || (q->global_agg && (a.func == TGPU_AGG_SUM || a.func == TGPU_AGG_AVG ||
+                                                       a.func == TGPU_AGG_MIN || a.func == TGPU_AGG_MAX));
         if (out_type == TGPU_DECIMAL128) {
             oc.decimal_precision = 38;
             oc.decimal_scale = (uint8_t)scale;
@@ -770,7 +782,7 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
     dq.fast_km = 0;
     dq.n_faggs = 0;
     {
-        bool ok = true;
+        bool ok = dq.n_parts > 0;  // the compiled folds read at least one key part
         for (int i = 0; i < dq.n_parts; ++i) ok = ok && !dq.parts[i].nullable;
         for (int a = 0; a < dq.n_aggs && ok; ++a) {
             const DevAgg &g = dq.aggs[a];
@@ -1219,6 +1231,13 @@ tgpu_status enqueue(tgpu_query *q) {
     return TGPU_OK;
 }
 
+// A global aggregate whose WHERE kept no row still answers one row (COUNTs 0,
+// the rest NULL), unless OFFSET or LIMIT 0 drops it.
+void set_empty_global_row(tgpu_query *q, uint64_t groups) {
+    q->synth_empty = q->global_agg && groups == 0 && q->offset == 0 && q->limit != 0;
+    if (q->synth_empty) q->result_rows = 1;
+}
+
 tgpu_status finish(tgpu_query *q) {
     for (;;) {
         CU(cudaStreamSynchronize(q->stream));
@@ -1266,6 +1285,7 @@ tgpu_status finish(tgpu_query *q) {
     }
     q->synced = true;
     q->result_rows = q->h_counts[2];
+    set_empty_global_row(q, q->h_counts[0]);
     tgpu_query_stats &s = q->stats;
     s.rows_scanned = q->rows_scanned;
     s.rows_selected = q->h_counts[4];
@@ -1549,7 +1569,14 @@ tgpu_status tgpu_query_next(tgpu_query *q, tgpu_batch *b, int32_t *done) {
     const uint64_t n = std::min<uint64_t>(b->capacity_rows, q->result_rows - q->returned);
     const size_t nc = q->schema.size();
     std::vector<std::vector<uint8_t>> vbytes(nc);
-    if (q->h_packed) {
+    if (q->synth_empty) {
+        // the global aggregate's row over no input: zero values, COUNTs valid
+        for (size_t c = 0; c < nc; ++c) {
+            if (n && b->values && b->values[c]) std::memset(b->values[c], 0, q->schema[c].elem_bytes);
+            const int func = q->df.outs[c].func;
+            vbytes[c].assign(n, (func == TGPU_AGG_COUNT || func == TGPU_AGG_COUNT_DISTINCT) ? 1 : 0);
+        }
+    } else if (q->h_packed) {
         // rows a batch already packed into host memory
         size_t off = 8;
         for (size_t c = 0; c < nc; ++c) {
@@ -1970,6 +1997,7 @@ tgpu_status tgpu_batch_synchronize(tgpu_query_batch *b) {
         q->synced = true;
         q->returned = 0;
         q->result_rows = c[2];
+        set_empty_global_row(q, c[0]);
         q->pack_rows = b->stage_rows[i];
         q->h_packed = q->pack_rows ? b->h_stage + b->stage_off[i] : nullptr;
         q->stats.rows_scanned = q->rows_scanned;

@@ -126,6 +126,7 @@ struct DevQuery {
     DevKeyPart parts[MAX_GROUP_KEYS];
     int32_t n_parts;
     int32_t key_words;        // 1 or 2
+    uint64_t key_or;          // OR'ed into every packed key: 1 for a global aggregate (its one group), else 0
     DevAgg aggs[MAX_AGGS];
     int32_t n_aggs;
     // compiled fast fold: key mode (0 = none, 1 = one NOT NULL part, 2 = several
@@ -210,7 +211,7 @@ struct DevFinal {
     int32_t n_order;
     int32_t n_having;
     int32_t sort_words;       // words of one encoded sort key
-    int32_t pad;
+    int32_t global_avg;       // a global aggregate's AVG: sum / (n * 10^scale), else sum / n / 10^scale
     DevKeyPart parts[MAX_GROUP_KEYS];
     int32_t part_types[MAX_GROUP_KEYS];
     DevOut outs[MAX_AGGS];

@@ -87,7 +87,11 @@ __device__ EmitVal emit_agg(const DevFinal &f, const unsigned long long *st, int
                 int64_t hi = (int64_t)lo < 0 ? -1 : 0;
                 if (o.kind == AK_SUM_I128) i128_of_split(st[o.word], st[o.word + 1], lo, hi);
                 else if (o.kind == AK_SUM_I128C) hi = (int64_t)st[o.word + 1];
-                v.f = i128_to_f64(lo, hi) / (double)den / POW10[o.scale];
+                // avgValue (v2_shape_group_topn.zig:1438-1446) divides by the
+                // count, then by 10^scale; the global aggregate's emitRow
+                // (v2_global_aggregate.zig:1872-1877) by count x 10^scale
+                v.f = f.global_avg ? i128_to_f64(lo, hi) / ((double)den * POW10[o.scale])
+                                   : i128_to_f64(lo, hi) / (double)den / POW10[o.scale];
             }
             return v;
         }

@@ -131,7 +131,7 @@ __device__ __forceinline__ bool pred_holds(const DevQuery &q, const DevPred &p, 
 // Packed key: parts LSB-first, a nullable part's slice is payload | valid-bit
 // and all-zero for NULL (v2_shape_group_topn.zig:105-119, :2076-2092).
 __device__ __forceinline__ void pack_key(const DevQuery &q, uint64_t r, uint64_t &k0, uint64_t &k1) {
-    k0 = 0;
+    k0 = q.key_or;
     k1 = 0;
     for (int i = 0; i < q.n_parts; ++i) {
         const DevKeyPart &kp = q.parts[i];
