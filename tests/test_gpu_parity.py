@@ -435,7 +435,7 @@ GLOBAL_AGGS = [AggSpec("count", None, "c"), AggSpec("sum", "amount", "s"), AggSp
                AggSpec("min", "amount", "mn"), AggSpec("max", "d", "md")]
 
 
-@pytest.mark.parametrize("where", [None, FILTER, [Pred("d", ">", 10_000_000)]], ids=["all", "filtered", "empty"])
+@pytest.mark.parametrize("where", [[], FILTER, [Pred("d", ">", 10_000_000)]], ids=["all", "filtered", "empty"])
 def test_global_aggregate(where):
     cols = filtered_cols(2_000_000, 200_000)
     got, st = run_both(cols, Request([], GLOBAL_AGGS, where=where), ordered=True)
@@ -455,7 +455,7 @@ def test_global_aggregate_nullable_float_and_distinct():
             AggSpec("min", "w", "mn"), AggSpec("count_distinct", "u", "du"), AggSpec("sum", "w", "sw")]
     run_both(cols, Request([], aggs), ordered=True)
     run_both(cols, Request([], aggs, flags=DPART), ordered=True)
-    # every v NULL where the WHERE keeps rows: SUM/AVG NULL, COUNT(v) 0
+    # a narrow WHERE (a few hundred rows, some v NULL)
     run_both(cols, Request([], aggs, where=[Pred("w", "between", 5, 5)]), ordered=True)
 
 
