@@ -198,7 +198,10 @@ typedef struct tgpu_sort_spec {
 
 #define TGPU_NO_LIMIT UINT64_MAX
 
-/* Mirror of GroupTopNRequest (v2_shape_group_topn.zig:63-101) in plain C. */
+/* Mirror of GroupTopNRequest (v2_shape_group_topn.zig:63-101) in plain C.
+ * n_group_cols = 0 is the global aggregate (v2_global_aggregate.zig Request,
+ * :51-65): exactly one row (COUNTs 0 and other aggregates NULL when no row
+ * passes), HAVING declined. */
 typedef struct tgpu_request {
     const int32_t *group_cols;   uint32_t n_group_cols;
     const tgpu_agg_spec *aggs;   uint32_t n_aggs;
