@@ -111,10 +111,10 @@ def _rank(rank, world, port, out):
     dist.destroy_process_group()
 
 
-def test_two_rank_sharded_aggregation_matches_one_node():
+@pytest.mark.parametrize("world", [2, 3])
+def test_sharded_aggregation_matches_one_node(world):
     import oracle
 
-    world = 2
     with mp.Manager() as m:
         out = m.dict()
         mp.spawn(_rank, args=(world, _free_port(), out), nprocs=world, join=True)
