@@ -412,8 +412,37 @@ def group_by_limit() -> Case:
     return c
 
 
+# ------------------------------------------------- global (no GROUP BY) --
+
+def global_stats() -> Case:
+    """count_star_stats_test.zig: the scan path of two global aggregates
+    (:87-130 COUNT/MIN/MAX, :166-204 SUM/AVG/COUNT over a nullable INT and a
+    DOUBLE); the rows its DELETEs remove are left out by a WHERE here."""
+    ids = np.arange(600, dtype=np.int64)
+    v_ok = ids % 3 != 0
+    cols = [Column("id", abi.BIGINT, ids), Column("k", abi.BIGINT, 1000 - ids),
+            Column("k2", abi.BIGINT, 2 * ids), Column("v", abi.INT, ids.astype(np.int32), validity=v_ok),
+            Column("f", abi.DOUBLE, ids + 0.5)]
+    c = Case("global_stats", cols, 65536)
+    cmm = [AggSpec("count", None, "c"), AggSpec("min", "k", "mn"), AggSpec("max", "id", "mx")]
+    # the first test's table holds ids 0..499
+    c.queries.append(Query("count_min_max", Request([], cmm, where=[Pred("id", "between", 0, 499)]), ordered=True,
+                           expected=[[500, 501, 499]]))
+    # after DELETE ... WHERE id >= 499
+    c.queries.append(Query("count_min_max_deleted", Request([], cmm, where=[Pred("id", "between", 0, 498)]),
+                           ordered=True, expected=[[499, 502, 498]]))
+    sac = [AggSpec("sum", "k2", "sk"), AggSpec("avg", "v", "av"), AggSpec("count", "v", "cv"), AggSpec("sum", "f", "sf")]
+    # sum 2*id = 359400; v non-NULL on 400 rows summing 120000; sum (id + 0.5) = 180000
+    c.queries.append(Query("sum_avg_count", Request([], sac, where=[Pred("id", ">=", 0)]), ordered=True,
+                           expected=[[359400, 300.0, 400, 180000.0]]))
+    # after DELETE ... WHERE id < 9
+    c.queries.append(Query("sum_avg_count_deleted", Request([], sac, where=[Pred("id", ">=", 9)]), ordered=True,
+                           expected=[[359400 - 72, (120000.0 - 27.0) / 394.0, 394, 180000.0 - 40.5]]))
+    return c
+
+
 ALL_CASES = [decimal_sum_avg, decimal_grouped, bigint_wrap, nullable_aggs, filtered_compound, wide_keys,
-             distinct_double, between, group_by_limit]
+             distinct_double, between, group_by_limit, global_stats]
 
 
 def build_case(fn) -> Case:
