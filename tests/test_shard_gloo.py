@@ -54,6 +54,9 @@ def _requests():
                 having=[HavingSpec("c", ">", 40_000)]),
         Request(["g"], [AggSpec("avg", "v", "av"), AggSpec("count", "v", "cv"), AggSpec("count_distinct", "u", "du")],
                 [SortSpec("du", True), SortSpec("g")]),
+        # a page without ORDER BY is taken in packed-key order: negative g and
+        # the nullable u's validity bit decide it
+        Request(["g", "u"], [AggSpec("count", None, "c")], limit=40, offset=3),
     ]
 
 
