@@ -412,6 +412,54 @@ def group_by_limit() -> Case:
     return c
 
 
+# --------------------------------------------- exact grouped COUNT(DISTINCT) --
+
+def combined_distinct() -> Case:
+    """aggregate_test.zig:887-940 (per-group distinct counts; a value shared
+    by two groups counts in both; NULLs never count; top-2 by the count) and
+    :942-990 (COUNT, SUM and COUNT(DISTINCT) side by side).  The reference
+    cuts 2-row row groups, which only changes its tiling."""
+    rows = [(1, 1, 100), (2, 1, 100), (3, 1, 200), (4, 1, None), (5, 2, 100), (6, 2, 300), (7, 2, 300),
+            (8, 3, None), (9, 3, None), (10, 4, 500)]
+    cols = [Column("id", abi.BIGINT, np.array([r[0] for r in rows], np.int64)),
+            Column("r", abi.INT, np.array([r[1] for r in rows], np.int32)),
+            Column("u", abi.BIGINT, np.array([r[2] or 0 for r in rows], np.int64),
+                   validity=np.array([r[2] is not None for r in rows], bool))]
+    c = Case("combined_distinct", cols, 65536)
+    cd = [AggSpec("count_distinct", "u", "u")]
+    c.queries.append(Query("per_group", Request(["r"], cd), expected=[[1, 2], [2, 2], [3, 0], [4, 1]]))
+    # ORDER BY u DESC LIMIT 2: the two count-2 groups, tie broken by the packed key
+    c.queries.append(Query("top2", Request(["r"], cd, [SortSpec("u", True)], limit=2), ordered=True,
+                           expected=[[1, 2], [2, 2]]))
+    return c
+
+
+def distinct_beside_aggs() -> Case:
+    """aggregate_test.zig:942-990 (Q09 shape)."""
+    cols = [Column("id", abi.BIGINT, np.array([1, 2, 3, 4], np.int64)),
+            Column("r", abi.INT, np.array([1, 1, 1, 2], np.int32)),
+            Column("u", abi.BIGINT, np.array([7, 7, 9, 5], np.int64), validity=np.ones(4, bool))]
+    c = Case("distinct_beside_aggs", cols, 65536)
+    aggs = [AggSpec("count", None, "c"), AggSpec("sum", "u", "s"), AggSpec("count_distinct", "u", "nd")]
+    c.queries.append(Query("q09", Request(["r"], aggs), expected=[[1, 3, 23, 2], [2, 1, 5, 1]]))
+    return c
+
+
+def distinct_string_group() -> Case:
+    """aggregate_test.zig:1003-1040: string groups (here packed dictionary
+    ids: alpha 0, beta 1, gamma 2) over an int distinct; NULLs excluded."""
+    codes = [0, 0, 0, 1, 1, 2]
+    u = [1, 1, 2, 1, None, None]
+    cols = [Column("id", abi.BIGINT, np.arange(1, 7, dtype=np.int64)),
+            Column("s", abi.DICT32, np.array(codes, np.int32)),
+            Column("u", abi.BIGINT, np.array([x or 0 for x in u], np.int64),
+                   validity=np.array([x is not None for x in u], bool))]
+    c = Case("distinct_string_group", cols, 65536)
+    c.queries.append(Query("by_string", Request(["s"], [AggSpec("count_distinct", "u", "u")]),
+                           expected=[[0, 2], [1, 1], [2, 0]]))
+    return c
+
+
 # ------------------------------------------------- global (no GROUP BY) --
 
 def global_stats() -> Case:
@@ -442,7 +490,8 @@ def global_stats() -> Case:
 
 
 ALL_CASES = [decimal_sum_avg, decimal_grouped, bigint_wrap, nullable_aggs, filtered_compound, wide_keys,
-             distinct_double, between, group_by_limit, global_stats]
+             distinct_double, between, group_by_limit, global_stats, combined_distinct, distinct_beside_aggs,
+             distinct_string_group]
 
 
 def build_case(fn) -> Case:
