@@ -501,6 +501,18 @@ tgpu_status tgpu_tuning_set(const tgpu_tuning *entries, uint32_t n);
 /* Copy up to `cap` entries out; returns the table size. */
 uint32_t tgpu_tuning_get(tgpu_tuning *entries, uint32_t cap);
 
+/* ------------------------------------------------------ failure testing -- */
+
+/* No counterpart in thinDB (its executor has no device waits).  The staged
+ * scan and the COUNT(DISTINCT) partition kernel wait on bulk asynchronous
+ * copies with a bounded wait (default about 2 s of SM clock); a wait that
+ * runs out sets a status bit, the kernel lets its own copies land and
+ * returns, and the query reports TGPU_ERR_DEVICE_TIMEOUT.  This sets that
+ * bound in SM clocks for queries executed from now on (0 = the default), so
+ * a test can make the waits run out and check that the status comes back
+ * and that the next query on the same context is correct.  Process-wide. */
+tgpu_status tgpu_debug_set_wait_limit(uint64_t sm_cycles);
+
 /* ------------------------------------------------- allocation-free call -- */
 
 /* No counterpart in thinDB.  For callers that cannot let the library
@@ -517,10 +529,15 @@ uint32_t tgpu_tuning_get(tgpu_tuning *entries, uint32_t cap);
  * buffers of TGPU_NOALLOC_MAX_GROUPS values each; *out_groups (device memory)
  * receives the number of groups.  SUM is BIGINT and wraps, as thinDB's.
  * More than TGPU_NOALLOC_MAX_GROUPS distinct keys returns
- * TGPU_ERR_INVALID_ARGUMENT.  The first call on a device looks up the
- * array's device address and zeroes it: make that first call before any
- * stream capture.  The call is synchronous (it reads back a status word).
- * All calls share the array: calls that overlap on the GPU race. */
+ * TGPU_ERR_INVALID_ARGUMENT; a group-table probe that runs past its limit
+ * with fewer groups (clustered key hashes) returns TGPU_ERR_INTERNAL.  When
+ * the call returns an error, *out_groups and the output buffers are
+ * undefined.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress): make that first call before any stream
+ * capture.  Every call clears the parts of the array it reads on `stream`
+ * (any stream, blocking or not); the call is synchronous (it reads back a
+ * status word).  All calls share the array: calls that overlap on the GPU
+ * race. */
 #define TGPU_NOALLOC_MAX_GROUPS 65536
 tgpu_status tgpu_group_by_i64_noalloc(const int64_t *keys, const int64_t *values, uint64_t n_rows,
                                       int64_t *out_keys, int64_t *out_count, int64_t *out_sum,

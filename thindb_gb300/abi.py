@@ -216,4 +216,5 @@ SIGNATURES += [
     ("tgpu_request_shape", C.c_int, [C.c_void_p, C.POINTER(Request), C.c_int32, C.POINTER(Shape)]),
     ("tgpu_tuning_set", C.c_int, [C.POINTER(Tuning), C.c_uint32]),
     ("tgpu_tuning_get", C.c_uint32, [C.POINTER(Tuning), C.c_uint32]),
+    ("tgpu_debug_set_wait_limit", C.c_int, [C.c_uint64]),
 ]

@@ -41,6 +41,11 @@ tgpu_status fail(tgpu_status s, const std::string &msg) {
 void tgpu::set_error(const char *msg) { g_err = msg ? msg : ""; }
 
 namespace {
+std::atomic<long long> g_wait_limit{0};
+}
+long long tgpu::device_wait_limit() { return g_wait_limit.load(std::memory_order_relaxed); }
+
+namespace {
 
 #define CU(call)                                                                                 \
     do {                                                                                         \
@@ -1172,6 +1177,7 @@ tgpu_status enqueue(tgpu_query *q) {
     q->table_buf.dirty = true;  // until the clear kernel has run
     q->occ_buf.dirty = true;
 
+    dq.wait_cycles = device_wait_limit();
     CU(cudaMemsetAsync(q->d_ctrl, 0, 16, s));
     CU(cudaMemsetAsync(q->d_counts, 0, 8 * 8, s));
     const bool timing = (q->flags & TGPU_FLAG_TIMING) != 0;
@@ -1249,11 +1255,18 @@ tgpu_status finish(tgpu_query *q) {
             q->result_rows = 0;
             return fail(TGPU_ERR_CANCELLED, "query cancelled");
         }
-        if (status & (ST_WAIT_TIMEOUT | ST_BAD_INDEX)) {
+        if (status & ST_WAIT_TIMEOUT) {
+            // a bounded device wait on a bulk copy gave up; the kernel drained
+            // its copies and returned, so the context and the query stay usable
             q->synced = true;
             q->result_rows = 0;
-            return fail(TGPU_ERR_INTERNAL, status & ST_WAIT_TIMEOUT ? "a staged column copy never completed"
-                                                                     : "a device bounds check failed");
+            return fail(TGPU_ERR_DEVICE_TIMEOUT, "a bulk column or pair copy did not complete within the "
+                                                 "device wait limit");
+        }
+        if (status & ST_BAD_INDEX) {
+            q->synced = true;
+            q->result_rows = 0;
+            return fail(TGPU_ERR_INTERNAL, "a device bounds check failed");
         }
         if (status & (ST_TABLE_FULL | ST_DISTINCT_FULL)) {
             if (++q->retries > 4) return fail(TGPU_ERR_INTERNAL, "group table kept overflowing");
@@ -1371,6 +1384,12 @@ tgpu_status query_create(tgpu_table *table, const tgpu_request *req, int batched
 extern "C" {
 
 uint32_t tgpu_abi_version(void) { return TGPU_ABI_VERSION; }
+
+tgpu_status tgpu_debug_set_wait_limit(uint64_t sm_cycles) {
+    if (sm_cycles > (uint64_t)1 << 40) return fail(TGPU_ERR_INVALID_ARGUMENT, "wait limit above 2^40 SM clocks");
+    g_wait_limit.store((long long)sm_cycles, std::memory_order_relaxed);
+    return TGPU_OK;
+}
 
 const char *tgpu_build_info(void) {
     static char buf[128];
@@ -1646,7 +1665,9 @@ struct tgpu_query_batch {
     std::vector<DevQuery> h_qs;
     std::vector<DevFinal> h_fs;
     std::vector<DevFinalBufs> h_bs;
-    std::vector<uint2> items;               // {query, first chunk of a row group}, row group major
+    std::vector<uint2> items;               // {query, first chunk of a row group}, by fold class, row group major
+    uint32_t class_off[BATCH_CLASSES + 1] = {0};  // items of fold class c: [class_off[c], class_off[c + 1])
+    int class_grid[BATCH_CLASSES] = {0};
     Buffer dev_buf;                         // one pooled allocation for every array below
     void *dev = nullptr;
     DevQuery *d_qs = nullptr;
@@ -1788,16 +1809,22 @@ tgpu_status batch_descriptors(tgpu_query_batch *b) {
         b->any_topk |= fb.rank == 1;
     }
     if (!b->d_items) {
-        // row group major: every query that keeps row group g, then g + 1, ...
+        // per fold class, row group major: every query of the class that
+        // keeps row group g, then g + 1, ...
         std::vector<size_t> pos(Q, 0);
-        for (uint32_t g = 0; g < b->t->n_rg; ++g)
-            for (uint32_t i = 0; i < Q; ++i) {
-                const std::vector<uint32_t> &rl = b->qs[i]->rg_list;
-                if (pos[i] < rl.size() && rl[pos[i]] == g) {
-                    b->items.push_back(make_uint2(i, (uint32_t)(pos[i] * b->h_qs[i].chunks_per_rg)));
-                    ++pos[i];
+        for (int cls = 0; cls < BATCH_CLASSES; ++cls) {
+            b->class_off[cls] = (uint32_t)b->items.size();
+            for (uint32_t g = 0; g < b->t->n_rg; ++g)
+                for (uint32_t i = 0; i < Q; ++i) {
+                    if (batch_fold_class(b->h_qs[i]) != cls) continue;
+                    const std::vector<uint32_t> &rl = b->qs[i]->rg_list;
+                    if (pos[i] < rl.size() && rl[pos[i]] == g) {
+                        b->items.push_back(make_uint2(i, (uint32_t)(pos[i] * b->h_qs[i].chunks_per_rg)));
+                        ++pos[i];
+                    }
                 }
-            }
+        }
+        b->class_off[BATCH_CLASSES] = (uint32_t)b->items.size();
         tgpu_status ist = g_scratch_pool.take(sizeof(uint2) * std::max<size_t>(1, b->items.size()), b->stream,
                                               &b->items_buf);
         if (ist != TGPU_OK) return ist;
@@ -1813,7 +1840,9 @@ tgpu_status batch_descriptors(tgpu_query_batch *b) {
     DeviceCtx *dev;
     tgpu_status st = device_ctx(&dev);
     if (st != TGPU_OK) return st;
-    b->grid = batch_scan_grid(b->max_aggs, b->smem, dev->sms);
+    for (int cls = 0; cls < BATCH_CLASSES; ++cls)
+        b->class_grid[cls] =
+            b->class_off[cls + 1] > b->class_off[cls] ? batch_scan_grid(cls, b->smem, dev->sms) : 0;
     b->descriptors_dirty = false;
     b->stats.work_items = b->items.size();
     return TGPU_OK;
@@ -1827,15 +1856,21 @@ tgpu_status batch_enqueue_work(tgpu_query_batch *b, bool capturing) {
     CU(cudaMemsetAsync(b->d_ctrl, 0, 8, s));
     CU(cudaMemsetAsync(b->d_counts, 0, 64 * (size_t)Q, s));
     CU(cudaMemsetAsync(b->d_qctrl, 0, 16 * (size_t)Q, s));
-    CU(launch_batch_scan(b->d_qs, b->d_items, (uint32_t)b->items.size(), b->max_aggs, b->smem, b->grid,
-                         (const volatile int *)b->d_cancel, b->d_ctrl + 1, s));
+    uint32_t scans = 0;
+    for (int cls = 0; cls < BATCH_CLASSES; ++cls) {
+        const uint32_t n = b->class_off[cls + 1] - b->class_off[cls];
+        if (!n) continue;
+        CU(launch_batch_scan(cls, b->d_qs, b->d_items + b->class_off[cls], n, b->smem, b->class_grid[cls],
+                             (const volatile int *)b->d_cancel, b->d_ctrl + 1, s));
+        ++scans;
+    }
     CU(launch_finalize_batch(b->d_fs, b->d_bs, Q, b->max_cpt_blocks, b->max_cand_blocks, b->topk_widths,
                              b->max_rows, b->max_words, s));
     CU(cudaMemcpyAsync(b->h_counts, b->d_counts, 64 * (size_t)Q, cudaMemcpyDeviceToHost, s));
     CU(cudaMemcpyAsync(b->h_counts + 8 * (size_t)Q, b->d_qctrl, 16 * (size_t)Q, cudaMemcpyDeviceToHost, s));
     CU(cudaMemcpyAsync(b->h_counts + 10 * (size_t)Q, b->d_ctrl, 8, cudaMemcpyDeviceToHost, s));
     if (!capturing) CU(cudaEventRecord(b->ev[1], s));
-    b->stats.kernel_launches = 1 + 5 + std::max(1, 2 * __builtin_popcount(b->topk_widths));
+    b->stats.kernel_launches = scans + 5 + std::max(1, 2 * __builtin_popcount(b->topk_widths));
     return TGPU_OK;
 }
 

@@ -41,15 +41,19 @@ __device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
     return done != 0;
 }
 
-// Bounded wait for phase `parity` of `bar` to complete.
-__device__ __noinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// Bounded wait for phase `parity` of `bar` to complete: false after `limit`
+// SM clocks (0 = WAIT_CYCLES).  A short limit (the test hook
+// tgpu_debug_set_wait_limit) checks the clock on every test.
+__device__ __noinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long long limit = 0) {
     if (mbar_test(bar, parity)) return true;
+    if (limit <= 0) limit = WAIT_CYCLES;
+    const uint32_t every = limit < (1LL << 20) ? 0u : 63u;
     const long long t0 = clock64();
     for (uint32_t i = 1;; ++i) {
         if (mbar_test(bar, parity)) return true;
-        if ((i & 63) == 0) {
-            if (clock64() - t0 > WAIT_CYCLES) return false;
-            __nanosleep(32);
+        if ((i & every) == 0) {
+            if (clock64() - t0 > limit) return false;
+            if (every) __nanosleep(32);
         }
     }
 }

@@ -52,7 +52,8 @@ __device__ __forceinline__ void dp_issue(const ulonglong2 *buf, const uint32_t *
 __global__ void __launch_bounds__(DP_THREADS, 1)
     distinct_partition_kernel(const ulonglong2 *__restrict__ buf, const uint32_t *__restrict__ cursor, uint32_t cap,
                               uint32_t n_parts, uint32_t S, unsigned long long *table, uint64_t max_gid,
-                              int32_t slot_words, int32_t key_words, int32_t word, unsigned int *status) {
+                              int32_t slot_words, int32_t key_words, int32_t word, unsigned int *status,
+                              long long wait_cycles) {
     extern __shared__ __align__(16) unsigned char smem[];
     DpHeader &h = *(DpHeader *)smem;
     ulonglong2 *ring = (ulonglong2 *)(smem + DP_HEADER);
@@ -75,7 +76,7 @@ __global__ void __launch_bounds__(DP_THREADS, 1)
     for (; i < my_n; ++i) {
         const uint32_t s = i % S;
         for (uint32_t j = threadIdx.x; j < DPART_SLOTS; j += DP_THREADS) slots[j] = DP_EMPTY;
-        if (!mbar_wait(&h.bars[s], (i / S) & 1u)) {
+        if (!mbar_wait(&h.bars[s], (i / S) & 1u, wait_cycles)) {
             atomicOr(status, ST_WAIT_TIMEOUT);
             h.stop = 1;
         }
@@ -121,7 +122,8 @@ __global__ void __launch_bounds__(DP_THREADS, 1)
         }
     }
     if (h.stop && threadIdx.x == 0) {
-        // leave no copy in flight into this CTA's shared memory (bounded)
+        // leave no copy in flight into this CTA's shared memory (bounded by
+        // the built-in limit: the copies are real and land)
         for (uint32_t j = i; j < issued; ++j) (void)mbar_wait(&h.bars[j % S], (j / S) & 1u);
     }
 }
@@ -165,7 +167,7 @@ cudaError_t launch_distinct_partitions(const DevQuery &q, int word, cudaStream_t
     const uint32_t grid = std::min<uint32_t>(n_parts, (uint32_t)d.sms);
     distinct_partition_kernel<<<grid, DP_THREADS, smem, s>>>(q.dpart_buf, q.dpart_cursor, q.dpart_cap, n_parts,
                                                               d.stages, q.table, q.cap, q.slot_words, q.key_words,
-                                                              word, q.status);
+                                                              word, q.status, q.wait_cycles);
     return cudaGetLastError();
 }
 

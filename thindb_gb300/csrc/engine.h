@@ -166,6 +166,7 @@ struct DevQuery {
     int32_t n_pf;
     int32_t pf_cols[8];
     // control
+    long long wait_cycles;                // bound of the bulk-copy waits in SM clocks, 0 = WAIT_CYCLES
     unsigned int *tile_counter;
     unsigned int *status;
     const volatile int *cancel;           // host-mapped cancel flag (may be nullptr)
@@ -277,6 +278,10 @@ constexpr int DPART_MAX_BITS = 20;      // 2^20 partitions: 64 GB of pairs for 3
 // distinct count (table word `word` of slot gid).
 cudaError_t launch_distinct_partitions(const DevQuery &q, int word, cudaStream_t s);
 
+// Bound of the device's bulk-copy waits for queries planned from now on, in
+// SM clocks (0 = the built-in ~2 s); set by tgpu_debug_set_wait_limit.
+long long device_wait_limit();
+
 // Message returned by tgpu_last_error_message() on this thread (api.cpp).
 void set_error(const char *msg);
 
@@ -287,10 +292,16 @@ int scan_grid_size(const DevQuery &q, int device_sms);
 int fast_fold_id(const DevQuery &q);
 size_t scan_smem_bytes(const DevQuery &q);
 cudaError_t launch_scan(const DevQuery &q, int grid, cudaStream_t s);
-// many queries, one persistent kernel over (query, row group) work items
-int batch_scan_grid(int max_aggs, size_t smem, int sms);
-// items[i] = {query, first chunk of one of its row groups}
-cudaError_t launch_batch_scan(const DevQuery *qs, const uint2 *items, uint32_t n_items, int max_aggs, size_t smem,
+// many queries, one persistent kernel per fold class over (query, row group)
+// work items: class = the compiled fold's id, or the interpreter for up to 4
+// or up to 16 aggregates
+constexpr int BATCH_GENERIC4 = 12;
+constexpr int BATCH_GENERIC16 = 13;
+constexpr int BATCH_CLASSES = 14;
+int batch_fold_class(const DevQuery &q);
+int batch_scan_grid(int cls, size_t smem, int sms);
+// items[i] = {query, first chunk of one of its row groups}, every query of class cls
+cudaError_t launch_batch_scan(int cls, const DevQuery *qs, const uint2 *items, uint32_t n_items, size_t smem,
                               int grid, const volatile int *cancel, unsigned int *status, cudaStream_t s);
 // compaction, top-k / all-groups selection, gather and clear for every query of a batch
 // single-query top-k straight from the occupancy bitmap (counts[0] groups,

@@ -108,17 +108,18 @@ tgpu_status tgpu_group_by_i64_noalloc(const int64_t *keys, const int64_t *values
     }
     unsigned long long *base;
     {
-        // first call on this device: look up the scratch's device address
-        // and zero it once (later calls leave it ready for the next)
+        // first call on this device: look up the scratch's device address.
+        // Nothing is zeroed here: every call clears the table, bitmap and
+        // counters it reads on its own stream below, and the rest of the
+        // array is written before it is read.
         std::lock_guard<std::mutex> lk(g_na_mu);
         if (!g_na_addr[dev]) {
             unsigned long long *p = nullptr;
-            if (cudaGetSymbolAddress((void **)&p, g_noalloc_scratch) != cudaSuccess || !p) {
+            const cudaError_t e = cudaGetSymbolAddress((void **)&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p) {
                 cudaGetLastError();
-                return TGPU_ERR_CUDA;
-            }
-            if (cudaMemset(p, 0, sizeof(g_noalloc_scratch)) != cudaSuccess) {
-                cudaGetLastError();
+                set_error(e != cudaSuccess ? cudaGetErrorString(e)
+                                           : "tgpu_group_by_i64_noalloc: the scratch array has no device address");
                 return TGPU_ERR_CUDA;
             }
             g_na_addr[dev] = p;
@@ -217,10 +218,21 @@ tgpu_status tgpu_group_by_i64_noalloc(const int64_t *keys, const int64_t *values
     NA_TRY(cudaMemcpyAsync(&status, L.ctrl + 1, 4, cudaMemcpyDeviceToHost, s));
     NA_TRY(cudaStreamSynchronize(s));
 #undef NA_TRY
-    if ((status & ST_TABLE_FULL) || groups > NA_MAX_GROUPS) {
+    if (groups > NA_MAX_GROUPS) {
         set_error("tgpu_group_by_i64_noalloc: more than 65,536 distinct keys; its fixed scratch holds at most "
                   "65,536 groups (use tgpu_query_create for larger results)");
         return TGPU_ERR_INVALID_ARGUMENT;
+    }
+    if (status & ST_TABLE_FULL) {
+        // at most 65,536 groups, yet a bounded probe ran past its limit
+        // (keys whose hashes cluster): not a size the caller chose
+        set_error("tgpu_group_by_i64_noalloc: a group-table probe ran past its limit (clustered key hashes); "
+                  "use tgpu_query_create, which regrows its table");
+        return TGPU_ERR_INTERNAL;
+    }
+    if (status) {
+        set_error("tgpu_group_by_i64_noalloc: a device bounds check failed");
+        return TGPU_ERR_INTERNAL;
     }
     return TGPU_OK;
 }

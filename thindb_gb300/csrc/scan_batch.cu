@@ -1,22 +1,23 @@
-// scan_batch.cu — the batched persistent scan kernel (many queries, one
-// launch) and its launchers.
+// scan_batch.cu — the batched persistent scan kernels (many queries, one
+// launch per fold class) and their launchers.
 #include "scan_impl.cuh"
 
 namespace tgpu {
 
 namespace {
 
-// Many queries in one persistent kernel.  A work item is (query, one row
-// group of that query's surviving row groups); the host lists the items row
-// group by row group, every query of a row group in turn, so the CTAs running
-// at any moment read the same few row groups and all but the first query of
-// each row group finds its columns in L2 (the table streams from HBM about
-// once per batch, not once per query).  CTA b takes items b, b + grid, ...;
-// its 16 warps split the item's chunks, and the CTA's shared-memory table
-// belongs to the item's query (flushed when the next item moves to another
-// query).
-template <int NA>
-__global__ void __launch_bounds__(SCAN_THREADS, NA <= 4 ? 2 : 1)
+// Many queries of one fold class in one persistent kernel.  A work item is
+// (query, one row group of that query's surviving row groups); the host
+// lists a class's items row group by row group, every query of a row group
+// in turn, so the CTAs running at any moment read the same few row groups
+// and all but the first query of each row group finds its columns in L2.
+// CTA b takes items b, b + grid, ...; its 16 warps split the item's chunks,
+// and the CTA's shared-memory table belongs to the item's query (flushed
+// when the next item moves to another query).  One kernel per fold class
+// (rather than one kernel switching between every compiled fold) keeps each
+// kernel's code as small as a single-query scan's.
+template <class P, int MINB>
+__global__ void __launch_bounds__(SCAN_THREADS, MINB)
     batch_scan_kernel(const DevQuery *__restrict__ qs, const uint2 *__restrict__ items, uint32_t n_items,
                       const volatile int *cancel, unsigned int *batch_status) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -53,7 +54,19 @@ __global__ void __launch_bounds__(SCAN_THREADS, NA <= 4 ? 2 : 1)
         if (qn < 0) break;  // a CTA that got no item at all (cur == qn == -1)
         const DevQuery &q = qs[qn];
         const uint32_t end = min(it.y + q.chunks_per_rg, q.n_chunks);
-        for (uint32_t c = it.y + warp; c < end; c += SCAN_WARPS) scan_chunk_dispatch<NA>(q, sm, c, selected);
+        for (uint32_t c = it.y + warp; c < end; c += SCAN_WARPS) scan_chunk<P>(q, sm, c, selected);
+    }
+}
+
+// Kernel of fold class `cls` (batch_fold_class).
+const void *batch_kernel(int cls) {
+    switch (cls) {
+#define TGPU_BK(I, KM, A, B, C2, D) \
+    case I: return (const void *)batch_scan_kernel<FastFold<KM, A, B, C2, D>, 2>;
+        TGPU_FAST_FOLDS(TGPU_BK)
+#undef TGPU_BK
+        case BATCH_GENERIC4: return (const void *)batch_scan_kernel<GenericFold<4>, 2>;
+        default: return (const void *)batch_scan_kernel<GenericFold<16>, 1>;
     }
 }
 
@@ -70,25 +83,22 @@ int blocks_per_sm(const void *kernel, size_t smem) {
 
 }  // namespace
 
-int batch_scan_grid(int max_aggs, size_t smem, int sms) {
-    return sms * (max_aggs <= 4 ? blocks_per_sm((const void *)batch_scan_kernel<4>, smem)
-                                : blocks_per_sm((const void *)batch_scan_kernel<16>, smem));
+int batch_fold_class(const DevQuery &q) {
+    if (q.n_aggs > 4) return BATCH_GENERIC16;
+    return q.fast_id >= 0 ? q.fast_id : BATCH_GENERIC4;
 }
 
-cudaError_t launch_batch_scan(const DevQuery *qs, const uint2 *items, uint32_t n_items, int max_aggs, size_t smem,
+int batch_scan_grid(int cls, size_t smem, int sms) { return sms * blocks_per_sm(batch_kernel(cls), smem); }
+
+cudaError_t launch_batch_scan(int cls, const DevQuery *qs, const uint2 *items, uint32_t n_items, size_t smem,
                               int grid, const volatile int *cancel, unsigned int *status, cudaStream_t s) {
     if (n_items == 0) return cudaSuccess;
     if ((uint32_t)grid > n_items) grid = (int)n_items;
-    if (max_aggs <= 4) {
-        cudaError_t e = cudaFuncSetAttribute(batch_scan_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        batch_scan_kernel<4><<<grid, SCAN_THREADS, smem, s>>>(qs, items, n_items, cancel, status);
-    } else {
-        cudaError_t e = cudaFuncSetAttribute(batch_scan_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        batch_scan_kernel<16><<<grid, SCAN_THREADS, smem, s>>>(qs, items, n_items, cancel, status);
-    }
-    return cudaGetLastError();
+    const void *fn = batch_kernel(cls);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    void *args[] = {(void *)&qs, (void *)&items, (void *)&n_items, (void *)&cancel, (void *)&status};
+    return cudaLaunchKernel(fn, dim3(grid), dim3(SCAN_THREADS), args, smem, s);
 }
 
 }  // namespace tgpu

@@ -1182,23 +1182,6 @@ __device__ __forceinline__ void scan_chunk_queue(const DevQuery &q, const ScanSm
     X(10, 2, AK_DISTINCT, AK_SUM_F64, AK_NONE, AK_NONE)                \
     X(11, 2, AK_NONE, AK_NONE, AK_NONE, AK_NONE)
 
-// The same work as scan_chunk<P> for the fold the plan's fast_id names.
-template <int NA>
-__device__ __forceinline__ void scan_chunk_dispatch(const DevQuery &q, const ScanSmem &sm, uint32_t c,
-                                                    unsigned long long &selected) {
-    if constexpr (NA > 4) {
-        scan_chunk<GenericFold<NA>>(q, sm, c, selected);  // wide plans: the interpreter
-    } else {
-        switch (q.fast_id) {
-#define TGPU_CASE(I, KM, A, B, C2, D) \
-    case I: scan_chunk<FastFold<KM, A, B, C2, D>>(q, sm, c, selected); break;
-            TGPU_FAST_FOLDS(TGPU_CASE)
-#undef TGPU_CASE
-            default: scan_chunk<GenericFold<NA>>(q, sm, c, selected); break;
-        }
-    }
-}
-
 }  // namespace
 
 }  // namespace tgpu

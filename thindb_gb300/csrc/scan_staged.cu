@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(STAGE_THREADS, 1)
     for (; i < my_n; ++i) {
         const uint32_t s = i % S;
         unsigned char *stage = ring + (size_t)s * sp.stage_bytes;
-        if (!mbar_wait(&bars[s], (i / S) & 1u)) {
+        if (!mbar_wait(&bars[s], (i / S) & 1u, q.wait_cycles)) {
             atomicOr(q.status, ST_WAIT_TIMEOUT);
             stop = 1;
         }
@@ -246,7 +246,8 @@ __global__ void __launch_bounds__(STAGE_THREADS, 1)
         }
     }
     if (stop) {
-        // leave no copy in flight into this CTA's shared memory (bounded)
+        // leave no copy in flight into this CTA's shared memory (bounded by
+        // the built-in limit, whatever the query's: the copies are real and land)
         if (threadIdx.x == 0)
             for (uint32_t j = i; j < issued; ++j) (void)mbar_wait(&bars[j % S], (j / S) & 1u);
         __syncthreads();

@@ -74,6 +74,12 @@ def load_tuning(path: str = TUNING_PATH) -> int:
     return len(entries)
 
 
+def set_device_wait_limit(sm_cycles: int) -> None:
+    """Bound of the device's bulk-copy waits in SM clocks for queries executed
+    from now on (0 = the built-in ~2 s); a test hook for the timeout path."""
+    _check(lib().tgpu_debug_set_wait_limit(sm_cycles))
+
+
 def clear_tuning() -> None:
     _check(lib().tgpu_tuning_set(None, 0))
 
@@ -97,6 +103,10 @@ class MemoryBudgetExceeded(EngineError):
     pass
 
 
+class DeviceTimeout(EngineError):
+    """A bounded device wait ran out (TGPU_ERR_DEVICE_TIMEOUT)."""
+
+
 class QueryCancelled(EngineError):
     pass
 
@@ -109,6 +119,8 @@ def _check(status: int) -> None:
         raise MemoryBudgetExceeded(status, msg)
     if status == abi.ERR_CANCELLED:
         raise QueryCancelled(status, msg)
+    if status == abi.ERR_DEVICE_TIMEOUT:
+        raise DeviceTimeout(status, msg)
     raise EngineError(status, msg)
 
 
