@@ -161,56 +161,88 @@ def columns_of(inputs, ndv=None):
 
 # ------------------------------------------------------------ CPU legs --
 
-def cpu_sample_rows(workload: str) -> int:
-    return {"filtered": 20_000_000, "plain": 16_777_216, "distinct": 10_000_000}[workload]
+DOP1_SAMPLE_ROWS = 10_000_000  # single-thread figure: a bounded prefix of the workload
 
 
-def run_oracle_sample(workload: str, n_sample: int, threads: int):
-    """The oracle (C++ restatement of thinDB's silo executor) over a bounded
-    sample of the workload; returns (rows/s, seconds)."""
+def oracle_columns(workload: str, inputs):
+    """engine.Column objects over host numpy views of the workload's columns."""
+    cols = columns_of(inputs)
+    for c in cols:
+        c.data = c.data.numpy() if hasattr(c.data, "numpy") else c.data
+    return cols
+
+
+def run_oracle(workload: str, cols, threads: int):
+    """The oracle (C++ restatement of thinDB's silo executor) over `cols`;
+    returns (result, seconds)."""
     import oracle
-    from thindb_gb300.engine import Column
 
-    if workload == "filtered":
-        d = datagen.filtered(n_sample, seed=2)
-        cols = [Column("k", abi.BIGINT, d["k"]), Column("amount", abi.DECIMAL64, d["amount"], scale=2),
-                Column("d", abi.DATE, d["d"])]
-    elif workload == "plain":
-        d = datagen.plain(n_sample, seed=1)
-        cols = [Column("k", abi.BIGINT, d["k"]), Column("v", abi.INT, d["v"])]
-    else:
-        d = datagen.distinct(n_sample, seed=3)
-        cols = [Column("region", abi.SMALLINT, d["region"]), Column("url", abi.DICT32, d["url"]),
-                Column("user_id", abi.BIGINT, d["user_id"]), Column("latency_ms", abi.DOUBLE, d["latency_ms"])]
     t = oracle.HostTable(cols)
     req = make_request(workload)
     t0 = time.perf_counter()
-    oracle.run(t, req, threads=threads)
-    dt = time.perf_counter() - t0
-    return n_sample / dt, dt
+    res = oracle.run(t, req, threads=threads)
+    return res, time.perf_counter() - t0
+
+
+def prefix_columns(cols, n):
+    from thindb_gb300.engine import Column
+
+    return [Column(c.name, c.type, c.data[:n], scale=c.scale) for c in cols]
+
+
+def same_result(got: dict, want: dict, keys: list, ordered: bool, rel_cols=()) -> bool:
+    """Bit-exact equality of two result dicts (DOUBLE sums in rel_cols within
+    1e-12 relative); unordered results are compared sorted by key."""
+    names = [k for k in want if not k.startswith("__")]
+    n = len(want[names[0]][0])
+    if any(len(got[k][0]) != n for k in names):
+        return False
+    og = ow = np.arange(n)
+    if not ordered:
+        og = np.lexsort([np.asarray(got[k][0]) for k in reversed(keys)])
+        ow = np.lexsort([np.asarray(want[k][0]) for k in reversed(keys)])
+    for k in names:
+        g, w = np.asarray(got[k][0])[og], np.asarray(want[k][0])[ow]
+        if k in rel_cols:
+            if n and float((np.abs(g - w) / np.maximum(np.abs(w), 1e-300)).max()) > 1e-12:
+                return False
+        elif not np.array_equal(g, w):
+            return False
+    return True
+
+
+PARITY = {  # group keys, ordered result, DOUBLE-sum columns
+    "filtered": (["k"], True, ()),
+    "plain": (["k"], False, ()),
+    "distinct": (["region", "url"], False, ("lat",)),
+}
 
 
 def reference_arm(args, wl):
+    """thinDB's CPU executor, restated (oracle/, C++; the Zig toolchain is
+    absent), over the same full workload as the GPU arm, all host threads."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    n_sample = cpu_sample_rows(args.workload)
+    inputs = make_inputs(args.workload, wl["rows"], pinned=False)
+    cols = oracle_columns(args.workload, inputs)
     for _ in range(max(0, min(args.warmup, 1))):
-        run_oracle_sample(args.workload, min(n_sample, 2_000_000), threads)
-    vals = []
+        run_oracle(args.workload, prefix_columns(cols, min(wl["rows"], 2_000_000)), threads)
+    secs = []
     for _ in range(args.steps):
-        v, dt = run_oracle_sample(args.workload, n_sample, threads)
-        vals.append(v)
-    value = statistics.median(vals)
+        _, dt = run_oracle(args.workload, cols, threads)
+        secs.append(dt)
+    ms = statistics.median(secs) * 1e3
+    value = wl["rows"] / (ms / 1e3)
     line = {
         "impl": "reference", "metric": "GROUP BY rows/s", "value": value, "unit": "rows/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": wl["rows"] / value * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": wl["dtype"],
         "data": "synthetic (seeded generator)",
         "config": {"workload": wl["name"], "rows": wl["rows"]},
         "cpu_baseline": {"value": value, "unit": "rows/s", "cores": threads, "kind": "port",
-                         "sample": f"first {n_sample:,} rows of the workload per step, all host threads; "
+                         "sample": f"the whole workload ({wl['rows']:,} rows) per step, {threads} host threads; "
                                    "C++ restatement of thinDB's silo executor (Zig toolchain absent)"},
         "e2e": {"value": value, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -240,7 +272,6 @@ def gpu_arm(args, wl):
 
     stream = torch.cuda.Stream()
     table = Table(columns_of(inputs), compute_ndv=True, stream=stream.cuda_stream)
-    ndv = {nm: table.ndv(nm) for nm, _, _, _ in inputs}
     req = make_request(args.workload, flags=abi.FLAG_TIMING, stream=stream.cuda_stream)
     q = try_build_group_topn(table, req)
     assert q is not None
@@ -279,37 +310,66 @@ def gpu_arm(args, wl):
     value = replicas.job_rows_per_s(n, world, ms_per_step)
     q.close()
 
-    # end to end through the C ABI from pinned host buffers
+    # end to end through the C ABI from pinned host buffers: registration
+    # (H2D copies, zone maps, NDV sketches), plan, execute, next (D2H)
     e2e_steps = max(1, min(args.steps, 5))
     d2h = sum(c.elem_bytes for c in out_schema) * st.result_rows
     e2e_times = []
     for i in range(e2e_steps + 1):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        t2 = Table(columns_of(inputs, ndv), compute_ndv=False, stream=stream.cuda_stream)
+        t2 = Table(columns_of(inputs), compute_ndv=True, stream=stream.cuda_stream)
         q2 = try_build_group_topn(t2, make_request(args.workload, stream=stream.cuda_stream))
         r2 = q2.collect()
         q2.close()
         t2.close()
         dt = time.perf_counter() - t0
-        if i > 0:  # the first pass warms the allocator
+        if i > 0:  # the first pass warms the column pool
             e2e_times.append(dt)
     e2e_value = n / statistics.median(e2e_times)
+    # the ceiling e2e is bounded by: the same bytes copied from the same
+    # pinned buffers by plain cudaMemcpyAsync, one per column
+    dev_bufs = [torch.empty(t.numel() * t.element_size(), dtype=torch.uint8, device="cuda") for _, _, t, _ in inputs]
+    h2d_ms = []
+    for i in range(4):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for b, (_, _, t, _) in zip(dev_bufs, inputs):
+                b.copy_(t.view(torch.uint8).reshape(-1), non_blocking=True)
+            e1.record(stream)
+        e1.synchronize()
+        if i:
+            h2d_ms.append(e0.elapsed_time(e1))
+    del dev_bufs
+    h2d_gbs = h2d_bytes / (statistics.median(h2d_ms) / 1e3) / 1e9
 
     peak, peak_kind = load_peak()
     scan_avg = statistics.mean(scan_ms)
     alg_bytes = n * wl["bytes_per_row"]
     achieved = alg_bytes / (scan_avg / 1e3) / 1e9
     traffic = load_traffic(args.workload)
+    scan_kernel = ("staged_scan_kernel" if st.flags & abi.STAT_STAGED else
+                   "pipe_scan_kernel" if st.flags & getattr(abi, "STAT_PIPE", 0) else "scan_group_kernel")
 
-    cpu = None
+    # the CPU baseline over the same table, whose result doubles as the
+    # parity check of the GPU result (outside the timed region)
+    cpu, parity = None, None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        n_sample = cpu_sample_rows(args.workload)
-        v, dt = run_oracle_sample(args.workload, n_sample, threads)
-        cpu = {"value": v, "unit": "rows/s", "cores": threads, "kind": "port",
-               "sample": f"first {n_sample:,} rows of the workload ({dt:.1f} s), all host threads; C++ "
-                         "restatement of thinDB's silo executor (Zig toolchain absent)"}
+        ocols = oracle_columns(args.workload, inputs)
+        want, dt_all = run_oracle(args.workload, ocols, threads)
+        keys, ordered, rel = PARITY[args.workload]
+        parity = same_result(res, want, keys, ordered, rel)
+        n1 = min(n, DOP1_SAMPLE_ROWS)
+        _, dt1 = run_oracle(args.workload, prefix_columns(ocols, n1), 1)
+        cpu = {"value": n / dt_all, "unit": "rows/s", "cores": threads, "kind": "port",
+               "sample": f"the whole workload ({n:,} rows, {dt_all:.2f} s) on {threads} threads; C++ restatement "
+                         "of thinDB's silo executor (Zig toolchain absent)",
+               "dop1": {"value": n1 / dt1, "unit": "rows/s", "cores": 1,
+                        "sample": f"first {n1:,} rows of the workload ({dt1:.2f} s) on 1 thread"},
+               "dop_all": {"value": n / dt_all, "unit": "rows/s", "cores": threads}}
 
     if rank == 0:
         line = {
@@ -325,10 +385,15 @@ def gpu_arm(args, wl):
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "scan_group_kernel", "kernel_ms": scan_avg,
-                         "algorithmic_bytes": alg_bytes, "peak_kind": peak_kind},
+                         "kernel": scan_kernel, "kernel_ms": scan_avg,
+                         "algorithmic_bytes": alg_bytes, "peak_kind": peak_kind,
+                         "step_achieved": alg_bytes / (ms_per_step / 1e3) / 1e9,
+                         "step_frac": alg_bytes / (ms_per_step / 1e3) / 1e9 / peak},
             "e2e": {"value": e2e_value, "unit": "rows/s", "h2d_bytes_per_step": h2d_bytes,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": statistics.median(e2e_times) * 1e3},
+                    "d2h_bytes_per_step": d2h, "ms_per_step": statistics.median(e2e_times) * 1e3,
+                    "h2d_ceiling_gbs": h2d_gbs, "h2d_ceiling_ms": statistics.median(h2d_ms),
+                    "frac_of_h2d_ceiling": statistics.median(h2d_ms) / (statistics.median(e2e_times) * 1e3)},
+            "parity": parity,
             "gpu_launches": launches,
             "clocks": clk,
             "cpu_baseline": cpu,

@@ -345,6 +345,24 @@ tgpu_status tgpu_query_execute(tgpu_query *q);
  * caller's buffers; *done = 1 once every row has been returned. */
 tgpu_status tgpu_query_next(tgpu_query *q, tgpu_batch *batch, int32_t *done);
 
+/* Late materialisation of a string group key.  A TGPU_DICT32 key groups by
+ * its 32-bit code and `next` returns codes; thinDB groups a string column by
+ * its table id the same way and reads the strings back at emit
+ * (v2_group_topn_engine.zig packedIdKeys; v2_shape_group_topn.zig:1741
+ * emitResultStageHashed; DESIGN.md §4.6 "Packed ids").  For output column
+ * `column` (a DICT32 group key whose table column has a dictionary), writes
+ * the strings of codes[0..n) contiguously into `bytes` with offsets[0] = 0
+ * and string i at [offsets[i], offsets[i + 1]); *bytes_needed receives the
+ * total.  bytes may be NULL (size query).  A row whose key is NULL carries
+ * code 0 in `next`'s buffer: skip it by its validity.  A code outside the
+ * dictionary, or a column that is not such a key, returns
+ * TGPU_ERR_INVALID_ARGUMENT.  ORDER BY a DICT32 key orders by the strings
+ * (bytewise, a proper prefix first), as thinDB's post-emit sort does
+ * (v2_shape_group_topn.zig:302-325); a key whose dictionary holds a string
+ * twice declines. */
+tgpu_status tgpu_query_key_strings(const tgpu_query *q, uint32_t column, const int32_t *codes, uint64_t n,
+                                   uint64_t *offsets, uint8_t *bytes, uint64_t bytes_cap, uint64_t *bytes_needed);
+
 /* Async-safe cancellation flag; the next tile boundary or `next` returns
  * TGPU_ERR_CANCELLED. */
 tgpu_status tgpu_query_cancel(tgpu_query *q);

@@ -77,6 +77,15 @@ class HostTable:
                 bm = np.packbits(np.asarray(c.validity, dtype=bool), bitorder="little")
                 self._keep.append(bm)
                 d.validity = bm.ctypes.data
+            if c.type == abi.DICT32 and c.dictionary is not None:
+                enc = [s.encode() if isinstance(s, str) else bytes(s) for s in c.dictionary]
+                offs = np.zeros(len(enc) + 1, dtype=np.uint32)
+                offs[1:] = np.cumsum([len(e) for e in enc], dtype=np.uint64).astype(np.uint32)
+                blob = np.frombuffer(b"".join(enc) or b"\0", dtype=np.uint8).copy()
+                self._keep += [offs, blob]
+                d.dict_offsets = offs.ctypes.data
+                d.dict_bytes = blob.ctypes.data
+                d.dict_size = len(enc)
         self.desc = abi.TableDesc()
         self.desc.columns = self.descs
         self.desc.n_columns = len(self.columns)

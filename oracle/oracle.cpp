@@ -19,6 +19,10 @@
 //   NULL results / nulls-first order .. v2_shape_group_topn.zig:1361-1424
 //   result order: ORDER BY keys, then
 //     the packed key ascending ........ v2_shape_group_topn.zig:1327-1335
+//   ORDER BY a string key: the strings
+//     compared bytewise, after the emit  v2_shape_group_topn.zig:302-325
+//     (finish_after_emit: a hashed key read by ORDER BY is ranked on the
+//     emitted values; a packed id reads its string back)
 //   silo grid shape (16-RG tiles, 256
 //     buckets, bucket-owned folds) .... silo_group_core.zig:11493, :9228, :9348
 #include "oracle.h"
@@ -142,6 +146,30 @@ struct Plan {
     bool global = false;  // no GROUP BY: v2_global_aggregate.zig, one output row
 };
 
+// Dictionary string i of a DICT32 column.
+inline std::pair<const uint8_t *, uint32_t> dict_string(const tgpu_column_desc &c, uint32_t i) {
+    return {c.dict_bytes + c.dict_offsets[i], c.dict_offsets[i + 1] - c.dict_offsets[i]};
+}
+
+// Bytewise order of two strings, a proper prefix first (std.mem.order on u8).
+int cmp_bytes(std::pair<const uint8_t *, uint32_t> a, std::pair<const uint8_t *, uint32_t> b) {
+    const uint32_t n = std::min(a.second, b.second);
+    const int c = n ? std::memcmp(a.first, b.first, n) : 0;
+    if (c) return c < 0 ? -1 : 1;
+    return a.second == b.second ? 0 : (a.second < b.second ? -1 : 1);
+}
+
+bool dict_unique(const tgpu_column_desc &c) {
+    if (!c.dict_size) return true;
+    std::vector<uint32_t> ix(c.dict_size);
+    for (uint32_t i = 0; i < c.dict_size; ++i) ix[i] = i;
+    std::sort(ix.begin(), ix.end(),
+              [&](uint32_t x, uint32_t y) { return cmp_bytes(dict_string(c, x), dict_string(c, y)) < 0; });
+    for (uint32_t i = 1; i < c.dict_size; ++i)
+        if (cmp_bytes(dict_string(c, ix[i - 1]), dict_string(c, ix[i])) == 0) return false;
+    return true;
+}
+
 // validateShape restated (v2_shape_group_topn.zig:2051-2370) for the shapes
 // this engine runs; strings (hashed keys) and wide decimals decline.
 int build_plan(const Table &t, const tgpu_request *req, Plan &p) {
@@ -159,6 +187,9 @@ int build_plan(const Table &t, const tgpu_request *req, Plan &p) {
         int w = type_bits(ty);
         if (w == 0) return fail(TGPU_DECLINE, "group key type");
         bool nl = t.cols[c].validity != nullptr;
+        // a packed id stands for its string only when no string has two ids
+        // (thinDB's table ids are one per value)
+        if (ty == TGPU_DICT32 && !dict_unique(t.cols[c])) return fail(TGPU_DECLINE, "dictionary repeats a string");
         KeyPart kp{c, ty, off, w + (nl ? 1 : 0), nl};
         off += kp.width;
         p.parts.push_back(kp);
@@ -226,6 +257,9 @@ int build_plan(const Table &t, const tgpu_request *req, Plan &p) {
         if (s.target == TGPU_SORT_AGG && (s.index < 0 || (uint32_t)s.index >= req->n_aggs))
             return fail(TGPU_DECLINE, "order key");
         if (s.target != TGPU_SORT_KEY && s.target != TGPU_SORT_AGG) return fail(TGPU_DECLINE, "order key");
+        if (s.target == TGPU_SORT_KEY && p.parts[s.index].type == TGPU_DICT32 &&
+            !t.cols[p.parts[s.index].col].dict_size)
+            return fail(TGPU_DECLINE, "ORDER BY a string key without its dictionary");
     }
     for (uint32_t i = 0; i < req->n_having; ++i) {
         const tgpu_having &h = req->having[i];
@@ -666,10 +700,23 @@ int run(const Table &t, const tgpu_request *req, int threads, Result &res) {
         auto order_val = [&](const Group &g, const tgpu_sort_spec &s) {
             return s.target == TGPU_SORT_KEY ? key_value(g, p.parts[s.index]) : agg_value(g, p.aggs[s.index], p.global);
         };
+        // a DICT32 key orders by its strings; a code outside the dictionary
+        // after every string, by code
+        auto order_cmp = [&](const Group &a, const Group &b, const tgpu_sort_spec &s) {
+            Value va = order_val(a, s), vb = order_val(b, s);
+            if (s.target != TGPU_SORT_KEY || p.parts[s.index].type != TGPU_DICT32 || va.null || vb.null)
+                return cmp_value(va, vb);
+            const tgpu_column_desc &c = t.cols[p.parts[s.index].col];
+            const uint32_t ca = (uint32_t)(int32_t)va.i, cb = (uint32_t)(int32_t)vb.i;
+            const bool ia = ca < c.dict_size, ib = cb < c.dict_size;
+            if (ia && ib) return cmp_bytes(dict_string(c, ca), dict_string(c, cb));
+            if (ia != ib) return ia ? -1 : 1;
+            return ca < cb ? -1 : (ca > cb ? 1 : 0);
+        };
         std::sort(keep.begin(), keep.end(), [&](uint32_t x, uint32_t y) {
             const Group &a = groups[x], &b = groups[y];
             for (uint32_t i = 0; i < req->n_order; ++i) {
-                int c = cmp_value(order_val(a, req->order[i]), order_val(b, req->order[i]));
+                int c = order_cmp(a, b, req->order[i]);
                 if (c == 0) continue;
                 return (c < 0) != (req->order[i].desc != 0);
             }

@@ -62,3 +62,26 @@ def test_oracle_global_aggregate_over_no_rows():
     # OFFSET past the row, or LIMIT 0: nothing
     assert oracle.run(host, Request([], aggs, limit=0))["c"][0].size == 0
     assert oracle.run(host, Request([], aggs, offset=1))["c"][0].size == 0
+
+
+def test_oracle_orders_string_keys_by_their_strings():
+    """ORDER BY a DICT32 key ranks strings bytewise (thinDB's post-emit sort,
+    v2_shape_group_topn.zig:302-325), not codes; a dictionary holding a string
+    twice declines."""
+    import numpy as np
+
+    from thindb_gb300 import abi
+    from thindb_gb300.engine import AggSpec, Column, Request, SortSpec
+
+    dic = ["pear", "apple", "b", "ab", "a", "zz", "a/b", "a.b"]
+    codes = np.array([0, 1, 2, 3, 4, 5, 6, 7, 1, 1, 4], dtype=np.int32)
+    cols = [Column("s", abi.DICT32, codes, dictionary=dic), Column("v", abi.BIGINT, np.arange(11, dtype=np.int64))]
+    for desc in (False, True):
+        r = oracle.run(oracle.HostTable(cols), Request(["s"], [AggSpec("count", None, "c")], [SortSpec("s", desc)]))
+        got = [dic[c] for c in r["s"][0]]
+        assert got == sorted(dic, reverse=desc)
+    dup = list(dic)
+    dup[2] = "pear"
+    with pytest.raises(oracle.OracleDecline):
+        oracle.run(oracle.HostTable([Column("s", abi.DICT32, codes, dictionary=dup), cols[1]]),
+                   Request(["s"], [AggSpec("count", None, "c")]))

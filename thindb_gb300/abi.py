@@ -136,6 +136,8 @@ SIGNATURES = [
     ("tgpu_query_execute", C.c_int, [C.c_void_p]),
     ("tgpu_query_next", C.c_int, [C.c_void_p, C.POINTER(Batch), C.POINTER(C.c_int32)]),
     ("tgpu_query_cancel", C.c_int, [C.c_void_p]),
+    ("tgpu_query_key_strings", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
+                                         C.c_uint64, C.POINTER(C.c_uint64)]),
     ("tgpu_query_get_stats", C.c_int, [C.c_void_p, C.POINTER(QueryStats)]),
     ("tgpu_query_destroy", C.c_int, [C.c_void_p]),
     ("tgpu_query_synchronize", C.c_int, [C.c_void_p]),

@@ -93,6 +93,8 @@ struct DeviceCtx {
     int id = -1;
     int sms = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t stats_stream = nullptr;  // registration statistics, beside the column copies
+    cudaMemPool_t col_pool = nullptr;     // table columns: stream-ordered, kept after free
 };
 
 std::mutex g_dev_mu;
@@ -109,6 +111,17 @@ tgpu_status device_ctx(DeviceCtx **out) {
         CU(cudaGetDevice(&id));
         CU(cudaDeviceGetAttribute(&g_dev.sms, cudaDevAttrMultiProcessorCount, id));
         CU(cudaStreamCreateWithFlags(&g_dev.stream, cudaStreamNonBlocking));
+        CU(cudaStreamCreateWithFlags(&g_dev.stats_stream, cudaStreamNonBlocking));
+        // Table columns come from a pool of our own that keeps freed memory
+        // (release threshold: never), so registering and dropping tables
+        // repeatedly does not pay cudaMalloc/cudaFree each time.
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = id;
+        CU(cudaMemPoolCreate(&g_dev.col_pool, &props));
+        uint64_t keep = UINT64_MAX;
+        CU(cudaMemPoolSetAttribute(g_dev.col_pool, cudaMemPoolAttrReleaseThreshold, &keep));
         g_dev.id = id;
     }
     *out = &g_dev;
@@ -272,7 +285,23 @@ struct Column {
     std::vector<uint32_t> znull;
     std::vector<uint32_t> dict_offsets;
     std::vector<uint8_t> dict_bytes;
+    // DICT32 with a dictionary: whether every string is there once, and each
+    // code's rank in the strings' bytewise order (device, dict size entries)
+    bool dict_unique = true;
+    uint32_t *d_rank = nullptr;
+    std::vector<uint32_t> h_rank;
+    uint32_t dict_size() const { return dict_offsets.size() > 1 ? (uint32_t)dict_offsets.size() - 1 : 0; }
 };
+
+// Bytewise order of dictionary strings a and b, a proper prefix first.
+int dict_cmp(const Column &c, uint32_t a, uint32_t b) {
+    const uint32_t la = c.dict_offsets[a + 1] - c.dict_offsets[a], lb = c.dict_offsets[b + 1] - c.dict_offsets[b];
+    const uint32_t n = std::min(la, lb);
+    const int r = n ? std::memcmp(c.dict_bytes.data() + c.dict_offsets[a], c.dict_bytes.data() + c.dict_offsets[b], n)
+                    : 0;
+    if (r) return r < 0 ? -1 : 1;
+    return la == lb ? 0 : (la < lb ? -1 : 1);
+}
 
 }  // namespace
 
@@ -282,13 +311,20 @@ struct tgpu_table {
     uint32_t n_rg = 0;
     std::vector<Column> cols;
     bool sketches = false;  // registered with compute_ndv: plans may sketch composite keys
+    cudaStream_t stream = nullptr;  // registration stream: the columns are freed on it
     mutable std::mutex key_mu;
     mutable std::map<std::vector<int32_t>, uint64_t> key_ndv;  // composite-key NDV per group-column list
     ~tgpu_table() {
+        // Queries on other streams that read the table have finished (a
+        // query's next/synchronize waits for it; destroying a table under a
+        // running query is a caller error).  Frees return the memory to the
+        // column pool in stream order.
         for (auto &c : cols) {
-            if (c.owned) cudaFree(c.d_data);
-            cudaFree(c.d_valid);
+            if (c.owned) cudaFreeAsync(c.d_data, stream);
+            if (c.d_valid) cudaFreeAsync(c.d_valid, stream);
+            if (c.d_rank) cudaFreeAsync(c.d_rank, stream);
         }
+        cudaStreamSynchronize(stream);
     }
 };
 
@@ -369,6 +405,7 @@ struct tgpu_query {
     uint64_t limit = TGPU_NO_LIMIT, offset = 0;
     uint64_t budget = 0;
     std::vector<tgpu_output_column> schema;
+    std::vector<int> key_cols;  // table column of each group key (output column i < key_cols.size())
     DevQuery dq{};
     DevFinal df{};
     std::vector<int> out_types;
@@ -629,6 +666,9 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
         const Column &col = t->cols[c];
         int bits = type_bits(col.type);
         if (bits == 0) return fail(TGPU_DECLINE, "group key type");
+        // a packed code stands for its string only when no string has two
+        // codes (thinDB's table ids are one per value)
+        if (col.type == TGPU_DICT32 && !col.dict_unique) return fail(TGPU_DECLINE, "dictionary repeats a string");
         DevKeyPart &kp = dq.parts[dq.n_parts];
         kp.col = used_col(dq, map, t, c);
         if (kp.col < 0) return fail(TGPU_DECLINE, "too many columns");
@@ -647,6 +687,7 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
         oc.nullable = col.nullable;
         oc.elem_bytes = type_bytes(col.type);
         q->schema.push_back(oc);
+        q->key_cols.push_back(c);
     }
     if (off > 128) return fail(TGPU_DECLINE, "packed key wider than 128 bits (hashed keys)");
     dq.key_words = off > 64 ? 2 : 1;
@@ -810,6 +851,14 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
               (s.target == TGPU_SORT_AGG && s.index >= 0 && (uint32_t)s.index < req->n_aggs)))
             return fail(TGPU_DECLINE, "order key");
         df.order[i] = DevOrder{s.target, s.index, s.desc ? 1 : 0, 0};
+        if (s.target == TGPU_SORT_KEY && df.part_types[s.index] == TGPU_DICT32) {
+            // thinDB ranks a string key on its emitted strings
+            // (v2_shape_group_topn.zig:302-325): here on each code's rank
+            const Column &col = t->cols[req->group_cols[s.index]];
+            if (!col.d_rank) return fail(TGPU_DECLINE, "ORDER BY a string key without its dictionary");
+            df.part_rank[s.index] = col.d_rank;
+            df.part_rank_n[s.index] = col.dict_size();
+        }
     }
     for (uint32_t i = 0; i < req->n_having; ++i) {
         const tgpu_having &h = req->having[i];
@@ -1411,23 +1460,49 @@ tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out) {
     t->rg_rows = desc->row_group_rows ? desc->row_group_rows : 65536u;
     t->sketches = desc->compute_ndv != 0;
     t->n_rg = (uint32_t)((t->n_rows + t->rg_rows - 1) / t->rg_rows);
+    t->stream = dev->stream;  // frees go on the library's stream (the caller's may be gone by then)
     const uint64_t n = t->n_rows;
     const uint64_t vwords = (n + 31) / 32 + 1;
-    int64_t *d_imin = nullptr, *d_imax = nullptr;
-    double *d_fmin = nullptr, *d_fmax = nullptr;
-    uint32_t *d_nulls = nullptr, *d_regs = nullptr;
-    const size_t nrg = std::max<uint32_t>(1, t->n_rg);
-    CU(cudaMallocAsync((void **)&d_imin, nrg * 8, s));
-    CU(cudaMallocAsync((void **)&d_imax, nrg * 8, s));
-    CU(cudaMallocAsync((void **)&d_fmin, nrg * 8, s));
-    CU(cudaMallocAsync((void **)&d_fmax, nrg * 8, s));
-    CU(cudaMallocAsync((void **)&d_nulls, nrg * 4, s));
-    CU(cudaMallocAsync((void **)&d_regs, (1u << HLL_P) * 4, s));
-    for (uint32_t i = 0; i < desc->n_columns; ++i) {
+    const uint32_t nc = desc->n_columns;
+    for (uint32_t i = 0; i < nc; ++i) {
         const tgpu_column_desc &cd = desc->columns[i];
         if (cd.type < TGPU_BOOLEAN || cd.type > TGPU_DICT32 || cd.type == TGPU_DECIMAL128)
             return fail(TGPU_ERR_UNSUPPORTED_TYPE, "column type");
         if (n && !cd.data) return fail(TGPU_ERR_INVALID_ARGUMENT, "column without data");
+        if (cd.type == TGPU_DICT32 && cd.dict_size && (!cd.dict_offsets || !cd.dict_bytes))
+            return fail(TGPU_ERR_INVALID_ARGUMENT, "dictionary without offsets or bytes");
+    }
+    // Statistics scratch, one slice per column: zone maps of every row group
+    // (min/max as i64 and f64, NULL counts) and an HLL register file.
+    const size_t nrg = std::max<uint32_t>(1, t->n_rg);
+    const size_t stat_bytes = nrg * (8 * 4 + 4);
+    const size_t reg_bytes = (size_t)(1u << HLL_P) * 4;
+    unsigned char *d_stats = nullptr;
+    CU(cudaMallocFromPoolAsync((void **)&d_stats, std::max<size_t>(1, nc) * (stat_bytes + reg_bytes), dev->col_pool, s));
+    struct StatsGuard {  // an error return leaves nothing allocated behind
+        unsigned char *&p;
+        cudaStream_t a, b;
+        ~StatsGuard() {
+            if (!p) return;
+            cudaStreamSynchronize(b);
+            cudaFreeAsync(p, a);
+        }
+    } stats_guard{d_stats, s, dev->stats_stream};
+    std::vector<unsigned char> h_stats(std::max<size_t>(1, nc) * (stat_bytes + reg_bytes));
+    // Column copies go back to back on s; each column's statistics run on the
+    // statistics stream once its copy has landed, beside the next copy.
+    std::vector<cudaEvent_t> landed(nc, nullptr);
+    struct EvGuard {
+        std::vector<cudaEvent_t> &v;
+        ~EvGuard() {
+            for (auto e : v)
+                if (e) cudaEventDestroy(e);
+        }
+    } guard{landed};
+    cudaStream_t ss = dev->stats_stream;
+    std::vector<bool> sketch(nc, false);
+    for (uint32_t i = 0; i < nc; ++i) {
+        const tgpu_column_desc &cd = desc->columns[i];
         t->cols.emplace_back();
         Column &c = t->cols.back();
         c.name = cd.name ? cd.name : "";
@@ -1440,43 +1515,73 @@ tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out) {
             c.d_data = const_cast<void *>(cd.data);
             c.owned = false;
         } else {
-            CU(cudaMalloc(&c.d_data, std::max<size_t>(bytes, 16)));
+            // a 16-byte multiple past the data: bulk copies of a last partial tile stay inside
+            CU(cudaMallocFromPoolAsync(&c.d_data, round_up(std::max<size_t>(bytes, 16), 16), dev->col_pool, s));
             c.owned = true;
             if (bytes) CU(cudaMemcpyAsync(c.d_data, cd.data, bytes, cudaMemcpyHostToDevice, s));
         }
         if (cd.validity) {
-            CU(cudaMalloc((void **)&c.d_valid, vwords * 4));
+            CU(cudaMallocFromPoolAsync((void **)&c.d_valid, vwords * 4, dev->col_pool, s));
             CU(cudaMemsetAsync(c.d_valid, 0, vwords * 4, s));
             CU(cudaMemcpyAsync(c.d_valid, cd.validity, (n + 7) / 8,
                                desc->location == TGPU_LOC_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
         }
         if (cd.type == TGPU_DICT32 && cd.dict_offsets && cd.dict_size) {
             c.dict_offsets.assign(cd.dict_offsets, cd.dict_offsets + cd.dict_size + 1);
+            for (uint32_t j = 0; j < cd.dict_size; ++j)
+                if (c.dict_offsets[j + 1] < c.dict_offsets[j])
+                    return fail(TGPU_ERR_INVALID_ARGUMENT, "dictionary offsets decrease");
             c.dict_bytes.assign(cd.dict_bytes, cd.dict_bytes + cd.dict_offsets[cd.dict_size]);
+            // each code's rank among the strings in bytewise order: ORDER BY a
+            // string key ranks on it (its packed code only stands for the string)
+            std::vector<uint32_t> ix(cd.dict_size);
+            for (uint32_t j = 0; j < cd.dict_size; ++j) ix[j] = j;
+            std::sort(ix.begin(), ix.end(), [&](uint32_t a, uint32_t b) { return dict_cmp(c, a, b) < 0; });
+            c.h_rank.resize(cd.dict_size);
+            for (uint32_t j = 0; j < cd.dict_size; ++j) {
+                c.h_rank[ix[j]] = j;
+                if (j && dict_cmp(c, ix[j - 1], ix[j]) == 0) c.dict_unique = false;
+            }
+            CU(cudaMallocFromPoolAsync((void **)&c.d_rank, (size_t)cd.dict_size * 4, dev->col_pool, s));
+            CU(cudaMemcpyAsync(c.d_rank, c.h_rank.data(), (size_t)cd.dict_size * 4, cudaMemcpyHostToDevice, s));
         }
-        c.zmin.resize(t->n_rg);
-        c.zmax.resize(t->n_rg);
-        c.zfmin.resize(t->n_rg);
-        c.zfmax.resize(t->n_rg);
-        c.znull.resize(t->n_rg);
-        if (t->n_rg) {
-            CU(launch_zone_maps(c.d_data, c.d_valid, c.type, n, t->rg_rows, t->n_rg, d_imin, d_imax, d_fmin, d_fmax,
-                                d_nulls, s));
-            CU(cudaMemcpyAsync(c.zmin.data(), d_imin, t->n_rg * 8, cudaMemcpyDeviceToHost, s));
-            CU(cudaMemcpyAsync(c.zmax.data(), d_imax, t->n_rg * 8, cudaMemcpyDeviceToHost, s));
-            CU(cudaMemcpyAsync(c.zfmin.data(), d_fmin, t->n_rg * 8, cudaMemcpyDeviceToHost, s));
-            CU(cudaMemcpyAsync(c.zfmax.data(), d_fmax, t->n_rg * 8, cudaMemcpyDeviceToHost, s));
-            CU(cudaMemcpyAsync(c.znull.data(), d_nulls, t->n_rg * 4, cudaMemcpyDeviceToHost, s));
-            CU(cudaStreamSynchronize(s));
-        }
+        CU(cudaEventCreateWithFlags(&landed[i], cudaEventDisableTiming));
+        CU(cudaEventRecord(landed[i], s));
+        CU(cudaStreamWaitEvent(ss, landed[i], 0));
+        unsigned char *st = d_stats + (size_t)i * (stat_bytes + reg_bytes);
+        int64_t *imin = (int64_t *)st, *imax = imin + nrg;
+        double *fmin = (double *)(imax + nrg), *fmax = fmin + nrg;
+        uint32_t *nulls = (uint32_t *)(fmax + nrg);
+        uint32_t *regs = (uint32_t *)(st + stat_bytes);
+        if (t->n_rg)
+            CU(launch_zone_maps(c.d_data, c.d_valid, c.type, n, t->rg_rows, t->n_rg, imin, imax, fmin, fmax, nulls, ss));
         c.ndv = cd.ndv_hint;
-        if (!c.ndv && desc->compute_ndv && n) {
-            CU(cudaMemsetAsync(d_regs, 0, (1u << HLL_P) * 4, s));
-            CU(launch_hll(c.d_data, c.d_valid, c.type, n, d_regs, s));
-            std::vector<uint32_t> regs(1u << HLL_P);
-            CU(cudaMemcpyAsync(regs.data(), d_regs, regs.size() * 4, cudaMemcpyDeviceToHost, s));
-            CU(cudaStreamSynchronize(s));
-            c.ndv = (uint64_t)std::llround(hll_estimate(regs));
+        sketch[i] = !c.ndv && desc->compute_ndv && n;
+        if (sketch[i]) {
+            CU(cudaMemsetAsync(regs, 0, reg_bytes, ss));
+            CU(launch_hll(c.d_data, c.d_valid, c.type, n, regs, ss));
+        }
+    }
+    // one read-back of every column's statistics
+    CU(cudaMemcpyAsync(h_stats.data(), d_stats, h_stats.size(), cudaMemcpyDeviceToHost, ss));
+    CU(cudaStreamSynchronize(ss));
+    CU(cudaFreeAsync(d_stats, s));
+    d_stats = nullptr;
+    CU(cudaStreamSynchronize(s));
+    for (uint32_t i = 0; i < nc; ++i) {
+        Column &c = t->cols[i];
+        const unsigned char *st = h_stats.data() + (size_t)i * (stat_bytes + reg_bytes);
+        const int64_t *imin = (const int64_t *)st, *imax = imin + nrg;
+        const double *fmin = (const double *)(imax + nrg), *fmax = fmin + nrg;
+        const uint32_t *nulls = (const uint32_t *)(fmax + nrg);
+        c.zmin.assign(imin, imin + t->n_rg);
+        c.zmax.assign(imax, imax + t->n_rg);
+        c.zfmin.assign(fmin, fmin + t->n_rg);
+        c.zfmax.assign(fmax, fmax + t->n_rg);
+        c.znull.assign(nulls, nulls + t->n_rg);
+        if (sketch[i]) {
+            const uint32_t *r = (const uint32_t *)(st + stat_bytes);
+            c.ndv = (uint64_t)std::llround(hll_estimate(std::vector<uint32_t>(r, r + (1u << HLL_P))));
         }
         if (!c.ndv) {
             // without a sketch: bounded by the type's domain and the row count
@@ -1485,13 +1590,6 @@ tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out) {
             c.ndv = std::max<uint64_t>(1, std::min<uint64_t>(dom, n));
         }
     }
-    CU(cudaFreeAsync(d_imin, s));
-    CU(cudaFreeAsync(d_imax, s));
-    CU(cudaFreeAsync(d_fmin, s));
-    CU(cudaFreeAsync(d_fmax, s));
-    CU(cudaFreeAsync(d_nulls, s));
-    CU(cudaFreeAsync(d_regs, s));
-    CU(cudaStreamSynchronize(s));
     *out = t.release();
     return TGPU_OK;
 }
@@ -1632,6 +1730,28 @@ tgpu_status tgpu_query_next(tgpu_query *q, tgpu_batch *b, int32_t *done) {
     q->returned += n;
     b->row_count = n;
     *done = q->returned >= q->result_rows ? 1 : 0;
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_query_key_strings(const tgpu_query *q, uint32_t column, const int32_t *codes, uint64_t n,
+                                   uint64_t *offsets, uint8_t *bytes, uint64_t bytes_cap, uint64_t *bytes_needed) {
+    if (!q || (n && (!codes || !offsets)) || !bytes_needed) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
+    if (column >= q->key_cols.size()) return fail(TGPU_ERR_INVALID_ARGUMENT, "not a group key column");
+    const Column &c = q->t->cols[q->key_cols[column]];
+    if (c.type != TGPU_DICT32 || !c.dict_size()) return fail(TGPU_ERR_INVALID_ARGUMENT, "not a DICT32 key with a dictionary");
+    const uint32_t ds = c.dict_size();
+    uint64_t total = 0;
+    offsets[0] = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        const uint32_t code = (uint32_t)codes[i];
+        if (code >= ds) return fail(TGPU_ERR_INVALID_ARGUMENT, "code outside the dictionary");
+        const uint32_t b = c.dict_offsets[code], len = c.dict_offsets[code + 1] - b;
+        if (bytes && total + len <= bytes_cap) std::memcpy(bytes + total, c.dict_bytes.data() + b, len);
+        total += len;
+        offsets[i + 1] = total;
+    }
+    *bytes_needed = total;
+    if (total > bytes_cap && bytes) return fail(TGPU_ERR_INVALID_ARGUMENT, "string buffer too small");
     return TGPU_OK;
 }
 

@@ -215,6 +215,10 @@ struct DevFinal {
     int32_t global_avg;       // a global aggregate's AVG: sum / (n * 10^scale), else sum / n / 10^scale
     DevKeyPart parts[MAX_GROUP_KEYS];
     int32_t part_types[MAX_GROUP_KEYS];
+    // ORDER BY a DICT32 key: code c ranks as part_rank[c] (its string's place
+    // in bytewise order) when c < part_rank_n, else after every string
+    const uint32_t *part_rank[MAX_GROUP_KEYS];
+    uint32_t part_rank_n[MAX_GROUP_KEYS];
     DevOut outs[MAX_AGGS];
     DevOrder order[MAX_ORDER];
     DevHaving having[MAX_AGGS];

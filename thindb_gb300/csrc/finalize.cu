@@ -185,6 +185,12 @@ __device__ __forceinline__ void order_words(const DevFinal &f, const DevOrder &o
     EmitVal v = o.target == TGPU_SORT_KEY ? emit_key(f, k0, k1, o.index) : emit_agg(f, st, o.index);
     hi = 0;
     lo = 0;
+    if (!v.null && o.target == TGPU_SORT_KEY && f.part_rank[o.index]) {
+        // a string key: the code's rank among the dictionary's strings
+        const uint32_t code = (uint32_t)v.lo, n = f.part_rank_n[o.index];
+        v.lo = code < n ? (uint64_t)__ldg(f.part_rank[o.index] + code) : (uint64_t)n + code;
+        v.hi = 0;
+    }
     if (!v.null) {
         if (v.is_f) {
             double d = v.f;

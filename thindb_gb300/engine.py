@@ -442,6 +442,35 @@ class Query:
             out[c.name] = (v, ok)
         return out
 
+    def key_strings(self, column: int, codes: np.ndarray) -> list:
+        """The strings of DICT32 key codes (late materialisation through
+        tgpu_query_key_strings); column is the output column index."""
+        codes = np.ascontiguousarray(codes, dtype=np.int32)
+        n = len(codes)
+        offs = np.zeros(n + 1, dtype=np.uint64)
+        need = C.c_uint64()
+        _check(lib().tgpu_query_key_strings(self.handle, column, codes.ctypes.data, n, offs.ctypes.data, None, 0,
+                                            C.byref(need)))
+        blob = np.zeros(max(1, need.value), dtype=np.uint8)
+        _check(lib().tgpu_query_key_strings(self.handle, column, codes.ctypes.data, n, offs.ctypes.data,
+                                            blob.ctypes.data, need.value, C.byref(need)))
+        raw = blob.tobytes()
+        return [raw[int(offs[i]):int(offs[i + 1])].decode() for i in range(n)]
+
+    def collect_strings(self, capacity: int = 1 << 20) -> dict:
+        """collect() with every DICT32 key column's codes replaced by its
+        strings (None for a NULL key)."""
+        out = self.collect(capacity)
+        for i, c in enumerate(self.schema):
+            if c.type != abi.DICT32 or i >= len(self.request.group_cols):
+                continue
+            vals, ok = out[c.name]
+            strs = self.key_strings(i, np.where(ok, vals, 0) if ok is not None else vals)
+            if ok is not None:
+                strs = [s if o else None for s, o in zip(strs, ok)]
+            out[c.name] = (strs, ok)
+        return out
+
     def _result_rows(self) -> Optional[int]:
         """Rows the current execution emits (a zero-row next runs or waits for
         it), so collect sizes its buffers to the result."""
