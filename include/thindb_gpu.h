@@ -256,6 +256,13 @@ typedef struct tgpu_request {
  * densely, the survivors compacted into a per-warp shared-memory ring and
  * folded in full batches. */
 #define TGPU_FLAG_QUEUE_SCAN 0x2000
+/* The pipelined scan: a producer warp per CTA streams every scanned column
+ * by bulk asynchronous copies into shared-memory ring slots owned by
+ * consumer warps, which filter and fold from there (compiled fold, NOT NULL
+ * columns, one range WHERE on an integer column or none).
+ * TGPU_FLAG_NO_PIPE: never. */
+#define TGPU_FLAG_PIPE_SCAN 0x4000
+#define TGPU_FLAG_NO_PIPE 0x8000
 
 /* ----------------------------------------------------------------- output -- */
 
@@ -306,6 +313,7 @@ typedef struct tgpu_query_stats {
 #define TGPU_STAT_STAGED 0x4    /* the staged (bulk-copy ring) scan ran */
 #define TGPU_STAT_DISTINCT_PARTITION 0x8  /* COUNT(DISTINCT) went through partitions */
 #define TGPU_STAT_QUEUE 0x10    /* queue mode (dense loads, per-warp survivor ring) */
+#define TGPU_STAT_PIPE 0x20     /* the pipelined (producer/consumer bulk-copy) scan ran */
 
 /* -------------------------------------------------------------- the API -- */
 

@@ -35,6 +35,10 @@ CASES = {
         ["k"], [AggSpec("count", None, "c"), AggSpec("sum", "amount", "s"), AggSpec("avg", "amount", "a")],
         [SortSpec("s", True)], limit=10, where=[Pred("d", "between", datagen.FILTER_LO, datagen.FILTER_HI)],
         flags=abi.FLAG_STAGED_SCAN), abi.STAT_STAGED),
+    "pipe_scan": (filtered, lambda: Request(
+        ["k"], [AggSpec("count", None, "c"), AggSpec("sum", "amount", "s"), AggSpec("avg", "amount", "a")],
+        [SortSpec("s", True)], limit=10, where=[Pred("d", "between", datagen.FILTER_LO, datagen.FILTER_HI)],
+        flags=abi.FLAG_PIPE_SCAN), abi.STAT_PIPE),
     "distinct_partitions": (distinct, lambda: Request(
         ["region", "url"], [AggSpec("count", None, "c"), AggSpec("count_distinct", "user_id", "u")],
         flags=abi.FLAG_DISTINCT_PARTITION), abi.STAT_DISTINCT_PARTITION),

@@ -53,11 +53,14 @@ FLAG_DISTINCT_PREFETCH = 0x400
 FLAG_DISTINCT_PARTITION = 0x800
 FLAG_NO_DISTINCT_PARTITION = 0x1000
 FLAG_QUEUE_SCAN = 0x2000
+FLAG_PIPE_SCAN = 0x4000
+FLAG_NO_PIPE = 0x8000
 STAT_TUNED = 0x1
 STAT_GATHER = 0x2
 STAT_STAGED = 0x4
 STAT_DISTINCT_PARTITION = 0x8
 STAT_QUEUE = 0x10
+STAT_PIPE = 0x20
 
 
 class ColumnDesc(C.Structure):

@@ -421,6 +421,9 @@ struct tgpu_query {
     int load_pct = 50;            // group-table load target
     bool tuned = false;           // settings taken from the tuning table
     bool staged = false;          // the staged (bulk-copy ring) scan runs this query
+    bool piped = false;           // the pipelined (producer/consumer) scan runs this query
+    PipePlan pp{};
+    int pipe_grid = 0;
     bool batched = false;         // created for a batch (runs inside the batched kernel)
     uint64_t dpart_rows = 0;      // rows that passed when the partitions overflowed
     bool dpart_off = false;       // repeated pairs overflowed a partition: global set
@@ -1202,6 +1205,21 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
             q->staged = true;
         }
     }
+    // the pipelined scan, on request
+    q->piped = false;
+    const bool want_pipe = !q->staged && !(q->flags & TGPU_FLAG_NO_PIPE) && (q->flags & TGPU_FLAG_PIPE_SCAN);
+    if (want_pipe && t->rg_rows % PIPE_TILE == 0) {
+        DevQuery probe = dq;
+        const uint64_t tiles = (uint64_t)dq.n_rg * (t->rg_rows / PIPE_TILE);
+        DeviceCtx *dev;
+        if (tiles > 0 && tiles < (1ULL << 32) && pipe_plan(probe, tiles, &q->pp) && device_ctx(&dev) == TGPU_OK) {
+            dq.cache_slots = probe.cache_slots;
+            dq.cache_probe = probe.cache_probe;
+            if (q->route == 1 && !(dq.cache_slots && dq.cache_probe == dq.cache_slots)) q->route = 2;
+            q->pipe_grid = (int)std::min<uint64_t>((uint64_t)dev->sms, std::max<uint64_t>(1, tiles / PIPE_CWARPS));
+            q->piped = true;
+        }
+    }
     return TGPU_OK;
 }
 
@@ -1236,6 +1254,9 @@ tgpu_status enqueue(tgpu_query *q) {
     if (dq.dpart_bits) CU(cudaMemsetAsync(dq.dpart_cursor, 0, (size_t)4 << dq.dpart_bits, s));
     if (q->staged) {
         CU(launch_staged_scan(dq, q->sp, q->stage_grid, s));
+        q->launches++;
+    } else if (q->piped) {
+        CU(launch_pipe_scan(dq, q->pp, q->pipe_grid, s));
         q->launches++;
     } else if (dq.n_chunks > 0) {
         CU(launch_scan(dq, q->grid, s));
@@ -1361,9 +1382,10 @@ tgpu_status finish(tgpu_query *q) {
     s.route = (uint32_t)q->route;
     s.retries = q->retries;
     s.kernel_launches = q->launches;
-    s.flags = (q->tuned ? TGPU_STAT_TUNED : 0) | (q->dq.gather == 1 && !q->staged ? TGPU_STAT_GATHER : 0) |
-              (q->dq.gather == 2 && !q->staged ? TGPU_STAT_QUEUE : 0) |
-              (q->staged ? TGPU_STAT_STAGED : 0) | (q->dq.dpart_bits ? TGPU_STAT_DISTINCT_PARTITION : 0);
+    s.flags = (q->tuned ? TGPU_STAT_TUNED : 0) | (q->dq.gather == 1 && !q->staged && !q->piped ? TGPU_STAT_GATHER : 0) |
+              (q->dq.gather == 2 && !q->staged && !q->piped ? TGPU_STAT_QUEUE : 0) |
+              (q->staged ? TGPU_STAT_STAGED : 0) | (q->piped ? TGPU_STAT_PIPE : 0) |
+              (q->dq.dpart_bits ? TGPU_STAT_DISTINCT_PARTITION : 0);
     s.device_bytes = q->table_buf.bytes + q->occ_buf.bytes + q->scratch_bytes;
     for (auto &b : q->dset_bufs) s.device_bytes += b.bytes;
     if (q->flags & TGPU_FLAG_TIMING) {
@@ -1406,7 +1428,8 @@ void apply_tuning(tgpu_query *q, const tgpu_request *req, int batched) {
     const int modes = TGPU_FLAG_DENSE_SCAN | TGPU_FLAG_GATHER_SCAN | TGPU_FLAG_NO_WARP_COMBINE |
                       TGPU_FLAG_STAGED_SCAN | TGPU_FLAG_NO_STAGED | TGPU_FLAG_NO_PREFETCH |
                       TGPU_FLAG_NO_CHUNK_PREFETCH | TGPU_FLAG_DISTINCT_PREFETCH | TGPU_FLAG_DISTINCT_PARTITION |
-                      TGPU_FLAG_NO_DISTINCT_PARTITION | TGPU_FLAG_QUEUE_SCAN;
+                      TGPU_FLAG_NO_DISTINCT_PARTITION | TGPU_FLAG_QUEUE_SCAN | TGPU_FLAG_PIPE_SCAN |
+                      TGPU_FLAG_NO_PIPE;
     const int own = modes | TGPU_FLAG_NO_TUNING;
     if (req->chunk_rows || req->cache_slots || req->table_load_pct || (req->flags & own)) return;
     const tgpu_shape s = shape_of(q, req, batched);
@@ -1475,7 +1498,9 @@ tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out) {
     // Statistics scratch, one slice per column: zone maps of every row group
     // (min/max as i64 and f64, NULL counts) and an HLL register file.
     const size_t nrg = std::max<uint32_t>(1, t->n_rg);
-    const size_t stat_bytes = nrg * (8 * 4 + 4);
+    // (rounded to 256 bytes so every column's slice, and the 8-byte arrays
+    // inside it, stay aligned whatever the row-group count)
+    const size_t stat_bytes = round_up(nrg * (8 * 4 + 4), 256);
     const size_t reg_bytes = (size_t)(1u << HLL_P) * 4;
     unsigned char *d_stats = nullptr;
     CU(cudaMallocFromPoolAsync((void **)&d_stats, std::max<size_t>(1, nc) * (stat_bytes + reg_bytes), dev->col_pool, s));

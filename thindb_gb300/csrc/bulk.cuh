@@ -18,6 +18,17 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(s_addr(bar)) : "memory");
 }
 
+// `count` arrivals per phase.
+__device__ __forceinline__ void mbar_init_n(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(s_addr(bar)), "r"(count) : "memory");
+}
+
+// A plain arrival (release: this thread's earlier shared-memory accesses are
+// ordered before the phase completes).
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(s_addr(bar)) : "memory");
+}
+
 __device__ __forceinline__ void mbar_init_fence() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }

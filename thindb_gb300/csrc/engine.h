@@ -273,6 +273,31 @@ struct StagePlan {
 bool stage_plan(DevQuery &q, uint64_t tile_count, StagePlan *sp);
 cudaError_t launch_staged_scan(const DevQuery &q, const StagePlan &sp, int grid, cudaStream_t s);
 
+// The pipelined scan (scan_pipe.cu): one producer warp streams tiles of
+// PIPE_TILE rows of every scanned column by bulk copies into ring slots owned
+// by PIPE_CWARPS consumer warps (`depth` slots each), which filter and fold
+// from shared memory.  Tile t covers rows [row0, row0 + PIPE_TILE) of
+// surviving row group t / tiles_per_rg.
+constexpr int PIPE_CWARPS = 16;
+constexpr int PIPE_THREADS = (PIPE_CWARPS + 1) * 32;
+constexpr uint32_t PIPE_TILE = 256;
+struct PipePlan {
+    uint32_t n_tiles;
+    uint32_t tiles_per_rg;
+    uint32_t depth;              // ring slots per consumer warp
+    uint32_t stage_bytes;        // bytes of one tile of every scanned column
+    uint32_t n_cols;
+    int32_t col[MAX_QCOLS];      // query column of staged column i
+    uint32_t off[MAX_QCOLS];     // its byte offset inside a stage
+    int32_t slot[MAX_QCOLS];     // staged index of query column c, -1 = not staged
+    uint32_t ctl_off, bar_off, cache_off, queue_off, ring_off, smem_bytes;
+};
+// Plan the pipelined scan for q (its cache_slots may shrink to fit); false
+// if the query does not qualify (compiled fold, NOT NULL 16-byte aligned
+// columns, one range WHERE on an integer column or none).
+bool pipe_plan(DevQuery &q, uint64_t tile_count, PipePlan *pp);
+cudaError_t launch_pipe_scan(const DevQuery &q, const PipePlan &pp, int grid, cudaStream_t s);
+
 // Partitioned COUNT(DISTINCT): pairs per partition (one CTA deduplicates a
 // partition in shared memory) and the partition's index-table slots.
 constexpr uint32_t DPART_CAP = 4096;     // 64 KB of pairs per ring stage; three stages + 32 KB of slots per SM
