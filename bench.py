@@ -44,6 +44,11 @@ WORKLOADS = {
         "name": "plain GROUP BY: 16,777,216 rows, k BIGINT over 1,024 values, v INT, COUNT/SUM/MIN/MAX",
         "rows": datagen.PLAIN_ROWS, "bytes_per_row": 12, "dtype": "int64",
     },
+    "topcount": {
+        "name": "ORDER BY COUNT(*) DESC LIMIT 10: 100M rows, k BIGINT Zipf(1.1) over 10M (the filtered table's key), "
+                "no WHERE; the two-pass count sketch",
+        "rows": datagen.FILTERED_ROWS, "bytes_per_row": 8, "dtype": "int64",
+    },
     "distinct": {
         "name": "composite key + COUNT(DISTINCT): 200M rows, (region SMALLINT, url DICT32), user_id BIGINT "
                 "Zipf(0.9) over 5M, latency DOUBLE, COUNT/COUNT(DISTINCT)/SUM(f64)",
@@ -215,6 +220,7 @@ PARITY = {  # group keys, ordered result, DOUBLE-sum columns
     "filtered": (["k"], True, ()),
     "plain": (["k"], False, ()),
     "distinct": (["region", "url"], False, ("lat",)),
+    "topcount": (["k"], True, ()),
 }
 
 
@@ -351,7 +357,7 @@ def gpu_arm(args, wl):
     achieved = alg_bytes / (scan_avg / 1e3) / 1e9
     traffic = load_traffic(args.workload)
     scan_kernel = ("staged_scan_kernel" if st.flags & abi.STAT_STAGED else
-                   "pipe_scan_kernel" if st.flags & getattr(abi, "STAT_PIPE", 0) else "scan_group_kernel")
+                   "pipe_scan_kernel" if st.flags & abi.STAT_PIPE else "scan_group_kernel")
 
     # the CPU baseline over the same table, whose result doubles as the
     # parity check of the GPU result (outside the timed region)
@@ -379,8 +385,10 @@ def gpu_arm(args, wl):
             "config": {"workload": wl["name"], "rows": n, "l2": "inputs larger than L2 (no flush)",
                        "selectivity": st.rows_selected / max(1, st.rows_scanned), "groups": st.groups,
                        "route": "shared-memory" if st.route == 1 else "global table",
-                       "scan": ("staged" if st.flags & abi.STAT_STAGED else "queue" if st.flags & abi.STAT_QUEUE
+                       "scan": ("staged" if st.flags & abi.STAT_STAGED else "pipelined" if st.flags & abi.STAT_PIPE
+                                else "queue" if st.flags & abi.STAT_QUEUE
                                 else "survivor gather" if st.flags & abi.STAT_GATHER else "in place"),
+                       "count_sketch": bool(st.flags & abi.STAT_COUNT_SKETCH),
                        "tuned": bool(st.flags & abi.STAT_TUNED),
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

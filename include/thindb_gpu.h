@@ -263,6 +263,15 @@ typedef struct tgpu_request {
  * TGPU_FLAG_NO_PIPE: never. */
 #define TGPU_FLAG_PIPE_SCAN 0x4000
 #define TGPU_FLAG_NO_PIPE 0x8000
+/* ORDER BY COUNT(*) DESC LIMIT k (k + OFFSET <= 1024, no HAVING, no
+ * COUNT(DISTINCT)) runs thinDB's two-pass count top-K
+ * (src/exec/count_topk_sketch.zig): a tally of 2^14 counters by key hash,
+ * then a grouping pass over the rows of the heavy counters only, exact (a
+ * filter pass that cannot prove its answer reruns over every row).  By
+ * default from 1M scanned rows; TGPU_FLAG_COUNT_SKETCH forces it on smaller
+ * inputs, TGPU_FLAG_NO_COUNT_SKETCH turns it off. */
+#define TGPU_FLAG_COUNT_SKETCH 0x10000
+#define TGPU_FLAG_NO_COUNT_SKETCH 0x20000
 
 /* ----------------------------------------------------------------- output -- */
 
@@ -314,6 +323,8 @@ typedef struct tgpu_query_stats {
 #define TGPU_STAT_DISTINCT_PARTITION 0x8  /* COUNT(DISTINCT) went through partitions */
 #define TGPU_STAT_QUEUE 0x10    /* queue mode (dense loads, per-warp survivor ring) */
 #define TGPU_STAT_PIPE 0x20     /* the pipelined (producer/consumer bulk-copy) scan ran */
+#define TGPU_STAT_COUNT_SKETCH 0x40  /* the count sketch's filter pass gave the answer */
+#define TGPU_STAT_SKETCH_RERUN 0x80  /* its filter pass could not prove the answer: every row regrouped */
 
 /* -------------------------------------------------------------- the API -- */
 

@@ -55,12 +55,16 @@ FLAG_NO_DISTINCT_PARTITION = 0x1000
 FLAG_QUEUE_SCAN = 0x2000
 FLAG_PIPE_SCAN = 0x4000
 FLAG_NO_PIPE = 0x8000
+FLAG_COUNT_SKETCH = 0x10000
+FLAG_NO_COUNT_SKETCH = 0x20000
 STAT_TUNED = 0x1
 STAT_GATHER = 0x2
 STAT_STAGED = 0x4
 STAT_DISTINCT_PARTITION = 0x8
 STAT_QUEUE = 0x10
 STAT_PIPE = 0x20
+STAT_COUNT_SKETCH = 0x40
+STAT_SKETCH_RERUN = 0x80
 
 
 class ColumnDesc(C.Structure):

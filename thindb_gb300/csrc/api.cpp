@@ -422,6 +422,11 @@ struct tgpu_query {
     bool tuned = false;           // settings taken from the tuning table
     bool staged = false;          // the staged (bulk-copy ring) scan runs this query
     bool piped = false;           // the pipelined (producer/consumer) scan runs this query
+    bool sketch = false;          // ORDER BY COUNT(*) DESC LIMIT k: the count sketch runs first
+    bool sketch_off = false;      // an inexact filter pass switched it off for this query
+    int sketch_order_agg = 0;     // the COUNT(*) aggregate it ranks by
+    uint32_t sketch_reruns = 0;
+    uint32_t *d_sketch = nullptr; // counts | keep bits | control
     PipePlan pp{};
     int pipe_grid = 0;
     bool batched = false;         // created for a batch (runs inside the batched kernel)
@@ -1080,6 +1085,7 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
         o_val.push_back(add(q->out_rows_max));
     }
     size_t o_ptrs = add(q->schema.size() * 8), o_vptrs = add(q->schema.size() * 8);
+    const size_t o_sketch = q->sketch ? add(((size_t)1 << SK_BITS) * 4 + ((size_t)1 << SK_BITS) / 8 + 64) : 0;
     (void)row_bytes;
 
     const size_t total = table_bytes + occ_bytes + dset_bytes + dpart_bytes + scratch;
@@ -1137,6 +1143,7 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
         q->d_out.push_back(base + o_out[c]);
         q->d_outvalid.push_back((uint8_t *)(base + o_val[c]));
     }
+    q->d_sketch = q->sketch ? (uint32_t *)(base + o_sketch) : nullptr;
     q->d_out_ptrs = (void **)(base + o_ptrs);
     q->d_valid_ptrs = (uint8_t **)(base + o_vptrs);
     CU(cudaMemcpyAsync(q->d_out_ptrs, q->d_out.data(), q->schema.size() * 8, cudaMemcpyHostToDevice, q->stream));
@@ -1223,6 +1230,21 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     return TGPU_OK;
 }
 
+// GROUP BY ... ORDER BY COUNT(*) DESC LIMIT k (k + OFFSET <= 1024, no
+// HAVING, no COUNT(DISTINCT)): the count sketch runs first, as thinDB routes
+// such a query to its two-pass top-K (v2_group_topn_engine.zig:1375,
+// count_topk_sketch.zig MAX_NEED :64), unless the input is small.
+bool sketch_eligible(const tgpu_query *q, const tgpu_request *req) {
+    if ((q->flags & TGPU_FLAG_NO_COUNT_SKETCH) || q->global_agg || req->n_order != 1 || req->n_having) return false;
+    const tgpu_sort_spec &o = req->order[0];
+    if (o.target != TGPU_SORT_AGG || !o.desc || q->limit == TGPU_NO_LIMIT || q->limit == 0 ||
+        q->offset + q->limit > SK_MAX_NEED)
+        return false;
+    if (req->aggs[o.index].func != TGPU_AGG_COUNT || q->dq.aggs[o.index].kind != AK_COUNT_ROWS) return false;
+    if (q->dq.needs_gid || q->dq.n_dsets) return false;
+    return q->rows_scanned >= SK_MIN_ROWS || (q->flags & TGPU_FLAG_COUNT_SKETCH);
+}
+
 tgpu_status enqueue(tgpu_query *q) {
     DevQuery &dq = q->dq;
     DevFinal &df = q->df;
@@ -1252,6 +1274,20 @@ tgpu_status enqueue(tgpu_query *q) {
         for (auto &e : q->ev) CU(cudaEventCreate(&e));
     if (timing) CU(cudaEventRecord(q->ev[0], s));
     if (dq.dpart_bits) CU(cudaMemsetAsync(dq.dpart_cursor, 0, (size_t)4 << dq.dpart_bits, s));
+    uint32_t *sk_counts = q->d_sketch, *sk_keep = sk_counts ? sk_counts + (1u << SK_BITS) : nullptr;
+    uint32_t *sk_ctl = sk_keep ? sk_keep + (1u << SK_BITS) / 32 : nullptr;
+    if (q->sketch && !q->sketch_off) {
+        DeviceCtx *dev;
+        tgpu_status dst = device_ctx(&dev);
+        if (dst != TGPU_OK) return dst;
+        CU(launch_count_sketch(dq, (uint32_t)(q->offset + q->limit), sk_counts, sk_keep, sk_ctl, dev->sms, s));
+        q->launches += 2;
+        dq.sk_keep = sk_keep;
+        dq.sk_on = sk_ctl;
+    } else {
+        dq.sk_keep = nullptr;
+        dq.sk_on = nullptr;
+    }
     if (q->staged) {
         CU(launch_staged_scan(dq, q->sp, q->stage_grid, s));
         q->launches++;
@@ -1300,6 +1336,15 @@ tgpu_status enqueue(tgpu_query *q) {
     if (timing) CU(cudaEventRecord(q->ev[2], s));
     CU(cudaMemcpyAsync(q->h_counts, q->d_counts, 5 * 8, cudaMemcpyDeviceToHost, s));
     CU(cudaMemcpyAsync(q->h_counts + 5, q->d_ctrl + 1, 4, cudaMemcpyDeviceToHost, s));
+    if (q->sketch && !q->sketch_off) {
+        // [6] on | threshold << 32, [7] the COUNT of the page's last row,
+        // [8] kept rows, [9] rows tallied (the exactness check in finish)
+        CU(cudaMemcpyAsync(q->h_counts + 6, sk_ctl, 8, cudaMemcpyDeviceToHost, s));
+        const size_t col = q->df.n_parts + (size_t)q->sketch_order_agg;
+        CU(cudaMemcpyAsync(q->h_counts + 7, (const char *)q->d_out[col] + (q->limit - 1) * 8, 8,
+                           cudaMemcpyDeviceToHost, s));
+        CU(cudaMemcpyAsync(q->h_counts + 8, sk_ctl + 2, 16, cudaMemcpyDeviceToHost, s));
+    }
     q->executed = true;
     q->synced = false;
     q->returned = 0;
@@ -1364,6 +1409,25 @@ tgpu_status finish(tgpu_query *q) {
             if (st != TGPU_OK) return st;
             continue;
         }
+        if (q->sketch && !q->sketch_off && (q->h_counts[6] & 0xFFFFFFFFu)) {
+            // CountSketch.exact (count_topk_sketch.zig:236-239): the kept
+            // groups' top `need` is the answer once no dropped group (fewer
+            // than `threshold` rows) can reach the need-th best.  thinDB
+            // accepts a need-th best of threshold - 1 rows, leaving a tie at
+            // the cut unordered; ties here break on the packed key, so a
+            // dropped group may not even tie: the need-th best must hold
+            // `threshold` rows.  Otherwise group every row.
+            const uint64_t need = q->offset + q->limit, found = q->h_counts[0];
+            const uint64_t thr = q->h_counts[6] >> 32, kth = q->h_counts[7];
+            const bool all_kept = q->h_counts[8] == q->h_counts[9];
+            if (!all_kept && !(found >= need && kth >= thr)) {
+                q->sketch_off = true;
+                q->sketch_reruns++;
+                tgpu_status st = enqueue(q);
+                if (st != TGPU_OK) return st;
+                continue;
+            }
+        }
         break;
     }
     q->synced = true;
@@ -1385,6 +1449,8 @@ tgpu_status finish(tgpu_query *q) {
     s.flags = (q->tuned ? TGPU_STAT_TUNED : 0) | (q->dq.gather == 1 && !q->staged && !q->piped ? TGPU_STAT_GATHER : 0) |
               (q->dq.gather == 2 && !q->staged && !q->piped ? TGPU_STAT_QUEUE : 0) |
               (q->staged ? TGPU_STAT_STAGED : 0) | (q->piped ? TGPU_STAT_PIPE : 0) |
+              (q->sketch && !q->sketch_off && (q->h_counts[6] & 0xFFFFFFFFu) ? TGPU_STAT_COUNT_SKETCH : 0) |
+              (q->sketch_reruns ? TGPU_STAT_SKETCH_RERUN : 0) |
               (q->dq.dpart_bits ? TGPU_STAT_DISTINCT_PARTITION : 0);
     s.device_bytes = q->table_buf.bytes + q->occ_buf.bytes + q->scratch_bytes;
     for (auto &b : q->dset_bufs) s.device_bytes += b.bytes;
@@ -1429,7 +1495,7 @@ void apply_tuning(tgpu_query *q, const tgpu_request *req, int batched) {
                       TGPU_FLAG_STAGED_SCAN | TGPU_FLAG_NO_STAGED | TGPU_FLAG_NO_PREFETCH |
                       TGPU_FLAG_NO_CHUNK_PREFETCH | TGPU_FLAG_DISTINCT_PREFETCH | TGPU_FLAG_DISTINCT_PARTITION |
                       TGPU_FLAG_NO_DISTINCT_PARTITION | TGPU_FLAG_QUEUE_SCAN | TGPU_FLAG_PIPE_SCAN |
-                      TGPU_FLAG_NO_PIPE;
+                      TGPU_FLAG_NO_PIPE | TGPU_FLAG_COUNT_SKETCH | TGPU_FLAG_NO_COUNT_SKETCH;
     const int own = modes | TGPU_FLAG_NO_TUNING;
     if (req->chunk_rows || req->cache_slots || req->table_load_pct || (req->flags & own)) return;
     const tgpu_shape s = shape_of(q, req, batched);
@@ -1667,6 +1733,8 @@ tgpu_status query_create(tgpu_table *table, const tgpu_request *req, int batched
     st = plan_query(q.get(), table, req);
     if (st != TGPU_OK) return st;
     apply_tuning(q.get(), req, batched);
+    q->sketch = !batched && sketch_eligible(q.get(), req);
+    q->sketch_order_agg = q->sketch ? req->order[0].index : 0;
     st = g_slab.take(&q->h_block);
     if (st != TGPU_OK) return st;
     q->h_counts = (unsigned long long *)q->h_block;

@@ -165,6 +165,11 @@ struct DevQuery {
     int32_t prefetch;
     int32_t n_pf;
     int32_t pf_cols[8];
+    // ORDER BY COUNT(*) DESC LIMIT k through the count sketch (sketch.cu):
+    // when *sk_on, only rows whose counter hash(key) >> (64 - SK_BITS) has
+    // its bit set in sk_keep fold; nullptr = every row folds
+    const uint32_t *sk_keep;
+    const uint32_t *sk_on;
     // control
     long long wait_cycles;                // bound of the bulk-copy waits in SM clocks, 0 = WAIT_CYCLES
     unsigned int *tile_counter;
@@ -284,7 +289,7 @@ constexpr uint32_t PIPE_TILE = 256;
 struct PipePlan {
     uint32_t n_tiles;
     uint32_t tiles_per_rg;
-    uint32_t depth;              // ring slots per consumer warp
+    uint32_t log_depth;          // log2 of the ring slots per consumer warp (1 or 2)
     uint32_t stage_bytes;        // bytes of one tile of every scanned column
     uint32_t n_cols;
     int32_t col[MAX_QCOLS];      // query column of staged column i
@@ -297,6 +302,15 @@ struct PipePlan {
 // columns, one range WHERE on an integer column or none).
 bool pipe_plan(DevQuery &q, uint64_t tile_count, PipePlan *pp);
 cudaError_t launch_pipe_scan(const DevQuery &q, const PipePlan &pp, int grid, cudaStream_t s);
+
+// The two-pass COUNT top-K sketch (sketch.cu): 2^SK_BITS counters, served
+// for OFFSET + LIMIT up to SK_MAX_NEED over at least SK_MIN_ROWS rows.
+constexpr int SK_BITS = 14;
+constexpr uint32_t SK_MAX_NEED = 1024;     // MAX_NEED, count_topk_sketch.zig:64
+constexpr uint64_t SK_MIN_ROWS = 1u << 20;
+// counts: 2^SK_BITS u32; keep: 2^SK_BITS bits; ctl: 8 u32 ([0] on, [1] threshold, ...)
+cudaError_t launch_count_sketch(const DevQuery &q, uint32_t need, uint32_t *counts, uint32_t *keep, uint32_t *ctl,
+                                int sms, cudaStream_t s);
 
 // Partitioned COUNT(DISTINCT): pairs per partition (one CTA deduplicates a
 // partition in shared memory) and the partition's index-table slots.

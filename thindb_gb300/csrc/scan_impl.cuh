@@ -539,10 +539,25 @@ __device__ __forceinline__ void load_row(const DevQuery &q, uint64_t row, bool m
     }
 }
 
+// The count sketch's filter pass: lanes whose key's counter is not kept
+// drop out of the fold (the whole active mask when the sketch is off).
+__device__ __forceinline__ unsigned sketch_keep(const DevQuery &q, uint64_t k0, uint64_t k1, unsigned active) {
+    if (!q.sk_keep || !__ldg(q.sk_on)) return active;
+    const int lane = threadIdx.x & 31;
+    bool me = (active >> lane) & 1u;
+    if (me) {
+        const uint32_t c = (uint32_t)(hash_key(k0, k1) >> (64 - SK_BITS));
+        me = (__ldg(q.sk_keep + (c >> 5)) >> (c & 31)) & 1u;
+    }
+    return __ballot_sync(FULL, me);
+}
+
 // Fold up to 32 gathered rows (bit i of `active` = lane i holds one).  One
 // out-of-line copy keeps the instruction footprint small.
 template <int NA>
 __device__ __noinline__ void fold_batch(const DevQuery &q, const ScanSmem sm, const RowVals<NA> &in, unsigned active) {
+    active = sketch_keep(q, in.k0, in.k1, active);
+    if (!active) return;
     const int lane = threadIdx.x & 31;
     const bool me = (active >> lane) & 1u;
     uint64_t val[NA];
@@ -844,6 +859,8 @@ struct FastFold {
     }
 
     __device__ __noinline__ static void fold(const DevQuery &q, const ScanSmem sm, const Row in, unsigned active) {
+        active = sketch_keep(q, in.k0, in.k1, active);
+        if (!active) return;
         const int lane = threadIdx.x & 31;
         const bool me = (active >> lane) & 1u;
         uint64_t val[NV];

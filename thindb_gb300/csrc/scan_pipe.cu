@@ -56,28 +56,33 @@ __device__ __forceinline__ void pipe_tile_rows(const DevQuery &q, const PipePlan
     rows = end > row0 ? (uint32_t)(end - row0) : 0;
 }
 
-// Producer warp: start tile t into `stage`, completing on `bar`.  A full tile
-// is one bulk copy per column (16-byte aligned and sized: the plan checks the
-// column bases, and PIPE_TILE rows of any width are a multiple of 16 bytes);
-// the warp copies a partial tile (the table's last rows) with plain loads.
-__device__ __noinline__ void pipe_issue(const DevQuery &q, const PipePlan &pp, uint32_t t, unsigned char *stage,
-                                        uint64_t *bar) {
-    const int lane = threadIdx.x & 31;
+// One producer lane: start tile t into `stage`, completing on `bar`.  A
+// full tile is one bulk copy per column (16-byte aligned and sized: the plan
+// checks the column bases, and PIPE_TILE rows of any width are a multiple of
+// 16 bytes).  A partial tile (the table's last rows) completes the phase at
+// once and its consumer copies the rows itself.
+__device__ __forceinline__ void pipe_issue(const DevQuery &q, const PipePlan &pp, uint32_t t, unsigned char *stage,
+                                           uint64_t *bar) {
     uint64_t row0;
     uint32_t rows;
     pipe_tile_rows(q, pp, t, row0, rows);
-    if (rows == PIPE_TILE) {
-        if (lane == 0) {
-            fence_proxy_async_smem();  // the consumer's reads of this slot precede the copies into it
-            mbar_arrive_tx(bar, pp.stage_bytes);
-            for (uint32_t i = 0; i < pp.n_cols; ++i) {
-                const DevCol &c = q.cols[pp.col[i]];
-                bulk_load(stage + pp.off[i], (const unsigned char *)c.data + row0 * (uint64_t)c.bytes,
-                          PIPE_TILE * (uint32_t)c.bytes, bar);
-            }
-        }
+    if (rows != PIPE_TILE) {
+        mbar_arrive(bar);
         return;
     }
+    fence_proxy_async_smem();  // the consumer's reads of this slot precede the copies into it
+    mbar_arrive_tx(bar, pp.stage_bytes);
+    for (uint32_t i = 0; i < pp.n_cols; ++i) {
+        const DevCol &c = q.cols[pp.col[i]];
+        bulk_load(stage + pp.off[i], (const unsigned char *)c.data + row0 * (uint64_t)c.bytes,
+                  PIPE_TILE * (uint32_t)c.bytes, bar);
+    }
+}
+
+// A consumer warp copies a partial tile's rows into its stage.
+__device__ __noinline__ void pipe_copy_partial(const DevQuery &q, const PipePlan &pp, uint64_t row0, uint32_t rows,
+                                               unsigned char *stage) {
+    const int lane = threadIdx.x & 31;
     for (uint32_t i = 0; i < pp.n_cols; ++i) {
         const DevCol &c = q.cols[pp.col[i]];
         const uint32_t n = rows * (uint32_t)c.bytes;
@@ -89,9 +94,7 @@ __device__ __noinline__ void pipe_issue(const DevQuery &q, const PipePlan &pp, u
             for (uint32_t b = lane; b < n; b += 32) dst[b] = __ldg(src + b);
         }
     }
-    __threadfence_block();
     __syncwarp();
-    if (lane == 0) mbar_arrive(bar);
 }
 
 __device__ __forceinline__ int64_t st_int(const DevCol &c, const unsigned char *p, uint32_t r) {
@@ -108,19 +111,58 @@ __device__ __forceinline__ double st_f64(const DevCol &c, const unsigned char *p
     return ((const double *)p)[r];
 }
 
+// Where a tile row's key and inputs sit in a stage (offsets and widths read
+// once per kernel, not per row).
+template <class P>
+struct TileLayout {
+    uint32_t key_off, key_bytes;
+    uint64_t key_mask;
+    uint32_t val_off[P::NV], val_bytes[P::NV];
+};
+
+template <class P>
+__device__ __forceinline__ TileLayout<P> tile_layout(const DevQuery &q, const PipePlan &pp) {
+    TileLayout<P> L;
+    const DevKeyPart &kp = q.parts[0];
+    L.key_off = pp.off[pp.slot[kp.col]];
+    L.key_bytes = (uint32_t)q.cols[kp.col].bytes;
+    L.key_mask = kp.payload < 64 ? (1ULL << kp.payload) - 1 : ~0ULL;
+#pragma unroll
+    for (int a = 0; a < P::NV; ++a) {
+        L.val_off[a] = 0;
+        L.val_bytes[a] = 8;
+        if (a < P::NA_) {
+            const int col = q.faggs[a].col;
+            L.val_off[a] = pp.off[pp.slot[col]];
+            L.val_bytes[a] = (uint32_t)q.cols[col].bytes;
+        }
+    }
+    return L;
+}
+
+// Sign-extended integer of `bytes` width at index r of p (BOOLEAN columns
+// never reach the compiled folds' inputs or one-part keys as signed: their
+// payload mask keeps the low bit).
+__device__ __forceinline__ int64_t ld_int(const unsigned char *p, uint32_t bytes, uint32_t r) {
+    switch (bytes) {
+        case 1: return (int64_t)(int8_t)p[r];
+        case 2: return (int64_t)((const int16_t *)p)[r];
+        case 4: return (int64_t)((const int32_t *)p)[r];
+        default: return ((const int64_t *)p)[r];
+    }
+}
+
 // Tile row r as the fold's row: packed key and inputs read from the stage.
 template <class P>
-__device__ __forceinline__ void pipe_row(const DevQuery &q, const PipePlan &pp, const unsigned char *stage, uint32_t r,
-                                         typename P::Row &rv) {
+__device__ __forceinline__ void pipe_row(const DevQuery &q, const PipePlan &pp, const TileLayout<P> &L,
+                                         const unsigned char *stage, uint32_t r, typename P::Row &rv) {
     rv = typename P::Row{};
     rv.k0 = 0;
     rv.k1 = 0;
 #pragma unroll
     for (int a = 0; a < P::NV; ++a) rv.val[a] = 0;
     if (P::KM_ == 1) {
-        const DevKeyPart &kp = q.parts[0];
-        const uint64_t raw = (uint64_t)st_int(q.cols[kp.col], stage + pp.off[pp.slot[kp.col]], r);
-        rv.k0 = kp.payload < 64 ? (raw & ((1ULL << kp.payload) - 1)) : raw;
+        rv.k0 = (uint64_t)ld_int(stage + L.key_off, L.key_bytes, r) & L.key_mask;
     } else {
         for (int i = 0; i < q.n_parts; ++i) {
             const DevKeyPart &kp = q.parts[i];
@@ -137,9 +179,11 @@ __device__ __forceinline__ void pipe_row(const DevQuery &q, const PipePlan &pp, 
     }
 #pragma unroll
     for (int a = 0; a < P::NA_; ++a) {
-        const int col = q.faggs[a].col;
-        const unsigned char *p = stage + pp.off[pp.slot[col]];
-        rv.val[a] = P::is_f(a) ? f64_bits(st_f64(q.cols[col], p, r)) : (uint64_t)st_int(q.cols[col], p, r);
+        const unsigned char *p = stage + L.val_off[a];
+        if (P::is_f(a))
+            rv.val[a] = L.val_bytes[a] == 4 ? f64_bits((double)((const float *)p)[r]) : ((const uint64_t *)p)[r];
+        else
+            rv.val[a] = (uint64_t)ld_int(p, L.val_bytes[a], r);
     }
 }
 
@@ -175,7 +219,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1)
     extern __shared__ __align__(128) unsigned char smem[];
     using Row = typename P::Row;
     static_assert(sizeof(Row) <= 24 + 8 * P::NV, "survivor rings sized in pipe_plan");
-    const uint32_t D = pp.depth;
+    const uint32_t D = 1u << pp.log_depth, DM = D - 1;
     uint64_t *full = (uint64_t *)(smem + pp.bar_off);
     uint64_t *empty = full + NCW * D;
     PipeCtl &ctl = *(PipeCtl *)(smem + pp.ctl_off);
@@ -191,7 +235,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1)
 
     if (threadIdx.x == 0) {
         for (uint32_t s = 0; s < NCW * D; ++s) {
-            mbar_init_n(&full[s], 1);   // the producer's arrive(.expect_tx)
+            mbar_init_n(&full[s], 1);   // the producer lane's arrive(.expect_tx)
             mbar_init_n(&empty[s], 1);  // the consumer's lane 0
         }
         mbar_init_fence();
@@ -203,27 +247,25 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1)
     unsigned long long selected = 0;
     if (warp == NCW) {
         // ---------------------------------------------------------- producer
-        uint32_t issued[NCW];
-#pragma unroll
-        for (int w = 0; w < NCW; ++w) issued[w] = 0;
+        // lane w keeps consumer w's slots filled; the lanes poll their own
+        // `empty` barriers side by side, so no consumer waits on another
+        const int w = lane;
+        const uint32_t nw = w < NCW ? n_of(w) : 0u;
+        uint32_t j = 0;
         long long last = clock64();
         for (;;) {
-            bool pending = false, progress = false;
-#pragma unroll
-            for (int w = 0; w < NCW; ++w) {
-                const uint32_t j = issued[w];
-                if (j >= n_of(w)) continue;
-                pending = true;
-                const uint32_t slot = w * D + j % D;
-                int free_slot = j < D;
-                if (!free_slot) free_slot = __shfl_sync(FULL, lane == 0 ? (int)mbar_test(&empty[slot], (j / D - 1) & 1u) : 0, 0);
-                if (!free_slot) continue;
-                pipe_issue(q, pp, blockIdx.x + (w + j * NCW) * G, ring + (size_t)slot * pp.stage_bytes, &full[slot]);
-                issued[w] = j + 1;
-                progress = true;
+            bool did = false;
+            if (j < nw) {
+                const uint32_t slot = w * D + (j & DM);
+                if (j < D || mbar_test(&empty[slot], ((j >> pp.log_depth) - 1) & 1u)) {
+                    pipe_issue(q, pp, blockIdx.x + (w + j * NCW) * G, ring + (size_t)slot * pp.stage_bytes,
+                               &full[slot]);
+                    ++j;
+                    did = true;
+                }
             }
-            if (!pending) break;
-            if (progress) {
+            if (!__any_sync(FULL, j < nw)) break;
+            if (__any_sync(FULL, did)) {
                 last = clock64();
                 continue;
             }
@@ -236,20 +278,19 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1)
                 break;
             }
         }
-#pragma unroll
-        for (int w = 0; w < NCW; ++w)
-            if (lane == w) ctl.issued[w] = issued[w];
+        if (w < NCW) ctl.issued[w] = j;
     } else {
         // --------------------------------------------------------- consumer
         const int w = warp;
         const uint32_t nw = n_of(w);
+        const TileLayout<P> L = tile_layout<P>(q, pp);
         Row *queue = (Row *)(smem + pp.queue_off) + (size_t)w * PQ;
         uint32_t qhead = 0, qcount = 0;
-        const unsigned char *pred_off = nullptr;
+        const uint32_t pred_off = q.n_preds ? pp.off[pp.slot[q.preds[0].col]] : 0u;
         uint32_t j = 0;
         for (; j < nw; ++j) {
-            const uint32_t slot = w * D + j % D;
-            if (!pipe_wait(&full[slot], (j / D) & 1u, limit, &ctl.stop)) {
+            const uint32_t slot = w * D + (j & DM);
+            if (!pipe_wait(&full[slot], (j >> pp.log_depth) & 1u, limit, &ctl.stop)) {
                 if (lane == 0 && !*(volatile int *)&ctl.stop) {
                     atomicOr(q.status, ST_WAIT_TIMEOUT);
                     ctl.stop = 1;
@@ -266,21 +307,22 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1)
                     break;
                 }
             }
-            const unsigned char *stage = ring + (size_t)slot * pp.stage_bytes;
+            unsigned char *stage = ring + (size_t)slot * pp.stage_bytes;
             uint64_t row0;
             uint32_t rows;
             pipe_tile_rows(q, pp, blockIdx.x + (w + j * NCW) * G, row0, rows);
+            if (rows != PIPE_TILE) pipe_copy_partial(q, pp, row0, rows, stage);
             if (q.n_preds) {
-                pred_off = stage + pp.off[pp.slot[q.preds[0].col]];
+                const unsigned char *pred = stage + pred_off;
                 for (uint32_t u = 0; u < rows; u += 32) {
                     const uint32_t r = u + lane;
-                    const bool pass = r < rows && pipe_pass(q, pred_off, r);
+                    const bool pass = r < rows && pipe_pass(q, pred, r);
                     const unsigned m = __ballot_sync(FULL, pass);
                     if (m == 0) continue;
                     selected += lane == 0 ? __popc(m) : 0;
                     if (pass) {
                         Row rv;
-                        pipe_row<P>(q, pp, stage, r, rv);
+                        pipe_row<P>(q, pp, L, stage, r, rv);
                         P::prefetch(q, rv, true);
                         queue[(qhead + qcount + __popc(m & ((1u << lane) - 1))) & (PQ - 1)] = rv;
                     }
@@ -302,7 +344,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1)
                 // before batch u folds; the slot is released after the last
                 Row cur;
                 bool me = lane < rows;
-                if (me) pipe_row<P>(q, pp, stage, lane, cur);
+                if (me) pipe_row<P>(q, pp, L, stage, lane, cur);
                 else cur = Row{};
                 P::prefetch(q, cur, me);
                 for (uint32_t u = 0; u < rows; u += 32) {
@@ -310,7 +352,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1)
                     Row nxt;
                     const uint32_t rn = u + 32 + lane;
                     const bool me_n = rn < rows;
-                    if (me_n) pipe_row<P>(q, pp, stage, rn, nxt);
+                    if (me_n) pipe_row<P>(q, pp, L, stage, rn, nxt);
                     else nxt = Row{};
                     P::prefetch(q, nxt, me_n);
                     if (u + 32 >= rows) {
@@ -338,7 +380,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1)
             const bool me = lane < (int)qcount;
             if (!me) rv = Row{};
             P::reserve(q, rv, me);
-            P::fold(q, sm, rv, qcount >= 32 ? FULL : ((1u << qcount) - 1));
+            P::fold(q, sm, rv, (1u << qcount) - 1);
         }
     }
     __syncthreads();
@@ -347,7 +389,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1)
         // the built-in limit, whatever the query's: the copies are real and land)
         for (int w = 0; w < NCW; ++w)
             for (uint32_t j = ctl.consumed[w]; j < ctl.issued[w]; ++j)
-                (void)mbar_wait(&full[w * D + j % D], (j / D) & 1u);
+                (void)mbar_wait(&full[w * D + (j & DM)], (j >> pp.log_depth) & 1u);
     }
     if (q.cache_slots) {
         __syncthreads();
@@ -416,8 +458,8 @@ bool pipe_plan(DevQuery &q, uint64_t tile_count, PipePlan *pp) {
     p.queue_off = (p.cache_off + cache_bytes(cache_slots) + 127) & ~127u;
     p.ring_off = (p.queue_off + queue_bytes + 127) & ~127u;
     if (p.ring_off + 2 * NCW * p.stage_bytes > budget) return false;
-    p.depth = std::min<uint32_t>(4, (budget - p.ring_off) / (NCW * p.stage_bytes));
-    p.smem_bytes = p.ring_off + p.depth * NCW * p.stage_bytes;
+    p.log_depth = (budget - p.ring_off) / (NCW * p.stage_bytes) >= 4 ? 2 : 1;  // 4 or 2 slots per consumer
+    p.smem_bytes = p.ring_off + (NCW << p.log_depth) * p.stage_bytes;
     static_assert(sizeof(PipeCtl) <= 256, "control block fits before the barriers");
     q.cache_slots = cache_slots;
     q.cache_probe = cache_probe;

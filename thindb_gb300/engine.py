@@ -462,7 +462,7 @@ class Query:
         strings (None for a NULL key)."""
         out = self.collect(capacity)
         for i, c in enumerate(self.schema):
-            if c.type != abi.DICT32 or i >= len(self.request.group_cols):
+            if c.type != abi.DICT32:  # only group keys come out as DICT32 (string aggregates decline)
                 continue
             vals, ok = out[c.name]
             strs = self.key_strings(i, np.where(ok, vals, 0) if ok is not None else vals)

@@ -39,6 +39,8 @@ def table_inputs(workload: str, n: int, pinned: bool = True) -> list:
     def buf(count, dtype):
         return torch.empty(count, dtype=dtype, pin_memory=pinned)
 
+    if workload == "topcount":
+        return table_inputs("filtered", n, pinned)[:1]
     if workload in ("filtered", "batched"):
         k, a, d = buf(n, torch.int64), buf(n, torch.int64), buf(n, torch.int32)
         datagen.filtered_into(n, 2, datagen.FILTERED_KEYS, k.data_ptr(), a.data_ptr(), d.data_ptr())
@@ -72,6 +74,10 @@ def workload_request(workload: str, flags: int = 0, stream: int = 0) -> Request:
         return Request(["k"], [AggSpec("count", None, "c"), AggSpec("sum", "amount", "s"),
                                AggSpec("avg", "amount", "a")], [SortSpec("s", True)], limit=10,
                        where=[Pred("d", "between", datagen.FILTER_LO, datagen.FILTER_HI)], flags=flags, stream=stream)
+    if workload == "topcount":
+        # the filtered table's Zipf key, every row: the heaviest ten groups
+        return Request(["k"], [AggSpec("count", None, "c")], [SortSpec("c", True)], limit=10, flags=flags,
+                       stream=stream)
     if workload == "plain":
         return Request(["k"], [AggSpec("count", None, "c"), AggSpec("sum", "v", "s"), AggSpec("min", "v", "mn"),
                                AggSpec("max", "v", "mx")], flags=flags, stream=stream)
