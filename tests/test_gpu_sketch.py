@@ -5,9 +5,31 @@ prove its answer — always equal to the oracle, which groups every row."""
 import numpy as np
 import pytest
 
-from test_gpu_parity import run_both
+import oracle
+from helpers import compare_results
 from thindb_gb300 import abi, datagen
-from thindb_gb300.engine import AggSpec, Column, Pred, Request, SortSpec
+from thindb_gb300.engine import AggSpec, Column, Pred, Request, SortSpec, Table, try_build_group_topn
+
+
+def run_both(cols, req):
+    """The page against the oracle's (which groups every row).  With the
+    sketch's filter pass the engine creates only the kept groups, so its
+    group count is compared only when every row was grouped."""
+    t = Table(cols)
+    q = try_build_group_topn(t, req)
+    assert q is not None
+    got = q.collect()
+    st = q.stats()
+    q.close()
+    t.close()
+    want = oracle.run(oracle.HostTable(cols), req, threads=4)
+    compare_results(got, want, len(req.group_cols), ordered=True)
+    assert st.rows_selected == want["__selected__"]
+    if not st.flags & abi.STAT_COUNT_SKETCH:
+        assert st.groups == want["__groups__"]
+    else:
+        assert st.groups < want["__groups__"]
+    return got, st
 
 pytestmark = pytest.mark.gpu
 SK = abi.FLAG_COUNT_SKETCH
@@ -24,11 +46,14 @@ def topcount(limit=10, offset=0, where=(), flags=SK, more=()):
                    where=list(where), flags=flags)
 
 
-@pytest.mark.parametrize("limit,offset", [(10, 0), (1, 0), (100, 23), (1000, 24)])
-def test_sketch_zipf_top_counts(limit, offset):
+# (LIMIT 1000 OFFSET 24 over 3M rows: the 1,024th group's count is about
+# the collision noise of a counter, so most counters would be kept: declines)
+@pytest.mark.parametrize("limit,offset,answered", [(10, 0, True), (1, 0, True), (100, 23, True),
+                                                   (1000, 24, False)])
+def test_sketch_zipf_top_counts(limit, offset, answered):
     cols = zipf_cols(3_000_000, 1_000_000)
     _, st = run_both(cols, topcount(limit, offset))
-    assert st.flags & abi.STAT_COUNT_SKETCH, "the sketch's filter pass should have answered"
+    assert bool(st.flags & abi.STAT_COUNT_SKETCH) == answered
     assert st.result_rows == limit
 
 

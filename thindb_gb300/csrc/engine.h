@@ -295,7 +295,7 @@ struct PipePlan {
     int32_t col[MAX_QCOLS];      // query column of staged column i
     uint32_t off[MAX_QCOLS];     // its byte offset inside a stage
     int32_t slot[MAX_QCOLS];     // staged index of query column c, -1 = not staged
-    uint32_t ctl_off, bar_off, cache_off, queue_off, ring_off, smem_bytes;
+    uint32_t ctl_off, bar_off, cache_off, queue_off, list_off, ring_off, smem_bytes;
 };
 // Plan the pipelined scan for q (its cache_slots may shrink to fit); false
 // if the query does not qualify (compiled fold, NOT NULL 16-byte aligned

@@ -170,14 +170,15 @@ __device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
 
 // Slot of `key` in the global table, inserting it if absent.  Slot `cap`
 // holds the all-zero key (zero is the empty marker).
-__device__ uint64_t global_slot(const DevQuery &q, uint64_t k0, uint64_t k1) {
+// (hk = hash_key(k0, k1), computed once by the caller)
+__device__ uint64_t global_slot(const DevQuery &q, uint64_t k0, uint64_t k1, uint64_t hk) {
     const uint64_t mask = q.cap - 1;
     if (k0 == 0 && k1 == 0) {
         uint32_t w = (uint32_t)(q.cap >> 5), b = 1u << (q.cap & 31);
         if (!(*((volatile uint32_t *)q.occ + w) & b)) atomicOr(q.occ + w, b);
         return q.cap;
     }
-    uint64_t h = hash_key(k0, k1) & mask;
+    uint64_t h = hk & mask;
     if (q.key_words == 1) {
         for (unsigned p = 0; p < MAX_PROBE; ++p) {
             unsigned long long *sp = q.table + h * (uint64_t)q.slot_words;
@@ -210,6 +211,10 @@ __device__ uint64_t global_slot(const DevQuery &q, uint64_t k0, uint64_t k1) {
     }
     atomicOr(q.status, ST_TABLE_FULL);
     return NO_GID;
+}
+
+__device__ __forceinline__ uint64_t global_slot(const DevQuery &q, uint64_t k0, uint64_t k1) {
+    return global_slot(q, k0, k1, hash_key(k0, k1));
 }
 
 // Insert (gid, value bits) into a distinct set; true when the pair is new.
@@ -441,10 +446,12 @@ __device__ __forceinline__ void cache_init(const DevQuery &q, const ScanSmem &sm
 
 // Find or claim the cache entry of a non-zero one-word key; -1 when the
 // bounded probe finds neither (the caller folds into the global table).
-__device__ __forceinline__ int cache_find(const DevQuery &q, const ScanSmem &sm, uint64_t k, bool &claimed) {
+// (hk = hash_key(k, 0), computed once by the caller)
+__device__ __forceinline__ int cache_find(const DevQuery &q, const ScanSmem &sm, uint64_t k, uint64_t hk,
+                                          bool &claimed) {
     const int C = q.cache_slots;
     const int limit = q.cache_probe;
-    uint32_t h = (uint32_t)hash_key(k, 0) & (C - 1);
+    uint32_t h = (uint32_t)hk & (C - 1);
     claimed = false;
     for (int p = 0; p < limit; ++p) {
         unsigned long long cur = sm.ckeys[h];
@@ -539,25 +546,10 @@ __device__ __forceinline__ void load_row(const DevQuery &q, uint64_t row, bool m
     }
 }
 
-// The count sketch's filter pass: lanes whose key's counter is not kept
-// drop out of the fold (the whole active mask when the sketch is off).
-__device__ __forceinline__ unsigned sketch_keep(const DevQuery &q, uint64_t k0, uint64_t k1, unsigned active) {
-    if (!q.sk_keep || !__ldg(q.sk_on)) return active;
-    const int lane = threadIdx.x & 31;
-    bool me = (active >> lane) & 1u;
-    if (me) {
-        const uint32_t c = (uint32_t)(hash_key(k0, k1) >> (64 - SK_BITS));
-        me = (__ldg(q.sk_keep + (c >> 5)) >> (c & 31)) & 1u;
-    }
-    return __ballot_sync(FULL, me);
-}
-
 // Fold up to 32 gathered rows (bit i of `active` = lane i holds one).  One
 // out-of-line copy keeps the instruction footprint small.
 template <int NA>
 __device__ __noinline__ void fold_batch(const DevQuery &q, const ScanSmem sm, const RowVals<NA> &in, unsigned active) {
-    active = sketch_keep(q, in.k0, in.k1, active);
-    if (!active) return;
     const int lane = threadIdx.x & 31;
     const bool me = (active >> lane) & 1u;
     uint64_t val[NA];
@@ -606,14 +598,15 @@ __device__ __noinline__ void fold_batch(const DevQuery &q, const ScanSmem sm, co
         bool done = false;
         if (q.cache_slots && q.key_words == 1 && k0 != 0) {
             bool claimed;
-            int e = cache_find(q, sm, k0, claimed);
+            const uint64_t hk = hash_key(k0, 0);
+            int e = cache_find(q, sm, k0, hk, claimed);
             if (e >= 0) {
                 if (claimed) {
-                    gid = (uint32_t)global_slot(q, k0, 0);
+                    gid = (uint32_t)global_slot(q, k0, 0, hk);
                     sm.cgid[e] = gid;
                 } else if (q.needs_gid) {
                     gid = *((volatile uint32_t *)sm.cgid + e);
-                    if (gid == NO_GID) gid = (uint32_t)global_slot(q, k0, 0);
+                    if (gid == NO_GID) gid = (uint32_t)global_slot(q, k0, 0, hk);
                 }
                 apply_states<NA>(q, sm.cstate + (size_t)e * q.state_words, true, acc);
                 done = true;
@@ -708,11 +701,22 @@ __device__ __forceinline__ bool row_passes(const DevQuery &q, uint64_t r) {
 // whose groups all live in shared memory.
 __device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
-__device__ __forceinline__ uint64_t prefetch_slot(const DevQuery &q, uint64_t k0, uint64_t k1, bool me) {
-    const uint64_t hk = hash_key(k0, k1);
+// The count sketch's filter pass (sketch.cu): whether a row of key hash hk
+// folds (always, without a sketch or when it declined).
+__device__ __forceinline__ bool sketch_kept(const DevQuery &q, uint64_t hk) {
+    if (!q.sk_keep || !__ldg(q.sk_on)) return true;
+    const uint32_t c = (uint32_t)(hk >> (64 - SK_BITS));
+    return (__ldg(q.sk_keep + (c >> 5)) >> (c & 31)) & 1u;
+}
+
+// Prefetch a row's slot (lane `me` holds a row); returns whether the row
+// folds — false for a row the count sketch drops, whose slot is not touched.
+__device__ __forceinline__ bool prefetch_slot(const DevQuery &q, uint64_t k0, uint64_t k1, bool me, uint64_t &hk) {
+    hk = hash_key(k0, k1);
+    me = me && sketch_kept(q, hk);
     if (me && (q.prefetch & PF_SLOT) && !(q.cache_slots && q.cache_probe == q.cache_slots))
         prefetch_l2(q.table + (hk & (q.cap - 1)) * (uint64_t)q.slot_words);
-    return hk;
+    return me;
 }
 
 // ------------------------------------------------------ fold policies --
@@ -730,8 +734,9 @@ struct GenericFold {
     __device__ __forceinline__ static void fold(const DevQuery &q, const ScanSmem &sm, const Row &rv, unsigned act) {
         fold_batch<NA>(q, sm, rv, act);
     }
-    __device__ __forceinline__ static void prefetch(const DevQuery &q, const Row &rv, bool me) {
-        (void)prefetch_slot(q, rv.k0, rv.k1, me);
+    __device__ __forceinline__ static bool prefetch(const DevQuery &q, const Row &rv, bool me) {
+        uint64_t hk;
+        return prefetch_slot(q, rv.k0, rv.k1, me, hk);
     }
     __device__ __forceinline__ static void reserve(const DevQuery &, Row &, bool) {}
 };
@@ -804,8 +809,10 @@ struct FastFold {
         }
     }
 
-    __device__ __forceinline__ static void prefetch(const DevQuery &q, const Row &rv, bool me) {
-        const uint64_t hk = prefetch_slot(q, rv.k0, rv.k1, me);
+    // returns whether the row folds (prefetch_slot)
+    __device__ __forceinline__ static bool prefetch(const DevQuery &q, const Row &rv, bool me) {
+        uint64_t hk;
+        me = prefetch_slot(q, rv.k0, rv.k1, me, hk);
         if (DISTINCT && me && (q.prefetch & PF_DISTINCT) && !q.dpart_bits) {
 #pragma unroll
             for (int a = 0; a < NA; ++a)
@@ -814,6 +821,7 @@ struct FastFold {
                     prefetch_l2(q.dset[d] + 2 * distinct_home(q, d, hk, rv.val[a]));
                 }
         }
+        return me;
     }
 
     // Partitioned COUNT(DISTINCT): reserve each row's pair place as soon as
@@ -859,8 +867,6 @@ struct FastFold {
     }
 
     __device__ __noinline__ static void fold(const DevQuery &q, const ScanSmem sm, const Row in, unsigned active) {
-        active = sketch_keep(q, in.k0, in.k1, active);
-        if (!active) return;
         const int lane = threadIdx.x & 31;
         const bool me = (active >> lane) & 1u;
         uint64_t val[NV];
@@ -939,23 +945,24 @@ struct FastFold {
         if (leader) {
             unsigned long long *st = nullptr;
             bool st_smem = false;
+            const uint64_t hk = hash_key(k0, k1);  // once for the shared and the global probe
             if (q.cache_slots && q.key_words == 1 && k0 != 0) {
                 bool claimed;
-                const int e = cache_find(q, sm, k0, claimed);
+                const int e = cache_find(q, sm, k0, hk, claimed);
                 if (e >= 0) {
                     if (claimed) {
-                        gid = (uint32_t)global_slot(q, k0, 0);
+                        gid = (uint32_t)global_slot(q, k0, 0, hk);
                         sm.cgid[e] = gid;
                     } else if (DISTINCT) {
                         gid = *((volatile uint32_t *)sm.cgid + e);
-                        if (gid == NO_GID) gid = (uint32_t)global_slot(q, k0, 0);
+                        if (gid == NO_GID) gid = (uint32_t)global_slot(q, k0, 0, hk);
                     }
                     st = sm.cstate + (size_t)e * q.state_words;
                     st_smem = true;
                 }
             }
             if (!st) {
-                gid = (uint32_t)global_slot(q, k0, k1);
+                gid = (uint32_t)global_slot(q, k0, k1, hk);
                 if (gid != NO_GID) st = q.table + (uint64_t)gid * q.slot_words + q.key_words;
             }
             if (st) {
@@ -1035,14 +1042,15 @@ __device__ __forceinline__ void scan_chunk(const DevQuery &q, const ScanSmem &sm
                 const uint64_t r = base + 32 * j + lane;
                 act[j] = __ballot_sync(FULL, r < row_end && row_passes(q, r));
             }
+            unsigned keep[L];  // rows that fold (the WHERE's, less any the count sketch drops)
 #pragma unroll
-            for (int j = 0; j < L; ++j) P::prefetch(q, rows[j], (act[j] >> lane) & 1u);
+            for (int j = 0; j < L; ++j) keep[j] = __ballot_sync(FULL, P::prefetch(q, rows[j], (act[j] >> lane) & 1u));
 #pragma unroll
-            for (int j = 0; j < L; ++j) P::reserve(q, rows[j], (act[j] >> lane) & 1u);
+            for (int j = 0; j < L; ++j) P::reserve(q, rows[j], (keep[j] >> lane) & 1u);
 #pragma unroll
             for (int j = 0; j < L; ++j) {
                 selected += (lane == 0) ? __popc(act[j]) : 0;
-                if (act[j]) P::fold(q, sm, rows[j], act[j]);
+                if (keep[j]) P::fold(q, sm, rows[j], keep[j]);
             }
         }
         return;
@@ -1090,17 +1098,14 @@ __device__ __forceinline__ void scan_chunk(const DevQuery &q, const ScanSmem &sm
             const uint32_t s = i + 32 * j + lane;
             P::load(q, row0 + list[s < n ? s : 0], s < n, rows[j]);
         }
+        unsigned keep[L];  // survivors that fold (less any the count sketch drops)
 #pragma unroll
-        for (int j = 0; j < L; ++j) P::prefetch(q, rows[j], i + 32 * j + lane < n);
+        for (int j = 0; j < L; ++j) keep[j] = __ballot_sync(FULL, P::prefetch(q, rows[j], i + 32 * j + lane < n));
 #pragma unroll
-        for (int j = 0; j < L; ++j) P::reserve(q, rows[j], i + 32 * j + lane < n);
+        for (int j = 0; j < L; ++j) P::reserve(q, rows[j], (keep[j] >> lane) & 1u);
 #pragma unroll
-        for (int j = 0; j < L; ++j) {
-            const uint32_t b = i + 32 * j;
-            if (b >= n) break;
-            const uint32_t left = n - b;
-            P::fold(q, sm, rows[j], left >= 32 ? FULL : ((1u << left) - 1));
-        }
+        for (int j = 0; j < L; ++j)
+            if (keep[j]) P::fold(q, sm, rows[j], keep[j]);
     }
 }
 
@@ -1174,11 +1179,10 @@ __device__ __forceinline__ void scan_chunk_queue(const DevQuery &q, const ScanSm
             const unsigned m = __ballot_sync(FULL, pass[j]);
             if (m == 0) continue;
             selected += (lane == 0) ? __popc(m) : 0;
-            if (pass[j]) {
-                wq.ring[(wq.head + wq.count + __popc(m & ((1u << lane) - 1))) & (WQ_ROWS - 1)] = rows[j];
-                P::prefetch(q, rows[j], true);
-            }
-            wq.count += __popc(m);
+            const bool kp = P::prefetch(q, rows[j], pass[j]);
+            const unsigned mk = __ballot_sync(FULL, kp);
+            if (kp) wq.ring[(wq.head + wq.count + __popc(mk & ((1u << lane) - 1))) & (WQ_ROWS - 1)] = rows[j];
+            wq.count += __popc(mk);
             wq_fold_full<P>(q, sm, wq);
         }
     }

@@ -39,6 +39,7 @@ namespace {
 
 constexpr int NCW = PIPE_CWARPS;
 constexpr uint32_t PQ = 64;  // survivor ring rows per consumer warp (< 32 left + one 32-row step)
+static_assert(PIPE_TILE <= 256, "survivor offsets of a tile are bytes");
 
 struct PipeCtl {
     int stop;
@@ -285,6 +286,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1)
         const uint32_t nw = n_of(w);
         const TileLayout<P> L = tile_layout<P>(q, pp);
         Row *queue = (Row *)(smem + pp.queue_off) + (size_t)w * PQ;
+        uint8_t *list = smem + pp.list_off + (size_t)w * PIPE_TILE;  // survivor offsets of the current tile
         uint32_t qhead = 0, qcount = 0;
         const uint32_t pred_off = q.n_preds ? pp.off[pp.slot[q.preds[0].col]] : 0u;
         uint32_t j = 0;
@@ -313,20 +315,28 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1)
             pipe_tile_rows(q, pp, blockIdx.x + (w + j * NCW) * G, row0, rows);
             if (rows != PIPE_TILE) pipe_copy_partial(q, pp, row0, rows, stage);
             if (q.n_preds) {
+                // the tile's survivors: their offsets first (ballot + popc),
+                // then their rows built and queued 32 at a time (every lane
+                // busy), folding each full batch of 32 queued rows
                 const unsigned char *pred = stage + pred_off;
+                uint32_t n = 0;
                 for (uint32_t u = 0; u < rows; u += 32) {
                     const uint32_t r = u + lane;
                     const bool pass = r < rows && pipe_pass(q, pred, r);
                     const unsigned m = __ballot_sync(FULL, pass);
-                    if (m == 0) continue;
-                    selected += lane == 0 ? __popc(m) : 0;
-                    if (pass) {
-                        Row rv;
-                        pipe_row<P>(q, pp, L, stage, r, rv);
-                        P::prefetch(q, rv, true);
-                        queue[(qhead + qcount + __popc(m & ((1u << lane) - 1))) & (PQ - 1)] = rv;
-                    }
-                    qcount += __popc(m);
+                    if (pass) list[n + __popc(m & ((1u << lane) - 1))] = (uint8_t)r;
+                    n += __popc(m);
+                }
+                __syncwarp();
+                selected += lane == 0 ? n : 0;
+                for (uint32_t b = 0; b < n; b += 32) {
+                    const uint32_t i = b + lane;
+                    Row rv{};
+                    if (i < n) pipe_row<P>(q, pp, L, stage, list[i], rv);
+                    const bool kp = P::prefetch(q, rv, i < n);  // less any row the count sketch drops
+                    const unsigned mk = __ballot_sync(FULL, kp);
+                    if (kp) queue[(qhead + qcount + __popc(mk & ((1u << lane) - 1))) & (PQ - 1)] = rv;
+                    qcount += __popc(mk);
                     if (qcount >= 32) {
                         __syncwarp();
                         Row rv = queue[(qhead + lane) & (PQ - 1)];
@@ -346,24 +356,25 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1)
                 bool me = lane < rows;
                 if (me) pipe_row<P>(q, pp, L, stage, lane, cur);
                 else cur = Row{};
-                P::prefetch(q, cur, me);
+                bool kp = P::prefetch(q, cur, me);  // less any row the count sketch drops
                 for (uint32_t u = 0; u < rows; u += 32) {
-                    const unsigned act = __ballot_sync(FULL, me);
+                    const unsigned act = __ballot_sync(FULL, me), keep = __ballot_sync(FULL, kp);
                     Row nxt;
                     const uint32_t rn = u + 32 + lane;
                     const bool me_n = rn < rows;
                     if (me_n) pipe_row<P>(q, pp, L, stage, rn, nxt);
                     else nxt = Row{};
-                    P::prefetch(q, nxt, me_n);
+                    const bool kp_n = P::prefetch(q, nxt, me_n);
                     if (u + 32 >= rows) {
                         __syncwarp();
                         if (lane == 0) mbar_arrive(&empty[slot]);
                     }
                     selected += lane == 0 ? __popc(act) : 0;
-                    P::reserve(q, cur, me);
-                    P::fold(q, sm, cur, act);
+                    P::reserve(q, cur, kp);
+                    if (keep) P::fold(q, sm, cur, keep);
                     cur = nxt;
                     me = me_n;
+                    kp = kp_n;
                 }
                 if (rows == 0) {
                     __syncwarp();
@@ -446,7 +457,9 @@ bool pipe_plan(DevQuery &q, uint64_t tile_count, PipePlan *pp) {
     const uint32_t queue_bytes = q.n_preds ? NCW * PQ * row_bytes : 0;
     auto cache_bytes = [&](int c) { return (uint32_t)c * (12u + 8u * (uint32_t)q.state_words); };
     const uint32_t fixed = 256 + 2 * NCW * 8 * 4;  // control + up to 4 slots per consumer
-    while (cache_slots > 0 && fixed + cache_bytes(cache_slots) + queue_bytes + 2 * NCW * p.stage_bytes > budget) {
+    const uint32_t list_bytes = q.n_preds ? NCW * PIPE_TILE : 0;
+    while (cache_slots > 0 &&
+           fixed + cache_bytes(cache_slots) + queue_bytes + list_bytes + 2 * NCW * p.stage_bytes + 256 > budget) {
         const bool resident = cache_probe == cache_slots;
         cache_slots >>= 1;
         cache_probe = resident ? 16 : std::min(cache_probe, cache_slots);
@@ -456,7 +469,8 @@ bool pipe_plan(DevQuery &q, uint64_t tile_count, PipePlan *pp) {
     p.bar_off = 256;
     p.cache_off = p.bar_off + 2 * NCW * 4 * 8;
     p.queue_off = (p.cache_off + cache_bytes(cache_slots) + 127) & ~127u;
-    p.ring_off = (p.queue_off + queue_bytes + 127) & ~127u;
+    p.list_off = p.queue_off + queue_bytes;
+    p.ring_off = (p.list_off + (q.n_preds ? NCW * PIPE_TILE : 0) + 127) & ~127u;
     if (p.ring_off + 2 * NCW * p.stage_bytes > budget) return false;
     p.log_depth = (budget - p.ring_off) / (NCW * p.stage_bytes) >= 4 ? 2 : 1;  // 4 or 2 slots per consumer
     p.smem_bytes = p.ring_off + (NCW << p.log_depth) * p.stage_bytes;

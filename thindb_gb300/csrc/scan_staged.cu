@@ -212,17 +212,18 @@ __global__ void __launch_bounds__(STAGE_THREADS, 1)
             const bool pass = r < rows && (pred == nullptr || stage_pass(q, pred, r));
             const unsigned m = __ballot_sync(0xFFFFFFFFu, pass);
             if (m == 0) continue;
+            Row rv{};
+            if (pass) stage_row<P>(q, sp, stage, r, rv);
+            const bool kp = P::prefetch(q, rv, pass);  // less any row the count sketch drops
+            const unsigned mk = __ballot_sync(0xFFFFFFFFu, kp);
             uint32_t pos = 0;
             if (lane == 0) {
-                pos = atomicAdd(&queue_n, (uint32_t)__popc(m));
+                pos = mk ? atomicAdd(&queue_n, (uint32_t)__popc(mk)) : 0u;
                 selected += __popc(m);
             }
             pos = __shfl_sync(0xFFFFFFFFu, pos, 0);
-            if (pass) {
-                Row rv;
-                stage_row<P>(q, sp, stage, r, rv);
-                P::prefetch(q, rv, true);
-                const uint32_t at = pos + __popc(m & ((1u << lane) - 1));
+            if (kp) {
+                const uint32_t at = pos + __popc(mk & ((1u << lane) - 1));
                 if (at < STAGE_QCAP) queue[at] = rv;
                 else atomicOr(q.status, ST_BAD_INDEX);  // cannot happen: <= FOLD_AT - 1 + one tile
             }

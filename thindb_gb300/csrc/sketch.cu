@@ -9,9 +9,14 @@
 // bounds each of them from above.
 // Settle (one CTA): the need-th largest counter (need = OFFSET + LIMIT) by
 // radix selection; the sketch declines when that counter is within the
-// collision noise of an even spread (collisionCeiling) or when the counters
-// at or above the threshold (half the need-th largest) hold more than a
-// quarter of the rows; otherwise the keep bitmap marks those counters.
+// collision noise of an even spread (collisionCeiling) or when more than an
+// eighth of the counters reach the threshold (half the need-th largest);
+// otherwise the keep bitmap marks those counters.  (thinDB declines when
+// the kept counters hold more than a quarter of the rows,
+// MAX_KEPT_FRACTION_DENOM: its filter pass costs per row.  Here the filter
+// pass folds the rows of a few heavy groups in the shared-memory hot-key
+// table, and what it saves is the groups it never creates: few kept
+// counters, not few kept rows, make it pay.)
 // Filter pass: the regular scan folds only rows whose counter is kept (the
 // folds test the bitmap, FastFold::fold / fold_batch).  Every kept group is
 // complete and every dropped group has fewer than `threshold` rows, so once
@@ -59,11 +64,13 @@ __global__ void __launch_bounds__(1024, 1)
                          uint32_t *__restrict__ ctl) {
     __shared__ uint32_t hist[256];
     __shared__ unsigned long long tot, kept;
+    __shared__ uint32_t kept_counters;
     __shared__ uint32_t prefix_s, remaining_s, kth_s, thr_s;
     __shared__ int on_s;
     if (threadIdx.x == 0) {
         tot = 0;
         kept = 0;
+        kept_counters = 0;
         prefix_s = 0;
         remaining_s = need;
     }
@@ -107,12 +114,15 @@ __global__ void __launch_bounds__(1024, 1)
     __syncthreads();
     const uint32_t thr = thr_s;
     unsigned long long k = 0;
-    for (uint32_t i = threadIdx.x; i < SK_N; i += blockDim.x) k += counts[i] >= thr ? counts[i] : 0u;
+    uint32_t kc = 0;
+    for (uint32_t i = threadIdx.x; i < SK_N; i += blockDim.x) {
+        k += counts[i] >= thr ? counts[i] : 0u;
+        kc += counts[i] >= thr ? 1u : 0u;
+    }
     atomicAdd(&kept, k);
+    atomicAdd(&kept_counters, kc);
     __syncthreads();
-    // a filter pass keeping more than a quarter of the rows does not pay
-    // (MAX_KEPT_FRACTION_DENOM, :37)
-    const int on = on_s && kept * 4 <= tot;
+    const int on = on_s && (uint64_t)kept_counters * 8 <= SK_N;
     for (uint32_t wd = threadIdx.x; wd < SK_N / 32; wd += blockDim.x) {
         uint32_t bits = 0;
         for (int b = 0; b < 32; ++b) bits |= (on && counts[wd * 32 + b] >= thr ? 1u : 0u) << b;
