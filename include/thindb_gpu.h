@@ -272,6 +272,14 @@ typedef struct tgpu_request {
  * inputs, TGPU_FLAG_NO_COUNT_SKETCH turns it off. */
 #define TGPU_FLAG_COUNT_SKETCH 0x10000
 #define TGPU_FLAG_NO_COUNT_SKETCH 0x20000
+/* Radix-partitioned route for high-cardinality keys (thinDB's bucket
+ * staging, silo_group_core.zig:9228, :9348): rows scattered by the top bits
+ * of their key hash into partitions whose groups fit one CTA's shared
+ * memory, then folded there (compiled fold, a key of at most 64 packed
+ * bits).  By default for one COUNT(DISTINCT) over 16M+ rows and 128K+
+ * estimated groups; TGPU_FLAG_RADIX forces it, TGPU_FLAG_NO_RADIX never. */
+#define TGPU_FLAG_RADIX 0x40000
+#define TGPU_FLAG_NO_RADIX 0x80000
 
 /* ----------------------------------------------------------------- output -- */
 
@@ -325,6 +333,7 @@ typedef struct tgpu_query_stats {
 #define TGPU_STAT_PIPE 0x20     /* the pipelined (producer/consumer bulk-copy) scan ran */
 #define TGPU_STAT_COUNT_SKETCH 0x40  /* the count sketch's filter pass gave the answer */
 #define TGPU_STAT_SKETCH_RERUN 0x80  /* its filter pass could not prove the answer: every row regrouped */
+#define TGPU_STAT_RADIX 0x100   /* the radix-partitioned route ran */
 
 /* -------------------------------------------------------------- the API -- */
 

@@ -57,6 +57,8 @@ FLAG_PIPE_SCAN = 0x4000
 FLAG_NO_PIPE = 0x8000
 FLAG_COUNT_SKETCH = 0x10000
 FLAG_NO_COUNT_SKETCH = 0x20000
+FLAG_RADIX = 0x40000
+FLAG_NO_RADIX = 0x80000
 STAT_TUNED = 0x1
 STAT_GATHER = 0x2
 STAT_STAGED = 0x4
@@ -65,6 +67,7 @@ STAT_QUEUE = 0x10
 STAT_PIPE = 0x20
 STAT_COUNT_SKETCH = 0x40
 STAT_SKETCH_RERUN = 0x80
+STAT_RADIX = 0x100
 
 
 class ColumnDesc(C.Structure):

@@ -422,6 +422,10 @@ struct tgpu_query {
     bool tuned = false;           // settings taken from the tuning table
     bool staged = false;          // the staged (bulk-copy ring) scan runs this query
     bool piped = false;           // the pipelined (producer/consumer) scan runs this query
+    bool radix = false;           // the radix-partitioned route runs this query
+    RadixPlan rp{};
+    uint64_t radix_cap_req = 0;   // records per partition after an overflow (0 = from the estimate)
+    Buffer radix_buf;
     bool sketch = false;          // ORDER BY COUNT(*) DESC LIMIT k: the count sketch runs first
     bool sketch_off = false;      // an inexact filter pass switched it off for this query
     int sketch_order_agg = 0;     // the COUNT(*) aggregate it ranks by
@@ -494,6 +498,8 @@ struct tgpu_query {
         g_scratch_pool.give(dpart_cursor_buf);
         g_scratch_pool.give(dpart_pairs_buf);
         dpart_cursor_buf = dpart_pairs_buf = Buffer();
+        g_scratch_pool.give(radix_buf);
+        radix_buf = Buffer();
         for (auto &b : dset_bufs) g_set_pool.give(b);
         dset_bufs.clear();
     }
@@ -1040,6 +1046,34 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
             if (dq.aggs[a].kind == AK_DISTINCT) q->dpart_word = dq.aggs[a].word;
         dpart_bytes = ((size_t)4 << bits) + ((size_t)DPART_CAP * 16 << bits);
     }
+    // the radix route: partitions of at most ~40% of a shared table's slots
+    // in groups; the partitions' buffers sized from the rows expected to pass
+    size_t radix_bytes = 0;
+    if (q->radix) {
+        RadixPlan &rp = q->rp;
+        rp = RadixPlan{};
+        const uint64_t per = RX_SLOTS * 2 / 5;
+        uint32_t bits = 1;
+        while (bits < RX_MAX_BITS && (q->groups_est >> bits) > per) ++bits;
+        rp.bits = bits;
+        if (dq.dpart_bits && dq.dpart_bits <= (int)bits) {
+            dq.dpart_bits = (int)bits + 1;  // at least two pair sub-partitions per partition
+            dpart_bytes = ((size_t)4 << dq.dpart_bits) + ((size_t)DPART_CAP * 16 << dq.dpart_bits);
+        }
+        rp.sub_bits = dq.dpart_bits ? (uint32_t)dq.dpart_bits - bits : 0u;
+        const uint64_t rows = std::max<uint64_t>(1, q->sel_est);
+        rp.cap = q->radix_cap_req ? q->radix_cap_req : ceil_div(rows * 5, (uint64_t)4 << bits) + RX_TILE;
+        rp.tiles_per_rg = q->t->rg_rows / RX_TILE;
+        rp.n_tiles = (uint32_t)q->rg_list.size() * rp.tiles_per_rg;
+        const uint64_t words = 1 + (uint64_t)dq.n_faggs;
+        radix_bytes = ((size_t)4 << bits) + ((size_t)rp.cap << bits) * words * 8;
+        dq.cache_slots = (int32_t)RX_SLOTS;  // the aggregate kernel's per-partition table
+        dq.cache_probe = (int32_t)RX_SLOTS;
+        const uint32_t cache = RX_SLOTS * (12u + 8u * (uint32_t)dq.state_words);
+        rp.dcur_off = (cache + 16 + 15) & ~15u;
+        rp.agg_smem = rp.dcur_off + (4u << rp.sub_bits);
+        rp.agg_per_sm = rp.agg_smem * 2 <= 227u * 1024 ? 2 : 1;
+    }
     std::vector<uint64_t> dcap;
     size_t dset_bytes = 0;
     for (uint64_t need : q->dset_need) {
@@ -1088,7 +1122,7 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     const size_t o_sketch = q->sketch ? add(((size_t)1 << SK_BITS) * 4 + ((size_t)1 << SK_BITS) / 8 + 64) : 0;
     (void)row_bytes;
 
-    const size_t total = table_bytes + occ_bytes + dset_bytes + dpart_bytes + scratch;
+    const size_t total = table_bytes + occ_bytes + dset_bytes + dpart_bytes + radix_bytes + scratch;
     if (q->budget && total > q->budget)
         return fail(TGPU_ERR_MEMORY_BUDGET, "query needs " + std::to_string(total) + " device bytes, budget " +
                                                 std::to_string(q->budget));
@@ -1114,6 +1148,11 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
         dq.dpart_buf = (ulonglong2 *)q->dpart_pairs_buf.p;
         dq.dset[0] = nullptr;
         dq.dset_cap[0] = 0;
+    }
+    if (q->radix) {
+        if ((st = g_scratch_pool.take(radix_bytes, q->stream, &q->radix_buf)) != TGPU_OK) return st;
+        q->rp.cursor = (uint32_t *)q->radix_buf.p;
+        q->rp.buf = (unsigned long long *)((char *)q->radix_buf.p + ((size_t)4 << q->rp.bits));
     }
     if (scratch > q->scratch_bytes) {
         g_scratch_pool.give(q->scratch_buf);
@@ -1234,6 +1273,17 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
 // HAVING, no COUNT(DISTINCT)): the count sketch runs first, as thinDB routes
 // such a query to its two-pass top-K (v2_group_topn_engine.zig:1375,
 // count_topk_sketch.zig MAX_NEED :64), unless the input is small.
+// The radix-partitioned route: a compiled fold over a key of at most 64
+// packed bits; by default for one COUNT(DISTINCT) over many rows and groups
+// (uniform high-cardinality keys, which the hot-key table cannot absorb).
+bool radix_eligible(const tgpu_query *q) {
+    const DevQuery &dq = q->dq;
+    if (q->batched || (q->flags & TGPU_FLAG_NO_RADIX) || q->staged || q->piped || q->global_agg) return false;
+    if (dq.fast_id < 0 || dq.key_words != 1 || q->t->rg_rows % RX_TILE != 0) return false;
+    if (q->flags & TGPU_FLAG_RADIX) return true;
+    return dq.n_dsets == 1 && q->rows_scanned >= (16ULL << 20) && q->groups_est >= (1ULL << 17);
+}
+
 bool sketch_eligible(const tgpu_query *q, const tgpu_request *req) {
     if ((q->flags & TGPU_FLAG_NO_COUNT_SKETCH) || q->global_agg || req->n_order != 1 || req->n_having) return false;
     const tgpu_sort_spec &o = req->order[0];
@@ -1288,7 +1338,13 @@ tgpu_status enqueue(tgpu_query *q) {
         dq.sk_keep = nullptr;
         dq.sk_on = nullptr;
     }
-    if (q->staged) {
+    if (q->radix) {
+        DeviceCtx *dev;
+        tgpu_status dst = device_ctx(&dev);
+        if (dst != TGPU_OK) return dst;
+        CU(launch_radix(dq, q->rp, dev->sms, s));
+        q->launches += 2;
+    } else if (q->staged) {
         CU(launch_staged_scan(dq, q->sp, q->stage_grid, s));
         q->launches++;
     } else if (q->piped) {
@@ -1383,6 +1439,19 @@ tgpu_status finish(tgpu_query *q) {
             q->result_rows = 0;
             return fail(TGPU_ERR_INTERNAL, "a device bounds check failed");
         }
+        if (status & ST_PART_FULL) {
+            // a radix partition held more rows than its buffer: the cursors
+            // counted every row, so size the buffers for the largest
+            if (++q->retries > 4) return fail(TGPU_ERR_INTERNAL, "radix partitions kept overflowing");
+            std::vector<uint32_t> cur((size_t)1 << q->rp.bits);
+            CU(cudaMemcpy(cur.data(), q->rp.cursor, cur.size() * 4, cudaMemcpyDeviceToHost));
+            q->radix_cap_req = (uint64_t)*std::max_element(cur.begin(), cur.end()) + RX_TILE;
+            tgpu_status st = size_workspace(q, q->dq.cap);
+            if (st != TGPU_OK) return st;
+            st = enqueue(q);
+            if (st != TGPU_OK) return st;
+            continue;
+        }
         if (status & (ST_TABLE_FULL | ST_DISTINCT_FULL)) {
             if (++q->retries > 4) return fail(TGPU_ERR_INTERNAL, "group table kept overflowing");
             if (status & ST_TABLE_FULL) q->groups_est = std::max<uint64_t>(q->groups_est * 4, 1024);
@@ -1450,7 +1519,7 @@ tgpu_status finish(tgpu_query *q) {
               (q->dq.gather == 2 && !q->staged && !q->piped ? TGPU_STAT_QUEUE : 0) |
               (q->staged ? TGPU_STAT_STAGED : 0) | (q->piped ? TGPU_STAT_PIPE : 0) |
               (q->sketch && !q->sketch_off && (q->h_counts[6] & 0xFFFFFFFFu) ? TGPU_STAT_COUNT_SKETCH : 0) |
-              (q->sketch_reruns ? TGPU_STAT_SKETCH_RERUN : 0) |
+              (q->sketch_reruns ? TGPU_STAT_SKETCH_RERUN : 0) | (q->radix ? TGPU_STAT_RADIX : 0) |
               (q->dq.dpart_bits ? TGPU_STAT_DISTINCT_PARTITION : 0);
     s.device_bytes = q->table_buf.bytes + q->occ_buf.bytes + q->scratch_bytes;
     for (auto &b : q->dset_bufs) s.device_bytes += b.bytes;
@@ -1495,7 +1564,8 @@ void apply_tuning(tgpu_query *q, const tgpu_request *req, int batched) {
                       TGPU_FLAG_STAGED_SCAN | TGPU_FLAG_NO_STAGED | TGPU_FLAG_NO_PREFETCH |
                       TGPU_FLAG_NO_CHUNK_PREFETCH | TGPU_FLAG_DISTINCT_PREFETCH | TGPU_FLAG_DISTINCT_PARTITION |
                       TGPU_FLAG_NO_DISTINCT_PARTITION | TGPU_FLAG_QUEUE_SCAN | TGPU_FLAG_PIPE_SCAN |
-                      TGPU_FLAG_NO_PIPE | TGPU_FLAG_COUNT_SKETCH | TGPU_FLAG_NO_COUNT_SKETCH;
+                      TGPU_FLAG_NO_PIPE | TGPU_FLAG_COUNT_SKETCH | TGPU_FLAG_NO_COUNT_SKETCH |
+                      TGPU_FLAG_RADIX | TGPU_FLAG_NO_RADIX;
     const int own = modes | TGPU_FLAG_NO_TUNING;
     if (req->chunk_rows || req->cache_slots || req->table_load_pct || (req->flags & own)) return;
     const tgpu_shape s = shape_of(q, req, batched);
@@ -1734,6 +1804,7 @@ tgpu_status query_create(tgpu_table *table, const tgpu_request *req, int batched
     if (st != TGPU_OK) return st;
     apply_tuning(q.get(), req, batched);
     q->sketch = !batched && sketch_eligible(q.get(), req);
+    q->radix = !q->sketch && radix_eligible(q.get());
     q->sketch_order_agg = q->sketch ? req->order[0].index : 0;
     st = g_slab.take(&q->h_block);
     if (st != TGPU_OK) return st;

@@ -42,6 +42,7 @@ constexpr unsigned ST_DISTINCT_FULL = 2u;   // a distinct set probe ran past MAX
 constexpr unsigned ST_CANCELLED = 4u;       // the host cancel flag was seen
 constexpr unsigned ST_BAD_INDEX = 8u;       // a bounds check caught an index (never expected)
 constexpr unsigned ST_WAIT_TIMEOUT = 16u;   // a bounded wait on an asynchronous copy gave up
+constexpr unsigned ST_PART_FULL = 32u;      // a radix partition buffer overflowed: resize and rerun
 constexpr unsigned MAX_PROBE = 4096;
 
 // DevQuery::prefetch bits
@@ -311,6 +312,28 @@ constexpr uint64_t SK_MIN_ROWS = 1u << 20;
 // counts: 2^SK_BITS u32; keep: 2^SK_BITS bits; ctl: 8 u32 ([0] on, [1] threshold, ...)
 cudaError_t launch_count_sketch(const DevQuery &q, uint32_t need, uint32_t *counts, uint32_t *keep, uint32_t *ctl,
                                 int sms, cudaStream_t s);
+
+// The radix-partitioned route (radix.cu): rows are scattered by the top
+// `bits` of their key hash into 2^bits partition buffers of `cap` records
+// (packed key + the compiled fold's inputs), then each partition's groups
+// are folded by one CTA in a shared-memory table of cache_slots entries.
+constexpr uint32_t RX_TILE = 2048;
+constexpr uint32_t RX_SLOTS = 4096;       // shared-memory group slots per partition
+constexpr uint32_t RX_MAX_BITS = 10;
+struct RadixPlan {
+    uint32_t bits;                // 2^bits partitions
+    uint32_t sub_bits;            // COUNT(DISTINCT): pair sub-partitions per partition
+    uint64_t cap;                 // records per partition buffer
+    uint32_t n_tiles, tiles_per_rg;
+    unsigned long long *buf;      // partition p's records at [p * cap, (p + 1) * cap), (1 + n_faggs) words each
+    uint32_t *cursor;             // records per partition (may pass cap: ST_PART_FULL)
+    uint32_t dcur_off;            // aggregate kernel: shared-memory offset of the sub-partition cursors
+    uint32_t agg_smem;
+    uint32_t agg_per_sm;
+    uint32_t pad;
+};
+size_t radix_scatter_smem(const DevQuery &q, uint32_t bits);
+cudaError_t launch_radix(const DevQuery &q, const RadixPlan &rp, int sms, cudaStream_t s);
 
 // Partitioned COUNT(DISTINCT): pairs per partition (one CTA deduplicates a
 // partition in shared memory) and the partition's index-table slots.
