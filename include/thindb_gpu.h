@@ -276,8 +276,7 @@ typedef struct tgpu_request {
  * staging, silo_group_core.zig:9228, :9348): rows scattered by the top bits
  * of their key hash into partitions whose groups fit one CTA's shared
  * memory, then folded there (compiled fold, a key of at most 64 packed
- * bits).  By default for one COUNT(DISTINCT) over 16M+ rows and 128K+
- * estimated groups; TGPU_FLAG_RADIX forces it, TGPU_FLAG_NO_RADIX never. */
+ * bits), on request: TGPU_FLAG_RADIX; TGPU_FLAG_NO_RADIX never. */
 #define TGPU_FLAG_RADIX 0x40000
 #define TGPU_FLAG_NO_RADIX 0x80000
 

@@ -1273,15 +1273,13 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
 // HAVING, no COUNT(DISTINCT)): the count sketch runs first, as thinDB routes
 // such a query to its two-pass top-K (v2_group_topn_engine.zig:1375,
 // count_topk_sketch.zig MAX_NEED :64), unless the input is small.
-// The radix-partitioned route: a compiled fold over a key of at most 64
-// packed bits; by default for one COUNT(DISTINCT) over many rows and groups
-// (uniform high-cardinality keys, which the hot-key table cannot absorb).
+// The radix-partitioned route, on request: a compiled fold over a key of at
+// most 64 packed bits.
 bool radix_eligible(const tgpu_query *q) {
     const DevQuery &dq = q->dq;
     if (q->batched || (q->flags & TGPU_FLAG_NO_RADIX) || q->staged || q->piped || q->global_agg) return false;
     if (dq.fast_id < 0 || dq.key_words != 1 || q->t->rg_rows % RX_TILE != 0) return false;
-    if (q->flags & TGPU_FLAG_RADIX) return true;
-    return dq.n_dsets == 1 && q->rows_scanned >= (16ULL << 20) && q->groups_est >= (1ULL << 17);
+    return (q->flags & TGPU_FLAG_RADIX) != 0;
 }
 
 bool sketch_eligible(const tgpu_query *q, const tgpu_request *req) {
