@@ -711,12 +711,14 @@ __device__ __forceinline__ bool sketch_kept(const DevQuery &q, uint64_t hk) {
 
 // Prefetch a row's slot (lane `me` holds a row); returns whether the row
 // folds — false for a row the count sketch drops, whose slot is not touched.
-__device__ __forceinline__ bool prefetch_slot(const DevQuery &q, uint64_t k0, uint64_t k1, bool me, uint64_t &hk) {
-    hk = hash_key(k0, k1);
-    me = me && sketch_kept(q, hk);
-    if (me && (q.prefetch & PF_SLOT) && !(q.cache_slots && q.cache_probe == q.cache_slots))
-        prefetch_l2(q.table + (hk & (q.cap - 1)) * (uint64_t)q.slot_words);
-    return me;
+// The key is hashed only when a prefetch or the sketch needs it.
+__device__ __forceinline__ bool prefetch_slot(const DevQuery &q, uint64_t k0, uint64_t k1, bool me) {
+    const bool pf = (q.prefetch & PF_SLOT) && !(q.cache_slots && q.cache_probe == q.cache_slots);
+    if (!me || (!pf && !q.sk_keep)) return me;
+    const uint64_t hk = hash_key(k0, k1);
+    if (!sketch_kept(q, hk)) return false;
+    if (pf) prefetch_l2(q.table + (hk & (q.cap - 1)) * (uint64_t)q.slot_words);
+    return true;
 }
 
 // ------------------------------------------------------ fold policies --
@@ -735,8 +737,7 @@ struct GenericFold {
         fold_batch<NA>(q, sm, rv, act);
     }
     __device__ __forceinline__ static bool prefetch(const DevQuery &q, const Row &rv, bool me) {
-        uint64_t hk;
-        return prefetch_slot(q, rv.k0, rv.k1, me, hk);
+        return prefetch_slot(q, rv.k0, rv.k1, me);
     }
     __device__ __forceinline__ static void reserve(const DevQuery &, Row &, bool) {}
 };
@@ -811,9 +812,9 @@ struct FastFold {
 
     // returns whether the row folds (prefetch_slot)
     __device__ __forceinline__ static bool prefetch(const DevQuery &q, const Row &rv, bool me) {
-        uint64_t hk;
-        me = prefetch_slot(q, rv.k0, rv.k1, me, hk);
+        me = prefetch_slot(q, rv.k0, rv.k1, me);
         if (DISTINCT && me && (q.prefetch & PF_DISTINCT) && !q.dpart_bits) {
+            const uint64_t hk = hash_key(rv.k0, rv.k1);
 #pragma unroll
             for (int a = 0; a < NA; ++a)
                 if (kind(a) == AK_DISTINCT) {
