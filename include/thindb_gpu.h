@@ -279,6 +279,10 @@ typedef struct tgpu_request {
  * bits), on request: TGPU_FLAG_RADIX; TGPU_FLAG_NO_RADIX never. */
 #define TGPU_FLAG_RADIX 0x40000
 #define TGPU_FLAG_NO_RADIX 0x80000
+/* Scan loop with one inlined fold call site (compiled folds; survivor
+ * gather or in place): batch i + 1 loads while batch i folds, instead of
+ * several batches folded through an out-of-line call. */
+#define TGPU_FLAG_INLINE_FOLD 0x100000
 
 /* ----------------------------------------------------------------- output -- */
 

@@ -59,6 +59,7 @@ FLAG_COUNT_SKETCH = 0x10000
 FLAG_NO_COUNT_SKETCH = 0x20000
 FLAG_RADIX = 0x40000
 FLAG_NO_RADIX = 0x80000
+FLAG_INLINE_FOLD = 0x100000
 STAT_TUNED = 0x1
 STAT_GATHER = 0x2
 STAT_STAGED = 0x4

@@ -956,6 +956,7 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     df.cap = cap;
 
     dq.warp_combine = (q->flags & TGPU_FLAG_NO_WARP_COMBINE) ? 0 : 1;
+    dq.inline_fold = (q->flags & TGPU_FLAG_INLINE_FOLD) ? 1 : 0;
     // survivors are compacted and folded 32 at a time (gather) unless the
     // WHERE is estimated to keep most rows: folding in place runs a fold per
     // 32 scanned rows, however few of them survive
@@ -1563,7 +1564,7 @@ void apply_tuning(tgpu_query *q, const tgpu_request *req, int batched) {
                       TGPU_FLAG_NO_CHUNK_PREFETCH | TGPU_FLAG_DISTINCT_PREFETCH | TGPU_FLAG_DISTINCT_PARTITION |
                       TGPU_FLAG_NO_DISTINCT_PARTITION | TGPU_FLAG_QUEUE_SCAN | TGPU_FLAG_PIPE_SCAN |
                       TGPU_FLAG_NO_PIPE | TGPU_FLAG_COUNT_SKETCH | TGPU_FLAG_NO_COUNT_SKETCH |
-                      TGPU_FLAG_RADIX | TGPU_FLAG_NO_RADIX;
+                      TGPU_FLAG_RADIX | TGPU_FLAG_NO_RADIX | TGPU_FLAG_INLINE_FOLD;
     const int own = modes | TGPU_FLAG_NO_TUNING;
     if (req->chunk_rows || req->cache_slots || req->table_load_pct || (req->flags & own)) return;
     const tgpu_shape s = shape_of(q, req, batched);

@@ -136,7 +136,7 @@ struct DevQuery {
     int32_t n_faggs;
     DevAgg faggs[4];
     int32_t fast_id;          // index of the matching compiled fold, -1 = interpreter
-    int32_t pad1;
+    int32_t inline_fold;      // scan loop with one inlined fold call site (scan_inline.cu)
     int32_t state_words;      // row count + slots
     int32_t slot_words;       // key_words + state_words rounded to a power of two
     int32_t needs_gid;        // a distinct aggregate needs each row's group slot
@@ -358,6 +358,9 @@ int scan_grid_size(const DevQuery &q, int device_sms);
 int fast_fold_id(const DevQuery &q);
 size_t scan_smem_bytes(const DevQuery &q);
 cudaError_t launch_scan(const DevQuery &q, int grid, cudaStream_t s);
+// the scan loop with one inlined fold call site (compiled folds; scan_inline.cu)
+const void *inline_scan_kernel(const DevQuery &q);
+cudaError_t launch_scan_inline(const DevQuery &q, int grid, size_t smem, cudaStream_t s);
 // many queries, one persistent kernel per fold class over (query, row group)
 // work items: class = the compiled fold's id, or the interpreter for up to 4
 // or up to 16 aggregates

@@ -107,13 +107,18 @@ bool scan_is_fast(const DevQuery &q) {
     return k.fn != kernel_of<GenericFold<4>, 2>().fn && k.fn != kernel_of<GenericFold<16>, 1>().fn;
 }
 
+// The inlined-fold loop serves compiled folds outside queue mode.
+static bool use_inline(const DevQuery &q) { return q.inline_fold && q.gather != 2 && inline_scan_kernel(q); }
+
 int scan_grid_size(const DevQuery &q, int sms) {
     // persistent grid: every CTA that fits on an SM at once
-    return sms * blocks_per_sm(pick_kernel(q).fn, scan_smem_bytes(q));
+    const void *fn = use_inline(q) ? inline_scan_kernel(q) : pick_kernel(q).fn;
+    return sms * blocks_per_sm(fn, scan_smem_bytes(q));
 }
 
 cudaError_t launch_scan(const DevQuery &q, int grid, cudaStream_t s) {
     const size_t smem = scan_smem_bytes(q);
+    if (use_inline(q)) return launch_scan_inline(q, grid, smem, s);
     const ScanKernel k = pick_kernel(q);
     cudaError_t e = cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

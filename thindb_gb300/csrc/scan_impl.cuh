@@ -867,7 +867,15 @@ struct FastFold {
         }
     }
 
+    // One out-of-line copy for the scan loops with several unrolled call
+    // sites (an inlined copy per site overflows the instruction cache) ...
     __device__ __noinline__ static void fold(const DevQuery &q, const ScanSmem sm, const Row in, unsigned active) {
+        fold_body(q, sm, in, active);
+    }
+
+    // ... and the body itself, inlined where a loop has one call site.
+    __device__ __forceinline__ static void fold_body(const DevQuery &q, const ScanSmem &sm, const Row &in,
+                                                     unsigned active) {
         const int lane = threadIdx.x & 31;
         const bool me = (active >> lane) & 1u;
         uint64_t val[NV];
@@ -1013,6 +1021,43 @@ __device__ __forceinline__ void prefetch_chunk(const DevQuery &q, uint32_t c) {
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(b16), "r"((uint32_t)(e16 - b16)) : "memory");
 }
 
+// The WHERE over rows [row0, row_end): the survivors' chunk offsets into
+// `list` (ballot + popc positions); returns their count.
+__device__ __forceinline__ uint32_t survivors(const DevQuery &q, uint64_t row0, uint64_t row_end, uint16_t *list) {
+    const int lane = threadIdx.x & 31;
+    uint32_t n = 0;
+    switch (q.fp_bytes) {
+        case 1: n = filter_range<signed char>(q, row0, row_end, list); break;
+        case 2: n = filter_range<short>(q, row0, row_end, list); break;
+        case 4: n = filter_range<int>(q, row0, row_end, list); break;
+        case 8: n = filter_range<long long>(q, row0, row_end, list); break;
+        default: break;
+    }
+    for (uint64_t b = row0; q.fp_bytes == 0 && b < row_end; b += 32 * FILTER_UNROLL) {
+        bool pass[FILTER_UNROLL];
+        // first predicate for all steps (its loads are independent), then the rest
+#pragma unroll
+        for (int u = 0; u < FILTER_UNROLL; ++u) {
+            const uint64_t r = b + u * 32 + lane;
+            pass[u] = r < row_end && pred_holds(q, q.preds[0], r);
+        }
+        for (int i = 1; i < q.n_preds; ++i) {
+#pragma unroll
+            for (int u = 0; u < FILTER_UNROLL; ++u) {
+                const uint64_t r = b + u * 32 + lane;
+                if (pass[u]) pass[u] = pred_holds(q, q.preds[i], r);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < FILTER_UNROLL; ++u) {
+            const unsigned m = __ballot_sync(FULL, pass[u]);
+            if (pass[u]) list[n + __popc(m & ((1u << lane) - 1))] = (uint16_t)(b + u * 32 + lane - row0);
+            n += __popc(m);
+        }
+    }
+    return n;
+}
+
 // One warp folds chunk c: filter + compaction, then batches of 32 survivors
 // (each batch's gathers issued before the previous batch folds).
 template <class P>
@@ -1058,36 +1103,7 @@ __device__ __forceinline__ void scan_chunk(const DevQuery &q, const ScanSmem &sm
     }
     // gather mode: the chunk's survivors first, then folds
     uint16_t *list = sm.wlist + (size_t)warp * q.chunk_rows;
-    uint32_t n = 0;
-    switch (q.fp_bytes) {
-        case 1: n = filter_range<signed char>(q, row0, row_end, list); break;
-        case 2: n = filter_range<short>(q, row0, row_end, list); break;
-        case 4: n = filter_range<int>(q, row0, row_end, list); break;
-        case 8: n = filter_range<long long>(q, row0, row_end, list); break;
-        default: break;
-    }
-    for (uint64_t b = row0; q.fp_bytes == 0 && b < row_end; b += 32 * FILTER_UNROLL) {
-        bool pass[FILTER_UNROLL];
-        // first predicate for all steps (its loads are independent), then the rest
-#pragma unroll
-        for (int u = 0; u < FILTER_UNROLL; ++u) {
-            const uint64_t r = b + u * 32 + lane;
-            pass[u] = r < row_end && pred_holds(q, q.preds[0], r);
-        }
-        for (int i = 1; i < q.n_preds; ++i) {
-#pragma unroll
-            for (int u = 0; u < FILTER_UNROLL; ++u) {
-                const uint64_t r = b + u * 32 + lane;
-                if (pass[u]) pass[u] = pred_holds(q, q.preds[i], r);
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < FILTER_UNROLL; ++u) {
-            const unsigned m = __ballot_sync(FULL, pass[u]);
-            if (pass[u]) list[n + __popc(m & ((1u << lane) - 1))] = (uint16_t)(b + u * 32 + lane - row0);
-            n += __popc(m);
-        }
-    }
+    const uint32_t n = survivors(q, row0, row_end, list);
     __syncwarp();
     selected += (lane == 0) ? n : 0;
     if (n == 0) return;
