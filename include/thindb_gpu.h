@@ -83,7 +83,11 @@ typedef enum tgpu_type {
     TGPU_FLOAT = 9,      /* f32 */
     TGPU_DOUBLE = 10,    /* f64 */
     TGPU_DECIMAL128 = 11,/* i128 little-endian (lo u64, hi i64): outputs only */
-    TGPU_DICT32 = 12     /* i32 code into the column's dictionary */
+    TGPU_DICT32 = 12,    /* i32 code into the column's dictionary */
+    TGPU_VARCHAR = 13    /* strings: `data` holds n_rows + 1 u32 offsets, `dict_bytes` the bytes;
+                          * row r is dict_bytes[data[r] .. data[r + 1]).  A group key only
+                          * (hashed: digest + exact byte check); in outputs an i64 row index
+                          * whose string tgpu_query_key_strings returns */
 } tgpu_type;
 
 typedef enum tgpu_location {
@@ -380,18 +384,21 @@ tgpu_status tgpu_query_next(tgpu_query *q, tgpu_batch *batch, int32_t *done);
  * its 32-bit code and `next` returns codes; thinDB groups a string column by
  * its table id the same way and reads the strings back at emit
  * (v2_group_topn_engine.zig packedIdKeys; v2_shape_group_topn.zig:1741
- * emitResultStageHashed; DESIGN.md §4.6 "Packed ids").  For output column
- * `column` (a DICT32 group key whose table column has a dictionary), writes
- * the strings of codes[0..n) contiguously into `bytes` with offsets[0] = 0
- * and string i at [offsets[i], offsets[i + 1]); *bytes_needed receives the
- * total.  bytes may be NULL (size query).  A row whose key is NULL carries
- * code 0 in `next`'s buffer: skip it by its validity.  A code outside the
- * dictionary, or a column that is not such a key, returns
+ * emitResultStageHashed; DESIGN.md §4.6 "Packed ids").  A TGPU_VARCHAR key
+ * is hashed (a digest places the group, the bytes decide equality) and
+ * `next` returns, per group, the i64 index of one of its rows (thinDB's
+ * rowref).  For output column `column` (such a key), writes the strings of
+ * values[0..n) — int32 codes for DICT32, int64 row indices for VARCHAR —
+ * contiguously into `bytes` with offsets[0] = 0 and string i at
+ * [offsets[i], offsets[i + 1]); *bytes_needed receives the total.  bytes may
+ * be NULL (size query).  A row whose key is NULL carries 0 in `next`'s
+ * buffer: skip it by its validity.  A code outside the dictionary, a row
+ * outside the table, or a column that is not such a key returns
  * TGPU_ERR_INVALID_ARGUMENT.  ORDER BY a DICT32 key orders by the strings
  * (bytewise, a proper prefix first), as thinDB's post-emit sort does
- * (v2_shape_group_topn.zig:302-325); a key whose dictionary holds a string
- * twice declines. */
-tgpu_status tgpu_query_key_strings(const tgpu_query *q, uint32_t column, const int32_t *codes, uint64_t n,
+ * (v2_shape_group_topn.zig:302-325); ORDER BY a hashed key declines; a
+ * DICT32 key whose dictionary holds a string twice declines. */
+tgpu_status tgpu_query_key_strings(const tgpu_query *q, uint32_t column, const void *values, uint64_t n,
                                    uint64_t *offsets, uint8_t *bytes, uint64_t bytes_cap, uint64_t *bytes_needed);
 
 /* Async-safe cancellation flag; the next tile boundary or `next` returns

@@ -14,7 +14,7 @@ from typing import Optional, Sequence
 import numpy as np
 
 from thindb_gb300 import abi
-from thindb_gb300.engine import NP_DTYPES, Column, Request, build_request
+from thindb_gb300.engine import NP_DTYPES, Column, Request, build_request, varchar_buffers
 
 from . import build as _build
 
@@ -66,13 +66,19 @@ class HostTable:
         for i, c in enumerate(self.columns):
             d = self.descs[i]
             nm = c.name.encode()
-            arr = np.ascontiguousarray(c.data, dtype=NP_DTYPES[c.type])
-            self._keep += [nm, arr]
             d.name = nm
             d.type = c.type
             d.decimal_precision = c.precision
             d.decimal_scale = c.scale
-            d.data = arr.ctypes.data
+            if c.type == abi.VARCHAR:
+                offs, blob = varchar_buffers(c.data)
+                self._keep += [nm, offs, blob]
+                d.data = offs.ctypes.data
+                d.dict_bytes = blob.ctypes.data
+            else:
+                arr = np.ascontiguousarray(c.data, dtype=NP_DTYPES[c.type])
+                self._keep += [nm, arr]
+                d.data = arr.ctypes.data
             if c.validity is not None:
                 bm = np.packbits(np.asarray(c.validity, dtype=bool), bitorder="little")
                 self._keep.append(bm)

@@ -21,6 +21,13 @@
 //     the packed key ascending ........ v2_shape_group_topn.zig:1327-1335
 //   ORDER BY a string key: the strings
 //     compared bytewise, after the emit  v2_shape_group_topn.zig:302-325
+//   hashed keys (a string part, or more
+//     than 128 packed bits): grouped by
+//     the parts' exact bytes / values,
+//     ordered among exact ties by a digest
+//     (thinDB: 128-bit Wyhash; here the
+//     engine's str_hash chain) ........ v2_shape_group_topn.zig:2055-2070;
+//                                       silo_group_core.zig:5284-5330, :6337
 //     (finish_after_emit: a hashed key read by ORDER BY is ranked on the
 //     emitted values; a packed id reads its string back)
 //   silo grid shape (16-RG tiles, 256
@@ -35,6 +42,7 @@
 #include <memory>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 typedef __int128 i128;
@@ -99,7 +107,7 @@ int elem_bytes(int t) {
 }
 bool is_float(int t) { return t == TGPU_FLOAT || t == TGPU_DOUBLE; }
 bool is_temporal(int t) { return t == TGPU_DATE || t == TGPU_DATETIME; }
-bool valid_type(int t) { return t >= TGPU_BOOLEAN && t <= TGPU_DICT32 && t != TGPU_DECIMAL128; }
+bool valid_type(int t) { return t >= TGPU_BOOLEAN && t <= TGPU_VARCHAR && t != TGPU_DECIMAL128; }
 
 struct Table {
     const tgpu_column_desc *cols;
@@ -124,7 +132,31 @@ struct Table {
         if (cols[c].type == TGPU_FLOAT) return (double)((const float *)cols[c].data)[r];
         return ((const double *)cols[c].data)[r];
     }
+    // TGPU_VARCHAR: data holds n + 1 u32 offsets, dict_bytes the bytes
+    const uint8_t *str(int c, uint64_t r, uint32_t &len) const {
+        const uint32_t *o = (const uint32_t *)cols[c].data;
+        len = o[r + 1] - o[r];
+        return cols[c].dict_bytes + o[r];
+    }
 };
+
+// The digest that orders exact ties among hashed keys — the engine's
+// (common.cuh str_hash / digest_step), restated: a string's length and bytes
+// as little-endian 8-byte words chained through mix64; an integer's value
+// bits; a NULL marker.
+uint64_t str_hash(const uint8_t *p, uint32_t n) {
+    uint64_t h = mix64((uint64_t)n ^ 0x9E3779B97F4A7C15ULL), w = 0;
+    uint32_t k = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        w |= (uint64_t)p[i] << (8 * k);
+        if (++k == 8) {
+            h = mix64(h ^ w);
+            w = 0;
+            k = 0;
+        }
+    }
+    return k ? mix64(h ^ w) : h;
+}
 
 struct KeyPart { int col, type, offset, width; bool nullable; };
 
@@ -140,6 +172,8 @@ struct AggPlan {
 
 struct Plan {
     std::vector<KeyPart> parts;
+    bool hashed = false;                       // string part or > 128 packed bits
+    const std::vector<uint64_t> *rep = nullptr;  // hashed: each passing row's group's first row
     std::vector<AggPlan> aggs;
     int n_slots = 0;
     int n_distinct = 0;
@@ -171,7 +205,7 @@ bool dict_unique(const tgpu_column_desc &c) {
 }
 
 // validateShape restated (v2_shape_group_topn.zig:2051-2370) for the shapes
-// this engine runs; strings (hashed keys) and wide decimals decline.
+// this engine runs; wide decimals decline.
 int build_plan(const Table &t, const tgpu_request *req, Plan &p) {
     if (req->n_group_cols > MAX_GROUP_KEYS) return fail(TGPU_DECLINE, "group key count");
     // No GROUP BY: the global aggregate (v2_global_aggregate.zig tryBuild
@@ -180,12 +214,20 @@ int build_plan(const Table &t, const tgpu_request *req, Plan &p) {
     if (p.global && req->n_having) return fail(TGPU_DECLINE, "HAVING on a global aggregate");
     if (req->n_aggs == 0 || req->n_aggs > MAX_AGGS) return fail(TGPU_DECLINE, "aggregate count");
     int off = 0;
+    int total = 0;
+    for (uint32_t i = 0; i < req->n_group_cols; ++i) {
+        const int c = req->group_cols[i];
+        if (c < 0 || (uint32_t)c >= t.ncols) return fail(TGPU_ERR_INVALID_ARGUMENT, "group column index");
+        const int ty = t.cols[c].type;
+        if (ty == TGPU_VARCHAR) p.hashed = true;
+        else if (type_bits(ty) == 0) return fail(TGPU_DECLINE, "group key type");
+        else total += type_bits(ty) + (t.cols[c].validity ? 1 : 0);
+    }
+    if (total > 128) p.hashed = true;  // validateShape :2067-2070
     for (uint32_t i = 0; i < req->n_group_cols; ++i) {
         int c = req->group_cols[i];
-        if (c < 0 || (uint32_t)c >= t.ncols) return fail(TGPU_ERR_INVALID_ARGUMENT, "group column index");
         int ty = t.cols[c].type;
-        int w = type_bits(ty);
-        if (w == 0) return fail(TGPU_DECLINE, "group key type");
+        int w = ty == TGPU_VARCHAR ? 0 : type_bits(ty);
         bool nl = t.cols[c].validity != nullptr;
         // a packed id stands for its string only when no string has two ids
         // (thinDB's table ids are one per value)
@@ -194,7 +236,7 @@ int build_plan(const Table &t, const tgpu_request *req, Plan &p) {
         off += kp.width;
         p.parts.push_back(kp);
     }
-    if (off > 128) return fail(TGPU_DECLINE, "packed key wider than 128 bits (hashed keys)");
+
     int next = 1;
     for (uint32_t i = 0; i < req->n_aggs; ++i) {
         const tgpu_agg_spec &a = req->aggs[i];
@@ -218,7 +260,7 @@ int build_plan(const Table &t, const tgpu_request *req, Plan &p) {
                 break;
             case TGPU_AGG_SUM: case TGPU_AGG_AVG: case TGPU_AGG_MIN: case TGPU_AGG_MAX: {
                 if (a.column < 0) return fail(TGPU_ERR_INVALID_ARGUMENT, "aggregate column");
-                if (ap.in_type == TGPU_DICT32) return fail(TGPU_DECLINE, "string aggregate");
+                if (ap.in_type == TGPU_DICT32 || ap.in_type == TGPU_VARCHAR) return fail(TGPU_DECLINE, "string aggregate");
                 if ((a.func == TGPU_AGG_SUM || a.func == TGPU_AGG_AVG) && is_temporal(ap.in_type))
                     return fail(TGPU_DECLINE, "temporal read as a number");
                 ap.wide = (a.func == TGPU_AGG_SUM || a.func == TGPU_AGG_AVG) && phys_of(ap.in_type) == P_I64;
@@ -237,6 +279,7 @@ int build_plan(const Table &t, const tgpu_request *req, Plan &p) {
             }
             case TGPU_AGG_COUNT_DISTINCT:
                 if (a.column < 0) return fail(TGPU_ERR_INVALID_ARGUMENT, "count distinct column");
+                if (ap.in_type == TGPU_VARCHAR) return fail(TGPU_DECLINE, "COUNT(DISTINCT) over a string column");
                 if (p.n_distinct >= MAX_DISTINCT) return fail(TGPU_DECLINE, "count distinct slot count");
                 if (next > MAX_AGGS) return fail(TGPU_DECLINE, "aggregate state count");
                 ap.distinct = true;
@@ -257,6 +300,7 @@ int build_plan(const Table &t, const tgpu_request *req, Plan &p) {
         if (s.target == TGPU_SORT_AGG && (s.index < 0 || (uint32_t)s.index >= req->n_aggs))
             return fail(TGPU_DECLINE, "order key");
         if (s.target != TGPU_SORT_KEY && s.target != TGPU_SORT_AGG) return fail(TGPU_DECLINE, "order key");
+        if (s.target == TGPU_SORT_KEY && p.hashed) return fail(TGPU_DECLINE, "ORDER BY a hashed key");
         if (s.target == TGPU_SORT_KEY && p.parts[s.index].type == TGPU_DICT32 &&
             !t.cols[p.parts[s.index].col].dict_size)
             return fail(TGPU_DECLINE, "ORDER BY a string key without its dictionary");
@@ -270,6 +314,7 @@ int build_plan(const Table &t, const tgpu_request *req, Plan &p) {
         const tgpu_predicate &w = req->where[i];
         if (w.column < 0 || (uint32_t)w.column >= t.ncols) return fail(TGPU_ERR_INVALID_ARGUMENT, "predicate column");
         if (w.op < TGPU_PRED_BETWEEN || w.op > TGPU_PRED_IS_NOT_NULL) return fail(TGPU_DECLINE, "predicate op");
+        if (t.cols[w.column].type == TGPU_VARCHAR) return fail(TGPU_DECLINE, "predicate on a string column");
         if (t.cols[w.column].type == TGPU_DICT32 && !(w.op == TGPU_PRED_EQ || w.op == TGPU_PRED_NE ||
                                                       w.op == TGPU_PRED_IS_NULL || w.op == TGPU_PRED_IS_NOT_NULL))
             return fail(TGPU_DECLINE, "string range predicate");
@@ -316,7 +361,49 @@ bool row_passes(const Table &t, const tgpu_request *req, uint64_t r) {
     return true;
 }
 
+// A hashed key's digest over row r's parts.
+uint64_t hashed_digest(const Table &t, const Plan &p, uint64_t r) {
+    uint64_t d = 0x243F6A8885A308D3ULL;
+    for (const KeyPart &kp : p.parts) {
+        uint64_t ph;
+        if (!t.valid(kp.col, r)) {
+            ph = 0x8000000000000001ULL;
+        } else if (kp.type == TGPU_VARCHAR) {
+            uint32_t n;
+            const uint8_t *s = t.str(kp.col, r, n);
+            ph = str_hash(s, n);
+        } else {
+            ph = mix64((uint64_t)t.ival(kp.col, r) ^ 0x6A09E667F3BCC909ULL);
+        }
+        d = mix64(d ^ ph);
+    }
+    return d;
+}
+
+// A hashed key's exact identity: per part a validity byte, then an
+// integer's 8 bytes or a string's u32 length and bytes.
+std::string exact_key(const Table &t, const Plan &p, uint64_t r) {
+    std::string k;
+    for (const KeyPart &kp : p.parts) {
+        const bool v = t.valid(kp.col, r);
+        k.push_back(v ? 1 : 0);
+        if (!v) continue;
+        if (kp.type == TGPU_VARCHAR) {
+            uint32_t n;
+            const uint8_t *s = t.str(kp.col, r, n);
+            k.append((const char *)&n, 4);
+            k.append((const char *)s, n);
+        } else {
+            const int64_t x = t.ival(kp.col, r);
+            k.append((const char *)&x, 8);
+        }
+    }
+    return k;
+}
+
 u128 pack_key(const Table &t, const Plan &p, uint64_t r) {
+    // a hashed key: the digest above the group's first passing row + 1
+    if (p.hashed) return ((u128)hashed_digest(t, p, r) << 64) | (u128)((*p.rep)[r] + 1);
     u128 key = 0;
     for (const KeyPart &kp : p.parts) {
         u128 slice = 0;
@@ -552,8 +639,15 @@ Value agg_value(const Group &g, const AggPlan &a, bool global) {
     }
 }
 
-Value key_value(const Group &g, const KeyPart &kp) {  // keyPartValue / keyPartIsNull, :1426-1470
+Value key_value(const Table &t, const Plan &p, const Group &g, const KeyPart &kp) {  // keyPartValue / keyPartIsNull, :1426-1470
     Value v;
+    if (p.hashed) {
+        // read at the group's first row; a string part emits that row
+        const uint64_t row = (uint64_t)g.key - 1;
+        if (!t.valid(kp.col, row)) { v.null = true; return v; }
+        v.i = kp.type == TGPU_VARCHAR ? (i128)row : (i128)t.ival(kp.col, row);
+        return v;
+    }
     int payload = kp.width - (kp.nullable ? 1 : 0);
     if (kp.nullable && !((g.key >> (kp.offset + kp.width - 1)) & 1)) { v.null = true; return v; }
     uint64_t raw = (uint64_t)(g.key >> kp.offset);
@@ -624,6 +718,18 @@ int run(const Table &t, const tgpu_request *req, int threads, Result &res) {
     int st = build_plan(t, req, p);
     if (st != TGPU_OK) return st;
 
+    // hashed keys: every passing row's group's first passing row (exact
+    // identity by bytes), the part of the packed key that tells groups apart
+    std::vector<uint64_t> rep;
+    if (p.hashed) {
+        rep.assign(t.nrows, 0);
+        std::unordered_map<std::string, uint64_t> first;
+        for (uint64_t r = 0; r < t.nrows; ++r) {
+            if (!row_passes(t, req, r)) continue;
+            rep[r] = first.emplace(exact_key(t, p, r), r).first->second;
+        }
+        p.rep = &rep;
+    }
     std::vector<Group> groups;
     uint64_t selected = 0;
     if (threads <= 1) {
@@ -698,7 +804,7 @@ int run(const Table &t, const tgpu_request *req, int threads, Result &res) {
     // ORDER BY, then the packed key (rowOrderBefore, :1327-1335)
     if (req->n_order > 0) {
         auto order_val = [&](const Group &g, const tgpu_sort_spec &s) {
-            return s.target == TGPU_SORT_KEY ? key_value(g, p.parts[s.index]) : agg_value(g, p.aggs[s.index], p.global);
+            return s.target == TGPU_SORT_KEY ? key_value(t, p, g, p.parts[s.index]) : agg_value(g, p.aggs[s.index], p.global);
         };
         // a DICT32 key orders by its strings; a code outside the dictionary
         // after every string, by code
@@ -764,7 +870,7 @@ int run(const Table &t, const tgpu_request *req, int threads, Result &res) {
     for (uint64_t r = begin; r < end; ++r) {
         const Group &g = groups[keep[r]];
         for (size_t i = 0; i < p.parts.size(); ++i) {
-            Value v = key_value(g, p.parts[i]);
+            Value v = key_value(t, p, g, p.parts[i]);
             put_int(res.data[i], p.parts[i].type, v.null ? 0 : v.i);
             res.valid[i].push_back(v.null ? 0 : 1);
         }

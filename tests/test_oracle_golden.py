@@ -85,3 +85,33 @@ def test_oracle_orders_string_keys_by_their_strings():
     with pytest.raises(oracle.OracleDecline):
         oracle.run(oracle.HostTable([Column("s", abi.DICT32, codes, dictionary=dup), cols[1]]),
                    Request(["s"], [AggSpec("count", None, "c")]))
+
+
+def test_oracle_groups_varchar_keys_by_bytes():
+    """A VARCHAR key is hashed (a digest places it, the bytes decide): the
+    oracle's groups equal a Python dict's over the same strings, NULLs in one
+    group, and ORDER BY the string key declines."""
+    import numpy as np
+
+    from thindb_gb300 import abi
+    from thindb_gb300.engine import AggSpec, Column, Request, SortSpec
+
+    rng = np.random.default_rng(3)
+    pool = ["", "a", "ab", "abc", "b", "ba", "zz/x.y", "a" * 40, "a" * 41, "0123456789abcdef"]
+    vals = [pool[i] for i in rng.integers(0, len(pool), 5000)]
+    ok = rng.random(5000) > 0.1
+    v = rng.integers(-100, 100, 5000).astype(np.int64)
+    cols = [Column("s", abi.VARCHAR, vals, validity=ok), Column("v", abi.BIGINT, v)]
+    r = oracle.run(oracle.HostTable(cols), Request(["s"], [AggSpec("count", None, "c"), AggSpec("sum", "v", "t")]),
+                   threads=4)
+    got = {}
+    for row, valid, c, t in zip(r["s"][0], r["s"][1], r["c"][0], r["t"][0]):
+        got[vals[row] if valid else None] = (int(c), int(t))
+    want = {}
+    for s, o, x in zip(vals, ok, v):
+        k = s if o else None
+        c, t = want.get(k, (0, 0))
+        want[k] = (c + 1, t + int(x))
+    assert got == want
+    with pytest.raises(oracle.OracleDecline):
+        oracle.run(oracle.HostTable(cols), Request(["s"], [AggSpec("count", None, "c")], [SortSpec("s")]))

@@ -15,12 +15,14 @@ STATUS_NAMES = {
 }
 
 # tgpu_type
-BOOLEAN, TINYINT, SMALLINT, INT, DATE, BIGINT, DATETIME, DECIMAL64, FLOAT, DOUBLE, DECIMAL128, DICT32 = range(1, 13)
+BOOLEAN, TINYINT, SMALLINT, INT, DATE, BIGINT, DATETIME, DECIMAL64, FLOAT, DOUBLE, DECIMAL128, DICT32, VARCHAR = \
+    range(1, 14)
 TYPE_NAMES = {BOOLEAN: "BOOLEAN", TINYINT: "TINYINT", SMALLINT: "SMALLINT", INT: "INT", DATE: "DATE",
               BIGINT: "BIGINT", DATETIME: "DATETIME", DECIMAL64: "DECIMAL64", FLOAT: "FLOAT", DOUBLE: "DOUBLE",
-              DECIMAL128: "DECIMAL128", DICT32: "DICT32"}
+              DECIMAL128: "DECIMAL128", DICT32: "DICT32", VARCHAR: "VARCHAR"}
+# (a VARCHAR output column holds one i64 row index per group)
 TYPE_BYTES = {BOOLEAN: 1, TINYINT: 1, SMALLINT: 2, INT: 4, DATE: 4, BIGINT: 8, DATETIME: 8, DECIMAL64: 8,
-              FLOAT: 4, DOUBLE: 8, DECIMAL128: 16, DICT32: 4}
+              FLOAT: 4, DOUBLE: 8, DECIMAL128: 16, DICT32: 4, VARCHAR: 8}
 
 LOC_HOST, LOC_DEVICE = 0, 1
 

@@ -290,6 +290,11 @@ struct Column {
     bool dict_unique = true;
     uint32_t *d_rank = nullptr;
     std::vector<uint32_t> h_rank;
+    // TGPU_VARCHAR: d_data holds the string bytes, d_offs the n_rows + 1
+    // offsets; host copies for late materialisation
+    uint32_t *d_offs = nullptr;
+    std::vector<uint32_t> str_offs;
+    std::vector<uint8_t> str_bytes;
     uint32_t dict_size() const { return dict_offsets.size() > 1 ? (uint32_t)dict_offsets.size() - 1 : 0; }
 };
 
@@ -323,6 +328,7 @@ struct tgpu_table {
             if (c.owned) cudaFreeAsync(c.d_data, stream);
             if (c.d_valid) cudaFreeAsync(c.d_valid, stream);
             if (c.d_rank) cudaFreeAsync(c.d_rank, stream);
+            if (c.d_offs) cudaFreeAsync(c.d_offs, stream);
         }
         cudaStreamSynchronize(stream);
     }
@@ -370,6 +376,7 @@ tgpu_status composite_ndv(const tgpu_table *t, const int32_t *cols, uint32_t n, 
         const Column &c = t->cols[cols[i]];
         k.data[i] = c.d_data;
         k.valid[i] = c.d_valid;
+        k.offs[i] = c.d_offs;
         k.type[i] = c.type;
     }
     std::vector<uint32_t> regs(1u << HLL_P);
@@ -597,6 +604,7 @@ int used_col(DevQuery &dq, std::vector<int> &map, const tgpu_table *t, int c) {
     DevCol &d = dq.cols[dq.n_cols];
     d.data = col.d_data;
     d.valid = col.d_valid;
+    d.offs = col.d_offs;
     d.type = col.type;
     d.bytes = type_bytes(col.type);
     map[c] = dq.n_cols++;
@@ -631,6 +639,7 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
             return fail(TGPU_ERR_INVALID_ARGUMENT, "predicate column index");
         if (w.op < TGPU_PRED_BETWEEN || w.op > TGPU_PRED_IS_NOT_NULL) return fail(TGPU_DECLINE, "predicate op");
         const Column &c = t->cols[w.column];
+        if (c.type == TGPU_VARCHAR) return fail(TGPU_DECLINE, "predicate on a string column");
         if (c.type == TGPU_DICT32 && !(w.op == TGPU_PRED_EQ || w.op == TGPU_PRED_NE || w.op == TGPU_PRED_IS_NULL ||
                                        w.op == TGPU_PRED_IS_NOT_NULL))
             return fail(TGPU_DECLINE, "string range predicate");
@@ -672,14 +681,27 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
         }
     }
 
-    // key layout
+    // key layout: packed (LSB-first parts) up to 128 bits; a string part or
+    // wider parts make the key hashed (validateShape, v2_shape_group_topn.zig:
+    // 2055-2070: a digest placing the group, its bytes deciding equality)
     int off = 0;
+    bool hashed = false;
+    {
+        int total = 0;
+        for (uint32_t i = 0; i < req->n_group_cols; ++i) {
+            const int c = req->group_cols[i];
+            if (c < 0 || (size_t)c >= t->cols.size()) return fail(TGPU_ERR_INVALID_ARGUMENT, "group column index");
+            const Column &col = t->cols[c];
+            if (col.type == TGPU_VARCHAR) hashed = true;
+            else if (type_bits(col.type) == 0) return fail(TGPU_DECLINE, "group key type");
+            else total += type_bits(col.type) + (col.nullable ? 1 : 0);
+        }
+        if (total > 128) hashed = true;
+    }
     for (uint32_t i = 0; i < req->n_group_cols; ++i) {
         int c = req->group_cols[i];
-        if (c < 0 || (size_t)c >= t->cols.size()) return fail(TGPU_ERR_INVALID_ARGUMENT, "group column index");
         const Column &col = t->cols[c];
-        int bits = type_bits(col.type);
-        if (bits == 0) return fail(TGPU_DECLINE, "group key type");
+        int bits = col.type == TGPU_VARCHAR ? 0 : type_bits(col.type);
         // a packed code stands for its string only when no string has two
         // codes (thinDB's table ids are one per value)
         if (col.type == TGPU_DICT32 && !col.dict_unique) return fail(TGPU_DECLINE, "dictionary repeats a string");
@@ -691,6 +713,7 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
         kp.nullable = col.nullable ? 1 : 0;
         df.parts[dq.n_parts] = kp;
         df.part_types[dq.n_parts] = col.type;
+        df.part_cols[dq.n_parts] = dq.cols[kp.col];
         dq.n_parts++;
         off += bits + kp.nullable;
         tgpu_output_column oc{};
@@ -699,12 +722,12 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
         oc.decimal_precision = (uint8_t)col.precision;
         oc.decimal_scale = (uint8_t)col.scale;
         oc.nullable = col.nullable;
-        oc.elem_bytes = type_bytes(col.type);
+        oc.elem_bytes = col.type == TGPU_VARCHAR ? 8 : type_bytes(col.type);  // a string key: its row
         q->schema.push_back(oc);
         q->key_cols.push_back(c);
     }
-    if (off > 128) return fail(TGPU_DECLINE, "packed key wider than 128 bits (hashed keys)");
-    dq.key_words = off > 64 ? 2 : 1;
+    dq.hashed = df.hashed = hashed ? 1 : 0;
+    dq.key_words = hashed || off > 64 ? 2 : 1;
     // a global aggregate's one group takes the packed key 1, not the empty
     // marker 0, so it lives in each CTA's shared-memory table
     dq.key_or = q->global_agg ? 1 : 0;
@@ -755,7 +778,7 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
                 break;
             case TGPU_AGG_SUM: case TGPU_AGG_AVG: case TGPU_AGG_MIN: case TGPU_AGG_MAX: {
                 if (a.column < 0) return fail(TGPU_ERR_INVALID_ARGUMENT, "aggregate column");
-                if (in_type == TGPU_DICT32) return fail(TGPU_DECLINE, "string aggregate");
+                if (in_type == TGPU_DICT32 || in_type == TGPU_VARCHAR) return fail(TGPU_DECLINE, "string aggregate");
                 bool sum = a.func == TGPU_AGG_SUM || a.func == TGPU_AGG_AVG;
                 if (sum && is_temporal(in_type)) return fail(TGPU_DECLINE, "temporal read as a number");
                 bool wide = sum && is_i64_phys(in_type);
@@ -794,6 +817,7 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
             }
             case TGPU_AGG_COUNT_DISTINCT:
                 if (a.column < 0) return fail(TGPU_ERR_INVALID_ARGUMENT, "count distinct column");
+                if (in_type == TGPU_VARCHAR) return fail(TGPU_DECLINE, "COUNT(DISTINCT) over a string column");
                 if (dq.n_dsets >= MAX_DISTINCT) return fail(TGPU_DECLINE, "count distinct slot count");
                 if (next > MAX_AGGS) return fail(TGPU_DECLINE, "aggregate state count");
                 g.kind = AK_DISTINCT;
@@ -842,7 +866,7 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
     dq.fast_km = 0;
     dq.n_faggs = 0;
     {
-        bool ok = dq.n_parts > 0;  // the compiled folds read at least one key part
+        bool ok = dq.n_parts > 0 && !dq.hashed;  // the compiled folds read at least one packed key part
         for (int i = 0; i < dq.n_parts; ++i) ok = ok && !dq.parts[i].nullable;
         for (int a = 0; a < dq.n_aggs && ok; ++a) {
             const DevAgg &g = dq.aggs[a];
@@ -865,6 +889,9 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
               (s.target == TGPU_SORT_AGG && s.index >= 0 && (uint32_t)s.index < req->n_aggs)))
             return fail(TGPU_DECLINE, "order key");
         df.order[i] = DevOrder{s.target, s.index, s.desc ? 1 : 0, 0};
+        // thinDB ranks a hashed key's parts after the emit (finish_after_emit,
+        // v2_shape_group_topn.zig:302-325); this operator does not
+        if (s.target == TGPU_SORT_KEY && dq.hashed) return fail(TGPU_DECLINE, "ORDER BY a hashed key");
         if (s.target == TGPU_SORT_KEY && df.part_types[s.index] == TGPU_DICT32) {
             // thinDB ranks a string key on its emitted strings
             // (v2_shape_group_topn.zig:302-325): here on each code's rank
@@ -955,7 +982,8 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     dq.cap = cap;
     df.cap = cap;
 
-    dq.warp_combine = (q->flags & TGPU_FLAG_NO_WARP_COMBINE) ? 0 : 1;
+    // (equal digests are not equal keys: a hashed key folds lane by lane)
+    dq.warp_combine = (q->flags & TGPU_FLAG_NO_WARP_COMBINE) || dq.hashed ? 0 : 1;
     dq.inline_fold = (q->flags & TGPU_FLAG_INLINE_FOLD) ? 1 : 0;
     // survivors are compacted and folded 32 at a time (gather) unless the
     // WHERE is estimated to keep most rows: folding in place runs a fold per
@@ -1290,7 +1318,7 @@ bool sketch_eligible(const tgpu_query *q, const tgpu_request *req) {
         q->offset + q->limit > SK_MAX_NEED)
         return false;
     if (req->aggs[o.index].func != TGPU_AGG_COUNT || q->dq.aggs[o.index].kind != AK_COUNT_ROWS) return false;
-    if (q->dq.needs_gid || q->dq.n_dsets) return false;
+    if (q->dq.needs_gid || q->dq.n_dsets || q->dq.hashed) return false;
     return q->rows_scanned >= SK_MIN_ROWS || (q->flags & TGPU_FLAG_COUNT_SKETCH);
 }
 
@@ -1624,9 +1652,10 @@ tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out) {
     const uint32_t nc = desc->n_columns;
     for (uint32_t i = 0; i < nc; ++i) {
         const tgpu_column_desc &cd = desc->columns[i];
-        if (cd.type < TGPU_BOOLEAN || cd.type > TGPU_DICT32 || cd.type == TGPU_DECIMAL128)
+        if (cd.type < TGPU_BOOLEAN || cd.type > TGPU_VARCHAR || cd.type == TGPU_DECIMAL128)
             return fail(TGPU_ERR_UNSUPPORTED_TYPE, "column type");
-        if (n && !cd.data) return fail(TGPU_ERR_INVALID_ARGUMENT, "column without data");
+        if (!cd.data && (n || cd.type == TGPU_VARCHAR)) return fail(TGPU_ERR_INVALID_ARGUMENT, "column without data");
+        if (cd.type == TGPU_VARCHAR && !cd.dict_bytes) return fail(TGPU_ERR_INVALID_ARGUMENT, "string column without bytes");
         if (cd.type == TGPU_DICT32 && cd.dict_size && (!cd.dict_offsets || !cd.dict_bytes))
             return fail(TGPU_ERR_INVALID_ARGUMENT, "dictionary without offsets or bytes");
     }
@@ -1671,7 +1700,26 @@ tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out) {
         c.scale = cd.decimal_scale;
         c.nullable = cd.validity != nullptr;
         const size_t bytes = n * type_bytes(cd.type);
-        if (desc->location == TGPU_LOC_DEVICE) {
+        if (cd.type == TGPU_VARCHAR) {
+            // offsets and bytes: host copies (late materialisation) and device copies
+            c.str_offs.resize(n + 1);
+            const bool dev_src = desc->location == TGPU_LOC_DEVICE;
+            CU(cudaMemcpyAsync(c.str_offs.data(), cd.data, (n + 1) * 4,
+                               dev_src ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost, s));
+            CU(cudaStreamSynchronize(s));
+            for (uint64_t r = 0; r < n; ++r)
+                if (c.str_offs[r + 1] < c.str_offs[r]) return fail(TGPU_ERR_INVALID_ARGUMENT, "string offsets decrease");
+            const size_t nb = c.str_offs[n];
+            c.str_bytes.resize(std::max<size_t>(nb, 1));
+            if (nb) CU(cudaMemcpyAsync(c.str_bytes.data(), cd.dict_bytes, nb,
+                                       dev_src ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost, s));
+            CU(cudaMallocFromPoolAsync((void **)&c.d_offs, (n + 1) * 4, dev->col_pool, s));
+            CU(cudaMemcpyAsync(c.d_offs, c.str_offs.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s));
+            CU(cudaMallocFromPoolAsync(&c.d_data, round_up(std::max<size_t>(nb, 16), 16), dev->col_pool, s));
+            c.owned = true;
+            CU(cudaStreamSynchronize(s));
+            if (nb) CU(cudaMemcpyAsync(c.d_data, c.str_bytes.data(), nb, cudaMemcpyHostToDevice, s));
+        } else if (desc->location == TGPU_LOC_DEVICE) {
             c.d_data = const_cast<void *>(cd.data);
             c.owned = false;
         } else {
@@ -1713,13 +1761,13 @@ tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out) {
         double *fmin = (double *)(imax + nrg), *fmax = fmin + nrg;
         uint32_t *nulls = (uint32_t *)(fmax + nrg);
         uint32_t *regs = (uint32_t *)(st + stat_bytes);
-        if (t->n_rg)
+        if (t->n_rg && c.type != TGPU_VARCHAR)  // strings: no zone maps (no WHERE on them here)
             CU(launch_zone_maps(c.d_data, c.d_valid, c.type, n, t->rg_rows, t->n_rg, imin, imax, fmin, fmax, nulls, ss));
         c.ndv = cd.ndv_hint;
         sketch[i] = !c.ndv && desc->compute_ndv && n;
         if (sketch[i]) {
             CU(cudaMemsetAsync(regs, 0, reg_bytes, ss));
-            CU(launch_hll(c.d_data, c.d_valid, c.type, n, regs, ss));
+            CU(launch_hll(c.d_data, c.d_valid, c.type, n, regs, ss, c.d_offs));
         }
     }
     // one read-back of every column's statistics
@@ -1896,20 +1944,31 @@ tgpu_status tgpu_query_next(tgpu_query *q, tgpu_batch *b, int32_t *done) {
     return TGPU_OK;
 }
 
-tgpu_status tgpu_query_key_strings(const tgpu_query *q, uint32_t column, const int32_t *codes, uint64_t n,
+tgpu_status tgpu_query_key_strings(const tgpu_query *q, uint32_t column, const void *values, uint64_t n,
                                    uint64_t *offsets, uint8_t *bytes, uint64_t bytes_cap, uint64_t *bytes_needed) {
-    if (!q || (n && (!codes || !offsets)) || !bytes_needed) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
+    if (!q || (n && (!values || !offsets)) || !bytes_needed) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
     if (column >= q->key_cols.size()) return fail(TGPU_ERR_INVALID_ARGUMENT, "not a group key column");
     const Column &c = q->t->cols[q->key_cols[column]];
-    if (c.type != TGPU_DICT32 || !c.dict_size()) return fail(TGPU_ERR_INVALID_ARGUMENT, "not a DICT32 key with a dictionary");
-    const uint32_t ds = c.dict_size();
+    const bool dict = c.type == TGPU_DICT32 && c.dict_size();
+    if (!dict && c.type != TGPU_VARCHAR)
+        return fail(TGPU_ERR_INVALID_ARGUMENT, "not a string key (DICT32 with a dictionary, or VARCHAR)");
     uint64_t total = 0;
     offsets[0] = 0;
     for (uint64_t i = 0; i < n; ++i) {
-        const uint32_t code = (uint32_t)codes[i];
-        if (code >= ds) return fail(TGPU_ERR_INVALID_ARGUMENT, "code outside the dictionary");
-        const uint32_t b = c.dict_offsets[code], len = c.dict_offsets[code + 1] - b;
-        if (bytes && total + len <= bytes_cap) std::memcpy(bytes + total, c.dict_bytes.data() + b, len);
+        uint64_t b, len;
+        if (dict) {
+            const uint32_t code = (uint32_t)((const int32_t *)values)[i];
+            if (code >= c.dict_size()) return fail(TGPU_ERR_INVALID_ARGUMENT, "code outside the dictionary");
+            b = c.dict_offsets[code];
+            len = c.dict_offsets[code + 1] - b;
+        } else {
+            const uint64_t row = (uint64_t)((const int64_t *)values)[i];
+            if (row >= q->t->n_rows) return fail(TGPU_ERR_INVALID_ARGUMENT, "row index outside the table");
+            b = c.str_offs[row];
+            len = c.str_offs[row + 1] - b;
+        }
+        const uint8_t *src = dict ? c.dict_bytes.data() + b : c.str_bytes.data() + b;
+        if (bytes && total + len <= bytes_cap) std::memcpy(bytes + total, src, len);
         total += len;
         offsets[i + 1] = total;
     }

@@ -26,6 +26,34 @@ __host__ __device__ __forceinline__ void i128_of_split(uint64_t w0, uint64_t w1,
     hi = ((int64_t)w1 >> 32) + (lo < w0 ? 1 : 0);
 }
 
+// Digest of a string's bytes for the hashed-key layout: the length, then the
+// bytes as little-endian 8-byte words (the last one zero-padded), chained
+// through mix64.  (thinDB digests string keys with a 128-bit Wyhash,
+// stringKeyDigest; the digest only places a group and orders exact ties —
+// equality is always decided on the bytes.)
+__host__ __device__ inline uint64_t str_hash(const uint8_t *p, uint32_t n) {
+    uint64_t h = mix64((uint64_t)n ^ 0x9E3779B97F4A7C15ULL), w = 0;
+    uint32_t k = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        w |= (uint64_t)p[i] << (8 * k);
+        if (++k == 8) {
+            h = mix64(h ^ w);
+            w = 0;
+            k = 0;
+        }
+    }
+    return k ? mix64(h ^ w) : h;
+}
+
+// One key part's contribution to a hashed key's digest: a NULL marker, a
+// string's str_hash, or an integer's value bits; chained from HASHED_SEED.
+constexpr uint64_t HASHED_SEED = 0x243F6A8885A308D3ULL;
+constexpr uint64_t HASHED_NULL = 0x8000000000000001ULL;
+__host__ __device__ __forceinline__ uint64_t digest_step(uint64_t d, uint64_t part) { return mix64(d ^ part); }
+__host__ __device__ __forceinline__ uint64_t int_part_hash(int64_t v) {
+    return mix64((uint64_t)v ^ 0x6A09E667F3BCC909ULL);
+}
+
 __host__ __device__ __forceinline__ uint64_t hash_key(uint64_t lo, uint64_t hi) {
     // hashU128 (group_table.zig:52-55): mix64(lo ^ mix64(hi))
     return mix64(lo ^ mix64(hi));

@@ -69,10 +69,11 @@ enum AggKind : int32_t {
 };
 
 struct DevCol {
-    const void *data;
+    const void *data;       // values; TGPU_VARCHAR: the string bytes
     const uint32_t *valid;  // validity bitmap as little-endian u32 words, nullptr = NOT NULL
+    const uint32_t *offs;   // TGPU_VARCHAR: row r's bytes at [offs[r], offs[r + 1]); else nullptr
     int32_t type;           // tgpu_type
-    int32_t bytes;          // element width
+    int32_t bytes;          // element width (TGPU_VARCHAR: 0)
 };
 
 struct DevPred {
@@ -127,6 +128,11 @@ struct DevQuery {
     DevKeyPart parts[MAX_GROUP_KEYS];
     int32_t n_parts;
     int32_t key_words;        // 1 or 2
+    // hashed keys (a string part, or parts wider than 128 bits): word 1 is
+    // the parts' digest, word 0 the representative row + 1; equal digests
+    // are told apart by comparing the rows' key parts
+    int32_t hashed;
+    int32_t pad_h;
     uint64_t key_or;          // OR'ed into every packed key: 1 for a global aggregate (its one group), else 0
     DevAgg aggs[MAX_AGGS];
     int32_t n_aggs;
@@ -219,6 +225,9 @@ struct DevFinal {
     int32_t n_having;
     int32_t sort_words;       // words of one encoded sort key
     int32_t global_avg;       // a global aggregate's AVG: sum / (n * 10^scale), else sum / n / 10^scale
+    int32_t hashed;           // hashed keys: key parts are read from part_cols at the representative row
+    int32_t pad_h;
+    DevCol part_cols[MAX_GROUP_KEYS];
     DevKeyPart parts[MAX_GROUP_KEYS];
     int32_t part_types[MAX_GROUP_KEYS];
     // ORDER BY a DICT32 key: code c ranks as part_rank[c] (its string's place
@@ -411,11 +420,12 @@ cudaError_t launch_zone_maps(const void *data, const uint32_t *valid, int32_t ty
                              uint32_t rg_rows, uint32_t n_rg, int64_t *imin, int64_t *imax, double *fmin,
                              double *fmax, uint32_t *nulls, cudaStream_t s);
 cudaError_t launch_hll(const void *data, const uint32_t *valid, int32_t type, uint64_t n_rows, uint32_t *regs,
-                       cudaStream_t s);
+                       cudaStream_t s, const uint32_t *offs = nullptr);
 // Columns of a composite key for its HyperLogLog sketch.
 struct KeySketchCols {
     const void *data[MAX_GROUP_KEYS];
     const uint32_t *valid[MAX_GROUP_KEYS];
+    const uint32_t *offs[MAX_GROUP_KEYS];  // TGPU_VARCHAR parts
     int32_t type[MAX_GROUP_KEYS];
     int32_t n;
 };

@@ -120,6 +120,30 @@ __device__ __forceinline__ void slot_key(const DevFinal &f, uint32_t gid, uint64
 __device__ EmitVal emit_key(const DevFinal &f, uint64_t k0, uint64_t k1, int p) {
     const DevKeyPart &kp = f.parts[p];
     EmitVal v{false, false, 0, 0, 0.0};
+    if (f.hashed) {
+        // a hashed key's parts are read at the group's representative row
+        // (word 0 - 1); a string part emits that row (thinDB's rowref,
+        // materialised on the host by tgpu_query_key_strings)
+        const uint64_t row = k0 - 1;
+        const DevCol &c = f.part_cols[p];
+        if (c.valid && !((__ldg(c.valid + (row >> 5)) >> (row & 31)) & 1u)) {
+            v.null = true;
+            return v;
+        }
+        int64_t x;
+        if (c.offs) x = (int64_t)row;
+        else switch (c.bytes) {
+                case 1: x = f.part_types[p] == TGPU_BOOLEAN ? (int64_t)__ldg((const uint8_t *)c.data + row)
+                                                          : (int64_t)__ldg((const int8_t *)c.data + row);
+                    break;
+                case 2: x = __ldg((const int16_t *)c.data + row); break;
+                case 4: x = __ldg((const int32_t *)c.data + row); break;
+                default: x = (int64_t)__ldg((const long long *)c.data + row); break;
+            }
+        v.lo = (uint64_t)x;
+        v.hi = x < 0 ? -1 : 0;
+        return v;
+    }
     auto bit = [&](int b) -> uint64_t { return b < 64 ? (k0 >> b) & 1 : (k1 >> (b - 64)) & 1; };
     if (kp.nullable && !bit(kp.offset + kp.payload)) {
         v.null = true;

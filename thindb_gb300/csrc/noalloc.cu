@@ -136,8 +136,8 @@ tgpu_status tgpu_group_by_i64_noalloc(const int64_t *keys, const int64_t *values
     q.n_rg = (uint32_t)((n_rows + 65535) / 65536);
     q.chunk_rows = 1024;
     q.n_chunks = (uint32_t)((n_rows + q.chunk_rows - 1) / q.chunk_rows);
-    q.cols[0] = DevCol{keys, nullptr, TGPU_BIGINT, 8};
-    q.cols[1] = DevCol{values, nullptr, TGPU_BIGINT, 8};
+    q.cols[0] = DevCol{keys, nullptr, nullptr, TGPU_BIGINT, 8};
+    q.cols[1] = DevCol{values, nullptr, nullptr, TGPU_BIGINT, 8};
     q.n_cols = 2;
     q.parts[0] = DevKeyPart{0, 0, 64, 0};
     q.n_parts = 1;

@@ -128,9 +128,58 @@ __device__ __forceinline__ bool pred_holds(const DevQuery &q, const DevPred &p, 
     return p.is_float ? cmp_f(p.op, col_f64(c, r), p.flo, p.fhi) : cmp_int(p.op, col_int_stream(c, r, q.shared_scan != 0), p.lo, p.hi);
 }
 
+// A hashed key's digest over row r's parts (a string's str_hash, an
+// integer's value bits, a NULL marker), chained from HASHED_SEED.
+__device__ uint64_t hashed_digest(const DevQuery &q, uint64_t r) {
+    uint64_t d = HASHED_SEED;
+    for (int i = 0; i < q.n_parts; ++i) {
+        const DevCol &c = q.cols[q.parts[i].col];
+        if (!col_valid(c, r)) {
+            d = digest_step(d, HASHED_NULL);
+            continue;
+        }
+        if (c.offs) {
+            const uint32_t b = c.offs[r], e = c.offs[r + 1];
+            d = digest_step(d, str_hash((const uint8_t *)c.data + b, e - b));
+        } else {
+            d = digest_step(d, int_part_hash(col_int(c, r)));
+        }
+    }
+    return d;
+}
+
+// Whether rows a and b hold the same key (every part: NULL alike, equal
+// integers, strings of equal bytes) — the exact check behind a digest match
+// (ExactKey, silo_group_core.zig:6337).
+__device__ bool keys_equal(const DevQuery &q, uint64_t a, uint64_t b) {
+    for (int i = 0; i < q.n_parts; ++i) {
+        const DevCol &c = q.cols[q.parts[i].col];
+        const bool va = col_valid(c, a), vb = col_valid(c, b);
+        if (va != vb) return false;
+        if (!va) continue;
+        if (c.offs) {
+            const uint32_t ab = c.offs[a], ae = c.offs[a + 1], bb = c.offs[b], be = c.offs[b + 1];
+            if (ae - ab != be - bb) return false;
+            const uint8_t *pa = (const uint8_t *)c.data + ab, *pb = (const uint8_t *)c.data + bb;
+            for (uint32_t j = 0; j < ae - ab; ++j)
+                if (pa[j] != pb[j]) return false;
+        } else if (col_int(c, a) != col_int(c, b)) {
+            return false;
+        }
+    }
+    return true;
+}
+
 // Packed key: parts LSB-first, a nullable part's slice is payload | valid-bit
-// and all-zero for NULL (v2_shape_group_topn.zig:105-119, :2076-2092).
+// and all-zero for NULL (v2_shape_group_topn.zig:105-119, :2076-2092).  A
+// hashed key: word 1 the digest, word 0 the row + 1 (the group's
+// representative row once it claims a slot).
 __device__ __forceinline__ void pack_key(const DevQuery &q, uint64_t r, uint64_t &k0, uint64_t &k1) {
+    if (q.hashed) {
+        k1 = hashed_digest(q, r);
+        k0 = r + 1;
+        return;
+    }
     k0 = q.key_or;
     k1 = 0;
     for (int i = 0; i < q.n_parts; ++i) {
@@ -215,6 +264,33 @@ __device__ uint64_t global_slot(const DevQuery &q, uint64_t k0, uint64_t k1, uin
 
 __device__ __forceinline__ uint64_t global_slot(const DevQuery &q, uint64_t k0, uint64_t k1) {
     return global_slot(q, k0, k1, hash_key(k0, k1));
+}
+
+// A hashed key's slot: probe by the digest (word 1); a slot holding the same
+// digest is the group only if its representative row (word 0 - 1) holds the
+// same key; claiming writes (row + 1, digest) in one 16-byte CAS.
+__device__ uint64_t global_slot_hashed(const DevQuery &q, uint64_t row, uint64_t digest) {
+    const uint64_t mask = q.cap - 1;
+    uint64_t h = mix64(digest) & mask;
+    const ulonglong2 mine = make_ulonglong2(row + 1, digest);
+    for (unsigned p = 0; p < MAX_PROBE; ++p) {
+        unsigned long long *sp = q.table + h * (uint64_t)q.slot_words;
+        const ulonglong2 cur = cas128(sp, make_ulonglong2(0, 0), mine);
+        if (cur.x == 0 && cur.y == 0) {
+            atomicOr(q.occ + (h >> 5), 1u << (h & 31));
+            return h;
+        }
+        if (cur.y == digest && keys_equal(q, row, cur.x - 1)) return h;
+        h = (h + 1) & mask;
+    }
+    atomicOr(q.status, ST_TABLE_FULL);
+    return NO_GID;
+}
+
+// A hash that every row of one group shares: the packed key's, or a hashed
+// key's digest (its word 0 is the row).
+__device__ __forceinline__ uint64_t group_hash(const DevQuery &q, uint64_t k0, uint64_t k1) {
+    return q.hashed ? mix64(k1) : hash_key(k0, k1);
 }
 
 // Insert (gid, value bits) into a distinct set; true when the pair is new.
@@ -613,7 +689,7 @@ __device__ __noinline__ void fold_batch(const DevQuery &q, const ScanSmem sm, co
             }
         }
         if (!done) {
-            gid = (uint32_t)global_slot(q, k0, k1);
+            gid = (uint32_t)(q.hashed ? global_slot_hashed(q, k0 - 1, k1) : global_slot(q, k0, k1));
             if (gid != NO_GID) apply_states<NA>(q, q.table + (uint64_t)gid * q.slot_words + q.key_words, false, acc);
         }
     }
@@ -628,8 +704,8 @@ __device__ __noinline__ void fold_batch(const DevQuery &q, const ScanSmem sm, co
                 const DevAgg &g = q.aggs[a];
                 if (g.kind != AK_DISTINCT || !((ok >> a) & 1u)) continue;
                 uint64_t bits = g.is_float_in ? canon_f64_bits(bits_f64(val[a])) : val[a];
-                if (q.dpart_bits) dpart_append(q, hash_key(k0, k1), gid, bits);
-                else if (distinct_insert(q, g.dset, gid, bits, hash_key(k0, k1))) red_add(gst + g.word, 1ULL, false);
+                if (q.dpart_bits) dpart_append(q, group_hash(q, k0, k1), gid, bits);
+                else if (distinct_insert(q, g.dset, gid, bits, group_hash(q, k0, k1))) red_add(gst + g.word, 1ULL, false);
             }
         }
     }
@@ -713,7 +789,7 @@ __device__ __forceinline__ bool sketch_kept(const DevQuery &q, uint64_t hk) {
 // folds — false for a row the count sketch drops, whose slot is not touched.
 // The key is hashed only when a prefetch or the sketch needs it.
 __device__ __forceinline__ bool prefetch_slot(const DevQuery &q, uint64_t k0, uint64_t k1, bool me) {
-    const bool pf = (q.prefetch & PF_SLOT) && !(q.cache_slots && q.cache_probe == q.cache_slots);
+    const bool pf = (q.prefetch & PF_SLOT) && !(q.cache_slots && q.cache_probe == q.cache_slots) && !q.hashed;
     if (!me || (!pf && !q.sk_keep)) return me;
     const uint64_t hk = hash_key(k0, k1);
     if (!sketch_kept(q, hk)) return false;

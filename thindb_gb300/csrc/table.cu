@@ -104,14 +104,16 @@ constexpr int HLL_M = 1 << HLL_P;
 
 // HyperLogLog registers: index = top HLL_P bits of mix64(value bits), rank =
 // leading zeros of the rest + 1 (Flajolet et al. 2007).
-__global__ void hll_kernel(const void *data, const uint32_t *valid, int32_t type, uint64_t n_rows, uint32_t *regs) {
+__global__ void hll_kernel(const void *data, const uint32_t *valid, int32_t type, uint64_t n_rows, uint32_t *regs,
+                           const uint32_t *offs) {
     extern __shared__ uint32_t sreg[];
     for (int i = threadIdx.x; i < HLL_M; i += blockDim.x) sreg[i] = 0;
     __syncthreads();
     const bool is_f = type == TGPU_FLOAT || type == TGPU_DOUBLE;
     for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += (uint64_t)gridDim.x * blockDim.x) {
         if (!valid_at(valid, r)) continue;
-        uint64_t bits = is_f ? canon_f64_bits(f_at(data, type, r)) : (uint64_t)int_at(data, type, r);
+        uint64_t bits = offs ? str_hash((const uint8_t *)data + offs[r], offs[r + 1] - offs[r])
+                             : is_f ? canon_f64_bits(f_at(data, type, r)) : (uint64_t)int_at(data, type, r);
         uint64_t h = mix64(bits ^ 0x6A09E667F3BCC909ULL);
         uint32_t idx = (uint32_t)(h >> (64 - HLL_P));
         uint64_t w = (h << HLL_P) | (1ULL << (HLL_P - 1));
@@ -138,7 +140,8 @@ __global__ void key_hll_kernel(const __grid_constant__ KeySketchCols k, uint64_t
             const bool is_f = k.type[i] == TGPU_FLOAT || k.type[i] == TGPU_DOUBLE;
             uint64_t bits = 0x8000000000000001ULL;  // NULL
             if (valid_at(k.valid[i], r))
-                bits = is_f ? canon_f64_bits(f_at(k.data[i], k.type[i], r)) : (uint64_t)int_at(k.data[i], k.type[i], r);
+                bits = k.offs[i] ? str_hash((const uint8_t *)k.data[i] + k.offs[i][r], k.offs[i][r + 1] - k.offs[i][r])
+                       : is_f ? canon_f64_bits(f_at(k.data[i], k.type[i], r)) : (uint64_t)int_at(k.data[i], k.type[i], r);
             h = mix64(h ^ bits);
         }
         uint32_t idx = (uint32_t)(h >> (64 - HLL_P));
@@ -162,13 +165,13 @@ cudaError_t launch_zone_maps(const void *data, const uint32_t *valid, int32_t ty
 }
 
 cudaError_t launch_hll(const void *data, const uint32_t *valid, int32_t type, uint64_t n_rows, uint32_t *regs,
-                       cudaStream_t s) {
+                       cudaStream_t s, const uint32_t *offs) {
     if (n_rows == 0) return cudaSuccess;
     int grid = (int)std::min<uint64_t>((n_rows + 1023) / 1024, 1024);
     size_t smem = HLL_M * sizeof(uint32_t);
     cudaError_t e = cudaFuncSetAttribute(hll_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    hll_kernel<<<grid, 512, smem, s>>>(data, valid, type, n_rows, regs);
+    hll_kernel<<<grid, 512, smem, s>>>(data, valid, type, n_rows, regs, offs);
     return cudaGetLastError();
 }
 

@@ -126,7 +126,17 @@ def _check(status: int) -> None:
 
 NP_DTYPES = {abi.BOOLEAN: np.uint8, abi.TINYINT: np.int8, abi.SMALLINT: np.int16, abi.INT: np.int32,
              abi.DATE: np.int32, abi.BIGINT: np.int64, abi.DATETIME: np.int64, abi.DECIMAL64: np.int64,
-             abi.FLOAT: np.float32, abi.DOUBLE: np.float64, abi.DICT32: np.int32}
+             abi.FLOAT: np.float32, abi.DOUBLE: np.float64, abi.DICT32: np.int32, abi.VARCHAR: np.int64}
+
+
+def varchar_buffers(values) -> tuple:
+    """A VARCHAR column's (u32 offsets of n + 1, u8 bytes) from a list of
+    str/bytes values (None for NULL: an empty string under a validity bit)."""
+    enc = [b"" if v is None else (v.encode() if isinstance(v, str) else bytes(v)) for v in values]
+    offs = np.zeros(len(enc) + 1, dtype=np.uint32)
+    offs[1:] = np.cumsum([len(e) for e in enc], dtype=np.uint64).astype(np.uint32)
+    blob = np.frombuffer(b"".join(enc) or b"\0", dtype=np.uint8).copy()
+    return offs, blob
 
 
 def decimal128_to_ints(raw: np.ndarray) -> list[int]:
@@ -183,7 +193,14 @@ class Table:
             d.type = c.type
             d.decimal_precision = c.precision
             d.decimal_scale = c.scale
-            if location == "host":
+            if c.type == abi.VARCHAR:
+                if location != "host":
+                    raise ValueError("VARCHAR columns register from host values")
+                offs, blob = varchar_buffers(c.data)
+                self._keep += [offs, blob]
+                d.data = _ptr(offs)
+                d.dict_bytes = _ptr(blob)
+            elif location == "host":
                 arr = np.ascontiguousarray(c.data, dtype=NP_DTYPES[c.type]) if not hasattr(c.data, "data_ptr") else c.data
                 self._keep.append(arr)
                 d.data = _ptr(arr)
@@ -445,7 +462,7 @@ class Query:
     def key_strings(self, column: int, codes: np.ndarray) -> list:
         """The strings of DICT32 key codes (late materialisation through
         tgpu_query_key_strings); column is the output column index."""
-        codes = np.ascontiguousarray(codes, dtype=np.int32)
+        codes = np.ascontiguousarray(codes, dtype=np.int64 if self.schema[column].type == abi.VARCHAR else np.int32)
         n = len(codes)
         offs = np.zeros(n + 1, dtype=np.uint64)
         need = C.c_uint64()
@@ -462,7 +479,7 @@ class Query:
         strings (None for a NULL key)."""
         out = self.collect(capacity)
         for i, c in enumerate(self.schema):
-            if c.type != abi.DICT32:  # only group keys come out as DICT32 (string aggregates decline)
+            if c.type not in (abi.DICT32, abi.VARCHAR):  # only group keys come out as strings
                 continue
             vals, ok = out[c.name]
             strs = self.key_strings(i, np.where(ok, vals, 0) if ok is not None else vals)
