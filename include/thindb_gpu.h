@@ -356,6 +356,31 @@ const char *tgpu_last_error_message(void);
  * Replaces opening an `api.Table` snapshot for the scan (scan.zig:470). */
 tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out);
 tgpu_status tgpu_table_destroy(tgpu_table *table);
+
+/* One column of a segment's schema, in schema order. */
+typedef struct tgpu_segment_column {
+    const char *name;
+    int32_t type;               /* tgpu_type: integer family, DATE/DATETIME, DECIMAL64, FLOAT, DOUBLE */
+    uint8_t decimal_precision;
+    uint8_t decimal_scale;
+    uint8_t reserved[2];
+} tgpu_segment_column;
+
+/* Register a table from a thinDB segment file image (host memory, `bytes`
+ * long; src/storage/format.zig layout, version 17 as
+ * segment_reader.zig:1388 requires): the header and each
+ * row group's 12-byte column-block headers are checked on the host, the
+ * image is copied to the device once, and the column blocks are decoded
+ * there — raw, frame-of-reference (FOR) and run-length (RLE) payloads with
+ * their validity bitmaps (segment_reader.zig decodeColumnPayload :1730,
+ * forBlockOf :1809, rleBlockOf :2133) — straight into the resident columns;
+ * zone maps and NDV sketches follow as in tgpu_table_register.  Row groups
+ * keep the segment's size.  Blocks stored zstd- or lz4-compressed or with
+ * integer-stream transforms, string columns and dictionary / FSST blocks
+ * return TGPU_ERR_UNSUPPORTED_TYPE; a malformed image
+ * TGPU_ERR_INVALID_ARGUMENT. */
+tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, const tgpu_segment_column *columns,
+                                        uint32_t n_columns, int32_t compute_ndv, void *stream, tgpu_table **out);
 /* Row count, row-group count and a column's NDV estimate (-1 column = none). */
 tgpu_status tgpu_table_info(const tgpu_table *table, int32_t column,
                             uint64_t *n_rows, uint32_t *n_row_groups, uint64_t *ndv);

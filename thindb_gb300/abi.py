@@ -233,3 +233,14 @@ SIGNATURES += [
     ("tgpu_tuning_get", C.c_uint32, [C.POINTER(Tuning), C.c_uint32]),
     ("tgpu_debug_set_wait_limit", C.c_int, [C.c_uint64]),
 ]
+
+
+class SegmentColumn(C.Structure):
+    _fields_ = [("name", C.c_char_p), ("type", C.c_int32), ("decimal_precision", C.c_uint8),
+                ("decimal_scale", C.c_uint8), ("reserved", C.c_uint8 * 2)]
+
+
+SIGNATURES += [
+    ("tgpu_table_register_segment", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(SegmentColumn), C.c_uint32,
+                                              C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
+]

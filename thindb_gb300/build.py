@@ -21,7 +21,7 @@ BUILD = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-ENGINE_SOURCES = ["api.cpp", "scan.cu", "scan_inline.cu", "scan_batch.cu", "scan_staged.cu", "scan_pipe.cu", "sketch.cu", "radix.cu", "distinct.cu", "finalize.cu", "table.cu", "noalloc.cu"]
+ENGINE_SOURCES = ["api.cpp", "scan.cu", "scan_inline.cu", "scan_batch.cu", "scan_staged.cu", "scan_pipe.cu", "sketch.cu", "radix.cu", "segment.cu", "distinct.cu", "finalize.cu", "table.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:
@@ -67,7 +67,7 @@ def build_engine(verbose: bool = False, ptxas_v: bool = False) -> str:
             if ptxas_v and s.endswith(".cu"):
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)
-    with ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
+    with ThreadPoolExecutor(max_workers=min(max(8, os.cpu_count() or 8), max(1, len(jobs)))) as ex:
         for f in [ex.submit(_run, j) for j in jobs]:
             f.result()
     if _stale(so, objs) or jobs:

@@ -1802,6 +1802,178 @@ tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out) {
     return TGPU_OK;
 }
 
+tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, const tgpu_segment_column *columns,
+                                        uint32_t n_columns, int32_t compute_ndv, void *stream, tgpu_table **out) {
+    if (!image || !columns || !n_columns || !out) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
+    auto u16 = [&](uint64_t o) { uint16_t v; std::memcpy(&v, image + o, 2); return v; };
+    auto u32 = [&](uint64_t o) { uint32_t v; std::memcpy(&v, image + o, 4); return v; };
+    auto u64 = [&](uint64_t o) { uint64_t v; std::memcpy(&v, image + o, 8); return v; };
+    // header and trailer (format.zig:1-38)
+    if (bytes < 32 + 8 || std::memcmp(image, "tDBS", 4) != 0 || std::memcmp(image + bytes - 4, "tDBS", 4) != 0)
+        return fail(TGPU_ERR_INVALID_ARGUMENT, "not a segment image (magic)");
+    const uint16_t version = u16(4);
+    // segment_reader.zig:1388 reads the current version only
+    if (version != 17) return fail(TGPU_ERR_UNSUPPORTED_TYPE, "segment version other than 17");
+    const uint64_t n = u64(24);
+    for (uint32_t c = 0; c < n_columns; ++c) {
+        const int ty = columns[c].type;
+        if (ty < TGPU_BOOLEAN || ty > TGPU_DOUBLE)
+            return fail(TGPU_ERR_UNSUPPORTED_TYPE, "segment column type (string columns live in string tables)");
+    }
+    // the row groups' blocks
+    std::vector<std::vector<SegBlock>> blocks(n_columns);
+    std::vector<uint32_t> run_starts;
+    std::vector<bool> nullable(n_columns, false);
+    uint64_t pos = 32, done = 0;
+    uint32_t rg_rows = 0;
+    const uint64_t end = bytes - 8;
+    while (done < n) {
+        if (pos + 8 > end) return fail(TGPU_ERR_INVALID_ARGUMENT, "segment truncated in a row-group header");
+        const uint32_t rows = u32(pos);
+        pos += 8;
+        if (rows == 0 || done + rows > n) return fail(TGPU_ERR_INVALID_ARGUMENT, "row-group row count");
+        if (!rg_rows) rg_rows = rows;
+        for (uint32_t c = 0; c < n_columns; ++c) {
+            if (pos + 12 > end) return fail(TGPU_ERR_INVALID_ARGUMENT, "segment truncated in a block header");
+            const uint8_t comp = image[pos], flags = image[pos + 1], enc = image[pos + 2];
+            const uint32_t usize = u32(pos + 4), ssize = u32(pos + 8);
+            const uint64_t payload = pos + 12;
+            if (comp != 0) return fail(TGPU_ERR_UNSUPPORTED_TYPE, "compressed column block (zstd/lz4)");
+            if (flags & 2) return fail(TGPU_ERR_UNSUPPORTED_TYPE, "column block with integer-stream transforms");
+            if (ssize != usize || payload + ssize > end) return fail(TGPU_ERR_INVALID_ARGUMENT, "column block size");
+            const bool has_nulls = flags & 1;
+            const uint32_t bm = has_nulls ? (rows + 7) / 8 : 0;
+            const int ty = columns[c].type;
+            const uint32_t elem = (uint32_t)type_bytes(ty);
+            const bool integer = !is_float_t(ty);
+            SegBlock b{};
+            b.row0 = done;
+            b.payload = payload;
+            b.values = bm;
+            b.rows = rows;
+            b.encoding = enc;
+            b.has_nulls = has_nulls;
+            b.width = elem;
+            if (enc == 0) {
+                if ((uint64_t)bm + (uint64_t)rows * elem > usize) return fail(TGPU_ERR_INVALID_ARGUMENT, "raw block size");
+            } else if (enc == 1) {
+                if (!integer || (uint64_t)bm + 20 > usize) return fail(TGPU_ERR_INVALID_ARGUMENT, "FOR block");
+                b.width = image[payload + bm + 16];
+                if ((b.width != 1 && b.width != 2 && b.width != 4 && b.width != 8) ||
+                    (uint64_t)bm + 20 + (uint64_t)rows * b.width > usize)
+                    return fail(TGPU_ERR_INVALID_ARGUMENT, "FOR block width");
+            } else if (enc == 3) {
+                if (!integer || (uint64_t)bm + 8 > usize) return fail(TGPU_ERR_INVALID_ARGUMENT, "RLE block");
+                b.runs = u32(payload + bm);
+                b.width = image[payload + bm + 4];
+                if (b.width == 0 || b.width > elem ||
+                    (uint64_t)bm + 8 + (uint64_t)b.runs * (b.width + 4) > usize || (b.runs == 0) != (rows == 0))
+                    return fail(TGPU_ERR_INVALID_ARGUMENT, "RLE block size");
+                b.run0 = (uint32_t)run_starts.size();
+                const uint64_t lens = payload + bm + 8 + (uint64_t)b.runs * b.width;
+                uint64_t at = 0;
+                for (uint32_t r = 0; r < b.runs; ++r) {
+                    run_starts.push_back((uint32_t)at);
+                    at += u32(lens + 4ull * r);
+                }
+                if (at != rows) return fail(TGPU_ERR_INVALID_ARGUMENT, "RLE run lengths do not add up to the rows");
+            } else {
+                return fail(TGPU_ERR_UNSUPPORTED_TYPE, "column block encoding (dictionary / FSST)");
+            }
+            nullable[c] = nullable[c] || has_nulls;
+            blocks[c].push_back(b);
+            pos = payload + ssize;
+        }
+        done += rows;
+    }
+    DeviceCtx *dev;
+    tgpu_status st = device_ctx(&dev);
+    if (st != TGPU_OK) return st;
+    cudaStream_t s = stream ? (cudaStream_t)stream : dev->stream;
+    // the image, the block lists and the run starts, then every column decoded
+    std::vector<SegBlock> all;
+    std::vector<uint32_t> first(n_columns + 1, 0);
+    for (uint32_t c = 0; c < n_columns; ++c) {
+        first[c] = (uint32_t)all.size();
+        all.insert(all.end(), blocks[c].begin(), blocks[c].end());
+    }
+    first[n_columns] = (uint32_t)all.size();
+    uint8_t *d_image = nullptr;
+    SegBlock *d_blocks = nullptr;
+    uint32_t *d_runs = nullptr;
+    std::vector<void *> data(n_columns, nullptr);
+    std::vector<uint32_t *> valid(n_columns, nullptr);
+    auto release = [&](bool keep_data) {
+        cudaStreamSynchronize(s);
+        if (d_image) cudaFreeAsync(d_image, s);
+        if (d_blocks) cudaFreeAsync(d_blocks, s);
+        if (d_runs) cudaFreeAsync(d_runs, s);
+        for (uint32_t c = 0; c < n_columns; ++c) {
+            if (valid[c]) cudaFreeAsync(valid[c], s);
+            if (!keep_data && data[c]) cudaFreeAsync(data[c], s);
+        }
+        cudaStreamSynchronize(s);
+    };
+    cudaError_t e = cudaMallocFromPoolAsync((void **)&d_image, bytes, dev->col_pool, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_image, image, bytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMallocFromPoolAsync((void **)&d_blocks, std::max<size_t>(1, all.size()) * sizeof(SegBlock), dev->col_pool, s);
+    if (e == cudaSuccess && !all.empty())
+        e = cudaMemcpyAsync(d_blocks, all.data(), all.size() * sizeof(SegBlock), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMallocFromPoolAsync((void **)&d_runs, std::max<size_t>(1, run_starts.size()) * 4, dev->col_pool, s);
+    if (e == cudaSuccess && !run_starts.empty())
+        e = cudaMemcpyAsync(d_runs, run_starts.data(), run_starts.size() * 4, cudaMemcpyHostToDevice, s);
+    for (uint32_t c = 0; c < n_columns && e == cudaSuccess; ++c) {
+        const size_t elem = (size_t)type_bytes(columns[c].type);
+        e = cudaMallocFromPoolAsync(&data[c], round_up(std::max<size_t>(n * elem, 16), 16), dev->col_pool, s);
+        if (e == cudaSuccess && nullable[c]) {
+            const size_t vw = ((n + 31) / 32 + 1) * 4;
+            e = cudaMallocFromPoolAsync((void **)&valid[c], vw, dev->col_pool, s);
+            if (e == cudaSuccess) e = cudaMemsetAsync(valid[c], 0, vw, s);
+        }
+        if (e == cudaSuccess)
+            e = launch_decode_blocks(d_image, d_blocks + first[c], first[c + 1] - first[c], d_runs, data[c],
+                                     (uint32_t)elem, valid[c], s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        release(false);
+        return fail(TGPU_ERR_CUDA, std::string("segment decode: ") + cudaGetErrorString(e));
+    }
+    // register the decoded columns in place, then hand them to the table
+    std::vector<tgpu_column_desc> cd(n_columns);
+    for (uint32_t c = 0; c < n_columns; ++c) {
+        cd[c] = tgpu_column_desc{};
+        cd[c].name = columns[c].name;
+        cd[c].type = columns[c].type;
+        cd[c].decimal_precision = columns[c].decimal_precision;
+        cd[c].decimal_scale = columns[c].decimal_scale;
+        cd[c].data = data[c];
+        cd[c].validity = (const uint8_t *)valid[c];
+    }
+    tgpu_table_desc td{};
+    td.columns = cd.data();
+    td.n_columns = n_columns;
+    td.row_group_rows = rg_rows ? rg_rows : 65536;
+    td.n_rows = n;
+    td.location = TGPU_LOC_DEVICE;
+    td.compute_ndv = compute_ndv;
+    td.stream = s;
+    tgpu_table *t = nullptr;
+    st = tgpu_table_register(&td, &t);
+    if (st != TGPU_OK) {
+        const std::string msg = g_err;
+        release(false);
+        return fail(st, msg);
+    }
+    for (uint32_t c = 0; c < n_columns; ++c) t->cols[c].owned = true;  // freed with the table
+    release(true);
+    *out = t;
+    return TGPU_OK;
+}
+
 tgpu_status tgpu_table_destroy(tgpu_table *table) {
     if (!table) return fail(TGPU_ERR_INVALID_ARGUMENT, "null table");
     delete table;

@@ -344,6 +344,25 @@ struct RadixPlan {
 size_t radix_scatter_smem(const DevQuery &q, uint32_t bits);
 cudaError_t launch_radix(const DevQuery &q, const RadixPlan &rp, int sms, cudaStream_t s);
 
+// One column block of a thinDB segment image (segment.cu): rows
+// [row0, row0 + rows) of its column, payload at image offset `payload`, the
+// value region `values` bytes into it (past the validity bitmap).
+struct SegBlock {
+    uint64_t row0;
+    uint64_t payload;
+    uint32_t values;
+    uint32_t rows;
+    uint32_t encoding;   // 0 raw, 1 FOR, 3 RLE (format.Encoding)
+    uint32_t width;      // FOR delta / RLE value width in bytes
+    uint32_t runs;       // RLE runs
+    uint32_t run0;       // RLE: index of its first run start in the run-start array
+    uint32_t has_nulls;
+    uint32_t pad;
+};
+cudaError_t launch_decode_blocks(const uint8_t *image, const SegBlock *blocks, uint32_t n_blocks,
+                                 const uint32_t *run_starts, void *out, uint32_t bytes, uint32_t *valid,
+                                 cudaStream_t s);
+
 // Partitioned COUNT(DISTINCT): pairs per partition (one CTA deduplicates a
 // partition in shared memory) and the partition's index-table slots.
 constexpr uint32_t DPART_CAP = 4096;     // 64 KB of pairs per ring stage; three stages + 32 KB of slots per SM

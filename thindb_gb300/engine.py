@@ -238,6 +238,38 @@ class Table:
             self._keep = []  # copied into HBM
         self.row_group_rows = row_group_rows
 
+    @classmethod
+    def from_segment(cls, image: bytes, columns: Sequence[Column], compute_ndv: bool = True,
+                     stream: int = 0) -> "Table":
+        """Register a thinDB segment file image (src/storage/format.zig layout):
+        `columns` name the schema in order (name, type, decimal scale and
+        precision; `data` unused).  The blocks decode on the device; the row
+        groups keep the segment's size."""
+        self = cls.__new__(cls)
+        self.columns = list(columns)
+        if not self.columns:
+            raise ValueError("a table needs columns")
+        buf = np.frombuffer(bytes(image), dtype=np.uint8)
+        names = [c.name.encode() for c in self.columns]
+        descs = (abi.SegmentColumn * len(self.columns))()
+        for i, c in enumerate(self.columns):
+            descs[i].name = names[i]
+            descs[i].type = c.type
+            descs[i].decimal_precision = c.precision
+            descs[i].decimal_scale = c.scale
+        h = C.c_void_p()
+        _check(lib().tgpu_table_register_segment(_ptr(buf) if buf.size else None, buf.size, descs,
+                                                 len(self.columns), 1 if compute_ndv else 0, stream or None,
+                                                 C.byref(h)))
+        self.handle = h
+        self._keep = []
+        rows, groups = C.c_uint64(), C.c_uint32()
+        _check(lib().tgpu_table_info(h, -1, C.byref(rows), C.byref(groups), None))
+        self.n_rows = rows.value
+        self.row_group_rows = 0
+        self.n_row_groups = groups.value
+        return self
+
     def col_index(self, name: str) -> int:
         for i, c in enumerate(self.columns):
             if c.name.lower() == name.lower():
