@@ -13,7 +13,7 @@ One step = one execution of that query over the whole table.
 Inputs (2.0 GB) are larger than L2 (129 MB), so no flush between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload filtered|plain|distinct]
+                  [--workload filtered|plain|topcount|distinct|batched|served|segment]
 """
 from __future__ import annotations
 
@@ -67,9 +67,9 @@ def load_peak():
         return 6800.0, "fallback"
 
 
-def load_traffic(workload):
-    """dram bytes per scan launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", f"scan_{workload}_traffic.json")
+def load_traffic(workload, kernel="scan"):
+    """dram bytes per launch of the dominant kernel from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}_{workload}_traffic.json")
     try:
         with open(p) as f:
             return json.load(f).get("dram_bytes_per_launch")
@@ -541,13 +541,159 @@ def served_arm(args):
         t.close()
 
 
+# ------------------------------------------------------ segment ingest --
+
+SEGMENT_RG_ROWS = 65_536
+SEGMENT_BASE_GROUPS = 64      # rows written by the segment writer, then repeated
+SEGMENT_TIMES = 25            # 64 x 25 row groups of 65,536 rows = 104,857,600 rows
+SEGMENT_NAME = ("segment ingest: a thinDB segment image (version 17, no block compression) of 1,600 row groups "
+                "x 65,536 rows (104,857,600 rows), 8 columns: SMALLINT/DATE runs (RLE), BIGINT x2 and DECIMAL64 "
+                "(FOR widths 2/4/4), DOUBLE, BOOLEAN, TINYINT (raw); 4 nullable columns (validity bitmaps)")
+
+
+def segment_image(rows: int = 0):
+    """A seeded segment image: the writer's first 64 row groups, repeated."""
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    from segments import replicate, sample_table, write_segment
+
+    base = SEGMENT_BASE_GROUPS * SEGMENT_RG_ROWS
+    times = SEGMENT_TIMES
+    if rows:
+        base = min(base, rows)
+        times = max(1, -(-rows // base))
+    names, types, values, validity = sample_table(base)
+    image, _ = write_segment(types, values, validity, row_group_rows=SEGMENT_RG_ROWS)
+    if times > 1:
+        image = replicate(image, len(types), times)
+    return names, types, validity, image, base * times
+
+
+def segment_schema(names, types):
+    from thindb_gb300.engine import Column
+    return [Column(nm, ty, None, scale=2 if ty == abi.DECIMAL64 else 0, precision=12)
+            for nm, ty in zip(names, types)]
+
+
+def segment_oracle(image, types, validity, threads):
+    import oracle
+    t0 = time.perf_counter()
+    out = oracle.decode_segment(image, types, [v is not None for v in validity], threads=threads)
+    return out, time.perf_counter() - t0
+
+
+def segment_reference_arm(args):
+    """The CPU decode of the same image (oracle/segment.cpp, a C++
+    restatement of thinDB's segment reader; the Zig toolchain is absent), all
+    host threads."""
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    names, types, validity, image, n = segment_image(args.rows)
+    threads = os.cpu_count() or 1
+    segment_oracle(image, types, validity, threads)
+    secs = [segment_oracle(image, types, validity, threads)[1] for _ in range(args.steps)]
+    ms = statistics.median(secs) * 1e3
+    value = n / (ms / 1e3)
+    print(json.dumps({
+        "impl": "reference", "metric": "segment ingest rows/s", "value": value, "unit": "rows/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/int64",
+        "data": "synthetic (seeded generator)", "config": {"workload": SEGMENT_NAME, "rows": n},
+        "cpu_baseline": {"value": value, "unit": "rows/s", "cores": threads, "kind": "port",
+                         "sample": f"the whole image ({len(image) / 1e9:.2f} GB) decoded per step on {threads} "
+                                   "threads; C++ restatement of thinDB's segment reader (Zig toolchain absent)"},
+        "e2e": {"value": value, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def segment_arm(args):
+    """Register the image as a table, K times: host walk, H2D copy of the
+    image, one decode launch, zone maps and NDV sketches.  value: rows/s of
+    the device work once the image is resident (decode + statistics); e2e:
+    rows/s of the whole call from a pinned host image."""
+    import torch
+
+    from thindb_gb300.engine import Table
+
+    torch.cuda.set_device(0)
+    names, types, validity, image, n = segment_image(args.rows)
+    host = torch.empty(len(image), dtype=torch.uint8, pin_memory=True)
+    host.numpy()[:] = np.frombuffer(image, dtype=np.uint8)
+    schema = segment_schema(names, types)
+    stream = torch.cuda.Stream()
+    for _ in range(args.warmup):
+        Table.from_segment(host, schema, stream=stream.cuda_stream).close()
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    torch.cuda.synchronize()
+    stats, wall = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        t = Table.from_segment(host, schema, stream=stream.cuda_stream)
+        wall.append(time.perf_counter() - t0)
+        st = t.load_stats()
+        stats.append((st.h2d_ms, st.decode_ms, st.stats_ms, st.total_ms))
+        t.close()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    decode_ms = statistics.mean(s[1] for s in stats)
+    device_ms = statistics.median(s[1] + s[2] for s in stats)
+    e2e_ms = statistics.median(wall) * 1e3
+    t = Table.from_segment(host, schema, stream=stream.cuda_stream)
+    st = t.load_stats()
+    alg = st.image_bytes + st.decoded_bytes
+    peak, peak_kind = load_peak()
+    achieved = alg / (decode_ms / 1e3) / 1e9
+    # parity: every decoded column bit-exact with the CPU decode of the image
+    cpu, parity = None, None
+    threads = os.cpu_count() or 1
+    if not args.no_cpu:
+        want, dt_all = segment_oracle(image, types, validity, threads)
+        parity = True
+        for nm, (wv, wok) in zip(names, want):
+            gv, gok = t.read_column(nm)
+            parity = parity and bool(np.array_equal(gv.view(np.uint8), wv.view(np.uint8)))
+            parity = parity and (bool(gok.all()) if wok is None else bool(np.array_equal(gok, wok)))
+        del want
+        base_rows = SEGMENT_BASE_GROUPS * SEGMENT_RG_ROWS
+        _, types1, valid1, image1, n1 = segment_image(min(n, base_rows))
+        _, dt1 = segment_oracle(image1, types1, valid1, 1)
+        cpu = {"value": n / dt_all, "unit": "rows/s", "cores": threads, "kind": "port",
+               "sample": f"the whole image ({len(image) / 1e9:.2f} GB, {dt_all:.2f} s) on {threads} threads; "
+                         "C++ restatement of thinDB's segment reader (Zig toolchain absent)",
+               "dop1": {"value": n1 / dt1, "unit": "rows/s", "cores": 1,
+                        "sample": f"the first {n1:,} rows ({dt1:.2f} s) on 1 thread"}}
+    t.close()
+    line = {
+        "metric": "segment ingest rows/s", "value": n / (device_ms / 1e3), "unit": "rows/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": device_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8/int64", "data": "synthetic (seeded generator)",
+        "config": {"workload": SEGMENT_NAME, "rows": n, "image_bytes": st.image_bytes,
+                   "decoded_bytes": st.decoded_bytes, "blocks": st.blocks,
+                   "l2": "image and columns larger than L2 (no flush)",
+                   "value_covers": "decode launch + zone maps + NDV sketches, image resident"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": load_traffic("ingest", "decode"), "kernel": "decode_blocks_kernel", "kernel_ms": decode_ms,
+                     "algorithmic_bytes": alg, "peak_kind": peak_kind},
+        "e2e": {"value": n / (e2e_ms / 1e3), "unit": "rows/s", "h2d_bytes_per_step": st.image_bytes,
+                "d2h_bytes_per_step": 0, "ms_per_step": e2e_ms,
+                "h2d_ms": statistics.median(s[0] for s in stats),
+                "stats_ms": statistics.median(s[2] for s in stats)},
+        "parity": parity,
+        "gpu_launches": args.steps * (1 + 2 * len(types)),
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="filtered", choices=sorted(WORKLOADS) + ["batched", "served"])
+    ap.add_argument("--workload", default="filtered", choices=sorted(WORKLOADS) + ["batched", "served", "segment"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--rows", type=int, default=0, help="rows of the workload (default: its full size)")
     ap.add_argument("--queries", type=int, default=256, help="queries of the batched workload")
@@ -569,6 +715,12 @@ def main():
                               "run the default workload"}))
             return
         served_arm(args)
+        return
+    if args.workload == "segment":
+        if args.impl == "reference":
+            segment_reference_arm(args)
+        else:
+            segment_arm(args)
         return
     if args.workload == "batched":
         if args.impl == "reference":

@@ -381,6 +381,25 @@ typedef struct tgpu_segment_column {
  * TGPU_ERR_INVALID_ARGUMENT. */
 tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, const tgpu_segment_column *columns,
                                         uint32_t n_columns, int32_t compute_ndv, void *stream, tgpu_table **out);
+/* What registering a table from a segment image took (all zero for tables
+ * registered from columns). */
+typedef struct tgpu_load_stats {
+    uint64_t image_bytes;       /* segment image copied to the device */
+    uint64_t decoded_bytes;     /* column values and validity bytes the decode wrote */
+    uint32_t blocks;            /* column blocks decoded */
+    uint32_t kernel_launches;   /* decode launches */
+    double h2d_ms;              /* the image's host-to-device copy (device clock) */
+    double decode_ms;           /* the decode launch (device clock) */
+    double stats_ms;            /* zone maps and NDV sketches (host clock) */
+    double total_ms;            /* the whole call (host clock) */
+} tgpu_load_stats;
+tgpu_status tgpu_table_load_stats(const tgpu_table *table, tgpu_load_stats *out);
+/* Copy a registered column back to host memory: `values` receives n_rows
+ * values of the column's type, `validity` (may be null) (n_rows + 7) / 8
+ * bitmap bytes, bit set = value (all set for a NOT NULL column; the bits past
+ * the last row of the last byte are unspecified).  VARCHAR columns return
+ * TGPU_ERR_UNSUPPORTED_TYPE. */
+tgpu_status tgpu_table_read_column(const tgpu_table *table, uint32_t column, void *values, uint8_t *validity);
 /* Row count, row-group count and a column's NDV estimate (-1 column = none). */
 tgpu_status tgpu_table_info(const tgpu_table *table, int32_t column,
                             uint64_t *n_rows, uint32_t *n_row_groups, uint64_t *ndv);

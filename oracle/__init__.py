@@ -144,3 +144,33 @@ def run(table: HostTable, req: Request, threads: int = 1) -> dict:
 
 def i128_to_f64(lo: int, hi: int) -> float:
     return lib().orc_i128_to_f64(lo & ((1 << 64) - 1), hi)
+
+
+class SegmentError(Exception):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{abi.STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def decode_segment(image: bytes, types: Sequence[int], nullable: Sequence[bool], threads: int = 1) -> list:
+    """Decode a segment image (segment.cpp) into [(values, validity or None)]
+    per column; `nullable[c]` asks for column c's validity."""
+    L = lib()
+    if not hasattr(L, "_seg_bound"):
+        L.orc_segment_decode.restype = C.c_int
+        L.orc_segment_decode.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(C.c_uint32), C.c_uint32,
+                                         C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int]
+        L.orc_segment_error.restype = C.c_char_p
+        L._seg_bound = True
+    buf = np.frombuffer(bytes(image), dtype=np.uint8)
+    n = int(buf[24:32].view(np.uint64)[0]) if buf.size >= 32 else 0
+    nc = len(types)
+    elem = (C.c_uint32 * nc)(*[abi.TYPE_BYTES[t] for t in types])
+    vals = [np.zeros(n, dtype=NP_DTYPES[t]) for t in types]
+    bms = [np.zeros((n + 7) // 8 + 1, dtype=np.uint8) if nullable[c] else None for c, t in enumerate(types)]
+    outs = (C.c_void_p * nc)(*[v.ctypes.data for v in vals])
+    valid = (C.c_void_p * nc)(*[b.ctypes.data if b is not None else None for b in bms])
+    st = L.orc_segment_decode(buf.ctypes.data, buf.size, elem, nc, outs, valid, threads)
+    if st != abi.OK:
+        raise SegmentError(st, L.orc_segment_error().decode())
+    return [(v, None if b is None else np.unpackbits(b, bitorder="little")[:n].astype(bool)) for v, b in zip(vals, bms)]

@@ -155,12 +155,73 @@ def write_segment(types: Sequence[int], values: Sequence[np.ndarray],
             out += struct.pack("<BBBBII", 0, flags, enc, 0, len(payload), len(payload)) + payload
             lens.append(len(out) - offs[-1])
         groups.append((g0, len(out) - g0, r1 - r0, offs, lens))
+    return bytes(out + _footer(groups, len(types))), headers
+
+
+def _footer(groups, n_cols: int) -> bytes:
     foot = bytearray(struct.pack("<I", len(groups)))
     for g0, glen, grows, offs, lens in groups:
         foot += struct.pack("<QII", g0, glen, grows)
-        foot += bytes(FOOTER_STATS_BYTES * len(types))
+        foot += bytes(FOOTER_STATS_BYTES * n_cols)
         foot += b"".join(struct.pack("<Q", o) for o in offs)
         foot += b"".join(struct.pack("<I", ln) for ln in lens)
     foot += struct.pack("<I", 0)                      # no string tables
     foot += struct.pack("<I", len(foot) + 8) + b"tDBS"
-    return bytes(out + foot), headers
+    return bytes(foot)
+
+
+def _groups(image: bytes, n_cols: int) -> list:
+    """(offset, length, rows, block offsets, block lengths) of every row group."""
+    n = struct.unpack_from("<Q", image, 24)[0]
+    pos, done, groups = 32, 0, []
+    while done < n:
+        g0 = pos
+        rows = struct.unpack_from("<I", image, pos)[0]
+        pos += 8
+        offs, lens = [], []
+        for _ in range(n_cols):
+            size = struct.unpack_from("<I", image, pos + 8)[0]
+            offs.append(pos)
+            lens.append(12 + size)
+            pos += 12 + size
+        groups.append((g0, pos - g0, rows, offs, lens))
+        done += rows
+    return groups
+
+
+def replicate(image: bytes, n_cols: int, times: int) -> bytes:
+    """The segment with its row groups repeated `times` times (a large image
+    from a small one; the footer is rebuilt)."""
+    groups = _groups(image, n_cols)
+    body = image[32:groups[-1][0] + groups[-1][1]] if groups else b""
+    n = struct.unpack_from("<Q", image, 24)[0]
+    head = bytearray(image[:32])
+    struct.pack_into("<Q", head, 24, n * times)
+    shifted = []
+    for k in range(times):
+        d = k * len(body)
+        shifted += [(g0 + d, gl, gr, [o + d for o in offs], lens) for g0, gl, gr, offs, lens in groups]
+    return bytes(head) + body * times + _footer(shifted, n_cols)
+
+
+def sample_table(n: int, seed: int = 7) -> tuple:
+    """An eight-column table of the encodings a thinDB table stores: names,
+    types, values and validity (None = NOT NULL).  region SMALLINT (runs of
+    500: RLE), day DATE (sorted: RLE), user BIGINT over 50k (FOR width 2),
+    amount BIGINT +-1e9 (FOR width 4), price DOUBLE (raw), flag BOOLEAN,
+    tiny TINYINT (raw), cents DECIMAL64 +-1e6 (FOR width 4); day, user, price
+    and tiny are nullable."""
+    rng = np.random.default_rng(seed)
+    names = ["region", "day", "user", "amount", "price", "flag", "tiny", "cents"]
+    types = [abi.SMALLINT, abi.DATE, abi.BIGINT, abi.BIGINT, abi.DOUBLE, abi.BOOLEAN, abi.TINYINT, abi.DECIMAL64]
+    values = [np.repeat(rng.integers(0, 6, n // 500 + 1), 500)[:n].astype(np.int16),
+              (19000 + np.arange(n) // 997).astype(np.int32),
+              rng.integers(0, 50_000, n).astype(np.int64),
+              rng.integers(-10**9, 10**9, n).astype(np.int64),
+              np.round(rng.random(n) * 1000, 2),
+              (rng.random(n) > 0.7).astype(np.uint8),
+              rng.integers(-100, 100, n).astype(np.int8),
+              rng.integers(-10**6, 10**6, n).astype(np.int64)]
+    validity = [None, rng.random(n) > 0.02, rng.random(n) > 0.05, None, rng.random(n) > 0.1, None,
+                rng.random(n) > 0.2, None]
+    return names, types, values, validity

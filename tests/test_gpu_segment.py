@@ -105,3 +105,24 @@ def test_ten_million_rows_auto_encodings():
     for req in REQUESTS[:3]:
         run_and_compare(t, cols, req, ordered=bool(req.order_specs))
     t.close()
+
+
+@pytest.mark.parametrize("encoding", [None, "raw", "for", "for8", "rle"])
+@pytest.mark.parametrize("rg", [65_536, 1_000, 37])
+def test_decoded_columns_are_bit_exact_with_the_oracle_decode(encoding, rg):
+    # row groups of 1,000 and 37 rows put block boundaries inside validity words
+    cols = columns(150_001 if rg > 37 else 20_001, 6)
+    image, _ = write_segment([c.type for c in cols], [c.data for c in cols], [c.validity for c in cols],
+                             row_group_rows=rg, encoding=encoding)
+    t = Table.from_segment(image, [Column(c.name, c.type, None, scale=c.scale, precision=c.precision) for c in cols])
+    want = oracle.decode_segment(image, [c.type for c in cols], [c.validity is not None for c in cols])
+    for c, (wv, wok) in zip(cols, want):
+        gv, gok = t.read_column(c.name)
+        assert np.array_equal(gv.view(np.uint8), wv.view(np.uint8)), c.name
+        if wok is None:
+            assert gok.all()
+        else:
+            assert np.array_equal(gok, wok), c.name
+    st = t.load_stats()
+    assert st.image_bytes == len(image) and st.kernel_launches == 1 and st.blocks == len(cols) * -(-t.n_rows // rg)
+    t.close()

@@ -170,3 +170,45 @@ def test_unsupported_blocks_are_reported(what):
     with pytest.raises(EngineError) as e:
         register(image, types)
     assert e.value.status == abi.ERR_UNSUPPORTED_TYPE, str(e.value)
+
+
+@pytest.mark.parametrize("encoding", [None, "raw", "for", "for8", "rle"])
+@pytest.mark.parametrize("rg", [1024, 1000])
+def test_oracle_decode_matches_the_writer_input(encoding, rg):
+    import oracle
+    rng = np.random.default_rng(5)
+    n = 7_777
+    types = [abi.INT, abi.BIGINT, abi.DOUBLE, abi.TINYINT, abi.DATETIME]
+    values = [np.repeat(rng.integers(-3, 3, n // 10 + 1), 10)[:n].astype(np.int32),
+              rng.integers(-2**63, 2**63 - 1, n, dtype=np.int64), rng.random(n),
+              rng.integers(-128, 127, n).astype(np.int8), (10**12 + rng.integers(0, 10**6, n)).astype(np.int64)]
+    validity = [rng.random(n) > 0.3, None, rng.random(n) > 0.5, rng.random(n) > 0.9, None]
+    image, _ = write_segment(types, values, validity, row_group_rows=rg, encoding=encoding)
+    for threads in (1, 4):
+        got = oracle.decode_segment(image, types, [v is not None for v in validity], threads=threads)
+        for c, (vals, ok) in enumerate(got):
+            want_ok = np.ones(n, bool) if validity[c] is None else validity[c]
+            if validity[c] is None:
+                assert ok is None
+            else:
+                assert np.array_equal(ok, want_ok)
+            assert np.array_equal(vals[want_ok], np.asarray(values[c])[want_ok])
+
+
+def test_replicated_image_repeats_the_rows():
+    import oracle
+    from golden.segments import replicate, sample_table
+    names, types, values, validity = sample_table(3_000)
+    image, _ = write_segment(types, values, validity, row_group_rows=1024)
+    big = replicate(image, len(types), 3)
+    got = oracle.decode_segment(big, types, [v is not None for v in validity])
+    for c, (vals, ok) in enumerate(got):
+        want_ok = np.ones(3_000, bool) if validity[c] is None else validity[c]
+        okr = np.tile(want_ok, 3)
+        assert np.array_equal(vals[okr], np.tile(values[c], 3)[okr])
+        if validity[c] is not None:
+            assert np.array_equal(ok, okr)
+    # the footer's size and trailing magic
+    assert big[-4:] == b"tDBS"
+    fsize = struct.unpack_from("<I", big, len(big) - 8)[0]
+    assert struct.unpack_from("<I", big, len(big) - fsize)[0] == 9  # row groups: 3 x 3

@@ -240,7 +240,15 @@ class SegmentColumn(C.Structure):
                 ("decimal_scale", C.c_uint8), ("reserved", C.c_uint8 * 2)]
 
 
+class LoadStats(C.Structure):
+    _fields_ = [("image_bytes", C.c_uint64), ("decoded_bytes", C.c_uint64), ("blocks", C.c_uint32),
+                ("kernel_launches", C.c_uint32), ("h2d_ms", C.c_double), ("decode_ms", C.c_double),
+                ("stats_ms", C.c_double), ("total_ms", C.c_double)]
+
+
 SIGNATURES += [
+    ("tgpu_table_load_stats", C.c_int, [C.c_void_p, C.POINTER(LoadStats)]),
+    ("tgpu_table_read_column", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     ("tgpu_table_register_segment", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(SegmentColumn), C.c_uint32,
                                               C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
 ]

@@ -319,6 +319,7 @@ struct tgpu_table {
     cudaStream_t stream = nullptr;  // registration stream: the columns are freed on it
     mutable std::mutex key_mu;
     mutable std::map<std::vector<int32_t>, uint64_t> key_ndv;  // composite-key NDV per group-column list
+    tgpu_load_stats load{};  // registration from a segment image
     ~tgpu_table() {
         // Queries on other streams that read the table have finished (a
         // query's next/synchronize waits for it; destroying a table under a
@@ -1805,6 +1806,7 @@ tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out) {
 tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, const tgpu_segment_column *columns,
                                         uint32_t n_columns, int32_t compute_ndv, void *stream, tgpu_table **out) {
     if (!image || !columns || !n_columns || !out) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
+    const auto t_call = std::chrono::steady_clock::now();
     auto u16 = [&](uint64_t o) { uint16_t v; std::memcpy(&v, image + o, 2); return v; };
     auto u32 = [&](uint64_t o) { uint32_t v; std::memcpy(&v, image + o, 4); return v; };
     auto u64 = [&](uint64_t o) { uint64_t v; std::memcpy(&v, image + o, 8); return v; };
@@ -1854,6 +1856,7 @@ tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, co
             b.encoding = enc;
             b.has_nulls = has_nulls;
             b.width = elem;
+            b.elem = elem;
             if (enc == 0) {
                 if ((uint64_t)bm + (uint64_t)rows * elem > usize) return fail(TGPU_ERR_INVALID_ARGUMENT, "raw block size");
             } else if (enc == 1) {
@@ -1866,7 +1869,7 @@ tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, co
                 if (!integer || (uint64_t)bm + 8 > usize) return fail(TGPU_ERR_INVALID_ARGUMENT, "RLE block");
                 b.runs = u32(payload + bm);
                 b.width = image[payload + bm + 4];
-                if (b.width == 0 || b.width > elem ||
+                if ((b.width != 1 && b.width != 2 && b.width != 4 && b.width != 8) || b.width > elem ||
                     (uint64_t)bm + 8 + (uint64_t)b.runs * (b.width + 4) > usize || (b.runs == 0) != (rows == 0))
                     return fail(TGPU_ERR_INVALID_ARGUMENT, "RLE block size");
                 b.run0 = (uint32_t)run_starts.size();
@@ -1890,19 +1893,14 @@ tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, co
     tgpu_status st = device_ctx(&dev);
     if (st != TGPU_OK) return st;
     cudaStream_t s = stream ? (cudaStream_t)stream : dev->stream;
-    // the image, the block lists and the run starts, then every column decoded
-    std::vector<SegBlock> all;
-    std::vector<uint32_t> first(n_columns + 1, 0);
-    for (uint32_t c = 0; c < n_columns; ++c) {
-        first[c] = (uint32_t)all.size();
-        all.insert(all.end(), blocks[c].begin(), blocks[c].end());
-    }
-    first[n_columns] = (uint32_t)all.size();
+    // columns and validity words first (the blocks point into them), then the
+    // image, the block list and the run starts, then one decode launch
     uint8_t *d_image = nullptr;
     SegBlock *d_blocks = nullptr;
     uint32_t *d_runs = nullptr;
     std::vector<void *> data(n_columns, nullptr);
     std::vector<uint32_t *> valid(n_columns, nullptr);
+    cudaEvent_t ev[4] = {};
     auto release = [&](bool keep_data) {
         cudaStreamSynchronize(s);
         if (d_image) cudaFreeAsync(d_image, s);
@@ -1913,8 +1911,32 @@ tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, co
             if (!keep_data && data[c]) cudaFreeAsync(data[c], s);
         }
         cudaStreamSynchronize(s);
+        for (cudaEvent_t &e : ev)
+            if (e) cudaEventDestroy(e);
     };
-    cudaError_t e = cudaMallocFromPoolAsync((void **)&d_image, bytes, dev->col_pool, s);
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaEventCreate(&ev[k]);
+    uint64_t decoded = 0;
+    for (uint32_t c = 0; c < n_columns && e == cudaSuccess; ++c) {
+        const size_t elem = (size_t)type_bytes(columns[c].type);
+        e = cudaMallocFromPoolAsync(&data[c], round_up(std::max<size_t>(n * elem, 16), 16), dev->col_pool, s);
+        decoded += n * elem;
+        if (e == cudaSuccess && nullable[c]) {
+            const size_t vw = ((n + 31) / 32 + 1) * 4;
+            e = cudaMallocFromPoolAsync((void **)&valid[c], vw, dev->col_pool, s);
+            if (e == cudaSuccess) e = cudaMemsetAsync(valid[c], 0, vw, s);
+            decoded += (n + 7) / 8;
+        }
+    }
+    std::vector<SegBlock> all;
+    for (uint32_t c = 0; c < n_columns; ++c)
+        for (SegBlock b : blocks[c]) {
+            b.out = data[c];
+            b.valid = valid[c];
+            all.push_back(b);
+        }
+    if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
+    if (e == cudaSuccess) e = cudaMallocFromPoolAsync((void **)&d_image, bytes + SEG_IMAGE_PAD, dev->col_pool, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_image, image, bytes, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
         e = cudaMallocFromPoolAsync((void **)&d_blocks, std::max<size_t>(1, all.size()) * sizeof(SegBlock), dev->col_pool, s);
@@ -1924,24 +1946,23 @@ tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, co
         e = cudaMallocFromPoolAsync((void **)&d_runs, std::max<size_t>(1, run_starts.size()) * 4, dev->col_pool, s);
     if (e == cudaSuccess && !run_starts.empty())
         e = cudaMemcpyAsync(d_runs, run_starts.data(), run_starts.size() * 4, cudaMemcpyHostToDevice, s);
-    for (uint32_t c = 0; c < n_columns && e == cudaSuccess; ++c) {
-        const size_t elem = (size_t)type_bytes(columns[c].type);
-        e = cudaMallocFromPoolAsync(&data[c], round_up(std::max<size_t>(n * elem, 16), 16), dev->col_pool, s);
-        if (e == cudaSuccess && nullable[c]) {
-            const size_t vw = ((n + 31) / 32 + 1) * 4;
-            e = cudaMallocFromPoolAsync((void **)&valid[c], vw, dev->col_pool, s);
-            if (e == cudaSuccess) e = cudaMemsetAsync(valid[c], 0, vw, s);
-        }
-        if (e == cudaSuccess)
-            e = launch_decode_blocks(d_image, d_blocks + first[c], first[c + 1] - first[c], d_runs, data[c],
-                                     (uint32_t)elem, valid[c], s);
-    }
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1], s);
+    if (e == cudaSuccess) e = launch_decode_blocks(d_image, d_blocks, (uint32_t)all.size(), d_runs, s);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[2], s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
         cudaGetLastError();
         release(false);
         return fail(TGPU_ERR_CUDA, std::string("segment decode: ") + cudaGetErrorString(e));
     }
+    tgpu_load_stats ls{};
+    ls.image_bytes = bytes;
+    ls.decoded_bytes = decoded;
+    ls.blocks = (uint32_t)all.size();
+    ls.kernel_launches = all.empty() ? 0 : 1;
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, ev[0], ev[1]) == cudaSuccess) ls.h2d_ms = ms;
+    if (cudaEventElapsedTime(&ms, ev[1], ev[2]) == cudaSuccess) ls.decode_ms = ms;
     // register the decoded columns in place, then hand them to the table
     std::vector<tgpu_column_desc> cd(n_columns);
     for (uint32_t c = 0; c < n_columns; ++c) {
@@ -1962,15 +1983,42 @@ tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, co
     td.compute_ndv = compute_ndv;
     td.stream = s;
     tgpu_table *t = nullptr;
+    const auto r0 = std::chrono::steady_clock::now();
     st = tgpu_table_register(&td, &t);
     if (st != TGPU_OK) {
         const std::string msg = g_err;
         release(false);
         return fail(st, msg);
     }
+    const auto r1 = std::chrono::steady_clock::now();
+    ls.stats_ms = std::chrono::duration<double, std::milli>(r1 - r0).count();
     for (uint32_t c = 0; c < n_columns; ++c) t->cols[c].owned = true;  // freed with the table
     release(true);
+    ls.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_call).count();
+    t->load = ls;
     *out = t;
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_table_read_column(const tgpu_table *t, uint32_t column, void *values, uint8_t *validity) {
+    if (!t || !values || column >= t->cols.size()) return fail(TGPU_ERR_INVALID_ARGUMENT, "null table or bad column");
+    const Column &c = t->cols[column];
+    if (c.type == TGPU_VARCHAR) return fail(TGPU_ERR_UNSUPPORTED_TYPE, "VARCHAR columns read back by key strings");
+    const size_t n = t->n_rows, bytes = n * type_bytes(c.type), vb = (n + 7) / 8;
+    cudaError_t e = cudaSuccess;
+    if (bytes) e = cudaMemcpyAsync(values, c.d_data, bytes, cudaMemcpyDeviceToHost, t->stream);
+    if (e == cudaSuccess && validity && vb) {
+        if (c.d_valid) e = cudaMemcpyAsync(validity, c.d_valid, vb, cudaMemcpyDeviceToHost, t->stream);
+        else std::memset(validity, 0xFF, vb);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(t->stream);
+    if (e != cudaSuccess) return fail(TGPU_ERR_CUDA, std::string("read column: ") + cudaGetErrorString(e));
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_table_load_stats(const tgpu_table *table, tgpu_load_stats *out) {
+    if (!table || !out) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
+    *out = table->load;
     return TGPU_OK;
 }
 

@@ -348,20 +348,24 @@ cudaError_t launch_radix(const DevQuery &q, const RadixPlan &rp, int sms, cudaSt
 // [row0, row0 + rows) of its column, payload at image offset `payload`, the
 // value region `values` bytes into it (past the validity bitmap).
 struct SegBlock {
-    uint64_t row0;
-    uint64_t payload;
-    uint32_t values;
+    uint64_t row0;       // the block's first row in the table
+    uint64_t payload;    // byte offset of the payload in the image
+    void *out;           // the decoded column (elem bytes per row)
+    uint32_t *valid;     // the column's validity words (null: NOT NULL)
+    uint32_t values;     // payload offset of the values (past the validity bitmap)
     uint32_t rows;
     uint32_t encoding;   // 0 raw, 1 FOR, 3 RLE (format.Encoding)
-    uint32_t width;      // FOR delta / RLE value width in bytes
+    uint32_t width;      // FOR delta / RLE value / raw element width in bytes
     uint32_t runs;       // RLE runs
     uint32_t run0;       // RLE: index of its first run start in the run-start array
+    uint32_t elem;       // decoded element bytes (1, 2, 4, 8)
     uint32_t has_nulls;
-    uint32_t pad;
 };
+// Image buffers carry this many readable bytes past their end: the decoder
+// reads whole aligned words around unaligned values.
+constexpr uint32_t SEG_IMAGE_PAD = 16;
 cudaError_t launch_decode_blocks(const uint8_t *image, const SegBlock *blocks, uint32_t n_blocks,
-                                 const uint32_t *run_starts, void *out, uint32_t bytes, uint32_t *valid,
-                                 cudaStream_t s);
+                                 const uint32_t *run_starts, cudaStream_t s);
 
 // Partitioned COUNT(DISTINCT): pairs per partition (one CTA deduplicates a
 // partition in shared memory) and the partition's index-table slots.

@@ -16,31 +16,35 @@
 //   FOR  : i128 base, u8 width (1/2/4/8), 3 pad, rows x width unsigned LE
 //          deltas, value = base + delta (forBlockOf :1809, expandWidth);
 //   RLE  : u32 runs, u8 value width, 3 pad, runs x value, runs x u32 length
-//          (rleBlockOf, :2133).
+//          (rleBlockOf, :2098).
 // The host checks every header and bound, computes each RLE block's run
 // starts, and copies the image to the device once; decode_blocks_kernel then
-// expands every block of a column into the resident column (one CTA per
-// block) and sets its validity bits.  Blocks stored compressed (zstd, lz4)
-// or with integer-stream transforms, string columns (whose blocks live in
-// string tables) and dictionary / FSST encodings are not decoded here: the
-// call returns TGPU_ERR_UNSUPPORTED_TYPE.
-#include <cstring>
-#include <memory>
-#include <string>
-#include <vector>
-
+// expands every block of every column (one CTA per block, one launch) into
+// the resident columns and their validity words.  Payloads sit at arbitrary
+// byte offsets, so values are read as whole aligned 32-bit words and shifted
+// into place (the image buffer is padded past its end for the last word).
+// Blocks stored compressed (zstd, lz4) or with integer-stream transforms,
+// string columns (whose blocks live in string tables) and dictionary / FSST
+// encodings are not decoded here: the call returns TGPU_ERR_UNSUPPORTED_TYPE.
 #include "common.cuh"
 
 namespace tgpu {
 
 namespace {
 
-constexpr uint32_t ENC_RAW = 0, ENC_FOR = 1, ENC_RLE = 3;
+constexpr uint32_t ENC_RAW = 0, ENC_FOR = 1;
+constexpr int DECODE_THREADS = 512;
+constexpr uint32_t SMEM_RUNS = 4096;  // RLE run starts staged in shared memory up to this many runs
 
-__device__ __forceinline__ uint64_t ld_le(const uint8_t *p, uint32_t width) {
-    uint64_t v = 0;
-    for (uint32_t b = 0; b < width; ++b) v |= (uint64_t)p[b] << (8 * b);
-    return v;
+// Bytes p[0, w) (w = 1, 2, 4 or 8) as a little-endian integer, read as the
+// aligned words around them.
+__device__ __forceinline__ uint64_t ld_bytes(const uint8_t *p, uint32_t w) {
+    const uint32_t a = (uint32_t)((uintptr_t)p & 3u);
+    const uint32_t *q = (const uint32_t *)(p - a);
+    const uint32_t w0 = __ldg(q), w1 = __ldg(q + 1);
+    const uint32_t lo = __funnelshift_r(w0, w1, 8 * a);
+    if (w == 8) return ((uint64_t)__funnelshift_r(w1, __ldg(q + 2), 8 * a) << 32) | lo;
+    return w == 4 ? lo : lo & ((1u << (8 * w)) - 1u);
 }
 
 __device__ __forceinline__ void st_elem(void *out, uint32_t bytes, uint64_t row, uint64_t v) {
@@ -52,50 +56,74 @@ __device__ __forceinline__ void st_elem(void *out, uint32_t bytes, uint64_t row,
     }
 }
 
-// One CTA per block: expand the block's values into out[row0, row0 + rows)
-// (elements of `bytes` bytes) and OR its validity bits into `valid`.
-__global__ void decode_blocks_kernel(const uint8_t *__restrict__ image, const SegBlock *__restrict__ blocks,
-                                     const uint32_t *__restrict__ run_starts, void *out, uint32_t bytes,
-                                     uint32_t *valid) {
+// Validity: the block's bitmap bits land at table rows row0 + i.  A word that
+// lies wholly inside the block is stored; the (at most two) words it shares
+// with neighbouring blocks are OR'ed in.
+__device__ void decode_validity(const uint8_t *bm, const SegBlock &b) {
+    const uint64_t first = b.row0 >> 5, last = (b.row0 + b.rows - 1) >> 5;
+    for (uint64_t w = first + threadIdx.x; w <= last; w += blockDim.x) {
+        // block-local bit of the word's row 0 (negative for a word starting before the block)
+        const int64_t l0 = (int64_t)(w << 5) - (int64_t)b.row0;
+        uint32_t word = 0;
+        for (int byte = 0; byte < 5; ++byte) {
+            const int64_t bit = l0 + 8 * byte - (l0 & 7);  // bitmap bytes covering the word's 32 rows
+            if (bit + 8 <= 0 || bit >= (int64_t)b.rows) continue;
+            const uint32_t v = bm[bit >> 3];
+            const int64_t sh = bit - l0;                   // row of the word this byte's bit 0 lands on
+            if (sh >= 0) word |= sh < 32 ? v << sh : 0u;
+            else word |= v >> -sh;
+        }
+        const uint64_t r0 = w << 5;
+        const bool inner = r0 >= b.row0 && r0 + 32 <= b.row0 + b.rows;
+        if (inner) {
+            b.valid[w] = word;
+        } else {
+            // keep only the block's own rows
+            const int64_t lo = (int64_t)b.row0 - (int64_t)r0, hi = (int64_t)(b.row0 + b.rows) - (int64_t)r0;
+            uint32_t mask = ~0u;
+            if (lo > 0) mask &= ~0u << lo;
+            if (hi < 32) mask &= (1u << hi) - 1u;
+            if (word & mask) atomicOr(b.valid + w, word & mask);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(DECODE_THREADS) decode_blocks_kernel(const uint8_t *__restrict__ image,
+                                                                       const SegBlock *__restrict__ blocks,
+                                                                       const uint32_t *__restrict__ run_starts) {
+    __shared__ uint32_t s_starts[SMEM_RUNS];
     const SegBlock b = blocks[blockIdx.x];
     const uint8_t *p = image + b.payload;
-    if (b.has_nulls && valid) {
-        for (uint32_t i = threadIdx.x; i < b.rows; i += blockDim.x)
-            if ((p[i >> 3] >> (i & 7)) & 1u) {
-                const uint64_t r = b.row0 + i;
-                atomicOr(valid + (r >> 5), 1u << (r & 31));
-            }
-    }
+    if (b.has_nulls && b.valid) decode_validity(p, b);
     const uint8_t *v = p + b.values;
-    switch (b.encoding) {
-        case ENC_RAW:
-            for (uint32_t i = threadIdx.x; i < b.rows; i += blockDim.x)
-                st_elem(out, bytes, b.row0 + i, ld_le(v + (size_t)i * bytes, bytes));
-            break;
-        case ENC_FOR: {
-            // the add wraps in the element's width, as expandWidth's +%
-            const uint64_t base = ld_le(v, 8);
-            const uint8_t *codes = v + 20;
-            for (uint32_t i = threadIdx.x; i < b.rows; i += blockDim.x)
-                st_elem(out, bytes, b.row0 + i, base + ld_le(codes + (size_t)i * b.width, b.width));
-            break;
+    if (b.encoding == ENC_RAW) {
+        for (uint32_t i = threadIdx.x; i < b.rows; i += blockDim.x)
+            st_elem(b.out, b.elem, b.row0 + i, ld_bytes(v + (size_t)i * b.elem, b.elem));
+    } else if (b.encoding == ENC_FOR) {
+        // the add wraps in the element's width, as expandWidth's +%
+        const uint64_t base = ld_bytes(v, 8);
+        const uint8_t *codes = v + 20;
+        for (uint32_t i = threadIdx.x; i < b.rows; i += blockDim.x)
+            st_elem(b.out, b.elem, b.row0 + i, base + ld_bytes(codes + (size_t)i * b.width, b.width));
+    } else {  // RLE: each row finds its run among the run starts
+        const uint32_t *starts = run_starts + b.run0;
+        if (b.runs <= SMEM_RUNS) {
+            for (uint32_t r = threadIdx.x; r < b.runs; r += blockDim.x) s_starts[r] = starts[r];
+            __syncthreads();
+            starts = s_starts;
         }
-        default: {  // RLE: each row finds its run among the run starts
-            const uint32_t *starts = run_starts + b.run0;
-            const uint8_t *vals = v + 8;
-            for (uint32_t i = threadIdx.x; i < b.rows; i += blockDim.x) {
-                uint32_t lo = 0, hi = b.runs;  // the last run starting at or before i
-                while (hi - lo > 1) {
-                    const uint32_t mid = (lo + hi) / 2;
-                    if (starts[mid] <= i) lo = mid;
-                    else hi = mid;
-                }
-                // a value narrower than the element sign-extends as the writer truncated it
-                uint64_t x = ld_le(vals + (size_t)lo * b.width, b.width);
-                if (b.width < 8 && ((x >> (8 * b.width - 1)) & 1u)) x |= ~0ULL << (8 * b.width);
-                st_elem(out, bytes, b.row0 + i, x);
+        const uint8_t *vals = v + 8;
+        for (uint32_t i = threadIdx.x; i < b.rows; i += blockDim.x) {
+            uint32_t lo = 0, hi = b.runs;  // the last run starting at or before i
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) / 2;
+                if (starts[mid] <= i) lo = mid;
+                else hi = mid;
             }
-            break;
+            // a value narrower than the element sign-extends
+            uint64_t x = ld_bytes(vals + (size_t)lo * b.width, b.width);
+            if (b.width < 8 && ((x >> (8 * b.width - 1)) & 1u)) x |= ~0ULL << (8 * b.width);
+            st_elem(b.out, b.elem, b.row0 + i, x);
         }
     }
 }
@@ -103,10 +131,9 @@ __global__ void decode_blocks_kernel(const uint8_t *__restrict__ image, const Se
 }  // namespace
 
 cudaError_t launch_decode_blocks(const uint8_t *image, const SegBlock *blocks, uint32_t n_blocks,
-                                 const uint32_t *run_starts, void *out, uint32_t bytes, uint32_t *valid,
-                                 cudaStream_t s) {
+                                 const uint32_t *run_starts, cudaStream_t s) {
     if (!n_blocks) return cudaSuccess;
-    decode_blocks_kernel<<<n_blocks, 256, 0, s>>>(image, blocks, run_starts, out, bytes, valid);
+    decode_blocks_kernel<<<n_blocks, DECODE_THREADS, 0, s>>>(image, blocks, run_starts);
     return cudaGetLastError();
 }
 

@@ -241,15 +241,20 @@ class Table:
     @classmethod
     def from_segment(cls, image: bytes, columns: Sequence[Column], compute_ndv: bool = True,
                      stream: int = 0) -> "Table":
-        """Register a thinDB segment file image (src/storage/format.zig layout):
-        `columns` name the schema in order (name, type, decimal scale and
-        precision; `data` unused).  The blocks decode on the device; the row
+        """Register a thinDB segment file image (src/storage/format.zig layout;
+        bytes, a uint8 numpy array or a host tensor): `columns` name the
+        schema in order (name, type, decimal scale and precision; `data`
+        unused).  The blocks decode on the device; the row
         groups keep the segment's size."""
         self = cls.__new__(cls)
         self.columns = list(columns)
         if not self.columns:
             raise ValueError("a table needs columns")
-        buf = np.frombuffer(bytes(image), dtype=np.uint8)
+        if hasattr(image, "data_ptr"):  # a (pinned) host tensor
+            ptr, size = int(image.data_ptr()), int(image.numel() * image.element_size())
+        else:
+            buf = image if isinstance(image, np.ndarray) else np.frombuffer(image, dtype=np.uint8)
+            ptr, size = int(buf.ctypes.data), int(buf.nbytes)
         names = [c.name.encode() for c in self.columns]
         descs = (abi.SegmentColumn * len(self.columns))()
         for i, c in enumerate(self.columns):
@@ -258,7 +263,7 @@ class Table:
             descs[i].decimal_precision = c.precision
             descs[i].decimal_scale = c.scale
         h = C.c_void_p()
-        _check(lib().tgpu_table_register_segment(_ptr(buf) if buf.size else None, buf.size, descs,
+        _check(lib().tgpu_table_register_segment(ptr if size else None, size, descs,
                                                  len(self.columns), 1 if compute_ndv else 0, stream or None,
                                                  C.byref(h)))
         self.handle = h
@@ -269,6 +274,21 @@ class Table:
         self.row_group_rows = 0
         self.n_row_groups = groups.value
         return self
+
+    def read_column(self, name: str) -> tuple:
+        """A column's values and validity (bool per row) copied back to the host."""
+        i = self.col_index(name)
+        ty = self.columns[i].type
+        vals = np.empty(self.n_rows, dtype=NP_DTYPES[ty])
+        bm = np.empty((self.n_rows + 7) // 8 + 1, dtype=np.uint8)
+        _check(lib().tgpu_table_read_column(self.handle, i, vals.ctypes.data, bm.ctypes.data))
+        return vals, np.unpackbits(bm, bitorder="little")[:self.n_rows].astype(bool)
+
+    def load_stats(self) -> abi.LoadStats:
+        """Timings and byte counts of a registration from a segment image."""
+        st = abi.LoadStats()
+        _check(lib().tgpu_table_load_stats(self.handle, C.byref(st)))
+        return st
 
     def col_index(self, name: str) -> int:
         for i, c in enumerate(self.columns):
