@@ -1668,7 +1668,11 @@ tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out) {
     const size_t stat_bytes = round_up(nrg * (8 * 4 + 4), 256);
     const size_t reg_bytes = (size_t)(1u << HLL_P) * 4;
     unsigned char *d_stats = nullptr;
-    CU(cudaMallocFromPoolAsync((void **)&d_stats, std::max<size_t>(1, nc) * (stat_bytes + reg_bytes), dev->col_pool, s));
+    // (then one HLL scratch shared by the columns, whose statistics run in turn on one stream)
+    const size_t part_bytes = (size_t)STATS_GRID_MAX << HLL_P;
+    CU(cudaMallocFromPoolAsync((void **)&d_stats, std::max<size_t>(1, nc) * (stat_bytes + reg_bytes) + part_bytes,
+                               dev->col_pool, s));
+    uint8_t *d_part = d_stats + std::max<size_t>(1, nc) * (stat_bytes + reg_bytes);
     struct StatsGuard {  // an error return leaves nothing allocated behind
         unsigned char *&p;
         cudaStream_t a, b;
@@ -1762,11 +1766,13 @@ tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out) {
         double *fmin = (double *)(imax + nrg), *fmax = fmin + nrg;
         uint32_t *nulls = (uint32_t *)(fmax + nrg);
         uint32_t *regs = (uint32_t *)(st + stat_bytes);
-        if (t->n_rg && c.type != TGPU_VARCHAR)  // strings: no zone maps (no WHERE on them here)
-            CU(launch_zone_maps(c.d_data, c.d_valid, c.type, n, t->rg_rows, t->n_rg, imin, imax, fmin, fmax, nulls, ss));
         c.ndv = cd.ndv_hint;
         sketch[i] = !c.ndv && desc->compute_ndv && n;
-        if (sketch[i]) {
+        if (c.type != TGPU_VARCHAR) {
+            // zone maps and the sketch in one pass over the column
+            CU(launch_column_stats(c.d_data, c.d_valid, c.type, n, t->rg_rows, t->n_rg, imin, imax, fmin, fmax, nulls,
+                                   sketch[i] ? regs : nullptr, d_part, ss));
+        } else if (sketch[i]) {  // strings: no zone maps (no WHERE on them here)
             CU(cudaMemsetAsync(regs, 0, reg_bytes, ss));
             CU(launch_hll(c.d_data, c.d_valid, c.type, n, regs, ss, c.d_offs));
         }

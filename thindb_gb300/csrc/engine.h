@@ -439,11 +439,14 @@ cudaError_t launch_gather(const DevFinal &f, const uint32_t *sel, unsigned long 
 cudaError_t launch_clear(unsigned long long *table, uint64_t cap, int32_t slot_words, uint32_t *occ, cudaStream_t s);
 
 // table statistics
-cudaError_t launch_zone_maps(const void *data, const uint32_t *valid, int32_t type, uint64_t n_rows,
-                             uint32_t rg_rows, uint32_t n_rg, int64_t *imin, int64_t *imax, double *fmin,
-                             double *fmax, uint32_t *nulls, cudaStream_t s);
 cudaError_t launch_hll(const void *data, const uint32_t *valid, int32_t type, uint64_t n_rows, uint32_t *regs,
                        cudaStream_t s, const uint32_t *offs = nullptr);
+// Zone maps and (regs non-null) the HLL registers of a fixed-width column in
+// one pass; `part` is scratch of STATS_GRID_MAX x 2^HLL_P bytes.
+constexpr uint32_t STATS_GRID_MAX = 512;
+cudaError_t launch_column_stats(const void *data, const uint32_t *valid, int32_t type, uint64_t n_rows,
+                                uint32_t rg_rows, uint32_t n_rg, int64_t *imin, int64_t *imax, double *fmin,
+                                double *fmax, uint32_t *nulls, uint32_t *regs, uint8_t *part, cudaStream_t s);
 // Columns of a composite key for its HyperLogLog sketch.
 struct KeySketchCols {
     const void *data[MAX_GROUP_KEYS];

@@ -34,6 +34,7 @@ namespace {
 
 constexpr uint32_t ENC_RAW = 0, ENC_FOR = 1;
 constexpr int DECODE_THREADS = 512;
+constexpr int DECODE_UNROLL = 4;
 constexpr uint32_t SMEM_RUNS = 4096;  // RLE run starts staged in shared memory up to this many runs
 
 // Bytes p[0, w) (w = 1, 2, 4 or 8) as a little-endian integer, read as the
@@ -96,15 +97,27 @@ __global__ void __launch_bounds__(DECODE_THREADS) decode_blocks_kernel(const uin
     const uint8_t *p = image + b.payload;
     if (b.has_nulls && b.valid) decode_validity(p, b);
     const uint8_t *v = p + b.values;
-    if (b.encoding == ENC_RAW) {
-        for (uint32_t i = threadIdx.x; i < b.rows; i += blockDim.x)
-            st_elem(b.out, b.elem, b.row0 + i, ld_bytes(v + (size_t)i * b.elem, b.elem));
-    } else if (b.encoding == ENC_FOR) {
-        // the add wraps in the element's width, as expandWidth's +%
-        const uint64_t base = ld_bytes(v, 8);
-        const uint8_t *codes = v + 20;
-        for (uint32_t i = threadIdx.x; i < b.rows; i += blockDim.x)
-            st_elem(b.out, b.elem, b.row0 + i, base + ld_bytes(codes + (size_t)i * b.width, b.width));
+    if (b.encoding == ENC_RAW || b.encoding == ENC_FOR) {
+        // raw: base 0, codes of the element's width; FOR: the add wraps in the
+        // element's width, as expandWidth's +%.  Four rows per thread per
+        // pass, their loads issued before their stores.
+        const bool raw = b.encoding == ENC_RAW;
+        const uint64_t base = raw ? 0 : ld_bytes(v, 8);
+        const uint8_t *codes = raw ? v : v + 20;
+        const uint32_t w = raw ? b.elem : b.width, step = blockDim.x;
+        for (uint32_t i0 = threadIdx.x; i0 < b.rows; i0 += DECODE_UNROLL * step) {
+            uint64_t x[DECODE_UNROLL];
+#pragma unroll
+            for (int k = 0; k < DECODE_UNROLL; ++k) {
+                const uint32_t i = i0 + k * step;
+                x[k] = i < b.rows ? base + ld_bytes(codes + (size_t)i * w, w) : 0;
+            }
+#pragma unroll
+            for (int k = 0; k < DECODE_UNROLL; ++k) {
+                const uint32_t i = i0 + k * step;
+                if (i < b.rows) st_elem(b.out, b.elem, b.row0 + i, x[k]);
+            }
+        }
     } else {  // RLE: each row finds its run among the run starts
         const uint32_t *starts = run_starts + b.run0;
         if (b.runs <= SMEM_RUNS) {

@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <climits>
+#include <type_traits>
 
 #include <math_constants.h>
 
@@ -35,69 +36,6 @@ __device__ __forceinline__ int64_t int_at(const void *d, int32_t type, uint64_t 
 
 __device__ __forceinline__ double f_at(const void *d, int32_t type, uint64_t r) {
     return type == TGPU_FLOAT ? (double)((const float *)d)[r] : ((const double *)d)[r];
-}
-
-// One CTA per row group: min/max over the valid rows and the NULL count.
-__global__ void zone_map_kernel(const void *data, const uint32_t *valid, int32_t type, uint64_t n_rows,
-                                uint32_t rg_rows, int64_t *imin, int64_t *imax, double *zfmin, double *zfmax,
-                                uint32_t *nulls) {
-    __shared__ long long smin[32], smax[32];
-    __shared__ double sfmin[32], sfmax[32];
-    __shared__ unsigned snull[32];
-    const uint64_t b = (uint64_t)blockIdx.x * rg_rows, e = min(b + rg_rows, n_rows);
-    const bool is_f = type == TGPU_FLOAT || type == TGPU_DOUBLE;
-    long long mn = LLONG_MAX, mx = LLONG_MIN;
-    double fmn = DBL_MAX, fmx = -DBL_MAX;
-    unsigned nn = 0;
-    for (uint64_t r = b + threadIdx.x; r < e; r += blockDim.x) {
-        if (!valid_at(valid, r)) {
-            ++nn;
-            continue;
-        }
-        if (is_f) {
-            double x = f_at(data, type, r);
-            if (x == x) {
-                fmn = fmin(fmn, x);
-                fmx = fmax(fmx, x);
-            } else {
-                fmx = CUDART_INF;  // a NaN row can satisfy only open ranges; keep the map conservative
-            }
-        } else {
-            long long x = int_at(data, type, r);
-            mn = min(mn, x);
-            mx = max(mx, x);
-        }
-    }
-    for (int o = 16; o; o >>= 1) {
-        mn = min(mn, __shfl_down_sync(0xFFFFFFFFu, mn, o));
-        mx = max(mx, __shfl_down_sync(0xFFFFFFFFu, mx, o));
-        fmn = fmin(fmn, __shfl_down_sync(0xFFFFFFFFu, fmn, o));
-        fmx = fmax(fmx, __shfl_down_sync(0xFFFFFFFFu, fmx, o));
-        nn += __shfl_down_sync(0xFFFFFFFFu, nn, o);
-    }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) {
-        smin[warp] = mn;
-        smax[warp] = mx;
-        sfmin[warp] = fmn;
-        sfmax[warp] = fmx;
-        snull[warp] = nn;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
-            mn = min(mn, smin[w]);
-            mx = max(mx, smax[w]);
-            fmn = fmin(fmn, sfmin[w]);
-            fmx = fmax(fmx, sfmax[w]);
-            nn += snull[w];
-        }
-        imin[blockIdx.x] = mn;
-        imax[blockIdx.x] = mx;
-        zfmin[blockIdx.x] = fmn;
-        zfmax[blockIdx.x] = fmx;
-        nulls[blockIdx.x] = nn;
-    }
 }
 
 constexpr int HLL_M = 1 << HLL_P;
@@ -156,12 +94,153 @@ __global__ void key_hll_kernel(const __grid_constant__ KeySketchCols k, uint64_t
 
 }  // namespace
 
-cudaError_t launch_zone_maps(const void *data, const uint32_t *valid, int32_t type, uint64_t n_rows,
-                             uint32_t rg_rows, uint32_t n_rg, int64_t *imin, int64_t *imax, double *fmin,
-                             double *fmax, uint32_t *nulls, cudaStream_t s) {
-    if (n_rg == 0) return cudaSuccess;
-    zone_map_kernel<<<n_rg, 256, 0, s>>>(data, valid, type, n_rows, rg_rows, imin, imax, fmin, fmax, nulls);
+namespace {
+
+// Zone maps and the HyperLogLog registers of one fixed-width column in one
+// pass: persistent CTAs stride over the row groups (min/max/NULL count of
+// each, reduced in the CTA) and raise their own shared-memory registers;
+// each CTA then stores its registers as bytes to `part` (a row of HLL_M per
+// CTA) and hll_merge_kernel takes the maximum over the rows: one read of the
+// column, no global atomics.
+template <typename T>
+__global__ void __launch_bounds__(512) column_stats_kernel(const T *__restrict__ data, const uint32_t *__restrict__ valid,
+                                                           uint64_t n_rows, uint32_t rg_rows, uint32_t n_rg,
+                                                           int64_t *imin, int64_t *imax, double *zfmin, double *zfmax,
+                                                           uint32_t *nulls, uint8_t *part) {
+    extern __shared__ uint32_t sreg[];
+    __shared__ long long smin[16], smax[16];
+    __shared__ double sfmin[16], sfmax[16];
+    __shared__ unsigned snull[16];
+    constexpr bool is_f = std::is_floating_point<T>::value;
+    if (part) {
+        for (int i = threadIdx.x; i < HLL_M; i += blockDim.x) sreg[i] = 0;
+        __syncthreads();
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t g = blockIdx.x; g < n_rg; g += gridDim.x) {
+        const uint64_t b = (uint64_t)g * rg_rows, e = min(b + rg_rows, n_rows);
+        long long mn = LLONG_MAX, mx = LLONG_MIN;
+        double fmn = DBL_MAX, fmx = -DBL_MAX;
+        unsigned nn = 0;
+#pragma unroll 4
+        for (uint64_t r = b + threadIdx.x; r < e; r += blockDim.x) {
+            const bool ok = valid_at(valid, r);
+            const T x = data[r];
+            nn += ok ? 0u : 1u;
+            uint64_t bits;
+            if constexpr (is_f) {
+                const double d = (double)x;
+                if (ok) {
+                    if (d == d) {
+                        fmn = fmin(fmn, d);
+                        fmx = fmax(fmx, d);
+                    } else {
+                        fmx = CUDART_INF;  // a NaN row can satisfy only open ranges; keep the map conservative
+                    }
+                }
+                bits = canon_f64_bits(d);
+            } else {
+                const long long v = (long long)x;
+                if (ok) {
+                    mn = min(mn, v);
+                    mx = max(mx, v);
+                }
+                bits = (uint64_t)v;
+            }
+            if (part && ok) {
+                const uint64_t h = mix64(bits ^ 0x6A09E667F3BCC909ULL);
+                const uint32_t idx = (uint32_t)(h >> (64 - HLL_P));
+                const uint64_t w = (h << HLL_P) | (1ULL << (HLL_P - 1));
+                const uint32_t rank = (uint32_t)__clzll((long long)w) + 1;
+                if (rank > sreg[idx]) atomicMax(&sreg[idx], rank);
+            }
+        }
+        for (int o = 16; o; o >>= 1) {
+            mn = min(mn, __shfl_down_sync(0xFFFFFFFFu, mn, o));
+            mx = max(mx, __shfl_down_sync(0xFFFFFFFFu, mx, o));
+            fmn = fmin(fmn, __shfl_down_sync(0xFFFFFFFFu, fmn, o));
+            fmx = fmax(fmx, __shfl_down_sync(0xFFFFFFFFu, fmx, o));
+            nn += __shfl_down_sync(0xFFFFFFFFu, nn, o);
+        }
+        if (lane == 0) {
+            smin[warp] = mn;
+            smax[warp] = mx;
+            sfmin[warp] = fmn;
+            sfmax[warp] = fmx;
+            snull[warp] = nn;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+                mn = min(mn, smin[w]);
+                mx = max(mx, smax[w]);
+                fmn = fmin(fmn, sfmin[w]);
+                fmx = fmax(fmx, sfmax[w]);
+                nn += snull[w];
+            }
+            imin[g] = mn;
+            imax[g] = mx;
+            zfmin[g] = fmn;
+            zfmax[g] = fmx;
+            nulls[g] = nn;
+        }
+        __syncthreads();
+    }
+    if (part) {
+        __syncthreads();
+        uint8_t *row = part + (size_t)blockIdx.x * HLL_M;
+        for (int i = threadIdx.x; i < HLL_M; i += blockDim.x) row[i] = (uint8_t)sreg[i];
+    }
+}
+
+__global__ void hll_merge_kernel(const uint8_t *__restrict__ part, uint32_t rows, uint32_t *regs) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (uint32_t)HLL_M) return;
+    uint32_t m = 0;
+    for (uint32_t r = 0; r < rows; ++r) m = max(m, (uint32_t)part[(size_t)r * HLL_M + i]);
+    regs[i] = m;
+}
+
+template <typename T>
+cudaError_t launch_stats_t(const void *data, const uint32_t *valid, uint64_t n_rows, uint32_t rg_rows, uint32_t n_rg,
+                           int64_t *imin, int64_t *imax, double *fmin, double *fmax, uint32_t *nulls, uint32_t *regs,
+                           uint8_t *part, cudaStream_t s) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>({n_rg, 2u * (uint32_t)sms, STATS_GRID_MAX}));
+    const size_t smem = regs ? HLL_M * sizeof(uint32_t) : 0;
+    cudaError_t e = cudaFuncSetAttribute(column_stats_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         HLL_M * (int)sizeof(uint32_t));
+    if (e != cudaSuccess) return e;
+    column_stats_kernel<T><<<grid, 512, smem, s>>>((const T *)data, valid, n_rows, rg_rows, n_rg, imin, imax, fmin,
+                                                    fmax, nulls, regs ? part : nullptr);
+    e = cudaGetLastError();
+    if (e != cudaSuccess || !regs) return e;
+    hll_merge_kernel<<<HLL_M / 256, 256, 0, s>>>(part, grid, regs);
     return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_column_stats(const void *data, const uint32_t *valid, int32_t type, uint64_t n_rows,
+                                uint32_t rg_rows, uint32_t n_rg, int64_t *imin, int64_t *imax, double *fmin,
+                                double *fmax, uint32_t *nulls, uint32_t *regs, uint8_t *part, cudaStream_t s) {
+    if (n_rg == 0 || n_rows == 0) return cudaSuccess;
+    switch (type) {
+        case TGPU_BOOLEAN: return launch_stats_t<uint8_t>(data, valid, n_rows, rg_rows, n_rg, imin, imax, fmin, fmax, nulls, regs, part, s);
+        case TGPU_TINYINT: return launch_stats_t<int8_t>(data, valid, n_rows, rg_rows, n_rg, imin, imax, fmin, fmax, nulls, regs, part, s);
+        case TGPU_SMALLINT: return launch_stats_t<int16_t>(data, valid, n_rows, rg_rows, n_rg, imin, imax, fmin, fmax, nulls, regs, part, s);
+        case TGPU_INT: case TGPU_DATE: case TGPU_DICT32:
+            return launch_stats_t<int32_t>(data, valid, n_rows, rg_rows, n_rg, imin, imax, fmin, fmax, nulls, regs, part, s);
+        case TGPU_FLOAT: return launch_stats_t<float>(data, valid, n_rows, rg_rows, n_rg, imin, imax, fmin, fmax, nulls, regs, part, s);
+        case TGPU_DOUBLE: return launch_stats_t<double>(data, valid, n_rows, rg_rows, n_rg, imin, imax, fmin, fmax, nulls, regs, part, s);
+        default: return launch_stats_t<long long>(data, valid, n_rows, rg_rows, n_rg, imin, imax, fmin, fmax, nulls, regs, part, s);
+    }
 }
 
 cudaError_t launch_hll(const void *data, const uint32_t *valid, int32_t type, uint64_t n_rows, uint32_t *regs,
