@@ -606,10 +606,11 @@ def segment_reference_arm(args):
 
 
 def segment_arm(args):
-    """Register the image as a table, K times: host walk, H2D copy of the
-    image, one decode launch, zone maps and NDV sketches.  value: rows/s of
-    the device work once the image is resident (decode + statistics); e2e:
-    rows/s of the whole call from a pinned host image."""
+    """Register the image as a table, K times: host walk, then the image
+    copied in chunks of row groups, each chunk decoded and its zone maps and
+    NDV sketches taken while the next copies.  value: rows/s of that device
+    work (the decode and statistics launches' summed durations); e2e: rows/s
+    of the whole call from a pinned host image."""
     import torch
 
     from thindb_gb300.engine import Table
@@ -632,7 +633,7 @@ def segment_arm(args):
         t = Table.from_segment(host, schema, stream=stream.cuda_stream)
         wall.append(time.perf_counter() - t0)
         st = t.load_stats()
-        stats.append((st.h2d_ms, st.decode_ms, st.stats_ms, st.total_ms))
+        stats.append((st.h2d_ms, st.decode_ms, st.stats_ms, st.total_ms, st.pipeline_ms))
         t.close()
     torch.cuda.synchronize()
     clk = clocks.stop()
@@ -671,16 +672,20 @@ def segment_arm(args):
         "config": {"workload": SEGMENT_NAME, "rows": n, "image_bytes": st.image_bytes,
                    "decoded_bytes": st.decoded_bytes, "blocks": st.blocks,
                    "l2": "image and columns larger than L2 (no flush)",
-                   "value_covers": "decode launch + zone maps + NDV sketches, image resident"},
+                   "value_covers": "decode launches + zone-map / NDV-sketch launches (device time, summed)",
+                   "decode_ms": decode_ms, "stats_ms": statistics.mean(s[2] for s in stats)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": load_traffic("ingest", "decode"), "kernel": "decode_blocks_kernel", "kernel_ms": decode_ms,
                      "algorithmic_bytes": alg, "peak_kind": peak_kind},
         "e2e": {"value": n / (e2e_ms / 1e3), "unit": "rows/s", "h2d_bytes_per_step": st.image_bytes,
                 "d2h_bytes_per_step": 0, "ms_per_step": e2e_ms,
                 "h2d_ms": statistics.median(s[0] for s in stats),
-                "stats_ms": statistics.median(s[2] for s in stats)},
+                "pipeline_ms": statistics.median(s[4] for s in stats),
+                "chunks": st.chunks,
+                "how": "the image copied in chunks of row groups; each chunk decoded and its statistics taken "
+                       "while the next one copies"},
         "parity": parity,
-        "gpu_launches": args.steps * (1 + 2 * len(types)),
+        "gpu_launches": args.steps * st.kernel_launches,
         "clocks": clk,
         "cpu_baseline": cpu,
     }

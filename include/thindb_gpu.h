@@ -387,10 +387,13 @@ typedef struct tgpu_load_stats {
     uint64_t image_bytes;       /* segment image copied to the device */
     uint64_t decoded_bytes;     /* column values and validity bytes the decode wrote */
     uint32_t blocks;            /* column blocks decoded */
-    uint32_t kernel_launches;   /* decode launches */
-    double h2d_ms;              /* the image's host-to-device copy (device clock) */
-    double decode_ms;           /* the decode launch (device clock) */
-    double stats_ms;            /* zone maps and NDV sketches (host clock) */
+    uint32_t kernel_launches;   /* decode and statistics launches */
+    uint32_t chunks;            /* the image's copies, each decoded as it lands */
+    uint32_t reserved;
+    double h2d_ms;              /* first copy start to last copy end (device clock) */
+    double decode_ms;           /* the decode launches, summed (device clock) */
+    double stats_ms;            /* the zone-map / NDV-sketch launches, summed (device clock) */
+    double pipeline_ms;         /* first copy start to the last chunk's statistics (device clock) */
     double total_ms;            /* the whole call (host clock) */
 } tgpu_load_stats;
 tgpu_status tgpu_table_load_stats(const tgpu_table *table, tgpu_load_stats *out);

@@ -204,6 +204,23 @@ def replicate(image: bytes, n_cols: int, times: int) -> bytes:
     return bytes(head) + body * times + _footer(shifted, n_cols)
 
 
+def concat(images: Sequence[bytes], n_cols: int) -> bytes:
+    """One segment holding the row groups of several (same schema), in order:
+    row groups of differing sizes for the reader."""
+    head = bytearray(images[0][:32])
+    body, groups, total = bytearray(), [], 0
+    for im in images:
+        gs = _groups(im, n_cols)
+        if not gs:
+            continue
+        d = 32 + len(body) - gs[0][0]
+        body += im[gs[0][0]:gs[-1][0] + gs[-1][1]]
+        groups += [(g0 + d, gl, gr, [o + d for o in offs], lens) for g0, gl, gr, offs, lens in gs]
+        total += struct.unpack_from("<Q", im, 24)[0]
+    struct.pack_into("<Q", head, 24, total)
+    return bytes(head) + bytes(body) + _footer(groups, n_cols)
+
+
 def sample_table(n: int, seed: int = 7) -> tuple:
     """An eight-column table of the encodings a thinDB table stores: names,
     types, values and validity (None = NOT NULL).  region SMALLINT (runs of

@@ -1615,6 +1615,18 @@ void apply_tuning(tgpu_query *q, const tgpu_request *req, int batched) {
 
 tgpu_status query_create(tgpu_table *table, const tgpu_request *req, int batched, tgpu_query **out);
 
+struct StatsLayout {
+    size_t nrg, stat_bytes, reg_bytes;
+};
+StatsLayout stats_layout(uint32_t n_rg);
+// Statistics a caller has computed in the stats_layout of every column
+// (device), with which columns carry a sketch.
+struct PreStats {
+    const unsigned char *d_stats;
+    const std::vector<bool> *sketch;
+};
+tgpu_status register_table(const tgpu_table_desc *desc, tgpu_table **out, const PreStats *pre);
+
 // ================================================================ C ABI ====
 
 extern "C" {
@@ -1636,6 +1648,24 @@ const char *tgpu_build_info(void) {
 const char *tgpu_last_error_message(void) { return g_err.c_str(); }
 
 tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out) {
+    return register_table(desc, out, nullptr);
+}
+
+}  // extern "C"
+
+// Per-column statistics slices: zone maps of every row group (min/max as i64
+// and f64, NULL counts), rounded to 256 bytes so every column's slice and the
+// 8-byte arrays inside it stay aligned whatever the row-group count, then an
+// HLL register file.
+StatsLayout stats_layout(uint32_t n_rg) {
+    StatsLayout l;
+    l.nrg = std::max<uint32_t>(1, n_rg);
+    l.stat_bytes = round_up(l.nrg * (8 * 4 + 4), 256);
+    l.reg_bytes = (size_t)(1u << HLL_P) * 4;
+    return l;
+}
+
+tgpu_status register_table(const tgpu_table_desc *desc, tgpu_table **out, const PreStats *pre) {
     if (!desc || !out) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
     if (desc->n_columns == 0 || !desc->columns) return fail(TGPU_ERR_INVALID_ARGUMENT, "no columns");
     DeviceCtx *dev;
@@ -1660,19 +1690,19 @@ tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out) {
         if (cd.type == TGPU_DICT32 && cd.dict_size && (!cd.dict_offsets || !cd.dict_bytes))
             return fail(TGPU_ERR_INVALID_ARGUMENT, "dictionary without offsets or bytes");
     }
-    // Statistics scratch, one slice per column: zone maps of every row group
-    // (min/max as i64 and f64, NULL counts) and an HLL register file.
-    const size_t nrg = std::max<uint32_t>(1, t->n_rg);
-    // (rounded to 256 bytes so every column's slice, and the 8-byte arrays
-    // inside it, stay aligned whatever the row-group count)
-    const size_t stat_bytes = round_up(nrg * (8 * 4 + 4), 256);
-    const size_t reg_bytes = (size_t)(1u << HLL_P) * 4;
+    // Statistics scratch, one slice per column (stats_layout), then one HLL
+    // scratch shared by the columns, whose statistics run in turn on one
+    // stream; none when the caller computed them (pre).
+    const StatsLayout lay = stats_layout(t->n_rg);
+    const size_t nrg = lay.nrg, stat_bytes = lay.stat_bytes, reg_bytes = lay.reg_bytes;
     unsigned char *d_stats = nullptr;
-    // (then one HLL scratch shared by the columns, whose statistics run in turn on one stream)
-    const size_t part_bytes = (size_t)STATS_GRID_MAX << HLL_P;
-    CU(cudaMallocFromPoolAsync((void **)&d_stats, std::max<size_t>(1, nc) * (stat_bytes + reg_bytes) + part_bytes,
-                               dev->col_pool, s));
-    uint8_t *d_part = d_stats + std::max<size_t>(1, nc) * (stat_bytes + reg_bytes);
+    uint8_t *d_part = nullptr;
+    if (!pre) {
+        const size_t part_bytes = (size_t)STATS_GRID_MAX << HLL_P;
+        CU(cudaMallocFromPoolAsync((void **)&d_stats, std::max<size_t>(1, nc) * (stat_bytes + reg_bytes) + part_bytes,
+                                   dev->col_pool, s));
+        d_part = d_stats + std::max<size_t>(1, nc) * (stat_bytes + reg_bytes);
+    }
     struct StatsGuard {  // an error return leaves nothing allocated behind
         unsigned char *&p;
         cudaStream_t a, b;
@@ -1761,26 +1791,30 @@ tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out) {
         CU(cudaEventCreateWithFlags(&landed[i], cudaEventDisableTiming));
         CU(cudaEventRecord(landed[i], s));
         CU(cudaStreamWaitEvent(ss, landed[i], 0));
+        c.ndv = cd.ndv_hint;
+        sketch[i] = !c.ndv && desc->compute_ndv && n;
+        if (pre) {
+            sketch[i] = (*pre->sketch)[i];
+            continue;
+        }
         unsigned char *st = d_stats + (size_t)i * (stat_bytes + reg_bytes);
         int64_t *imin = (int64_t *)st, *imax = imin + nrg;
         double *fmin = (double *)(imax + nrg), *fmax = fmin + nrg;
         uint32_t *nulls = (uint32_t *)(fmax + nrg);
         uint32_t *regs = (uint32_t *)(st + stat_bytes);
-        c.ndv = cd.ndv_hint;
-        sketch[i] = !c.ndv && desc->compute_ndv && n;
         if (c.type != TGPU_VARCHAR) {
             // zone maps and the sketch in one pass over the column
-            CU(launch_column_stats(c.d_data, c.d_valid, c.type, n, t->rg_rows, t->n_rg, imin, imax, fmin, fmax, nulls,
-                                   sketch[i] ? regs : nullptr, d_part, ss));
+            CU(launch_column_stats(c.d_data, c.d_valid, c.type, n, t->rg_rows, 0, t->n_rg, imin, imax, fmin, fmax,
+                                   nulls, sketch[i] ? regs : nullptr, d_part, 0, ss));
         } else if (sketch[i]) {  // strings: no zone maps (no WHERE on them here)
             CU(cudaMemsetAsync(regs, 0, reg_bytes, ss));
             CU(launch_hll(c.d_data, c.d_valid, c.type, n, regs, ss, c.d_offs));
         }
     }
     // one read-back of every column's statistics
-    CU(cudaMemcpyAsync(h_stats.data(), d_stats, h_stats.size(), cudaMemcpyDeviceToHost, ss));
+    CU(cudaMemcpyAsync(h_stats.data(), pre ? pre->d_stats : d_stats, h_stats.size(), cudaMemcpyDeviceToHost, ss));
     CU(cudaStreamSynchronize(ss));
-    CU(cudaFreeAsync(d_stats, s));
+    if (d_stats) CU(cudaFreeAsync(d_stats, s));
     d_stats = nullptr;
     CU(cudaStreamSynchronize(s));
     for (uint32_t i = 0; i < nc; ++i) {
@@ -1809,6 +1843,8 @@ tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out) {
     return TGPU_OK;
 }
 
+extern "C" {
+
 tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, const tgpu_segment_column *columns,
                                         uint32_t n_columns, int32_t compute_ndv, void *stream, tgpu_table **out) {
     if (!image || !columns || !n_columns || !out) return fail(TGPU_ERR_INVALID_ARGUMENT, "null argument");
@@ -1832,12 +1868,16 @@ tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, co
     std::vector<std::vector<SegBlock>> blocks(n_columns);
     std::vector<uint32_t> run_starts;
     std::vector<bool> nullable(n_columns, false);
+    std::vector<uint64_t> rg_pos;  // each row group's header offset
+    std::vector<uint32_t> rg_n;    // and its rows
     uint64_t pos = 32, done = 0;
     uint32_t rg_rows = 0;
     const uint64_t end = bytes - 8;
     while (done < n) {
         if (pos + 8 > end) return fail(TGPU_ERR_INVALID_ARGUMENT, "segment truncated in a row-group header");
         const uint32_t rows = u32(pos);
+        rg_pos.push_back(pos);
+        rg_n.push_back(rows);
         pos += 8;
         if (rows == 0 || done + rows > n) return fail(TGPU_ERR_INVALID_ARGUMENT, "row-group row count");
         if (!rg_rows) rg_rows = rows;
@@ -1899,29 +1939,49 @@ tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, co
     tgpu_status st = device_ctx(&dev);
     if (st != TGPU_OK) return st;
     cudaStream_t s = stream ? (cudaStream_t)stream : dev->stream;
-    // columns and validity words first (the blocks point into them), then the
-    // image, the block list and the run starts, then one decode launch
+    cudaStream_t cs = dev->stats_stream;  // the image copies (the registration's statistics stream is idle here)
+    // The table's row groups are the segment's when every row group but the
+    // last has the first one's rows: the image then goes to the device in
+    // chunks of row groups, and each chunk is decoded and its statistics
+    // taken while the next one is copied.  Otherwise one chunk, and the
+    // statistics over the table's own row groups once it is decoded.
+    const uint32_t n_seg_rg = (uint32_t)rg_pos.size();
+    const uint32_t table_rg = rg_rows ? rg_rows : 65536u;
+    const uint32_t n_rg = (uint32_t)((n + table_rg - 1) / table_rg);
+    bool uniform = true;
+    for (uint32_t g = 0; g < n_seg_rg; ++g) uniform = uniform && (g + 1 == n_seg_rg ? rg_n[g] <= table_rg : rg_n[g] == table_rg);
+    const uint32_t per_chunk = uniform ? std::max<uint32_t>(1, (n_seg_rg + SEG_CHUNKS - 1) / SEG_CHUNKS)
+                                       : std::max<uint32_t>(1, n_seg_rg);
+    const uint32_t n_chunks = n_seg_rg ? (n_seg_rg + per_chunk - 1) / per_chunk : 0;
     uint8_t *d_image = nullptr;
     SegBlock *d_blocks = nullptr;
     uint32_t *d_runs = nullptr;
+    unsigned char *d_stats = nullptr;
     std::vector<void *> data(n_columns, nullptr);
     std::vector<uint32_t *> valid(n_columns, nullptr);
-    cudaEvent_t ev[4] = {};
+    std::vector<cudaEvent_t> ev;
     auto release = [&](bool keep_data) {
+        cudaStreamSynchronize(cs);
         cudaStreamSynchronize(s);
         if (d_image) cudaFreeAsync(d_image, s);
         if (d_blocks) cudaFreeAsync(d_blocks, s);
         if (d_runs) cudaFreeAsync(d_runs, s);
+        if (d_stats) cudaFreeAsync(d_stats, s);
         for (uint32_t c = 0; c < n_columns; ++c) {
             if (valid[c]) cudaFreeAsync(valid[c], s);
             if (!keep_data && data[c]) cudaFreeAsync(data[c], s);
         }
         cudaStreamSynchronize(s);
-        for (cudaEvent_t &e : ev)
-            if (e) cudaEventDestroy(e);
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
     };
     cudaError_t e = cudaSuccess;
-    for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaEventCreate(&ev[k]);
+    auto event = [&]() {
+        cudaEvent_t x = nullptr;
+        if (e == cudaSuccess) e = cudaEventCreate(&x);
+        if (e == cudaSuccess) ev.push_back(x);
+        return x;
+    };
+    // columns and validity words (the blocks point into them)
     uint64_t decoded = 0;
     for (uint32_t c = 0; c < n_columns && e == cudaSuccess; ++c) {
         const size_t elem = (size_t)type_bytes(columns[c].type);
@@ -1934,16 +1994,32 @@ tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, co
             decoded += (n + 7) / 8;
         }
     }
+    // the block list, chunk by chunk, and in a chunk column by column
     std::vector<SegBlock> all;
-    for (uint32_t c = 0; c < n_columns; ++c)
-        for (SegBlock b : blocks[c]) {
-            b.out = data[c];
-            b.valid = valid[c];
-            all.push_back(b);
-        }
-    if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
+    std::vector<uint32_t> chunk_first(n_chunks + 1, 0);
+    for (uint32_t k = 0; k < n_chunks; ++k) {
+        chunk_first[k] = (uint32_t)all.size();
+        const uint32_t g0 = k * per_chunk, g1 = std::min(n_seg_rg, g0 + per_chunk);
+        for (uint32_t c = 0; c < n_columns; ++c)
+            for (uint32_t g = g0; g < g1; ++g) {
+                SegBlock b = blocks[c][g];
+                b.out = data[c];
+                b.valid = valid[c];
+                all.push_back(b);
+            }
+    }
+    chunk_first[n_chunks] = (uint32_t)all.size();
+    // statistics slices as the registration lays them out, and the HLL scratch
+    const StatsLayout lay = stats_layout(n_rg);
+    const size_t slice = lay.stat_bytes + lay.reg_bytes;
+    std::vector<bool> sketch(n_columns, compute_ndv != 0 && n > 0);
+    if (e == cudaSuccess)
+        e = cudaMallocFromPoolAsync((void **)&d_stats, n_columns * slice + ((size_t)STATS_GRID_MAX << HLL_P),
+                                    dev->col_pool, s);
+    uint8_t *d_part = d_stats ? d_stats + n_columns * slice : nullptr;
+    for (uint32_t c = 0; c < n_columns && e == cudaSuccess; ++c)
+        e = cudaMemsetAsync(d_stats + c * slice + lay.stat_bytes, 0, lay.reg_bytes, s);
     if (e == cudaSuccess) e = cudaMallocFromPoolAsync((void **)&d_image, bytes + SEG_IMAGE_PAD, dev->col_pool, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(d_image, image, bytes, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
         e = cudaMallocFromPoolAsync((void **)&d_blocks, std::max<size_t>(1, all.size()) * sizeof(SegBlock), dev->col_pool, s);
     if (e == cudaSuccess && !all.empty())
@@ -1952,9 +2028,46 @@ tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, co
         e = cudaMallocFromPoolAsync((void **)&d_runs, std::max<size_t>(1, run_starts.size()) * 4, dev->col_pool, s);
     if (e == cudaSuccess && !run_starts.empty())
         e = cudaMemcpyAsync(d_runs, run_starts.data(), run_starts.size() * 4, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaEventRecord(ev[1], s);
-    if (e == cudaSuccess) e = launch_decode_blocks(d_image, d_blocks, (uint32_t)all.size(), d_runs, s);
-    if (e == cudaSuccess) e = cudaEventRecord(ev[2], s);
+    // the copies wait for the allocations; each chunk's work waits for its copy
+    cudaEvent_t ready = event(), copy0 = event(), copy1 = event();
+    if (e == cudaSuccess) e = cudaEventRecord(ready, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ready, 0);
+    if (e == cudaSuccess) e = cudaEventRecord(copy0, cs);
+    std::vector<cudaEvent_t> landed(n_chunks), dec0(n_chunks), dec1(n_chunks), st1(n_chunks);
+    for (uint32_t k = 0; k < n_chunks; ++k) {
+        landed[k] = event();
+        dec0[k] = event();
+        dec1[k] = event();
+        st1[k] = event();
+    }
+    uint32_t launches = 0;
+    for (uint32_t k = 0; k < n_chunks && e == cudaSuccess; ++k) {
+        const uint32_t g0 = k * per_chunk, g1 = std::min(n_seg_rg, g0 + per_chunk);
+        const uint64_t b0 = k ? rg_pos[g0] : 0, b1 = g1 < n_seg_rg ? rg_pos[g1] : bytes;
+        e = cudaMemcpyAsync(d_image + b0, image + b0, b1 - b0, cudaMemcpyHostToDevice, cs);
+        if (e == cudaSuccess) e = cudaEventRecord(landed[k], cs);
+        if (e == cudaSuccess && k + 1 == n_chunks) e = cudaEventRecord(copy1, cs);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, landed[k], 0);
+        if (e == cudaSuccess) e = cudaEventRecord(dec0[k], s);
+        if (e == cudaSuccess)
+            e = launch_decode_blocks(d_image, d_blocks + chunk_first[k], chunk_first[k + 1] - chunk_first[k], d_runs, s);
+        launches += 1;
+        if (e == cudaSuccess) e = cudaEventRecord(dec1[k], s);
+        // the chunk's row groups of the table (all of them when not uniform)
+        const uint32_t t0 = uniform ? g0 : 0, t1 = uniform ? g1 : n_rg;
+        for (uint32_t c = 0; c < n_columns && e == cudaSuccess; ++c) {
+            unsigned char *sl = d_stats + c * slice;
+            int64_t *imin = (int64_t *)sl, *imax = imin + lay.nrg;
+            double *fmin = (double *)(imax + lay.nrg), *fmax = fmin + lay.nrg;
+            uint32_t *nulls = (uint32_t *)(fmax + lay.nrg);
+            uint32_t *regs = (uint32_t *)(sl + lay.stat_bytes);
+            e = launch_column_stats(data[c], valid[c], columns[c].type, n, table_rg, t0, t1, imin, imax, fmin, fmax,
+                                    nulls, sketch[c] ? regs : nullptr, d_part, 1, s);
+            launches += sketch[c] ? 2 : 1;
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(st1[k], s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -1965,10 +2078,15 @@ tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, co
     ls.image_bytes = bytes;
     ls.decoded_bytes = decoded;
     ls.blocks = (uint32_t)all.size();
-    ls.kernel_launches = all.empty() ? 0 : 1;
+    ls.kernel_launches = launches;
+    ls.chunks = n_chunks;
     float ms = 0;
-    if (cudaEventElapsedTime(&ms, ev[0], ev[1]) == cudaSuccess) ls.h2d_ms = ms;
-    if (cudaEventElapsedTime(&ms, ev[1], ev[2]) == cudaSuccess) ls.decode_ms = ms;
+    if (n_chunks && cudaEventElapsedTime(&ms, copy0, copy1) == cudaSuccess) ls.h2d_ms = ms;
+    for (uint32_t k = 0; k < n_chunks; ++k) {
+        if (cudaEventElapsedTime(&ms, dec0[k], dec1[k]) == cudaSuccess) ls.decode_ms += ms;
+        if (cudaEventElapsedTime(&ms, dec1[k], st1[k]) == cudaSuccess) ls.stats_ms += ms;
+    }
+    if (n_chunks && cudaEventElapsedTime(&ms, copy0, st1[n_chunks - 1]) == cudaSuccess) ls.pipeline_ms = ms;
     // register the decoded columns in place, then hand them to the table
     std::vector<tgpu_column_desc> cd(n_columns);
     for (uint32_t c = 0; c < n_columns; ++c) {
@@ -1983,21 +2101,19 @@ tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, co
     tgpu_table_desc td{};
     td.columns = cd.data();
     td.n_columns = n_columns;
-    td.row_group_rows = rg_rows ? rg_rows : 65536;
+    td.row_group_rows = table_rg;
     td.n_rows = n;
     td.location = TGPU_LOC_DEVICE;
     td.compute_ndv = compute_ndv;
     td.stream = s;
     tgpu_table *t = nullptr;
-    const auto r0 = std::chrono::steady_clock::now();
-    st = tgpu_table_register(&td, &t);
+    const PreStats pre{d_stats, &sketch};
+    st = register_table(&td, &t, &pre);
     if (st != TGPU_OK) {
         const std::string msg = g_err;
         release(false);
         return fail(st, msg);
     }
-    const auto r1 = std::chrono::steady_clock::now();
-    ls.stats_ms = std::chrono::duration<double, std::milli>(r1 - r0).count();
     for (uint32_t c = 0; c < n_columns; ++c) t->cols[c].owned = true;  // freed with the table
     release(true);
     ls.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_call).count();

@@ -364,6 +364,8 @@ struct SegBlock {
 // Image buffers carry this many readable bytes past their end: the decoder
 // reads whole aligned words around unaligned values.
 constexpr uint32_t SEG_IMAGE_PAD = 16;
+// A segment image goes to the device in about this many chunks of row groups.
+constexpr uint32_t SEG_CHUNKS = 16;
 cudaError_t launch_decode_blocks(const uint8_t *image, const SegBlock *blocks, uint32_t n_blocks,
                                  const uint32_t *run_starts, cudaStream_t s);
 
@@ -441,12 +443,15 @@ cudaError_t launch_clear(unsigned long long *table, uint64_t cap, int32_t slot_w
 // table statistics
 cudaError_t launch_hll(const void *data, const uint32_t *valid, int32_t type, uint64_t n_rows, uint32_t *regs,
                        cudaStream_t s, const uint32_t *offs = nullptr);
-// Zone maps and (regs non-null) the HLL registers of a fixed-width column in
-// one pass; `part` is scratch of STATS_GRID_MAX x 2^HLL_P bytes.
+// Zone maps of row groups [g0, g1) and (regs non-null) the HLL registers of
+// their rows, for a fixed-width column in one pass; the registers are
+// replaced, or raised when `accumulate`.  `part` is scratch of
+// STATS_GRID_MAX x 2^HLL_P bytes.
 constexpr uint32_t STATS_GRID_MAX = 512;
 cudaError_t launch_column_stats(const void *data, const uint32_t *valid, int32_t type, uint64_t n_rows,
-                                uint32_t rg_rows, uint32_t n_rg, int64_t *imin, int64_t *imax, double *fmin,
-                                double *fmax, uint32_t *nulls, uint32_t *regs, uint8_t *part, cudaStream_t s);
+                                uint32_t rg_rows, uint32_t g0, uint32_t g1, int64_t *imin, int64_t *imax, double *fmin,
+                                double *fmax, uint32_t *nulls, uint32_t *regs, uint8_t *part, int accumulate,
+                                cudaStream_t s);
 // Columns of a composite key for its HyperLogLog sketch.
 struct KeySketchCols {
     const void *data[MAX_GROUP_KEYS];

@@ -104,7 +104,7 @@ namespace {
 // column, no global atomics.
 template <typename T>
 __global__ void __launch_bounds__(512) column_stats_kernel(const T *__restrict__ data, const uint32_t *__restrict__ valid,
-                                                           uint64_t n_rows, uint32_t rg_rows, uint32_t n_rg,
+                                                           uint64_t n_rows, uint32_t rg_rows, uint32_t g0, uint32_t g1,
                                                            int64_t *imin, int64_t *imax, double *zfmin, double *zfmax,
                                                            uint32_t *nulls, uint8_t *part) {
     extern __shared__ uint32_t sreg[];
@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(512) column_stats_kernel(const T *__restrict__
         __syncthreads();
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (uint32_t g = blockIdx.x; g < n_rg; g += gridDim.x) {
+    for (uint32_t g = g0 + blockIdx.x; g < g1; g += gridDim.x) {
         const uint64_t b = (uint64_t)g * rg_rows, e = min(b + rg_rows, n_rows);
         long long mn = LLONG_MAX, mx = LLONG_MIN;
         double fmn = DBL_MAX, fmx = -DBL_MAX;
@@ -193,18 +193,23 @@ __global__ void __launch_bounds__(512) column_stats_kernel(const T *__restrict__
     }
 }
 
-__global__ void hll_merge_kernel(const uint8_t *__restrict__ part, uint32_t rows, uint32_t *regs) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (uint32_t)HLL_M) return;
+// regs = max(regs (accumulate) or 0, every part row); four registers a thread
+__global__ void hll_merge_kernel(const uint8_t *__restrict__ part, uint32_t rows, uint32_t *regs, int accumulate) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;  // registers 4i .. 4i + 3
+    if (i >= (uint32_t)HLL_M / 4) return;
+    const uint32_t *p = (const uint32_t *)part + i;
     uint32_t m = 0;
-    for (uint32_t r = 0; r < rows; ++r) m = max(m, (uint32_t)part[(size_t)r * HLL_M + i]);
-    regs[i] = m;
+    for (uint32_t r = 0; r < rows; ++r) m = __vmaxu4(m, __ldg(p + (size_t)r * (HLL_M / 4)));
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t v = (m >> (8 * k)) & 0xFFu;
+        regs[4 * i + k] = accumulate ? max(regs[4 * i + k], v) : v;
+    }
 }
 
 template <typename T>
-cudaError_t launch_stats_t(const void *data, const uint32_t *valid, uint64_t n_rows, uint32_t rg_rows, uint32_t n_rg,
-                           int64_t *imin, int64_t *imax, double *fmin, double *fmax, uint32_t *nulls, uint32_t *regs,
-                           uint8_t *part, cudaStream_t s) {
+cudaError_t launch_stats_t(const void *data, const uint32_t *valid, uint64_t n_rows, uint32_t rg_rows, uint32_t g0,
+                           uint32_t g1, int64_t *imin, int64_t *imax, double *fmin, double *fmax, uint32_t *nulls,
+                           uint32_t *regs, uint8_t *part, int accumulate, cudaStream_t s) {
     static int sms = 0;
     if (!sms) {
         int dev = 0;
@@ -212,34 +217,35 @@ cudaError_t launch_stats_t(const void *data, const uint32_t *valid, uint64_t n_r
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 1;
     }
-    const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>({n_rg, 2u * (uint32_t)sms, STATS_GRID_MAX}));
+    const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>({g1 - g0, 2u * (uint32_t)sms, STATS_GRID_MAX}));
     const size_t smem = regs ? HLL_M * sizeof(uint32_t) : 0;
     cudaError_t e = cudaFuncSetAttribute(column_stats_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          HLL_M * (int)sizeof(uint32_t));
     if (e != cudaSuccess) return e;
-    column_stats_kernel<T><<<grid, 512, smem, s>>>((const T *)data, valid, n_rows, rg_rows, n_rg, imin, imax, fmin,
+    column_stats_kernel<T><<<grid, 512, smem, s>>>((const T *)data, valid, n_rows, rg_rows, g0, g1, imin, imax, fmin,
                                                     fmax, nulls, regs ? part : nullptr);
     e = cudaGetLastError();
     if (e != cudaSuccess || !regs) return e;
-    hll_merge_kernel<<<HLL_M / 256, 256, 0, s>>>(part, grid, regs);
+    hll_merge_kernel<<<HLL_M / 4 / 256, 256, 0, s>>>(part, grid, regs, accumulate);
     return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_column_stats(const void *data, const uint32_t *valid, int32_t type, uint64_t n_rows,
-                                uint32_t rg_rows, uint32_t n_rg, int64_t *imin, int64_t *imax, double *fmin,
-                                double *fmax, uint32_t *nulls, uint32_t *regs, uint8_t *part, cudaStream_t s) {
-    if (n_rg == 0 || n_rows == 0) return cudaSuccess;
+                                uint32_t rg_rows, uint32_t g0, uint32_t g1, int64_t *imin, int64_t *imax, double *fmin,
+                                double *fmax, uint32_t *nulls, uint32_t *regs, uint8_t *part, int accumulate,
+                                cudaStream_t s) {
+    if (g1 <= g0 || n_rows == 0) return cudaSuccess;
     switch (type) {
-        case TGPU_BOOLEAN: return launch_stats_t<uint8_t>(data, valid, n_rows, rg_rows, n_rg, imin, imax, fmin, fmax, nulls, regs, part, s);
-        case TGPU_TINYINT: return launch_stats_t<int8_t>(data, valid, n_rows, rg_rows, n_rg, imin, imax, fmin, fmax, nulls, regs, part, s);
-        case TGPU_SMALLINT: return launch_stats_t<int16_t>(data, valid, n_rows, rg_rows, n_rg, imin, imax, fmin, fmax, nulls, regs, part, s);
+        case TGPU_BOOLEAN: return launch_stats_t<uint8_t>(data, valid, n_rows, rg_rows, g0, g1, imin, imax, fmin, fmax, nulls, regs, part, accumulate, s);
+        case TGPU_TINYINT: return launch_stats_t<int8_t>(data, valid, n_rows, rg_rows, g0, g1, imin, imax, fmin, fmax, nulls, regs, part, accumulate, s);
+        case TGPU_SMALLINT: return launch_stats_t<int16_t>(data, valid, n_rows, rg_rows, g0, g1, imin, imax, fmin, fmax, nulls, regs, part, accumulate, s);
         case TGPU_INT: case TGPU_DATE: case TGPU_DICT32:
-            return launch_stats_t<int32_t>(data, valid, n_rows, rg_rows, n_rg, imin, imax, fmin, fmax, nulls, regs, part, s);
-        case TGPU_FLOAT: return launch_stats_t<float>(data, valid, n_rows, rg_rows, n_rg, imin, imax, fmin, fmax, nulls, regs, part, s);
-        case TGPU_DOUBLE: return launch_stats_t<double>(data, valid, n_rows, rg_rows, n_rg, imin, imax, fmin, fmax, nulls, regs, part, s);
-        default: return launch_stats_t<long long>(data, valid, n_rows, rg_rows, n_rg, imin, imax, fmin, fmax, nulls, regs, part, s);
+            return launch_stats_t<int32_t>(data, valid, n_rows, rg_rows, g0, g1, imin, imax, fmin, fmax, nulls, regs, part, accumulate, s);
+        case TGPU_FLOAT: return launch_stats_t<float>(data, valid, n_rows, rg_rows, g0, g1, imin, imax, fmin, fmax, nulls, regs, part, accumulate, s);
+        case TGPU_DOUBLE: return launch_stats_t<double>(data, valid, n_rows, rg_rows, g0, g1, imin, imax, fmin, fmax, nulls, regs, part, accumulate, s);
+        default: return launch_stats_t<long long>(data, valid, n_rows, rg_rows, g0, g1, imin, imax, fmin, fmax, nulls, regs, part, accumulate, s);
     }
 }
 
