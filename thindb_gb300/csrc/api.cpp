@@ -1994,7 +1994,10 @@ tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, co
             decoded += (n + 7) / 8;
         }
     }
-    // the block list, chunk by chunk, and in a chunk column by column
+    // the block list, chunk by chunk, and in a chunk column by column; with
+    // uniform row groups each block also takes its row group's zone map and
+    // its rows' sketch registers (a scratch row per block of the chunk)
+    const bool want_sketch = compute_ndv != 0 && n > 0;
     std::vector<SegBlock> all;
     std::vector<uint32_t> chunk_first(n_chunks + 1, 0);
     for (uint32_t k = 0; k < n_chunks; ++k) {
@@ -2005,18 +2008,25 @@ tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, co
                 SegBlock b = blocks[c][g];
                 b.out = data[c];
                 b.valid = valid[c];
+                b.col = c;
+                b.rg = g;
+                b.type = columns[c].type;
+                b.flags = uniform ? SEG_ZONE | (want_sketch ? SEG_SKETCH : 0u) : 0u;
+                b.part_row = c * per_chunk + (g - g0);
                 all.push_back(b);
             }
     }
     chunk_first[n_chunks] = (uint32_t)all.size();
-    // statistics slices as the registration lays them out, and the HLL scratch
+    // statistics slices as the registration lays them out, then the scratch:
+    // a register row per block of a chunk, or the column-pass scratch
     const StatsLayout lay = stats_layout(n_rg);
     const size_t slice = lay.stat_bytes + lay.reg_bytes;
-    std::vector<bool> sketch(n_columns, compute_ndv != 0 && n > 0);
+    std::vector<bool> sketch(n_columns, want_sketch);
+    const size_t part_bytes = uniform ? ((size_t)n_columns * per_chunk << HLL_P) : ((size_t)STATS_GRID_MAX << HLL_P);
     if (e == cudaSuccess)
-        e = cudaMallocFromPoolAsync((void **)&d_stats, n_columns * slice + ((size_t)STATS_GRID_MAX << HLL_P),
-                                    dev->col_pool, s);
+        e = cudaMallocFromPoolAsync((void **)&d_stats, n_columns * slice + part_bytes, dev->col_pool, s);
     uint8_t *d_part = d_stats ? d_stats + n_columns * slice : nullptr;
+    const SegStats sst{d_stats, slice, lay.stat_bytes, lay.nrg, d_part};
     for (uint32_t c = 0; c < n_columns && e == cudaSuccess; ++c)
         e = cudaMemsetAsync(d_stats + c * slice + lay.stat_bytes, 0, lay.reg_bytes, s);
     if (e == cudaSuccess) e = cudaMallocFromPoolAsync((void **)&d_image, bytes + SEG_IMAGE_PAD, dev->col_pool, s);
@@ -2050,20 +2060,26 @@ tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, co
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s, landed[k], 0);
         if (e == cudaSuccess) e = cudaEventRecord(dec0[k], s);
         if (e == cudaSuccess)
-            e = launch_decode_blocks(d_image, d_blocks + chunk_first[k], chunk_first[k + 1] - chunk_first[k], d_runs, s);
+            e = launch_decode_blocks(d_image, d_blocks + chunk_first[k], chunk_first[k + 1] - chunk_first[k], d_runs,
+                                     sst, s);
         launches += 1;
         if (e == cudaSuccess) e = cudaEventRecord(dec1[k], s);
-        // the chunk's row groups of the table (all of them when not uniform)
-        const uint32_t t0 = uniform ? g0 : 0, t1 = uniform ? g1 : n_rg;
-        for (uint32_t c = 0; c < n_columns && e == cudaSuccess; ++c) {
-            unsigned char *sl = d_stats + c * slice;
-            int64_t *imin = (int64_t *)sl, *imax = imin + lay.nrg;
-            double *fmin = (double *)(imax + lay.nrg), *fmax = fmin + lay.nrg;
-            uint32_t *nulls = (uint32_t *)(fmax + lay.nrg);
-            uint32_t *regs = (uint32_t *)(sl + lay.stat_bytes);
-            e = launch_column_stats(data[c], valid[c], columns[c].type, n, table_rg, t0, t1, imin, imax, fmin, fmax,
-                                    nulls, sketch[c] ? regs : nullptr, d_part, 1, s);
-            launches += sketch[c] ? 2 : 1;
+        if (uniform && want_sketch && e == cudaSuccess) {
+            // the chunk's register rows into the columns' registers, before the next chunk reuses them
+            e = launch_seg_hll_merge(sst, n_columns, g1 - g0, per_chunk, s);
+            launches += 1;
+        } else if (!uniform) {
+            // the table's own row groups, over the decoded columns
+            for (uint32_t c = 0; c < n_columns && e == cudaSuccess; ++c) {
+                unsigned char *sl = d_stats + c * slice;
+                int64_t *imin = (int64_t *)sl, *imax = imin + lay.nrg;
+                double *fmin = (double *)(imax + lay.nrg), *fmax = fmin + lay.nrg;
+                uint32_t *nulls = (uint32_t *)(fmax + lay.nrg);
+                uint32_t *regs = (uint32_t *)(sl + lay.stat_bytes);
+                e = launch_column_stats(data[c], valid[c], columns[c].type, n, table_rg, 0, n_rg, imin, imax, fmin,
+                                        fmax, nulls, sketch[c] ? regs : nullptr, d_part, 1, s);
+                launches += sketch[c] ? 2 : 1;
+            }
         }
         if (e == cudaSuccess) e = cudaEventRecord(st1[k], s);
     }

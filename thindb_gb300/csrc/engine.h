@@ -359,15 +359,33 @@ struct SegBlock {
     uint32_t runs;       // RLE runs
     uint32_t run0;       // RLE: index of its first run start in the run-start array
     uint32_t elem;       // decoded element bytes (1, 2, 4, 8)
-    uint32_t has_nulls;
+    uint32_t has_nulls;  // a validity bitmap prefixes the payload
+    // statistics taken while decoding (the block is one row group of the table)
+    uint32_t col;        // the column's statistics slice
+    uint32_t rg;         // the row group's zone-map entry
+    int32_t type;        // tgpu_type of the column
+    uint32_t flags;      // SEG_ZONE, SEG_SKETCH
+    uint32_t part_row;   // its HLL register row in the scratch
+    uint32_t pad;
 };
-// Image buffers carry this many readable bytes past their end: the decoder
-// reads whole aligned words around unaligned values.
+constexpr uint32_t SEG_ZONE = 1, SEG_SKETCH = 2;
+// Where decode_blocks_kernel leaves statistics: column c's slice at
+// stats + c * slice holds imin, imax (i64), fmin, fmax (f64) and NULL counts
+// (u32) of nrg row groups, and 2^HLL_P u32 registers at reg_off; part holds a
+// row of 2^HLL_P byte registers per block.
+struct SegStats {
+    unsigned char *stats;
+    uint64_t slice, reg_off, nrg;
+    uint8_t *part;
+};
 constexpr uint32_t SEG_IMAGE_PAD = 16;
 // A segment image goes to the device in about this many chunks of row groups.
 constexpr uint32_t SEG_CHUNKS = 16;
 cudaError_t launch_decode_blocks(const uint8_t *image, const SegBlock *blocks, uint32_t n_blocks,
-                                 const uint32_t *run_starts, cudaStream_t s);
+                                 const uint32_t *run_starts, const SegStats &st, cudaStream_t s);
+// Raise each column's registers to the maximum over its `rows` part rows
+// (column c's rows start at row c * stride).
+cudaError_t launch_seg_hll_merge(const SegStats &st, uint32_t n_cols, uint32_t rows, uint32_t stride, cudaStream_t s);
 
 // Partitioned COUNT(DISTINCT): pairs per partition (one CTA deduplicates a
 // partition in shared memory) and the partition's index-table slots.
