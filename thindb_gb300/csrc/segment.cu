@@ -29,6 +29,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <climits>
+#include <type_traits>
 
 #include <math_constants.h>
 
@@ -53,15 +54,6 @@ __device__ __forceinline__ uint64_t ld_bytes(const uint8_t *p, uint32_t w) {
     const uint32_t lo = __funnelshift_r(w0, w1, 8 * a);
     if (w == 8) return ((uint64_t)__funnelshift_r(w1, __ldg(q + 2), 8 * a) << 32) | lo;
     return w == 4 ? lo : lo & ((1u << (8 * w)) - 1u);
-}
-
-__device__ __forceinline__ void st_elem(void *out, uint32_t bytes, uint64_t row, uint64_t v) {
-    switch (bytes) {
-        case 1: ((uint8_t *)out)[row] = (uint8_t)v; break;
-        case 2: ((uint16_t *)out)[row] = (uint16_t)v; break;
-        case 4: ((uint32_t *)out)[row] = (uint32_t)v; break;
-        default: ((uint64_t *)out)[row] = v; break;
-    }
 }
 
 // Validity: the block's bitmap bits land at table rows row0 + i (all set
@@ -121,14 +113,17 @@ __device__ __forceinline__ void hll_raise(uint32_t *regs, uint32_t idx, uint32_t
     }
 }
 
-__device__ __forceinline__ void stat_row(Stat &st, const SegBlock &b, uint64_t x, bool ok, uint32_t *regs) {
-    if (!ok) {
-        ++st.nn;
-        return;
-    }
+template <typename T> __device__ __forceinline__ T from_bits(uint64_t x) {
+    if constexpr (std::is_same<T, float>::value) return __uint_as_float((uint32_t)x);
+    else if constexpr (std::is_same<T, double>::value) return __longlong_as_double((long long)x);
+    else return (T)x;  // the element's low bytes (a signed type sign-extends)
+}
+
+// One valid value into the thread's zone map and the block's registers.
+template <typename T> __device__ __forceinline__ void stat_value(Stat &st, T t, uint32_t *regs) {
     uint64_t bits;
-    if (b.type == TGPU_FLOAT || b.type == TGPU_DOUBLE) {
-        const double d = b.type == TGPU_FLOAT ? (double)__uint_as_float((uint32_t)x) : __longlong_as_double((long long)x);
+    if constexpr (std::is_floating_point<T>::value) {
+        const double d = (double)t;
         if (d == d) {
             st.fmn = fmin(st.fmn, d);
             st.fmx = fmax(st.fmx, d);
@@ -137,10 +132,7 @@ __device__ __forceinline__ void stat_row(Stat &st, const SegBlock &b, uint64_t x
         }
         bits = canon_f64_bits(d);
     } else {
-        // the typed value: sign-extended from the element, BOOLEAN unsigned
-        long long v = (long long)x;
-        if (b.elem < 8 && b.type != TGPU_BOOLEAN) v = (long long)(x << (64 - 8 * b.elem)) >> (64 - 8 * b.elem);
-        else if (b.elem < 8) v = (long long)(x & ((1ULL << (8 * b.elem)) - 1));
+        const long long v = (long long)t;
         st.mn = min(st.mn, v);
         st.mx = max(st.mx, v);
         bits = (uint64_t)v;
@@ -157,27 +149,49 @@ __device__ __forceinline__ bool bit_at(const uint8_t *bm, bool has_nulls, uint32
     return !has_nulls || ((bm[i >> 3] >> (i & 7)) & 1u);
 }
 
-__global__ void __launch_bounds__(DECODE_THREADS) decode_blocks_kernel(const uint8_t *__restrict__ image,
-                                                                       const SegBlock *__restrict__ blocks,
-                                                                       const uint32_t *__restrict__ run_starts,
-                                                                       const SegStats st) {
-    __shared__ uint32_t s_starts[SMEM_RUNS];
-    __shared__ uint32_t s_regs[HLL_BYTES / 4];  // byte registers
-    __shared__ long long s_mn[DECODE_THREADS / 32], s_mx[DECODE_THREADS / 32];
-    __shared__ double s_fmn[DECODE_THREADS / 32], s_fmx[DECODE_THREADS / 32];
-    __shared__ unsigned s_nn[DECODE_THREADS / 32];
-    const SegBlock b = blocks[blockIdx.x];
-    const uint8_t *p = image + b.payload;
+constexpr uint32_t DOM_WORDS = 65536 / 32;  // a bit per 16-bit code
+
+struct Smem {
+    uint32_t starts[SMEM_RUNS];    // RLE run starts
+    uint32_t regs[HLL_BYTES / 4];  // byte registers
+    uint32_t dom[DOM_WORDS];       // codes seen (raw 1-2 byte elements, FOR deltas of 1-2 bytes)
+    uint8_t seen[SMEM_RUNS];       // RLE runs with a valid row
+    long long mn[DECODE_THREADS / 32], mx[DECODE_THREADS / 32];
+    double fmn[DECODE_THREADS / 32], fmx[DECODE_THREADS / 32];
+    unsigned nn[DECODE_THREADS / 32];
+};
+
+// Decode one block of a column of element type T; with SEG_ZONE take the
+// block's zone map and (SEG_SKETCH) its sketch registers.  A block whose
+// codes span at most 2^16 values (1-2 byte raw elements, FOR deltas of 1-2
+// bytes) marks the codes it sees and takes the statistics once per code; an
+// RLE block marks its runs and takes them once per run; other blocks hash
+// every valid row.
+template <typename T>
+__device__ void decode_block(const SegBlock &b, const uint8_t *p, const uint32_t *__restrict__ run_starts,
+                             const SegStats &st, Smem &sm) {
     const bool zone = b.flags & SEG_ZONE;
-    uint32_t *regs = (b.flags & SEG_SKETCH) ? s_regs : nullptr;
-    if (regs) {
-        for (uint32_t i = threadIdx.x; i < HLL_BYTES / 4; i += blockDim.x) s_regs[i] = 0;
-        __syncthreads();
-    }
-    if (b.valid) decode_validity(p, b);
+    uint32_t *regs = (b.flags & SEG_SKETCH) ? sm.regs : nullptr;
+    const bool hn = b.has_nulls;
     const uint8_t *v = p + b.values;
+    T *out = (T *)b.out + b.row0;
+    const bool rle = b.encoding != ENC_RAW && b.encoding != ENC_FOR;
+    const bool staged = rle && b.runs <= SMEM_RUNS;
+    const bool dom = zone && !rle && (b.encoding == ENC_RAW ? sizeof(T) <= 2 : b.width <= 2);
+    if (regs)
+        for (uint32_t i = threadIdx.x; i < HLL_BYTES / 4; i += blockDim.x) sm.regs[i] = 0;
+    if (dom)
+        for (uint32_t i = threadIdx.x; i < DOM_WORDS; i += blockDim.x) sm.dom[i] = 0;
+    if (staged) {
+        for (uint32_t r = threadIdx.x; r < b.runs; r += blockDim.x) {
+            sm.starts[r] = run_starts[b.run0 + r];
+            sm.seen[r] = 0;
+        }
+    }
+    __syncthreads();
+    if (b.valid) decode_validity(p, b);
     Stat stat;
-    if (b.encoding == ENC_RAW || b.encoding == ENC_FOR) {
+    if (!rle) {
         // raw: base 0, codes of the element's width; FOR: the add wraps in the
         // element's width, as expandWidth's +%.  Four rows per thread per
         // pass, their loads issued before their stores.
@@ -186,41 +200,68 @@ __global__ void __launch_bounds__(DECODE_THREADS) decode_blocks_kernel(const uin
         const uint8_t *codes = raw ? v : v + 20;
         const uint32_t w = raw ? b.elem : b.width, step = blockDim.x;
         for (uint32_t i0 = threadIdx.x; i0 < b.rows; i0 += DECODE_UNROLL * step) {
-            uint64_t x[DECODE_UNROLL];
+            uint64_t c[DECODE_UNROLL];
 #pragma unroll
             for (int k = 0; k < DECODE_UNROLL; ++k) {
                 const uint32_t i = i0 + k * step;
-                x[k] = i < b.rows ? base + ld_bytes(codes + (size_t)i * w, w) : 0;
+                c[k] = i < b.rows ? ld_bytes(codes + (size_t)i * w, w) : 0;
             }
 #pragma unroll
             for (int k = 0; k < DECODE_UNROLL; ++k) {
                 const uint32_t i = i0 + k * step;
-                if (i < b.rows) {
-                    st_elem(b.out, b.elem, b.row0 + i, x[k]);
-                    if (zone) stat_row(stat, b, x[k], bit_at(p, b.has_nulls, i), regs);
+                if (i >= b.rows) continue;
+                const T t = from_bits<T>(base + c[k]);
+                out[i] = t;
+                if (!zone) continue;
+                if (!bit_at(p, hn, i)) {
+                    ++stat.nn;
+                } else if (dom) {
+                    const uint32_t code = (uint32_t)c[k] & 0xFFFFu, bit = 1u << (code & 31);
+                    if (!(sm.dom[code >> 5] & bit)) atomicOr(&sm.dom[code >> 5], bit);
+                } else {
+                    stat_value(stat, t, regs);
                 }
             }
         }
-    } else {  // RLE: each row finds its run among the run starts
-        const uint32_t *starts = run_starts + b.run0;
-        if (b.runs <= SMEM_RUNS) {
-            for (uint32_t r = threadIdx.x; r < b.runs; r += blockDim.x) s_starts[r] = starts[r];
+        if (dom) {
             __syncthreads();
-            starts = s_starts;
+            for (uint32_t wi = threadIdx.x; wi < DOM_WORDS; wi += blockDim.x)
+                for (uint32_t word = sm.dom[wi]; word; word &= word - 1)
+                    stat_value(stat, from_bits<T>(base + (wi * 32 + __ffs(word) - 1)), regs);
         }
+    } else {  // RLE: each row finds its run among the run starts
+        const uint32_t *starts = staged ? sm.starts : run_starts + b.run0;
         const uint8_t *vals = v + 8;
-        for (uint32_t i = threadIdx.x; i < b.rows; i += blockDim.x) {
-            uint32_t lo = 0, hi = b.runs;  // the last run starting at or before i
-            while (hi - lo > 1) {
-                const uint32_t mid = (lo + hi) / 2;
-                if (starts[mid] <= i) lo = mid;
-                else hi = mid;
-            }
+        const uint32_t vw = b.width;
+        auto run_value = [&](uint32_t r) {
             // a value narrower than the element sign-extends
-            uint64_t x = ld_bytes(vals + (size_t)lo * b.width, b.width);
-            if (b.width < 8 && ((x >> (8 * b.width - 1)) & 1u)) x |= ~0ULL << (8 * b.width);
-            st_elem(b.out, b.elem, b.row0 + i, x);
-            if (zone) stat_row(stat, b, x, bit_at(p, b.has_nulls, i), regs);
+            uint64_t x = ld_bytes(vals + (size_t)r * vw, vw);
+            if (vw < 8 && ((x >> (8 * vw - 1)) & 1u)) x |= ~0ULL << (8 * vw);
+            return from_bits<T>(x);
+        };
+        uint32_t lo = 0;  // the thread's rows ascend: its run index only moves forward
+        T t = run_value(0);
+        for (uint32_t i = threadIdx.x; i < b.rows; i += blockDim.x) {
+            if (lo + 1 < b.runs && starts[lo + 1] <= i) {
+                uint32_t hi = b.runs;  // the last run starting at or before i
+                ++lo;
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) / 2;
+                    if (starts[mid] <= i) lo = mid;
+                    else hi = mid;
+                }
+                t = run_value(lo);
+            }
+            out[i] = t;
+            if (!zone) continue;
+            if (!bit_at(p, hn, i)) ++stat.nn;
+            else if (staged) sm.seen[lo] = 1;
+            else stat_value(stat, t, regs);
+        }
+        if (zone && staged) {
+            __syncthreads();
+            for (uint32_t r = threadIdx.x; r < b.runs; r += blockDim.x)
+                if (sm.seen[r]) stat_value(stat, run_value(r), regs);
         }
     }
     if (!zone) return;
@@ -234,20 +275,20 @@ __global__ void __launch_bounds__(DECODE_THREADS) decode_blocks_kernel(const uin
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) {
-        s_mn[warp] = stat.mn;
-        s_mx[warp] = stat.mx;
-        s_fmn[warp] = stat.fmn;
-        s_fmx[warp] = stat.fmx;
-        s_nn[warp] = stat.nn;
+        sm.mn[warp] = stat.mn;
+        sm.mx[warp] = stat.mx;
+        sm.fmn[warp] = stat.fmn;
+        sm.fmx[warp] = stat.fmx;
+        sm.nn[warp] = stat.nn;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
-            stat.mn = min(stat.mn, s_mn[w]);
-            stat.mx = max(stat.mx, s_mx[w]);
-            stat.fmn = fmin(stat.fmn, s_fmn[w]);
-            stat.fmx = fmax(stat.fmx, s_fmx[w]);
-            stat.nn += s_nn[w];
+            stat.mn = min(stat.mn, sm.mn[w]);
+            stat.mx = max(stat.mx, sm.mx[w]);
+            stat.fmn = fmin(stat.fmn, sm.fmn[w]);
+            stat.fmx = fmax(stat.fmx, sm.fmx[w]);
+            stat.nn += sm.nn[w];
         }
         unsigned char *sl = st.stats + (size_t)b.col * st.slice;
         int64_t *imin = (int64_t *)sl, *imax = imin + st.nrg;
@@ -261,7 +302,26 @@ __global__ void __launch_bounds__(DECODE_THREADS) decode_blocks_kernel(const uin
     }
     if (regs) {  // the block's registers, a row of the scratch
         uint32_t *row = (uint32_t *)(st.part + (size_t)b.part_row * HLL_BYTES);
-        for (uint32_t i = threadIdx.x; i < HLL_BYTES / 4; i += blockDim.x) row[i] = s_regs[i];
+        for (uint32_t i = threadIdx.x; i < HLL_BYTES / 4; i += blockDim.x) row[i] = sm.regs[i];
+    }
+}
+
+__global__ void __launch_bounds__(DECODE_THREADS, 3) decode_blocks_kernel(const uint8_t *__restrict__ image,
+                                                                       const SegBlock *__restrict__ blocks,
+                                                                       const uint32_t *__restrict__ run_starts,
+                                                                       const SegStats st) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem &sm = *reinterpret_cast<Smem *>(smem_raw);
+    const SegBlock b = blocks[blockIdx.x];
+    const uint8_t *p = image + b.payload;
+    switch (b.type) {
+        case TGPU_BOOLEAN: decode_block<uint8_t>(b, p, run_starts, st, sm); break;
+        case TGPU_TINYINT: decode_block<int8_t>(b, p, run_starts, st, sm); break;
+        case TGPU_SMALLINT: decode_block<int16_t>(b, p, run_starts, st, sm); break;
+        case TGPU_INT: case TGPU_DATE: decode_block<int32_t>(b, p, run_starts, st, sm); break;
+        case TGPU_FLOAT: decode_block<float>(b, p, run_starts, st, sm); break;
+        case TGPU_DOUBLE: decode_block<double>(b, p, run_starts, st, sm); break;
+        default: decode_block<long long>(b, p, run_starts, st, sm); break;
     }
 }
 
@@ -290,7 +350,10 @@ __global__ void seg_hll_merge_kernel(const SegStats st, uint32_t rows, uint32_t 
 cudaError_t launch_decode_blocks(const uint8_t *image, const SegBlock *blocks, uint32_t n_blocks,
                                  const uint32_t *run_starts, const SegStats &st, cudaStream_t s) {
     if (!n_blocks) return cudaSuccess;
-    decode_blocks_kernel<<<n_blocks, DECODE_THREADS, 0, s>>>(image, blocks, run_starts, st);
+    cudaError_t e = cudaFuncSetAttribute(decode_blocks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(Smem));
+    if (e != cudaSuccess) return e;
+    decode_blocks_kernel<<<n_blocks, DECODE_THREADS, sizeof(Smem), s>>>(image, blocks, run_starts, st);
     return cudaGetLastError();
 }
 
