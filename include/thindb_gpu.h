@@ -390,10 +390,11 @@ typedef struct tgpu_load_stats {
     uint32_t kernel_launches;   /* decode and statistics launches */
     uint32_t chunks;            /* the image's copies, each decoded as it lands */
     uint32_t reserved;
-    double h2d_ms;              /* first copy start to last copy end (device clock) */
+    double h2d_ms;              /* first copy start to the last copy's end (device clock) */
     double decode_ms;           /* the decode launches, summed (device clock) */
     double stats_ms;            /* the zone-map / NDV-sketch launches, summed (device clock) */
-    double pipeline_ms;         /* first copy start to the last chunk's statistics (device clock) */
+    double pipeline_ms;         /* first copy start to the last chunk's work done (device clock) */
+    double first_decode_ms;     /* first copy start to the first decode start (device clock) */
     double total_ms;            /* the whole call (host clock) */
 } tgpu_load_stats;
 tgpu_status tgpu_table_load_stats(const tgpu_table *table, tgpu_load_stats *out);

@@ -244,7 +244,7 @@ class LoadStats(C.Structure):
     _fields_ = [("image_bytes", C.c_uint64), ("decoded_bytes", C.c_uint64), ("blocks", C.c_uint32),
                 ("kernel_launches", C.c_uint32), ("chunks", C.c_uint32), ("reserved", C.c_uint32),
                 ("h2d_ms", C.c_double), ("decode_ms", C.c_double), ("stats_ms", C.c_double),
-                ("pipeline_ms", C.c_double), ("total_ms", C.c_double)]
+                ("pipeline_ms", C.c_double), ("first_decode_ms", C.c_double), ("total_ms", C.c_double)]
 
 
 SIGNATURES += [

@@ -2022,11 +2022,13 @@ tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, co
     const StatsLayout lay = stats_layout(n_rg);
     const size_t slice = lay.stat_bytes + lay.reg_bytes;
     std::vector<bool> sketch(n_columns, want_sketch);
+    // (two register scratches: the chunks alternate between two streams)
     const size_t part_bytes = uniform ? ((size_t)n_columns * per_chunk << HLL_P) : ((size_t)STATS_GRID_MAX << HLL_P);
     if (e == cudaSuccess)
-        e = cudaMallocFromPoolAsync((void **)&d_stats, n_columns * slice + part_bytes, dev->col_pool, s);
+        e = cudaMallocFromPoolAsync((void **)&d_stats, n_columns * slice + 2 * part_bytes, dev->col_pool, s);
     uint8_t *d_part = d_stats ? d_stats + n_columns * slice : nullptr;
-    const SegStats sst{d_stats, slice, lay.stat_bytes, lay.nrg, d_part};
+    const SegStats sst_pair[2] = {{d_stats, slice, lay.stat_bytes, lay.nrg, d_part},
+                                  {d_stats, slice, lay.stat_bytes, lay.nrg, d_part ? d_part + part_bytes : nullptr}};
     for (uint32_t c = 0; c < n_columns && e == cudaSuccess; ++c)
         e = cudaMemsetAsync(d_stats + c * slice + lay.stat_bytes, 0, lay.reg_bytes, s);
     if (e == cudaSuccess) e = cudaMallocFromPoolAsync((void **)&d_image, bytes + SEG_IMAGE_PAD, dev->col_pool, s);
@@ -2038,50 +2040,67 @@ tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, co
         e = cudaMallocFromPoolAsync((void **)&d_runs, std::max<size_t>(1, run_starts.size()) * 4, dev->col_pool, s);
     if (e == cudaSuccess && !run_starts.empty())
         e = cudaMemcpyAsync(d_runs, run_starts.data(), run_starts.size() * 4, cudaMemcpyHostToDevice, s);
-    // the copies wait for the allocations; each chunk's work waits for its copy
+    // Chunks alternate between two streams, each copying a chunk and then
+    // decoding it, so one stream's copy runs beside the other's decode with
+    // no wait between the streams.  (A copy stream feeding a decode stream
+    // through events was observed to run every copy before the first decode
+    // whenever the whole pipeline was queued at once.)  A chunk's copy covers
+    // its row groups' bytes widened to 4 KiB boundaries, so every copy is
+    // aligned; neighbouring copies overlap by less than 4 KiB and write the
+    // same bytes there.
     cudaEvent_t ready = event(), copy0 = event(), copy1 = event();
+    const cudaStream_t pair[2] = {s, cs};
     if (e == cudaSuccess) e = cudaEventRecord(ready, s);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ready, 0);
-    if (e == cudaSuccess) e = cudaEventRecord(copy0, cs);
-    std::vector<cudaEvent_t> landed(n_chunks), dec0(n_chunks), dec1(n_chunks), st1(n_chunks);
+    if (e == cudaSuccess) e = cudaEventRecord(copy0, s);
+    std::vector<cudaEvent_t> landed(n_chunks), dec0(n_chunks), dec1(n_chunks), st1(n_chunks), done_ev(2);
     for (uint32_t k = 0; k < n_chunks; ++k) {
         landed[k] = event();
         dec0[k] = event();
         dec1[k] = event();
         st1[k] = event();
     }
+    done_ev[0] = event();
+    done_ev[1] = event();
     uint32_t launches = 0;
     for (uint32_t k = 0; k < n_chunks && e == cudaSuccess; ++k) {
+        const cudaStream_t q = pair[k & 1];
+        const SegStats &sst = sst_pair[k & 1];
         const uint32_t g0 = k * per_chunk, g1 = std::min(n_seg_rg, g0 + per_chunk);
-        const uint64_t b0 = k ? rg_pos[g0] : 0, b1 = g1 < n_seg_rg ? rg_pos[g1] : bytes;
-        e = cudaMemcpyAsync(d_image + b0, image + b0, b1 - b0, cudaMemcpyHostToDevice, cs);
-        if (e == cudaSuccess) e = cudaEventRecord(landed[k], cs);
-        if (e == cudaSuccess && k + 1 == n_chunks) e = cudaEventRecord(copy1, cs);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, landed[k], 0);
-        if (e == cudaSuccess) e = cudaEventRecord(dec0[k], s);
+        const uint64_t lo = k ? rg_pos[g0] / 4096 * 4096 : 0;
+        const uint64_t hi = g1 < n_seg_rg ? std::min<uint64_t>(bytes, round_up(rg_pos[g1], 4096)) : bytes;
+        e = cudaMemcpyAsync(d_image + lo, image + lo, hi - lo, cudaMemcpyHostToDevice, q);
+        if (e == cudaSuccess) e = cudaEventRecord(landed[k], q);
+        if (e == cudaSuccess) e = cudaEventRecord(dec0[k], q);
         if (e == cudaSuccess)
             e = launch_decode_blocks(d_image, d_blocks + chunk_first[k], chunk_first[k + 1] - chunk_first[k], d_runs,
-                                     sst, s);
+                                     sst, q);
         launches += 1;
-        if (e == cudaSuccess) e = cudaEventRecord(dec1[k], s);
+        if (e == cudaSuccess) e = cudaEventRecord(dec1[k], q);
         if (uniform && want_sketch && e == cudaSuccess) {
-            // the chunk's register rows into the columns' registers, before the next chunk reuses them
-            e = launch_seg_hll_merge(sst, n_columns, g1 - g0, per_chunk, s);
+            // the chunk's register rows into the columns' registers, before this stream's next chunk reuses them
+            e = launch_seg_hll_merge(sst, n_columns, g1 - g0, per_chunk, q);
             launches += 1;
-        } else if (!uniform) {
-            // the table's own row groups, over the decoded columns
-            for (uint32_t c = 0; c < n_columns && e == cudaSuccess; ++c) {
-                unsigned char *sl = d_stats + c * slice;
-                int64_t *imin = (int64_t *)sl, *imax = imin + lay.nrg;
-                double *fmin = (double *)(imax + lay.nrg), *fmax = fmin + lay.nrg;
-                uint32_t *nulls = (uint32_t *)(fmax + lay.nrg);
-                uint32_t *regs = (uint32_t *)(sl + lay.stat_bytes);
-                e = launch_column_stats(data[c], valid[c], columns[c].type, n, table_rg, 0, n_rg, imin, imax, fmin,
-                                        fmax, nulls, sketch[c] ? regs : nullptr, d_part, 1, s);
-                launches += sketch[c] ? 2 : 1;
-            }
         }
-        if (e == cudaSuccess) e = cudaEventRecord(st1[k], s);
+        if (e == cudaSuccess) e = cudaEventRecord(st1[k], q);
+    }
+    // not uniform: the table's own row groups, over the decoded columns
+    for (uint32_t q = 0; q < 2 && e == cudaSuccess; ++q) {
+        e = cudaEventRecord(done_ev[q], pair[q]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, done_ev[q], 0);
+    }
+    if (e == cudaSuccess && n_chunks) e = cudaEventRecord(copy1, s);
+    if (!uniform) {
+        for (uint32_t c = 0; c < n_columns && e == cudaSuccess; ++c) {
+            unsigned char *sl = d_stats + c * slice;
+            int64_t *imin = (int64_t *)sl, *imax = imin + lay.nrg;
+            double *fmin = (double *)(imax + lay.nrg), *fmax = fmin + lay.nrg;
+            uint32_t *nulls = (uint32_t *)(fmax + lay.nrg);
+            uint32_t *regs = (uint32_t *)(sl + lay.stat_bytes);
+            e = launch_column_stats(data[c], valid[c], columns[c].type, n, table_rg, 0, n_rg, imin, imax, fmin, fmax,
+                                    nulls, sketch[c] ? regs : nullptr, d_part, 1, s);
+            launches += sketch[c] ? 2 : 1;
+        }
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -2097,12 +2116,13 @@ tgpu_status tgpu_table_register_segment(const uint8_t *image, uint64_t bytes, co
     ls.kernel_launches = launches;
     ls.chunks = n_chunks;
     float ms = 0;
-    if (n_chunks && cudaEventElapsedTime(&ms, copy0, copy1) == cudaSuccess) ls.h2d_ms = ms;
     for (uint32_t k = 0; k < n_chunks; ++k) {
+        if (cudaEventElapsedTime(&ms, copy0, landed[k]) == cudaSuccess) ls.h2d_ms = std::max<double>(ls.h2d_ms, ms);
         if (cudaEventElapsedTime(&ms, dec0[k], dec1[k]) == cudaSuccess) ls.decode_ms += ms;
         if (cudaEventElapsedTime(&ms, dec1[k], st1[k]) == cudaSuccess) ls.stats_ms += ms;
     }
-    if (n_chunks && cudaEventElapsedTime(&ms, copy0, st1[n_chunks - 1]) == cudaSuccess) ls.pipeline_ms = ms;
+    if (n_chunks && cudaEventElapsedTime(&ms, copy0, copy1) == cudaSuccess) ls.pipeline_ms = ms;
+    if (n_chunks && cudaEventElapsedTime(&ms, copy0, dec0[0]) == cudaSuccess) ls.first_decode_ms = ms;
     // register the decoded columns in place, then hand them to the table
     std::vector<tgpu_column_desc> cd(n_columns);
     for (uint32_t c = 0; c < n_columns; ++c) {
