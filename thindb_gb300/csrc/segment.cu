@@ -119,6 +119,12 @@ template <typename T> __device__ __forceinline__ T from_bits(uint64_t x) {
     else return (T)x;  // the element's low bytes (a signed type sign-extends)
 }
 
+template <typename T> __device__ __forceinline__ uint64_t to_bits(T t) {
+    if constexpr (std::is_same<T, float>::value) return __float_as_uint(t);
+    else if constexpr (std::is_same<T, double>::value) return (uint64_t)__double_as_longlong(t);
+    else return (uint64_t)t;
+}
+
 // One valid value into the thread's zone map and the block's registers.
 template <typename T> __device__ __forceinline__ void stat_value(Stat &st, T t, uint32_t *regs) {
     uint64_t bits;
@@ -161,6 +167,93 @@ struct Smem {
     unsigned nn[DECODE_THREADS / 32];
 };
 
+// L bytes at p (unaligned) as (L + 3) / 4 little-endian words, read as the
+// aligned words around them (the image is padded past its end).
+template <int L> __device__ __forceinline__ void ld_stream(const uint8_t *p, uint32_t (&o)[(L + 3) / 4]) {
+    constexpr int NW = (L + 3) / 4;
+    const uint32_t a = (uint32_t)((uintptr_t)p & 3u);
+    const uint32_t *q = (const uint32_t *)(p - a);
+    uint32_t w[NW + 1];
+#pragma unroll
+    for (int j = 0; j <= NW; ++j) w[j] = __ldg(q + j);
+#pragma unroll
+    for (int j = 0; j < NW; ++j) o[j] = __funnelshift_r(w[j], w[j + 1], 8 * a);
+}
+
+// Code i (W bytes) of a word stream.
+template <int W, int N> __device__ __forceinline__ uint64_t code_at(const uint32_t (&o)[N], int i) {
+    if constexpr (W == 8) return (uint64_t)o[2 * i] | ((uint64_t)o[2 * i + 1] << 32);
+    else if constexpr (W == 4) return o[i];
+    else if constexpr (W == 2) return (o[i / 2] >> (16 * (i & 1))) & 0xFFFFu;
+    else return (o[i / 4] >> (8 * (i & 3))) & 0xFFu;
+}
+
+// Bits of one element: 32 for elements of up to 4 bytes.
+template <typename T> using bits_t = typename std::conditional<sizeof(T) == 8, uint64_t, uint32_t>::type;
+
+// K elements of T (their low bytes in x) as 16 bytes.
+template <typename T, int K> __device__ __forceinline__ uint4 pack16(const bits_t<T> (&x)[K]) {
+    uint32_t w[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if constexpr (sizeof(T) == 8) w[j] = (uint32_t)(x[j / 2] >> (32 * (j & 1)));
+        else if constexpr (sizeof(T) == 4) w[j] = (uint32_t)x[j];
+        else if constexpr (sizeof(T) == 2) w[j] = ((uint32_t)x[2 * j] & 0xFFFFu) | ((uint32_t)x[2 * j + 1] << 16);
+        else
+            w[j] = ((uint32_t)x[4 * j] & 0xFFu) | (((uint32_t)x[4 * j + 1] & 0xFFu) << 8) |
+                   (((uint32_t)x[4 * j + 2] & 0xFFu) << 16) | ((uint32_t)x[4 * j + 3] << 24);
+    }
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// Validity bits of rows i .. i + K - 1 (bit j = row i + j).
+template <int K> __device__ __forceinline__ uint32_t valid_bits(const uint8_t *bm, bool has_nulls, uint32_t i) {
+    if (!has_nulls) return (K == 32) ? ~0u : (1u << K) - 1u;
+    return (uint32_t)(ld_bytes(bm + (i >> 3), 4) >> (i & 7)) & ((1u << K) - 1u);
+}
+
+// One row's share of the statistics.
+template <typename T>
+__device__ __forceinline__ void stat_row(Stat &stat, bool ok, bool dom, uint32_t code, T t, Smem &sm, uint32_t *regs) {
+    if (!ok) {
+        ++stat.nn;
+    } else if (dom) {
+        const uint32_t bit = 1u << (code & 31);
+        if (!(sm.dom[(code & 0xFFFFu) >> 5] & bit)) atomicOr(&sm.dom[(code & 0xFFFFu) >> 5], bit);
+    } else {
+        stat_value(stat, t, regs);
+    }
+}
+
+// Raw / FOR rows with codes of W bytes, 16 output bytes per thread per pass
+// (K = 16 / sizeof(T) consecutive rows: one 16-byte store, their codes read
+// as a few aligned words).  The rows past the last whole pass go one by one.
+template <typename T, int W>
+__device__ void expand_vec(const SegBlock &b, const uint8_t *bm, const uint8_t *codes, uint64_t base, T *out,
+                           bool zone, bool dom, Stat &stat, Smem &sm, uint32_t *regs) {
+    constexpr int K = 16 / (int)sizeof(T), L = K * W;
+    const uint32_t whole = b.rows / K * K;
+    for (uint32_t e0 = threadIdx.x * K; e0 < whole; e0 += blockDim.x * K) {
+        uint32_t o[(L + 3) / 4];
+        ld_stream<L>(codes + (size_t)e0 * W, o);
+        bits_t<T> x[K];
+#pragma unroll
+        for (int i = 0; i < K; ++i) x[i] = (bits_t<T>)(base + code_at<W>(o, i));
+        *(uint4 *)(out + e0) = pack16<T, K>(x);
+        if (!zone) continue;
+        const uint32_t vb = valid_bits<K>(bm, b.has_nulls, e0);
+#pragma unroll
+        for (int i = 0; i < K; ++i)
+            stat_row<T>(stat, (vb >> i) & 1u, dom, (uint32_t)code_at<W>(o, i), from_bits<T>(x[i]), sm, regs);
+    }
+    for (uint32_t e = whole + threadIdx.x; e < b.rows; e += blockDim.x) {
+        const uint64_t c = ld_bytes(codes + (size_t)e * W, W);
+        const T t = from_bits<T>(base + c);
+        out[e] = t;
+        if (zone) stat_row<T>(stat, bit_at(bm, b.has_nulls, e), dom, (uint32_t)c, t, sm, regs);
+    }
+}
+
 // Decode one block of a column of element type T; with SEG_ZONE take the
 // block's zone map and (SEG_SKETCH) its sketch registers.  A block whose
 // codes span at most 2^16 values (1-2 byte raw elements, FOR deltas of 1-2
@@ -199,7 +292,16 @@ __device__ void decode_block(const SegBlock &b, const uint8_t *p, const uint32_t
         const uint64_t base = raw ? 0 : ld_bytes(v, 8);
         const uint8_t *codes = raw ? v : v + 20;
         const uint32_t w = raw ? b.elem : b.width, step = blockDim.x;
-        for (uint32_t i0 = threadIdx.x; i0 < b.rows; i0 += DECODE_UNROLL * step) {
+        // 16-byte stores need the block's first row on a 16-byte boundary;
+        // codes wider than the element (never written by thinDB) go row by row
+        const bool vec = ((uintptr_t)out & 15u) == 0 && w <= sizeof(T);
+        if (vec) {
+            if (w == 1) expand_vec<T, 1>(b, p, codes, base, out, zone, dom, stat, sm, regs);
+            else if (w == 2) expand_vec<T, (sizeof(T) >= 2 ? 2 : 1)>(b, p, codes, base, out, zone, dom, stat, sm, regs);
+            else if (w == 4) expand_vec<T, (sizeof(T) >= 4 ? 4 : 1)>(b, p, codes, base, out, zone, dom, stat, sm, regs);
+            else expand_vec<T, (sizeof(T) >= 8 ? 8 : 1)>(b, p, codes, base, out, zone, dom, stat, sm, regs);
+        }
+        for (uint32_t i0 = vec ? b.rows : threadIdx.x; i0 < b.rows; i0 += DECODE_UNROLL * step) {
             uint64_t c[DECODE_UNROLL];
 #pragma unroll
             for (int k = 0; k < DECODE_UNROLL; ++k) {
@@ -241,7 +343,39 @@ __device__ void decode_block(const SegBlock &b, const uint8_t *p, const uint32_t
         };
         uint32_t lo = 0;  // the thread's rows ascend: its run index only moves forward
         T t = run_value(0);
-        for (uint32_t i = threadIdx.x; i < b.rows; i += blockDim.x) {
+        // K consecutive rows per thread per pass and one 16-byte store (the
+        // block's first row on a 16-byte boundary); then the rest row by row
+        constexpr int K = 16 / (int)sizeof(T);
+        const bool vec = ((uintptr_t)out & 15u) == 0;
+        const uint32_t whole = vec ? b.rows / K * K : 0;
+        for (uint32_t e0 = threadIdx.x * K; e0 < whole; e0 += blockDim.x * K) {
+            if (lo + 1 < b.runs && starts[lo + 1] <= e0) {
+                uint32_t hi = b.runs;  // the last run starting at or before e0
+                ++lo;
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) / 2;
+                    if (starts[mid] <= e0) lo = mid;
+                    else hi = mid;
+                }
+                t = run_value(lo);
+            }
+            const uint32_t vb = zone ? valid_bits<K>(p, hn, e0) : 0u;
+            bits_t<T> x[K];
+#pragma unroll
+            for (int i = 0; i < K; ++i) {
+                while (lo + 1 < b.runs && starts[lo + 1] <= e0 + i) {
+                    ++lo;
+                    t = run_value(lo);
+                }
+                x[i] = (bits_t<T>)to_bits(t);
+                if (!zone) continue;
+                if (!((vb >> i) & 1u)) ++stat.nn;
+                else if (staged) sm.seen[lo] = 1;
+                else stat_value(stat, t, regs);
+            }
+            *(uint4 *)(out + e0) = pack16<T, K>(x);
+        }
+        for (uint32_t i = whole + threadIdx.x; i < b.rows; i += blockDim.x) {
             if (lo + 1 < b.runs && starts[lo + 1] <= i) {
                 uint32_t hi = b.runs;  // the last run starting at or before i
                 ++lo;
@@ -306,7 +440,7 @@ __device__ void decode_block(const SegBlock &b, const uint8_t *p, const uint32_t
     }
 }
 
-__global__ void __launch_bounds__(DECODE_THREADS, 3) decode_blocks_kernel(const uint8_t *__restrict__ image,
+__global__ void __launch_bounds__(DECODE_THREADS, 2) decode_blocks_kernel(const uint8_t *__restrict__ image,
                                                                        const SegBlock *__restrict__ blocks,
                                                                        const uint32_t *__restrict__ run_starts,
                                                                        const SegStats st) {
