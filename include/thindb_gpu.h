@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define TGPU_ABI_VERSION 1
+#define TGPU_ABI_VERSION 2
 
 /* ---------------------------------------------------------------- status -- */
 
@@ -142,13 +142,15 @@ typedef enum tgpu_agg_func {
     TGPU_AGG_AVG = 3,
     TGPU_AGG_MIN = 4,
     TGPU_AGG_MAX = 5,
-    TGPU_AGG_COUNT_DISTINCT = 6
+    TGPU_AGG_COUNT_DISTINCT = 6,
+    TGPU_AGG_UDF = 7             /* a registered user-defined aggregate (AggFunc.udf), named by udf_name */
 } tgpu_agg_func;
 
 typedef struct tgpu_agg_spec {
     int32_t func;                /* tgpu_agg_func */
     int32_t column;              /* input column index, -1 for COUNT(*) */
     const char *as;              /* output column name (may be NULL) */
+    const char *udf_name;        /* TGPU_AGG_UDF: the registry name (AggSpec.udf_name, aggregate.zig:240) */
 } tgpu_agg_spec;
 
 /* One conjunct of the fused WHERE (thinDB's scan fuses the conjunction of
@@ -404,6 +406,22 @@ tgpu_status tgpu_table_load_stats(const tgpu_table *table, tgpu_load_stats *out)
  * the last row of the last byte are unspecified).  VARCHAR columns return
  * TGPU_ERR_UNSUPPORTED_TYPE. */
 tgpu_status tgpu_table_read_column(const tgpu_table *table, uint32_t column, void *values, uint8_t *validity);
+/* thinDB's aggregate registry (udf.zig UdfRegistry.registerAggregate :870):
+ * the names of the host's user-defined aggregates, so that a request can
+ * name one (TGPU_AGG_UDF).  A name is case-insensitive, 1-63 characters of
+ * [A-Za-z0-9_] not starting with a digit, and not a built-in aggregate's
+ * (count, sum, avg, min, max, count_distinct, ...): those return
+ * TGPU_ERR_INVALID_ARGUMENT, as does registering a name twice.  The
+ * aggregate's code (AggregateUdf init / update / combine / finalize,
+ * udf.zig:88-102) is host code this operator does not run: a request with a
+ * registered TGPU_AGG_UDF aggregate returns TGPU_DECLINE from
+ * tgpu_query_create (the caller keeps thinDB's executor, whose silo runs
+ * registered aggregates, v2_shape_group_topn.zig:86, :170-177); an
+ * unregistered name returns TGPU_ERR_INVALID_ARGUMENT. */
+tgpu_status tgpu_aggregate_register(const char *name);
+tgpu_status tgpu_aggregate_unregister(const char *name);
+/* 1 when `name` is registered, else 0. */
+int32_t tgpu_aggregate_registered(const char *name);
 /* Row count, row-group count and a column's NDV estimate (-1 column = none). */
 tgpu_status tgpu_table_info(const tgpu_table *table, int32_t column,
                             uint64_t *n_rows, uint32_t *n_row_groups, uint64_t *ndv);

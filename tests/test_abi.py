@@ -46,7 +46,7 @@ def test_struct_sizes_match_c_layout():
     # sizes the header implies on LP64 (both x86_64 and aarch64)
     assert C.sizeof(abi.ColumnDesc) == 64
     assert C.sizeof(abi.TableDesc) == 40
-    assert C.sizeof(abi.AggSpec) == 16
+    assert C.sizeof(abi.AggSpec) == 24
     assert C.sizeof(abi.Predicate) == 40
     assert C.sizeof(abi.Request) == 136
     assert C.sizeof(abi.OutputColumn) == 80
@@ -139,3 +139,23 @@ def test_tuning_merge_keeps_untouched_shapes():
     # a second merge appends to the list
     _, by2, _ = merge_tables({"generated_by": by, "seconds": seconds, "entries": entries}, [], "cmd", 1.0)
     assert by2[:2] == by and by2[2] == "cmd --merge <this file>"
+
+
+def test_aggregate_registry_names():
+    """thinDB's registerAggregate rules: case-insensitive names, built-in names
+    and repeats refused (no device needed)."""
+    assert not engine.aggregate_registered("geo_mean")
+    engine.register_aggregate("Geo_Mean")
+    try:
+        assert engine.aggregate_registered("geo_mean") and engine.aggregate_registered("GEO_MEAN")
+        with pytest.raises(engine.EngineError) as e:
+            engine.register_aggregate("geo_mean")
+        assert e.value.status == abi.ERR_INVALID_ARGUMENT
+    finally:
+        engine.unregister_aggregate("GEO_MEAN")
+    assert not engine.aggregate_registered("geo_mean")
+    for bad in ("sum", "COUNT", "", "9lives", "has space", "x" * 64):
+        with pytest.raises(engine.EngineError):
+            engine.register_aggregate(bad)
+    with pytest.raises(engine.EngineError):
+        engine.unregister_aggregate("never_registered")

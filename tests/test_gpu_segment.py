@@ -150,3 +150,25 @@ def test_row_groups_of_differing_sizes():
                     where=[Pred("day", "between", 19000, 19001)])), 1, ordered=False)
     q.close()
     t.close()
+
+
+@pytest.mark.parametrize("rg", [65_536, 10_000])
+def test_statistics_match_a_table_registered_from_columns(rg):
+    # the decode's zone maps and sketches equal those taken from resident columns
+    cols = columns(400_000, 10)
+    seg = from_segment(cols, row_group_rows=rg)
+    ref = Table(cols, row_group_rows=rg)
+    for c in cols:
+        assert seg.ndv(c.name) == ref.ndv(c.name), c.name
+    for where in ([Pred("day", "between", 19100, 19150)], [Pred("user", "<", 100)], [Pred("price", ">", 999.5)],
+                  [Pred("amount", "between", -10**9, -10**9 + 10**6)]):
+        req = Request(["region"], [AggSpec("count", None, "c")], where=where)
+        pruned = []
+        for t in (seg, ref):
+            q = try_build_group_topn(t, req)
+            q.collect()
+            pruned.append(q.stats().row_groups_pruned)
+            q.close()
+        assert pruned[0] == pruned[1], where
+    seg.close()
+    ref.close()

@@ -3,7 +3,7 @@ from __future__ import annotations
 
 import ctypes as C
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 # tgpu_status
 OK, DECLINE, ERR_INVALID_ARGUMENT, ERR_MEMORY_BUDGET, ERR_UNSUPPORTED_TYPE, ERR_CANCELLED, ERR_CUDA, \
@@ -27,9 +27,9 @@ TYPE_BYTES = {BOOLEAN: 1, TINYINT: 1, SMALLINT: 2, INT: 4, DATE: 4, BIGINT: 8, D
 LOC_HOST, LOC_DEVICE = 0, 1
 
 # tgpu_agg_func
-AGG_COUNT, AGG_SUM, AGG_AVG, AGG_MIN, AGG_MAX, AGG_COUNT_DISTINCT = range(1, 7)
+AGG_COUNT, AGG_SUM, AGG_AVG, AGG_MIN, AGG_MAX, AGG_COUNT_DISTINCT, AGG_UDF = range(1, 8)
 AGG_BY_NAME = {"count": AGG_COUNT, "sum": AGG_SUM, "avg": AGG_AVG, "min": AGG_MIN, "max": AGG_MAX,
-               "count_distinct": AGG_COUNT_DISTINCT}
+               "count_distinct": AGG_COUNT_DISTINCT, "udf": AGG_UDF}
 
 # tgpu_pred_op
 PRED_BETWEEN, PRED_NOT_BETWEEN, PRED_EQ, PRED_NE, PRED_LT, PRED_LE, PRED_GT, PRED_GE, PRED_IS_NULL, \
@@ -87,7 +87,7 @@ class TableDesc(C.Structure):
 
 
 class AggSpec(C.Structure):
-    _fields_ = [("func", C.c_int32), ("column", C.c_int32), ("as_", C.c_char_p)]
+    _fields_ = [("func", C.c_int32), ("column", C.c_int32), ("as_", C.c_char_p), ("udf_name", C.c_char_p)]
 
 
 class Predicate(C.Structure):
@@ -249,6 +249,9 @@ class LoadStats(C.Structure):
 
 SIGNATURES += [
     ("tgpu_table_load_stats", C.c_int, [C.c_void_p, C.POINTER(LoadStats)]),
+    ("tgpu_aggregate_register", C.c_int, [C.c_char_p]),
+    ("tgpu_aggregate_unregister", C.c_int, [C.c_char_p]),
+    ("tgpu_aggregate_registered", C.c_int32, [C.c_char_p]),
     ("tgpu_table_read_column", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     ("tgpu_table_register_segment", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(SegmentColumn), C.c_uint32,
                                               C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),

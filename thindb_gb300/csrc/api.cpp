@@ -18,6 +18,7 @@
 #include <memory>
 #include <mutex>
 #include <random>
+#include <set>
 #include <string>
 #include <thread>
 #include <unordered_map>
@@ -616,7 +617,45 @@ int used_col(DevQuery &dq, std::vector<int> &map, const tgpu_table *t, int c) {
 // DATE / DECIMAL64 / packed-id keys up to 128 packed bits, COUNT/SUM/AVG/MIN/
 // MAX/COUNT(DISTINCT) within thinDB's 16 state slots.  Strings other than
 // packed ids (hashed keys) decline to the next route.
+// The registered user-defined aggregates' names, lower-cased.
+std::mutex g_udf_mu;
+std::set<std::string> g_udfs;
+
+// A registry name as thinDB's validateName / lowerName take it, or "" when invalid.
+std::string udf_key(const char *name) {
+    if (!name) return "";
+    std::string k;
+    for (const char *c = name; *c; ++c) {
+        const unsigned char ch = (unsigned char)*c;
+        const bool ok = (ch >= 'a' && ch <= 'z') || (ch >= 'A' && ch <= 'Z') || ch == '_' || (ch >= '0' && ch <= '9');
+        if (!ok || k.size() >= 63) return "";
+        k.push_back((char)((ch >= 'A' && ch <= 'Z') ? ch - 'A' + 'a' : ch));
+    }
+    if (k.empty() || (k[0] >= '0' && k[0] <= '9')) return "";
+    return k;
+}
+
+// Built-in aggregate names a registration may not take (isReservedAggregateName).
+bool udf_reserved(const std::string &k) {
+    static const char *const names[] = {"count", "sum", "avg", "min", "max", "count_distinct", "sum_distinct",
+                                        "avg_distinct", "any_value", "first", "last", "max_by", "min_by",
+                                        "percentile", "percentile_disc", "percentile_approx", "group_concat",
+                                        "approx_top_k", "stddev", "variance", "median"};
+    for (const char *n : names)
+        if (k == n) return true;
+    return false;
+}
+
 tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *req) {
+    // a user-defined aggregate runs on the host: decline it by name
+    for (uint32_t i = 0; i < req->n_aggs; ++i) {
+        if (req->aggs[i].func != TGPU_AGG_UDF) continue;
+        const std::string k = udf_key(req->aggs[i].udf_name);
+        std::lock_guard<std::mutex> lk(g_udf_mu);
+        if (k.empty() || !g_udfs.count(k))
+            return fail(TGPU_ERR_INVALID_ARGUMENT, std::string("unknown aggregate ") + (req->aggs[i].udf_name ? req->aggs[i].udf_name : "(null)"));
+        return fail(TGPU_DECLINE, "user-defined aggregate " + k + " runs on the host");
+    }
     DevQuery &dq = q->dq;
     DevFinal &df = q->df;
     std::memset(&dq, 0, sizeof(dq));
@@ -1651,6 +1690,28 @@ tgpu_status tgpu_table_register(const tgpu_table_desc *desc, tgpu_table **out) {
     return register_table(desc, out, nullptr);
 }
 
+tgpu_status tgpu_aggregate_register(const char *name) {
+    const std::string k = udf_key(name);
+    if (k.empty()) return fail(TGPU_ERR_INVALID_ARGUMENT, "aggregate name");
+    if (udf_reserved(k)) return fail(TGPU_ERR_INVALID_ARGUMENT, "a built-in aggregate's name");
+    std::lock_guard<std::mutex> lk(g_udf_mu);
+    if (!g_udfs.insert(k).second) return fail(TGPU_ERR_INVALID_ARGUMENT, "aggregate already registered");
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_aggregate_unregister(const char *name) {
+    const std::string k = udf_key(name);
+    std::lock_guard<std::mutex> lk(g_udf_mu);
+    if (k.empty() || !g_udfs.erase(k)) return fail(TGPU_ERR_INVALID_ARGUMENT, "aggregate not registered");
+    return TGPU_OK;
+}
+
+int32_t tgpu_aggregate_registered(const char *name) {
+    const std::string k = udf_key(name);
+    std::lock_guard<std::mutex> lk(g_udf_mu);
+    return !k.empty() && g_udfs.count(k) ? 1 : 0;
+}
+
 }  // extern "C"
 
 // Per-column statistics slices: zone maps of every row group (min/max as i64
@@ -2385,7 +2446,7 @@ struct tgpu_query_batch {
     std::vector<DevQuery> h_qs;
     std::vector<DevFinal> h_fs;
     std::vector<DevFinalBufs> h_bs;
-    std::vector<uint2> items;               // {query, first chunk of a row group}, by fold class, row group major
+    std::vector<uint4> items;               // {query, first chunk, end chunk, 0}, by fold class, window major
     uint32_t class_off[BATCH_CLASSES + 1] = {0};  // items of fold class c: [class_off[c], class_off[c + 1])
     int class_grid[BATCH_CLASSES] = {0};
     Buffer dev_buf;                         // one pooled allocation for every array below
@@ -2394,7 +2455,7 @@ struct tgpu_query_batch {
     DevFinal *d_fs = nullptr;
     DevFinalBufs *d_bs = nullptr;
     Buffer items_buf;                       // pooled
-    uint2 *d_items = nullptr;
+    uint4 *d_items = nullptr;
     unsigned int *d_ctrl = nullptr;         // [0] work counter, [1] status
     unsigned long long *d_counts = nullptr; // 8 per query
     unsigned int *d_qctrl = nullptr;        // 4 per query: tile counter, status
@@ -2529,28 +2590,35 @@ tgpu_status batch_descriptors(tgpu_query_batch *b) {
         b->any_topk |= fb.rank == 1;
     }
     if (!b->d_items) {
-        // per fold class, row group major: every query of the class that
-        // keeps row group g, then g + 1, ...
+        // per fold class, window major: the row groups go in windows of
+        // about BATCH_WINDOW_ROWS rows, and an item is one query's kept row
+        // groups of one window (one CTA, its shared table flushed once per
+        // item); every query of the class for window w, then w + 1, ..., so
+        // the CTAs running at any moment read the same window from L2
+        const uint32_t win = std::max<uint32_t>(1, (uint32_t)(BATCH_WINDOW_ROWS / std::max<uint32_t>(1, b->t->rg_rows)));
         std::vector<size_t> pos(Q, 0);
         for (int cls = 0; cls < BATCH_CLASSES; ++cls) {
             b->class_off[cls] = (uint32_t)b->items.size();
-            for (uint32_t g = 0; g < b->t->n_rg; ++g)
+            for (uint32_t g0 = 0; g0 < b->t->n_rg; g0 += win)
                 for (uint32_t i = 0; i < Q; ++i) {
                     if (batch_fold_class(b->h_qs[i]) != cls) continue;
                     const std::vector<uint32_t> &rl = b->qs[i]->rg_list;
-                    if (pos[i] < rl.size() && rl[pos[i]] == g) {
-                        b->items.push_back(make_uint2(i, (uint32_t)(pos[i] * b->h_qs[i].chunks_per_rg)));
-                        ++pos[i];
+                    const size_t p0 = pos[i];
+                    while (pos[i] < rl.size() && rl[pos[i]] < g0 + win) ++pos[i];
+                    if (pos[i] > p0) {
+                        const uint32_t cpr = b->h_qs[i].chunks_per_rg;
+                        b->items.push_back(make_uint4(i, (uint32_t)(p0 * cpr),
+                                                      std::min<uint32_t>((uint32_t)(pos[i] * cpr), b->h_qs[i].n_chunks), 0u));
                     }
                 }
         }
         b->class_off[BATCH_CLASSES] = (uint32_t)b->items.size();
-        tgpu_status ist = g_scratch_pool.take(sizeof(uint2) * std::max<size_t>(1, b->items.size()), b->stream,
+        tgpu_status ist = g_scratch_pool.take(sizeof(uint4) * std::max<size_t>(1, b->items.size()), b->stream,
                                               &b->items_buf);
         if (ist != TGPU_OK) return ist;
-        b->d_items = (uint2 *)b->items_buf.p;
+        b->d_items = (uint4 *)b->items_buf.p;
         if (!b->items.empty())
-            CU(cudaMemcpyAsync(b->d_items, b->items.data(), sizeof(uint2) * b->items.size(), cudaMemcpyHostToDevice,
+            CU(cudaMemcpyAsync(b->d_items, b->items.data(), sizeof(uint4) * b->items.size(), cudaMemcpyHostToDevice,
                                b->stream));
     }
     CU(cudaMemcpyAsync(b->d_qs, b->h_qs.data(), sizeof(DevQuery) * Q, cudaMemcpyHostToDevice, b->stream));
@@ -2811,7 +2879,7 @@ struct OwnedRequest {
     tgpu_request r{};
     std::vector<int32_t> group_cols;
     std::vector<tgpu_agg_spec> aggs;
-    std::vector<std::string> names;
+    std::vector<std::string> names, udf_names;
     std::vector<tgpu_predicate> where;
     std::vector<tgpu_having> having;
     std::vector<tgpu_sort_spec> order;
@@ -2820,8 +2888,15 @@ struct OwnedRequest {
         group_cols.assign(in.group_cols, in.group_cols + in.n_group_cols);
         aggs.assign(in.aggs, in.aggs + in.n_aggs);
         names.clear();
-        for (auto &a : aggs) names.push_back(a.as ? a.as : "");
-        for (size_t i = 0; i < aggs.size(); ++i) aggs[i].as = names[i].c_str();
+        udf_names.clear();
+        for (auto &a : aggs) {
+            names.push_back(a.as ? a.as : "");
+            udf_names.push_back(a.udf_name ? a.udf_name : "");
+        }
+        for (size_t i = 0; i < aggs.size(); ++i) {
+            aggs[i].as = names[i].c_str();
+            if (aggs[i].udf_name) aggs[i].udf_name = udf_names[i].c_str();
+        }
         where.assign(in.where, in.where + in.n_where);
         having.assign(in.having, in.having + in.n_having);
         order.assign(in.order, in.order + in.n_order);

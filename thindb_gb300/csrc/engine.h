@@ -419,10 +419,13 @@ cudaError_t launch_scan_inline(const DevQuery &q, int grid, size_t smem, cudaStr
 constexpr int BATCH_GENERIC4 = 12;
 constexpr int BATCH_GENERIC16 = 13;
 constexpr int BATCH_CLASSES = 14;
+// A batch work item: one query's kept row groups within a window of about
+// this many rows.
+constexpr uint64_t BATCH_WINDOW_ROWS = 1ull << 20;
 int batch_fold_class(const DevQuery &q);
 int batch_scan_grid(int cls, size_t smem, int sms);
 // items[i] = {query, first chunk of one of its row groups}, every query of class cls
-cudaError_t launch_batch_scan(int cls, const DevQuery *qs, const uint2 *items, uint32_t n_items, size_t smem,
+cudaError_t launch_batch_scan(int cls, const DevQuery *qs, const uint4 *items, uint32_t n_items, size_t smem,
                               int grid, const volatile int *cancel, unsigned int *status, cudaStream_t s);
 // compaction, top-k / all-groups selection, gather and clear for every query of a batch
 // single-query top-k straight from the occupancy bitmap (counts[0] groups,

@@ -7,18 +7,19 @@ namespace tgpu {
 namespace {
 
 // Many queries of one fold class in one persistent kernel.  A work item is
-// (query, one row group of that query's surviving row groups); the host
-// lists a class's items row group by row group, every query of a row group
-// in turn, so the CTAs running at any moment read the same few row groups
-// and all but the first query of each row group finds its columns in L2.
-// CTA b takes items b, b + grid, ...; its 16 warps split the item's chunks,
-// and the CTA's shared-memory table belongs to the item's query (flushed
-// when the next item moves to another query).  One kernel per fold class
+// (query, that query's surviving row groups within a window of about
+// BATCH_WINDOW_ROWS rows) as a chunk range; the host lists a class's items
+// window by window, every query of a window in turn, so the CTAs running at
+// any moment read the same window and all but the first query of it find
+// its columns in L2.  CTA b takes items b, b + grid, ...; its 16 warps split
+// the item's chunks, and the CTA's shared-memory table belongs to the item's
+// query (flushed when the next item moves to another query: once per item,
+// a few hundred times per query).  One kernel per fold class
 // (rather than one kernel switching between every compiled fold) keeps each
 // kernel's code as small as a single-query scan's.
 template <class P, int MINB>
 __global__ void __launch_bounds__(SCAN_THREADS, MINB)
-    batch_scan_kernel(const DevQuery *__restrict__ qs, const uint2 *__restrict__ items, uint32_t n_items,
+    batch_scan_kernel(const DevQuery *__restrict__ qs, const uint4 *__restrict__ items, uint32_t n_items,
                       const volatile int *cancel, unsigned int *batch_status) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -34,7 +35,7 @@ __global__ void __launch_bounds__(SCAN_THREADS, MINB)
             stop = __syncthreads_or(c) != 0;
             if (stop && threadIdx.x == 0) atomicOr(batch_status, ST_CANCELLED);
         }
-        const uint2 it = stop ? make_uint2(0xFFFFFFFFu, 0u) : items[item];
+        const uint4 it = stop ? make_uint4(0xFFFFFFFFu, 0u, 0u, 0u) : items[item];
         const int qn = stop ? -1 : (int)it.x;
         if (qn != cur) {
             if (cur >= 0) {
@@ -53,7 +54,7 @@ __global__ void __launch_bounds__(SCAN_THREADS, MINB)
         }
         if (qn < 0) break;  // a CTA that got no item at all (cur == qn == -1)
         const DevQuery &q = qs[qn];
-        const uint32_t end = min(it.y + q.chunks_per_rg, q.n_chunks);
+        const uint32_t end = min(it.z, q.n_chunks);
         for (uint32_t c = it.y + warp; c < end; c += SCAN_WARPS) scan_chunk<P>(q, sm, c, selected);
     }
 }
@@ -90,7 +91,7 @@ int batch_fold_class(const DevQuery &q) {
 
 int batch_scan_grid(int cls, size_t smem, int sms) { return sms * blocks_per_sm(batch_kernel(cls), smem); }
 
-cudaError_t launch_batch_scan(int cls, const DevQuery *qs, const uint2 *items, uint32_t n_items, size_t smem,
+cudaError_t launch_batch_scan(int cls, const DevQuery *qs, const uint4 *items, uint32_t n_items, size_t smem,
                               int grid, const volatile int *cancel, unsigned int *status, cudaStream_t s) {
     if (n_items == 0) return cudaSuccess;
     if ((uint32_t)grid > n_items) grid = (int)n_items;

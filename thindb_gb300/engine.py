@@ -80,6 +80,20 @@ def set_device_wait_limit(sm_cycles: int) -> None:
     _check(lib().tgpu_debug_set_wait_limit(sm_cycles))
 
 
+def register_aggregate(name: str) -> None:
+    """Record a host user-defined aggregate's name (thinDB's registerAggregate):
+    requests naming it decline to the caller's executor."""
+    _check(lib().tgpu_aggregate_register(name.encode()))
+
+
+def unregister_aggregate(name: str) -> None:
+    _check(lib().tgpu_aggregate_unregister(name.encode()))
+
+
+def aggregate_registered(name: str) -> bool:
+    return bool(lib().tgpu_aggregate_registered(name.encode()))
+
+
 def clear_tuning() -> None:
     _check(lib().tgpu_tuning_set(None, 0))
 
@@ -315,9 +329,10 @@ class Table:
 
 @dataclass
 class AggSpec:
-    func: str            # count | sum | avg | min | max | count_distinct
+    func: str            # count | sum | avg | min | max | count_distinct | udf
     col: Optional[str] = None
     as_: str = ""
+    udf_name: Optional[str] = None   # func "udf": the registered aggregate's name
 
 
 @dataclass
@@ -370,6 +385,10 @@ def build_request(table: Table, req: Request) -> tuple[abi.Request, list]:
         nm = (a.as_ or f"{a.func}_{a.col or 'star'}").encode()
         keep.append(nm)
         aggs[i].as_ = nm
+        if a.udf_name is not None:
+            un = a.udf_name.encode()
+            keep.append(un)
+            aggs[i].udf_name = un
     where = (abi.Predicate * max(1, len(req.where)))()
     for i, p in enumerate(req.where):
         ci = table.col_index(p.col)
