@@ -62,6 +62,8 @@ FLAG_NO_COUNT_SKETCH = 0x20000
 FLAG_RADIX = 0x40000
 FLAG_NO_RADIX = 0x80000
 FLAG_INLINE_FOLD = 0x100000
+FLAG_SPLIT_SCAN = 0x200000
+FLAG_NO_SPLIT = 0x400000
 STAT_TUNED = 0x1
 STAT_GATHER = 0x2
 STAT_STAGED = 0x4
@@ -71,6 +73,7 @@ STAT_PIPE = 0x20
 STAT_COUNT_SKETCH = 0x40
 STAT_SKETCH_RERUN = 0x80
 STAT_RADIX = 0x100
+STAT_SPLIT = 0x200
 
 
 class ColumnDesc(C.Structure):

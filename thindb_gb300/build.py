@@ -21,7 +21,7 @@ BUILD = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-ENGINE_SOURCES = ["api.cpp", "scan.cu", "scan_inline.cu", "scan_batch.cu", "scan_staged.cu", "scan_pipe.cu", "sketch.cu", "radix.cu", "segment.cu", "distinct.cu", "finalize.cu", "table.cu", "noalloc.cu"]
+ENGINE_SOURCES = ["api.cpp", "scan.cu", "scan_inline.cu", "scan_batch.cu", "scan_staged.cu", "scan_pipe.cu", "scan_split.cu", "sketch.cu", "radix.cu", "segment.cu", "distinct.cu", "finalize.cu", "table.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -431,6 +431,8 @@ struct tgpu_query {
     bool tuned = false;           // settings taken from the tuning table
     bool staged = false;          // the staged (bulk-copy ring) scan runs this query
     bool piped = false;           // the pipelined (producer/consumer) scan runs this query
+    bool split = false;           // the split scan (select pass, fold pass) runs this query
+    Buffer split_buf;             // its row list and count
     bool radix = false;           // the radix-partitioned route runs this query
     RadixPlan rp{};
     uint64_t radix_cap_req = 0;   // records per partition after an overflow (0 = from the estimate)
@@ -509,6 +511,8 @@ struct tgpu_query {
         dpart_cursor_buf = dpart_pairs_buf = Buffer();
         g_scratch_pool.give(radix_buf);
         radix_buf = Buffer();
+        g_scratch_pool.give(split_buf);
+        split_buf = Buffer();
         for (auto &b : dset_bufs) g_set_pool.give(b);
         dset_bufs.clear();
     }
@@ -1042,6 +1046,11 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
             else if (!dense_enough) dq.gather = 1;
         }
     }
+    // the split scan, on request: a survivor gather whose row numbers fit 32
+    // bits (not with the staged, pipelined or inlined-fold scans)
+    q->split = (q->flags & TGPU_FLAG_SPLIT_SCAN) && !(q->flags & TGPU_FLAG_NO_SPLIT) &&
+               !(q->flags & (TGPU_FLAG_STAGED_SCAN | TGPU_FLAG_PIPE_SCAN | TGPU_FLAG_INLINE_FOLD)) && !q->batched &&
+               dq.gather == 1 && q->t->n_rows < (1ULL << 32);
 
     // chunking: about eight chunks per warp of a two-CTA-per-SM grid
     {
@@ -1191,7 +1200,9 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     const size_t o_sketch = q->sketch ? add(((size_t)1 << SK_BITS) * 4 + ((size_t)1 << SK_BITS) / 8 + 64) : 0;
     (void)row_bytes;
 
-    const size_t total = table_bytes + occ_bytes + dset_bytes + dpart_bytes + radix_bytes + scratch;
+    // the split scan's row list: every row of the kept row groups, at most
+    const size_t split_bytes = q->split ? 256 + 4 * (size_t)q->rg_list.size() * q->t->rg_rows : 0;
+    const size_t total = table_bytes + occ_bytes + dset_bytes + dpart_bytes + radix_bytes + split_bytes + scratch;
     if (q->budget && total > q->budget)
         return fail(TGPU_ERR_MEMORY_BUDGET, "query needs " + std::to_string(total) + " device bytes, budget " +
                                                 std::to_string(q->budget));
@@ -1218,6 +1229,7 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
         dq.dset[0] = nullptr;
         dq.dset_cap[0] = 0;
     }
+    if (q->split && (st = g_scratch_pool.take(split_bytes, q->stream, &q->split_buf)) != TGPU_OK) return st;
     if (q->radix) {
         if ((st = g_scratch_pool.take(radix_bytes, q->stream, &q->radix_buf)) != TGPU_OK) return st;
         q->rp.cursor = (uint32_t *)q->radix_buf.p;
@@ -1417,6 +1429,13 @@ tgpu_status enqueue(tgpu_query *q) {
     } else if (q->piped) {
         CU(launch_pipe_scan(dq, q->pp, q->pipe_grid, s));
         q->launches++;
+    } else if (q->split && dq.n_chunks > 0) {
+        DeviceCtx *dev;
+        tgpu_status dst = device_ctx(&dev);
+        if (dst != TGPU_OK) return dst;
+        unsigned long long *n_sel = (unsigned long long *)q->split_buf.p;
+        CU(launch_split_scan(dq, (uint32_t *)((char *)q->split_buf.p + 256), n_sel, dev->sms, s));
+        q->launches += 2;
     } else if (dq.n_chunks > 0) {
         CU(launch_scan(dq, q->grid, s));
         q->launches++;
@@ -1582,9 +1601,10 @@ tgpu_status finish(tgpu_query *q) {
     s.route = (uint32_t)q->route;
     s.retries = q->retries;
     s.kernel_launches = q->launches;
-    s.flags = (q->tuned ? TGPU_STAT_TUNED : 0) | (q->dq.gather == 1 && !q->staged && !q->piped ? TGPU_STAT_GATHER : 0) |
+    s.flags = (q->tuned ? TGPU_STAT_TUNED : 0) |
+              (q->dq.gather == 1 && !q->staged && !q->piped && !q->split ? TGPU_STAT_GATHER : 0) |
               (q->dq.gather == 2 && !q->staged && !q->piped ? TGPU_STAT_QUEUE : 0) |
-              (q->staged ? TGPU_STAT_STAGED : 0) | (q->piped ? TGPU_STAT_PIPE : 0) |
+              (q->staged ? TGPU_STAT_STAGED : 0) | (q->piped ? TGPU_STAT_PIPE : 0) | (q->split ? TGPU_STAT_SPLIT : 0) |
               (q->sketch && !q->sketch_off && (q->h_counts[6] & 0xFFFFFFFFu) ? TGPU_STAT_COUNT_SKETCH : 0) |
               (q->sketch_reruns ? TGPU_STAT_SKETCH_RERUN : 0) | (q->radix ? TGPU_STAT_RADIX : 0) |
               (q->dq.dpart_bits ? TGPU_STAT_DISTINCT_PARTITION : 0);

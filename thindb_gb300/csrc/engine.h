@@ -312,6 +312,9 @@ struct PipePlan {
 // columns, one range WHERE on an integer column or none).
 bool pipe_plan(DevQuery &q, uint64_t tile_count, PipePlan *pp);
 cudaError_t launch_pipe_scan(const DevQuery &q, const PipePlan &pp, int grid, cudaStream_t s);
+// The split scan (scan_split.cu): select pass writing the surviving row
+// numbers to `rows` (count at n_rows), then the fold pass over them.
+cudaError_t launch_split_scan(const DevQuery &q, uint32_t *rows, unsigned long long *n_rows, int sms, cudaStream_t s);
 
 // The two-pass COUNT top-K sketch (sketch.cu): 2^SK_BITS counters, served
 // for OFFSET + LIMIT up to SK_MAX_NEED over at least SK_MIN_ROWS rows.
