@@ -386,6 +386,7 @@ def gpu_arm(args, wl):
                        "selectivity": st.rows_selected / max(1, st.rows_scanned), "groups": st.groups,
                        "route": "shared-memory" if st.route == 1 else "global table",
                        "scan": ("staged" if st.flags & abi.STAT_STAGED else "pipelined" if st.flags & abi.STAT_PIPE
+                                else "split (select pass, fold pass)" if st.flags & abi.STAT_SPLIT
                                 else "queue" if st.flags & abi.STAT_QUEUE
                                 else "survivor gather" if st.flags & abi.STAT_GATHER else "in place"),
                        "count_sketch": bool(st.flags & abi.STAT_COUNT_SKETCH),

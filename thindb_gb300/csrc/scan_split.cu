@@ -15,6 +15,63 @@ namespace tgpu {
 
 namespace {
 
+// The range test over rows [row0, row_end) with 16-byte loads: lane l holds
+// V = 16 / sizeof(T) consecutive rows of each 32 * V-row step, and the
+// survivors' chunk offsets go to `list` in row order (V ballots place them).
+// row0 and the column start on 16-byte boundaries; a vector that would run
+// past the table's last row is read element by element.
+template <typename T>
+__device__ __forceinline__ uint32_t filter_vec(const DevQuery &q, uint64_t row0, uint64_t row_end, uint16_t *list) {
+    constexpr int V = 16 / (int)sizeof(T), U = 4;  // U steps' loads in flight
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const T *col = (const T *)q.fp_data;
+    const int64_t lo = q.fp_lo, hi = q.fp_hi;
+    const bool neg = q.fp_negate != 0;
+    uint32_t n = 0;
+    for (uint64_t b = row0; b < row_end; b += (uint64_t)32 * V * U) {
+        int4 raw[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint64_t r = b + (uint64_t)u * 32 * V + (uint64_t)lane * V;
+            raw[u] = make_int4(0, 0, 0, 0);
+            if (r + V <= q.n_rows) {
+                if (r < row_end) raw[u] = __ldcs((const int4 *)(col + r));
+            } else {
+                T t[V];
+#pragma unroll
+                for (int j = 0; j < V; ++j) t[j] = r + j < row_end ? col[r + j] : T(0);
+                memcpy(&raw[u], t, 16);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint64_t r = b + (uint64_t)u * 32 * V + (uint64_t)lane * V;
+            T x[V];
+            memcpy(x, &raw[u], 16);
+            uint32_t own = 0;  // this lane's passing rows, bit j = row r + j
+#pragma unroll
+            for (int j = 0; j < V; ++j) {
+                const int64_t v = (int64_t)x[j];
+                own |= (uint32_t)(r + j < row_end && ((v >= lo && v <= hi) != neg)) << j;
+            }
+            uint32_t before = 0, total = 0;
+#pragma unroll
+            for (int j = 0; j < V; ++j) {
+                const unsigned m = __ballot_sync(FULL, (own >> j) & 1u);
+                before += __popc(m & lt);
+                total += __popc(m);
+            }
+            uint32_t at = n + before;
+#pragma unroll
+            for (int j = 0; j < V; ++j)
+                if ((own >> j) & 1u) list[at++] = (uint16_t)(r + j - row0);
+            n += total;
+        }
+    }
+    return n;
+}
+
 __global__ void __launch_bounds__(SCAN_THREADS) select_rows_kernel(const __grid_constant__ DevQuery q, uint32_t *rows,
                                                                    unsigned long long *n_rows) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -35,7 +92,15 @@ __global__ void __launch_bounds__(SCAN_THREADS) select_rows_kernel(const __grid_
         uint64_t row0, row_end;
         chunk_rows(q, c, row0, row_end);
         if (row0 >= row_end) continue;
-        const uint32_t n = survivors(q, row0, row_end, list);
+        uint32_t n;
+        const bool vec = ((uintptr_t)q.fp_data & 15u) == 0 && ((row0 * (uint64_t)q.fp_bytes) & 15u) == 0;
+        switch (vec ? q.fp_bytes : 0) {
+            case 1: n = filter_vec<signed char>(q, row0, row_end, list); break;
+            case 2: n = filter_vec<short>(q, row0, row_end, list); break;
+            case 4: n = filter_vec<int>(q, row0, row_end, list); break;
+            case 8: n = filter_vec<long long>(q, row0, row_end, list); break;
+            default: n = survivors(q, row0, row_end, list); break;
+        }
         __syncwarp();
         if (n) {
             unsigned long long at = 0;
@@ -97,6 +162,126 @@ __global__ void __launch_bounds__(SCAN_THREADS, MINB)
     }
 }
 
+// ---- the fold pass with its gathers staged by asynchronous copies ----
+// For a compiled fold over one 8-byte key part and 8-byte inputs (the
+// filtered DECIMAL shape): each warp owns a contiguous stretch of the row
+// list and keeps STAGE_DEPTH batches of 32 rows in flight as cp.async copies
+// of the key and input values into its shared-memory slots, so the gathers
+// need no registers while they wait; a batch folds once its copies have
+// landed, and its slot takes the batch STAGE_DEPTH ahead.
+
+constexpr int STAGE_DEPTH = 6;
+
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+template <class P>
+__global__ void __launch_bounds__(SCAN_THREADS, 2)
+    fold_rows_staged_kernel(const __grid_constant__ DevQuery q, const uint32_t *__restrict__ rows,
+                            const unsigned long long *__restrict__ n_rows, uint32_t stage_off) {
+    static_assert(P::KM_ == 1, "one key part");
+    constexpr int NA = P::NA_, W = 1 + NA;  // words a row stages: the key, then each input
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const ScanSmem sm = carve(q, smem_raw);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // this warp's slots: STAGE_DEPTH x W x 32 words
+    unsigned long long *slots =
+        (unsigned long long *)(smem_raw + stage_off) + (size_t)warp * STAGE_DEPTH * W * 32;
+    cache_init(q, sm);
+    __syncthreads();
+    const uint64_t n = *n_rows;
+    const uint64_t warps = (uint64_t)gridDim.x * SCAN_WARPS, gw = (uint64_t)blockIdx.x * SCAN_WARPS + warp;
+    const uint64_t per = (n + warps * 32 - 1) / (warps * 32) * 32;  // whole batches per warp
+    const uint64_t begin = min(n, gw * per), end = min(n, begin + per);
+    const uint64_t nb = (end - begin + 31) / 32;
+    const DevKeyPart &kp = q.parts[0];
+    const unsigned long long *kcol = (const unsigned long long *)q.cols[kp.col].data;
+    const unsigned long long *vcol[NA > 0 ? NA : 1];
+#pragma unroll
+    for (int a = 0; a < NA; ++a) vcol[a] = (const unsigned long long *)q.cols[q.faggs[a].col].data;
+    const uint64_t kmask = kp.payload < 64 ? ((1ULL << kp.payload) - 1) : ~0ULL;
+    auto issue = [&](uint64_t b) {  // batch b's copies into its slot
+        if (b < nb) {
+            const uint64_t s = begin + b * 32 + lane;
+            if (s < end) {
+                const uint32_t r = __ldcs(rows + s);
+                unsigned long long *dst = slots + (size_t)(b % STAGE_DEPTH) * W * 32 + lane;
+                cp_async8(dst, kcol + r);
+#pragma unroll
+                for (int a = 0; a < NA; ++a) cp_async8(dst + (a + 1) * 32, vcol[a] + r);
+            }
+        }
+        cp_async_commit();  // an empty group keeps the group count in step
+    };
+#pragma unroll
+    for (int d = 0; d < STAGE_DEPTH; ++d) issue(d);
+    for (uint64_t b = 0; b < nb; ++b) {
+        if (((b & 255) == 255) && q.cancel) {
+            int stop = 0;
+            if (lane == 0) stop = *q.cancel;
+            if (__shfl_sync(FULL, stop, 0)) {
+                if (lane == 0) atomicOr(q.status, ST_CANCELLED);
+                break;
+            }
+        }
+        cp_async_wait<STAGE_DEPTH - 1>();  // batch b's group has landed
+        __syncwarp();
+        const unsigned long long *src = slots + (size_t)(b % STAGE_DEPTH) * W * 32 + lane;
+        const bool me = begin + b * 32 + lane < end;
+        typename P::Row rv;
+        rv.k0 = me ? (src[0] & kmask) : 0;
+        rv.k1 = 0;
+#pragma unroll
+        for (int a = 0; a < P::NV; ++a) rv.val[a] = (me && a < NA) ? src[(a + 1) * 32] : 0;
+        __syncwarp();
+        issue(b + STAGE_DEPTH);  // the slot is free again
+        const unsigned keep = __ballot_sync(FULL, P::prefetch(q, rv, me));
+        P::reserve(q, rv, (keep >> lane) & 1u);
+        if (keep) P::fold(q, sm, rv, keep);
+    }
+    cp_async_wait<0>();
+    if (q.cache_slots) {
+        __syncthreads();
+        cache_flush(q, sm);
+    }
+}
+
+// The staged fold applies to a compiled fold whose one key part and every
+// input are 8-byte NOT NULL columns.
+bool staged_fold_ok(const DevQuery &q) {
+    if (q.fast_km != 1 || q.n_parts != 1 || q.n_faggs > 3) return false;
+    const DevCol &k = q.cols[q.parts[0].col];
+    if (k.bytes != 8 || k.valid || k.offs) return false;
+    for (int a = 0; a < q.n_faggs; ++a) {
+        if (q.faggs[a].col < 0) return false;
+        const DevCol &c = q.cols[q.faggs[a].col];
+        if (c.bytes != 8 || c.valid || c.offs) return false;
+    }
+    return true;
+}
+
+template <int KM, int A, int B, int C2, int D>
+const void *staged_kernel_of() {
+    if constexpr (KM == 1) return (const void *)fold_rows_staged_kernel<FastFold<KM, A, B, C2, D>>;
+    else return nullptr;
+}
+
+const void *fold_rows_staged_fn(const DevQuery &q) {
+    switch (fast_fold_id(q)) {
+#define TGPU_STAGED(I, KM, A, B, C2, D) \
+    case I: return staged_kernel_of<KM, A, B, C2, D>();
+        TGPU_FAST_FOLDS(TGPU_STAGED)
+#undef TGPU_STAGED
+        default: return nullptr;
+    }
+}
+
 const void *fold_rows_fn(const DevQuery &q) {
     switch (fast_fold_id(q)) {
 #define TGPU_SPLIT(I, KM, A, B, C2, D) \
@@ -141,12 +326,23 @@ cudaError_t launch_split_scan(const DevQuery &q, uint32_t *rows, unsigned long l
     if (e != cudaSuccess) return e;
     select_rows_kernel<<<sgrid, SCAN_THREADS, ss, s>>>(q, rows, n_rows);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const unsigned long long *cn = n_rows;
+    const void *staged = staged_fold_ok(q) ? fold_rows_staged_fn(q) : nullptr;
+    if (staged) {
+        const size_t base = (split_fold_smem(q) + 15) & ~(size_t)15;
+        const uint32_t off = (uint32_t)base;
+        const size_t fs = base + (size_t)SCAN_WARPS * STAGE_DEPTH * (1 + q.n_faggs) * 32 * 8;
+        const int fgrid = sms * per_sm(staged, fs);
+        e = cudaFuncSetAttribute(staged, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fs);
+        if (e != cudaSuccess) return e;
+        void *args[] = {(void *)&q, (void *)&rows, (void *)&cn, (void *)&off};
+        return cudaLaunchKernel(staged, dim3(fgrid), dim3(SCAN_THREADS), args, fs, s);
+    }
     const size_t fs = split_fold_smem(q);
     const void *fn = fold_rows_fn(q);
     const int fgrid = sms * per_sm(fn, fs);
     e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fs);
     if (e != cudaSuccess) return e;
-    const unsigned long long *cn = n_rows;
     void *args[] = {(void *)&q, (void *)&rows, (void *)&cn};
     return cudaLaunchKernel(fn, dim3(fgrid), dim3(SCAN_THREADS), args, fs, s);
 }
