@@ -357,7 +357,8 @@ def gpu_arm(args, wl):
     achieved = alg_bytes / (scan_avg / 1e3) / 1e9
     traffic = load_traffic(args.workload)
     scan_kernel = ("staged_scan_kernel" if st.flags & abi.STAT_STAGED else
-                   "pipe_scan_kernel" if st.flags & abi.STAT_PIPE else "scan_group_kernel")
+                   "pipe_scan_kernel" if st.flags & abi.STAT_PIPE else
+                   "select_rows_kernel + fold_rows_staged_kernel" if st.flags & abi.STAT_SPLIT else "scan_group_kernel")
 
     # the CPU baseline over the same table, whose result doubles as the
     # parity check of the GPU result (outside the timed region)
@@ -386,7 +387,7 @@ def gpu_arm(args, wl):
                        "selectivity": st.rows_selected / max(1, st.rows_scanned), "groups": st.groups,
                        "route": "shared-memory" if st.route == 1 else "global table",
                        "scan": ("staged" if st.flags & abi.STAT_STAGED else "pipelined" if st.flags & abi.STAT_PIPE
-                                else "split (select pass, fold pass)" if st.flags & abi.STAT_SPLIT
+                                else "survivor gather, split (select pass, fold pass)" if st.flags & abi.STAT_SPLIT
                                 else "queue" if st.flags & abi.STAT_QUEUE
                                 else "survivor gather" if st.flags & abi.STAT_GATHER else "in place"),
                        "count_sketch": bool(st.flags & abi.STAT_COUNT_SKETCH),

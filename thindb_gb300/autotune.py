@@ -48,7 +48,8 @@ KNOBS = {
     "flags": [0, abi.FLAG_STAGED_SCAN, abi.FLAG_DENSE_SCAN, abi.FLAG_GATHER_SCAN, abi.FLAG_QUEUE_SCAN,
               abi.FLAG_NO_WARP_COMBINE,
               abi.FLAG_NO_PREFETCH, abi.FLAG_NO_CHUNK_PREFETCH, abi.FLAG_NO_PREFETCH | abi.FLAG_NO_CHUNK_PREFETCH,
-              abi.FLAG_DISTINCT_PREFETCH, abi.FLAG_NO_DISTINCT_PARTITION],
+              abi.FLAG_DISTINCT_PREFETCH, abi.FLAG_NO_DISTINCT_PARTITION,
+              abi.FLAG_NO_SPLIT | abi.FLAG_NO_PREFETCH | abi.FLAG_NO_CHUNK_PREFETCH],
     "chunk_rows": [0, 512, 1024, 2048, 4096],
     "cache_slots": [0, -1, 256, 1024, 4096],
     "table_load_pct": [0, 25, 70],

@@ -1046,9 +1046,9 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
             else if (!dense_enough) dq.gather = 1;
         }
     }
-    // the split scan, on request: a survivor gather whose row numbers fit 32
-    // bits (not with the staged, pipelined or inlined-fold scans)
-    q->split = (q->flags & TGPU_FLAG_SPLIT_SCAN) && !(q->flags & TGPU_FLAG_NO_SPLIT) &&
+    // the split scan runs a survivor gather whose row numbers fit 32 bits
+    // (not with the staged, pipelined or inlined-fold scans, nor in batches)
+    q->split = !(q->flags & TGPU_FLAG_NO_SPLIT) &&
                !(q->flags & (TGPU_FLAG_STAGED_SCAN | TGPU_FLAG_PIPE_SCAN | TGPU_FLAG_INLINE_FOLD)) && !q->batched &&
                dq.gather == 1 && q->t->n_rows < (1ULL << 32);
 
@@ -1602,7 +1602,7 @@ tgpu_status finish(tgpu_query *q) {
     s.retries = q->retries;
     s.kernel_launches = q->launches;
     s.flags = (q->tuned ? TGPU_STAT_TUNED : 0) |
-              (q->dq.gather == 1 && !q->staged && !q->piped && !q->split ? TGPU_STAT_GATHER : 0) |
+              (q->dq.gather == 1 && !q->staged && !q->piped ? TGPU_STAT_GATHER : 0) |
               (q->dq.gather == 2 && !q->staged && !q->piped ? TGPU_STAT_QUEUE : 0) |
               (q->staged ? TGPU_STAT_STAGED : 0) | (q->piped ? TGPU_STAT_PIPE : 0) | (q->split ? TGPU_STAT_SPLIT : 0) |
               (q->sketch && !q->sketch_off && (q->h_counts[6] & 0xFFFFFFFFu) ? TGPU_STAT_COUNT_SKETCH : 0) |

@@ -15,6 +15,8 @@ namespace tgpu {
 
 namespace {
 
+constexpr uint32_t SELECT_SPAN = 2048;  // rows a warp filters before it writes their survivors out
+
 // The range test over rows [row0, row_end) with 16-byte loads: lane l holds
 // V = 16 / sizeof(T) consecutive rows of each 32 * V-row step, and the
 // survivors' chunk offsets go to `list` in row order (V ballots place them).
@@ -76,7 +78,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) select_rows_kernel(const __grid_
                                                                    unsigned long long *n_rows) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint16_t *list = (uint16_t *)smem_raw + (size_t)warp * q.chunk_rows;
+    uint16_t *list = (uint16_t *)smem_raw + (size_t)warp * SELECT_SPAN;
     unsigned long long selected = 0;
     const uint32_t nw = gridDim.x * SCAN_WARPS;
     uint32_t k = 0;
@@ -89,27 +91,30 @@ __global__ void __launch_bounds__(SCAN_THREADS) select_rows_kernel(const __grid_
                 break;
             }
         }
-        uint64_t row0, row_end;
-        chunk_rows(q, c, row0, row_end);
-        if (row0 >= row_end) continue;
-        uint32_t n;
-        const bool vec = ((uintptr_t)q.fp_data & 15u) == 0 && ((row0 * (uint64_t)q.fp_bytes) & 15u) == 0;
-        switch (vec ? q.fp_bytes : 0) {
-            case 1: n = filter_vec<signed char>(q, row0, row_end, list); break;
-            case 2: n = filter_vec<short>(q, row0, row_end, list); break;
-            case 4: n = filter_vec<int>(q, row0, row_end, list); break;
-            case 8: n = filter_vec<long long>(q, row0, row_end, list); break;
-            default: n = survivors(q, row0, row_end, list); break;
+        uint64_t c0, c1;
+        chunk_rows(q, c, c0, c1);
+        // the chunk in spans of at most SELECT_SPAN rows (the list's room)
+        for (uint64_t row0 = c0; row0 < c1; row0 += SELECT_SPAN) {
+            const uint64_t row_end = min(c1, row0 + SELECT_SPAN);
+            uint32_t n;
+            const bool vec = ((uintptr_t)q.fp_data & 15u) == 0 && ((row0 * (uint64_t)q.fp_bytes) & 15u) == 0;
+            switch (vec ? q.fp_bytes : 0) {
+                case 1: n = filter_vec<signed char>(q, row0, row_end, list); break;
+                case 2: n = filter_vec<short>(q, row0, row_end, list); break;
+                case 4: n = filter_vec<int>(q, row0, row_end, list); break;
+                case 8: n = filter_vec<long long>(q, row0, row_end, list); break;
+                default: n = survivors(q, row0, row_end, list); break;
+            }
+            __syncwarp();
+            if (n) {
+                unsigned long long at = 0;
+                if (lane == 0) at = atomicAdd(n_rows, (unsigned long long)n);
+                at = __shfl_sync(FULL, at, 0);
+                for (uint32_t i = lane; i < n; i += 32) rows[at + i] = (uint32_t)(row0 + list[i]);
+                selected += lane == 0 ? n : 0;
+            }
+            __syncwarp();
         }
-        __syncwarp();
-        if (n) {
-            unsigned long long at = 0;
-            if (lane == 0) at = atomicAdd(n_rows, (unsigned long long)n);
-            at = __shfl_sync(FULL, at, 0);
-            for (uint32_t i = lane; i < n; i += 32) rows[at + i] = (uint32_t)(row0 + list[i]);
-            selected += lane == 0 ? n : 0;
-        }
-        __syncwarp();
     }
     if (lane == 0 && selected) atomicAdd(q.selected_rows, selected);
 }
@@ -170,7 +175,7 @@ __global__ void __launch_bounds__(SCAN_THREADS, MINB)
 // need no registers while they wait; a batch folds once its copies have
 // landed, and its slot takes the batch STAGE_DEPTH ahead.
 
-constexpr int STAGE_DEPTH = 6;
+constexpr int STAGE_DEPTH = 2;
 
 __device__ __forceinline__ void cp_async8(void *dst, const void *src) {
     const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
@@ -231,7 +236,6 @@ __global__ void __launch_bounds__(SCAN_THREADS, 2)
             }
         }
         cp_async_wait<STAGE_DEPTH - 1>();  // batch b's group has landed
-        __syncwarp();
         const unsigned long long *src = slots + (size_t)(b % STAGE_DEPTH) * W * 32 + lane;
         const bool me = begin + b * 32 + lane < end;
         typename P::Row rv;
@@ -306,7 +310,7 @@ int per_sm(const void *fn, size_t smem) {
 
 }  // namespace
 
-size_t split_select_smem(const DevQuery &q) { return (size_t)SCAN_WARPS * q.chunk_rows * 2; }
+size_t split_select_smem(const DevQuery &) { return (size_t)SCAN_WARPS * SELECT_SPAN * 2; }
 
 size_t split_fold_smem(const DevQuery &q) {
     DevQuery f = q;
