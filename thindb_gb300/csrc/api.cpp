@@ -1048,9 +1048,11 @@ tgpu_status size_workspace(tgpu_query *q, uint64_t cap) {
     }
     // the split scan runs a survivor gather whose row numbers fit 32 bits
     // (not with the staged, pipelined or inlined-fold scans, nor in batches)
+    // (and the count sketch's filter pass: its select pass keeps the rows of
+    // kept counters)
     q->split = !(q->flags & TGPU_FLAG_NO_SPLIT) &&
                !(q->flags & (TGPU_FLAG_STAGED_SCAN | TGPU_FLAG_PIPE_SCAN | TGPU_FLAG_INLINE_FOLD)) && !q->batched &&
-               dq.gather == 1 && q->t->n_rows < (1ULL << 32);
+               (dq.gather == 1 || q->sketch) && q->t->n_rows < (1ULL << 32);
 
     // chunking: about eight chunks per warp of a two-CTA-per-SM grid
     {
@@ -1429,7 +1431,7 @@ tgpu_status enqueue(tgpu_query *q) {
     } else if (q->piped) {
         CU(launch_pipe_scan(dq, q->pp, q->pipe_grid, s));
         q->launches++;
-    } else if (q->split && dq.n_chunks > 0) {
+    } else if (q->split && (dq.gather == 1 || (q->sketch && !q->sketch_off)) && dq.n_chunks > 0) {
         DeviceCtx *dev;
         tgpu_status dst = device_ctx(&dev);
         if (dst != TGPU_OK) return dst;
@@ -1604,7 +1606,8 @@ tgpu_status finish(tgpu_query *q) {
     s.flags = (q->tuned ? TGPU_STAT_TUNED : 0) |
               (q->dq.gather == 1 && !q->staged && !q->piped ? TGPU_STAT_GATHER : 0) |
               (q->dq.gather == 2 && !q->staged && !q->piped ? TGPU_STAT_QUEUE : 0) |
-              (q->staged ? TGPU_STAT_STAGED : 0) | (q->piped ? TGPU_STAT_PIPE : 0) | (q->split ? TGPU_STAT_SPLIT : 0) |
+              (q->staged ? TGPU_STAT_STAGED : 0) | (q->piped ? TGPU_STAT_PIPE : 0) |
+              (q->split && (q->dq.gather == 1 || (q->sketch && !q->sketch_off)) ? TGPU_STAT_SPLIT : 0) |
               (q->sketch && !q->sketch_off && (q->h_counts[6] & 0xFFFFFFFFu) ? TGPU_STAT_COUNT_SKETCH : 0) |
               (q->sketch_reruns ? TGPU_STAT_SKETCH_RERUN : 0) | (q->radix ? TGPU_STAT_RADIX : 0) |
               (q->dq.dpart_bits ? TGPU_STAT_DISTINCT_PARTITION : 0);

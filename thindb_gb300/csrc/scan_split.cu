@@ -1,6 +1,9 @@
 // scan_split.cu — the split scan: the WHERE as its own streaming pass that
 // writes the surviving row numbers, then a fold pass over that list.
 //
+// With the count sketch on, the select pass also drops the rows whose key's
+// counter is not kept, so the fold pass sees only candidate rows.
+//
 // The fused gather-mode scan (scan_chunk) runs filter -> compaction ->
 // gather -> fold per warp and chunk, so every warp waits on its own filter
 // before its gathers can start.  Split, the select pass only streams the
@@ -98,20 +101,46 @@ __global__ void __launch_bounds__(SCAN_THREADS) select_rows_kernel(const __grid_
             const uint64_t row_end = min(c1, row0 + SELECT_SPAN);
             uint32_t n;
             const bool vec = ((uintptr_t)q.fp_data & 15u) == 0 && ((row0 * (uint64_t)q.fp_bytes) & 15u) == 0;
-            switch (vec ? q.fp_bytes : 0) {
-                case 1: n = filter_vec<signed char>(q, row0, row_end, list); break;
-                case 2: n = filter_vec<short>(q, row0, row_end, list); break;
-                case 4: n = filter_vec<int>(q, row0, row_end, list); break;
-                case 8: n = filter_vec<long long>(q, row0, row_end, list); break;
-                default: n = survivors(q, row0, row_end, list); break;
+            if (q.n_preds == 0) {  // no WHERE: every row (the count sketch below picks)
+                n = (uint32_t)(row_end - row0);
+                for (uint32_t i = lane; i < n; i += 32) list[i] = (uint16_t)i;
+            } else {
+                switch (vec ? q.fp_bytes : 0) {
+                    case 1: n = filter_vec<signed char>(q, row0, row_end, list); break;
+                    case 2: n = filter_vec<short>(q, row0, row_end, list); break;
+                    case 4: n = filter_vec<int>(q, row0, row_end, list); break;
+                    case 8: n = filter_vec<long long>(q, row0, row_end, list); break;
+                    default: n = survivors(q, row0, row_end, list); break;
+                }
             }
             __syncwarp();
+            selected += lane == 0 ? n : 0;  // the WHERE's rows, whatever the sketch keeps
+            if (n && q.sk_keep && __ldg(q.sk_on)) {
+                // the count sketch's filter: keep the rows whose key's counter
+                // is kept (the tally's pack_key + hash_key), compacted in place
+                uint32_t m = 0;
+                for (uint32_t g = 0; g < n; g += 32) {
+                    const uint32_t i = g + lane;
+                    const uint16_t off = i < n ? list[i] : 0;
+                    bool kept = false;
+                    if (i < n) {
+                        uint64_t k0, k1;
+                        pack_key(q, row0 + off, k0, k1);
+                        kept = sketch_kept(q, hash_key(k0, k1));
+                    }
+                    const unsigned b = __ballot_sync(FULL, kept);
+                    __syncwarp();
+                    if (kept) list[m + __popc(b & ((1u << lane) - 1u))] = off;
+                    m += __popc(b);
+                }
+                __syncwarp();
+                n = m;
+            }
             if (n) {
                 unsigned long long at = 0;
                 if (lane == 0) at = atomicAdd(n_rows, (unsigned long long)n);
                 at = __shfl_sync(FULL, at, 0);
                 for (uint32_t i = lane; i < n; i += 32) rows[at + i] = (uint32_t)(row0 + list[i]);
-                selected += lane == 0 ? n : 0;
             }
             __syncwarp();
         }
