@@ -193,16 +193,19 @@ __global__ void __launch_bounds__(512) column_stats_kernel(const T *__restrict__
     }
 }
 
-// regs = max(regs (accumulate) or 0, every part row); four registers a thread
-__global__ void hll_merge_kernel(const uint8_t *__restrict__ part, uint32_t rows, uint32_t *regs, int accumulate) {
+// regs = max(regs, every part row): grid (HLL_M / 4 / 256, slices); a
+// thread takes four registers over a slice of the rows and raises them with
+// atomicMax (regs start zeroed, or hold earlier rows' maxima)
+__global__ void hll_merge_kernel(const uint8_t *__restrict__ part, uint32_t rows, uint32_t *regs) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;  // registers 4i .. 4i + 3
     if (i >= (uint32_t)HLL_M / 4) return;
+    const uint32_t per = (rows + gridDim.y - 1) / gridDim.y, r0 = blockIdx.y * per, r1 = min(rows, r0 + per);
     const uint32_t *p = (const uint32_t *)part + i;
     uint32_t m = 0;
-    for (uint32_t r = 0; r < rows; ++r) m = __vmaxu4(m, __ldg(p + (size_t)r * (HLL_M / 4)));
+    for (uint32_t r = r0; r < r1; ++r) m = __vmaxu4(m, __ldg(p + (size_t)r * (HLL_M / 4)));
     for (int k = 0; k < 4; ++k) {
         const uint32_t v = (m >> (8 * k)) & 0xFFu;
-        regs[4 * i + k] = accumulate ? max(regs[4 * i + k], v) : v;
+        if (v) atomicMax(regs + 4 * i + k, v);
     }
 }
 
@@ -226,7 +229,11 @@ cudaError_t launch_stats_t(const void *data, const uint32_t *valid, uint64_t n_r
                                                     fmax, nulls, regs ? part : nullptr);
     e = cudaGetLastError();
     if (e != cudaSuccess || !regs) return e;
-    hll_merge_kernel<<<HLL_M / 4 / 256, 256, 0, s>>>(part, grid, regs, accumulate);
+    if (!accumulate) {
+        e = cudaMemsetAsync(regs, 0, HLL_M * sizeof(uint32_t), s);
+        if (e != cudaSuccess) return e;
+    }
+    hll_merge_kernel<<<dim3(HLL_M / 4 / 256, std::min<uint32_t>(grid, 16)), 256, 0, s>>>(part, grid, regs);
     return cudaGetLastError();
 }
 
