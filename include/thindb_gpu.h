@@ -289,10 +289,11 @@ typedef struct tgpu_request {
  * gather or in place): batch i + 1 loads while batch i folds, instead of
  * several batches folded through an out-of-line call. */
 #define TGPU_FLAG_INLINE_FOLD 0x100000
-/* Split scan for a filtered survivor gather: the WHERE as a streaming pass
- * that writes the surviving row numbers (4 bytes each), then a fold pass
- * over that list in full batches.  TGPU_FLAG_SPLIT_SCAN asks for it,
- * TGPU_FLAG_NO_SPLIT keeps the fused scan. */
+/* Split scan for a filtered survivor gather (the default for one): the
+ * WHERE as a streaming pass that writes the surviving row numbers (4 bytes
+ * each), then a fold pass over that list in full batches.
+ * TGPU_FLAG_NO_SPLIT keeps the fused scan; TGPU_FLAG_SPLIT_SCAN is
+ * accepted for requests that name it. */
 #define TGPU_FLAG_SPLIT_SCAN 0x200000
 #define TGPU_FLAG_NO_SPLIT 0x400000
 
@@ -349,7 +350,7 @@ typedef struct tgpu_query_stats {
 #define TGPU_STAT_COUNT_SKETCH 0x40  /* the count sketch's filter pass gave the answer */
 #define TGPU_STAT_SKETCH_RERUN 0x80  /* its filter pass could not prove the answer: every row regrouped */
 #define TGPU_STAT_RADIX 0x100   /* the radix-partitioned route ran */
-#define TGPU_STAT_SPLIT 0x200   /* the split scan (select pass, then fold pass) ran */
+#define TGPU_STAT_SPLIT 0x200   /* the survivor gather ran as the split scan (select pass, fold pass) */
 
 /* -------------------------------------------------------------- the API -- */
 
