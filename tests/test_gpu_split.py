@@ -74,3 +74,35 @@ def test_split_with_pruned_row_groups():
     _, st = run_both(cols, req)
     _assert_split(st)
     assert st.row_groups_pruned > 0
+
+
+@pytest.mark.parametrize("col,op,lo,hi", [
+    ("i", "between", -2**40, 2**40),          # clamped to the INT range: every row
+    ("i", "between", -5, 5),
+    ("i", "not_between", -1000, 1000),
+    ("i", "between", 10, 5),                  # empty
+    ("i", "not_between", 10, 5),              # every row
+    ("i", "between", 2**31, 2**33),           # above every INT: no row
+    ("i", ">", 2**31 - 10, 0),
+    ("s", "between", -300, 300),
+    ("t", "not_between", -3, 3),
+    ("t", "=", -128, 0),
+    ("b", "between", -2**63, -2**62),
+    ("b", "<", 0, 0),
+])
+def test_split_range_tests_at_the_type_edges(col, op, lo, hi):
+    n = 700_001
+    rng = np.random.default_rng(12)
+    i32 = rng.integers(-2**31, 2**31, n, dtype=np.int64).astype(np.int32)
+    i32[:1000] = np.array([-2**31, 2**31 - 1, 0, -1, 1] * 200, dtype=np.int32)
+    cols = [Column("k", abi.INT, rng.integers(0, 3_000, n).astype(np.int32)),
+            Column("i", abi.INT, i32),
+            Column("s", abi.SMALLINT, rng.integers(-2**15, 2**15, n).astype(np.int16)),
+            Column("t", abi.TINYINT, rng.integers(-128, 128, n).astype(np.int8)),
+            Column("b", abi.BIGINT, rng.integers(-2**63, 2**63 - 1, n, dtype=np.int64)),
+            Column("v", abi.BIGINT, rng.integers(-10**6, 10**6, n).astype(np.int64))]
+    req = Request(["k"], [AggSpec("count", None, "c"), AggSpec("sum", "v", "s")], where=[Pred(col, op, lo, hi)],
+                  flags=SPLIT)
+    _, st = run_both(cols, req)
+    if st.rows_selected:
+        _assert_split(st)

@@ -12,6 +12,9 @@
 // full, and a warp's LOOKAHEAD batches of gathers are in flight at once with
 // their row numbers known up front.  The list costs 4 bytes per survivor
 // written and read again.
+#include <climits>
+#include <type_traits>
+
 #include "scan_impl.cuh"
 
 namespace tgpu {
@@ -31,8 +34,20 @@ __device__ __forceinline__ uint32_t filter_vec(const DevQuery &q, uint64_t row0,
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const T *col = (const T *)q.fp_data;
-    const int64_t lo = q.fp_lo, hi = q.fp_hi;
     const bool neg = q.fp_negate != 0;
+    // the range as one unsigned compare, x - lo <= hi - lo, in the width the
+    // values need (32 bits for elements of up to 4 bytes; an empty range
+    // becomes lo = 1, hi = 0)
+    using C = typename std::conditional<sizeof(T) == 8, long long, int>::type;
+    using UC = typename std::conditional<sizeof(T) == 8, unsigned long long, unsigned>::type;
+    int64_t lo64 = q.fp_lo, hi64 = q.fp_hi;
+    if (sizeof(T) < 8) {
+        lo64 = max(lo64, (int64_t)INT_MIN);
+        hi64 = min(hi64, (int64_t)INT_MAX);
+    }
+    const bool empty = lo64 > hi64;
+    const UC lo = (UC)(C)lo64;  // (unsigned arithmetic: x - lo wraps, as the compare wants)
+    const UC span = empty ? (UC)0 : (UC)((uint64_t)hi64 - (uint64_t)lo64);
     uint32_t n = 0;
     for (uint64_t b = row0; b < row_end; b += (uint64_t)32 * V * U) {
         int4 raw[U];
@@ -57,8 +72,8 @@ __device__ __forceinline__ uint32_t filter_vec(const DevQuery &q, uint64_t row0,
             uint32_t own = 0;  // this lane's passing rows, bit j = row r + j
 #pragma unroll
             for (int j = 0; j < V; ++j) {
-                const int64_t v = (int64_t)x[j];
-                own |= (uint32_t)(r + j < row_end && ((v >= lo && v <= hi) != neg)) << j;
+                const bool in = !empty && (UC)((UC)(C)x[j] - lo) <= span;
+                own |= (uint32_t)(r + j < row_end && in != neg) << j;
             }
             uint32_t before = 0, total = 0;
 #pragma unroll
