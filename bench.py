@@ -385,6 +385,7 @@ def gpu_arm(args, wl):
             "vs_baseline": None, "dtype": wl["dtype"], "data": "synthetic (seeded generator)",
             "config": {"workload": wl["name"], "rows": n, "l2": "inputs larger than L2 (no flush)",
                        "selectivity": st.rows_selected / max(1, st.rows_scanned), "groups": st.groups,
+                       "table_capacity": st.table_capacity,
                        "route": "shared-memory" if st.route == 1 else "global table",
                        "scan": ("staged" if st.flags & abi.STAT_STAGED else "pipelined" if st.flags & abi.STAT_PIPE
                                 else "survivor gather, split (select pass, fold pass)" if st.flags & abi.STAT_SPLIT
