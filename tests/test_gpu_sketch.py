@@ -103,3 +103,21 @@ def test_sketch_off_and_batched_shapes_unchanged():
     cols = zipf_cols(1_500_000, 300_000)
     _, st = run_both(cols, topcount(10, flags=abi.FLAG_NO_COUNT_SKETCH))
     assert not st.flags & abi.STAT_COUNT_SKETCH
+
+
+@pytest.mark.parametrize("rg", [65_536, 1_001])
+def test_sketch_filter_with_odd_row_groups_and_tail(rg):
+    # 1,001-row groups put every other select span on an odd row (the
+    # vector keep test needs 16-byte alignment) and the table ends mid-vector
+    cols = zipf_cols(2_000_001, 300_000, seed=8)
+    t = Table(cols, row_group_rows=rg)
+    req = topcount(10)
+    q = try_build_group_topn(t, req)
+    got = q.collect()
+    st = q.stats()
+    q.close()
+    t.close()
+    want = oracle.run(oracle.HostTable(cols, rg), req, threads=4)
+    compare_results(got, want, 1, ordered=True)
+    assert st.rows_selected == want["__selected__"]
+    assert st.flags & abi.STAT_COUNT_SKETCH and st.flags & abi.STAT_SPLIT

@@ -92,6 +92,55 @@ __device__ __forceinline__ uint32_t filter_vec(const DevQuery &q, uint64_t row0,
     return n;
 }
 
+// The count sketch's filter over rows [row0, row_end) of a table with no
+// WHERE and one NOT NULL 8-byte key part: two keys a lane per 16-byte load,
+// the kept rows' chunk offsets to `list` in row order.  (pack_key of such a
+// key is key_or | the masked value, so the hash is the tally's.)
+__device__ __forceinline__ uint32_t keep_vec(const DevQuery &q, uint64_t row0, uint64_t row_end, uint16_t *list) {
+    constexpr int V = 2, U = 4;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const DevKeyPart &kp = q.parts[0];
+    const unsigned long long *col = (const unsigned long long *)q.cols[kp.col].data;
+    const uint64_t mask = kp.payload < 64 ? ((1ULL << kp.payload) - 1) : ~0ULL;
+    uint32_t n = 0;
+    for (uint64_t b = row0; b < row_end; b += (uint64_t)32 * V * U) {
+        ulonglong2 raw[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint64_t r = b + (uint64_t)u * 32 * V + (uint64_t)lane * V;
+            raw[u] = make_ulonglong2(0, 0);
+            if (r + V <= q.n_rows) {
+                if (r < row_end) raw[u] = __ldcs((const ulonglong2 *)(col + r));
+            } else if (r < row_end) {
+                raw[u].x = col[r];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint64_t r = b + (uint64_t)u * 32 * V + (uint64_t)lane * V;
+            const uint64_t k[V] = {raw[u].x, raw[u].y};
+            uint32_t own = 0;
+#pragma unroll
+            for (int j = 0; j < V; ++j)
+                own |= (uint32_t)(r + j < row_end && sketch_kept(q, hash_key(q.key_or | (k[j] & mask), 0))) << j;
+            uint32_t before = 0, total = 0;
+#pragma unroll
+            for (int j = 0; j < V; ++j) {
+                const unsigned m = __ballot_sync(FULL, (own >> j) & 1u);
+                before += __popc(m & lt);
+                total += __popc(m);
+            }
+            uint32_t at = n + before;
+#pragma unroll
+            for (int j = 0; j < V; ++j)
+                if ((own >> j) & 1u) list[at++] = (uint16_t)(r + j - row0);
+            n += total;
+        }
+    }
+    return n;
+}
+
 __global__ void __launch_bounds__(SCAN_THREADS) select_rows_kernel(const __grid_constant__ DevQuery q, uint32_t *rows,
                                                                    unsigned long long *n_rows) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -99,6 +148,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) select_rows_kernel(const __grid_
     uint16_t *list = (uint16_t *)smem_raw + (size_t)warp * SELECT_SPAN;
     unsigned long long selected = 0;
     const uint32_t nw = gridDim.x * SCAN_WARPS;
+    // one NOT NULL 8-byte key part at bit 0, not hashed, 16-byte aligned: keep_vec
+    const bool fast_key = q.n_parts == 1 && !q.hashed && q.parts[0].offset == 0 && !q.parts[0].nullable &&
+                          q.cols[q.parts[0].col].bytes == 8 && !q.cols[q.parts[0].col].valid &&
+                          ((uintptr_t)q.cols[q.parts[0].col].data & 15u) == 0;
     uint32_t k = 0;
     for (uint32_t c = blockIdx.x * SCAN_WARPS + warp; c < q.n_chunks; c += nw, ++k) {
         if ((k & 31) == 31 && q.cancel) {
@@ -116,7 +169,12 @@ __global__ void __launch_bounds__(SCAN_THREADS) select_rows_kernel(const __grid_
             const uint64_t row_end = min(c1, row0 + SELECT_SPAN);
             uint32_t n;
             const bool vec = ((uintptr_t)q.fp_data & 15u) == 0 && ((row0 * (uint64_t)q.fp_bytes) & 15u) == 0;
-            if (q.n_preds == 0) {  // no WHERE: every row (the count sketch below picks)
+            const bool sketch = q.sk_keep && __ldg(q.sk_on);
+            bool kept_done = false;  // the sketch's keep test already applied
+            if (q.n_preds == 0 && sketch && fast_key && (row0 & 1) == 0) {
+                n = keep_vec(q, row0, row_end, list);
+                kept_done = true;
+            } else if (q.n_preds == 0) {  // no WHERE: every row (the count sketch below picks)
                 n = (uint32_t)(row_end - row0);
                 for (uint32_t i = lane; i < n; i += 32) list[i] = (uint16_t)i;
             } else {
@@ -129,8 +187,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) select_rows_kernel(const __grid_
                 }
             }
             __syncwarp();
-            selected += lane == 0 ? n : 0;  // the WHERE's rows, whatever the sketch keeps
-            if (n && q.sk_keep && __ldg(q.sk_on)) {
+            // the WHERE's rows, whatever the sketch keeps
+            selected += lane == 0 ? (kept_done ? row_end - row0 : n) : 0;
+            if (n && sketch && !kept_done) {
                 // the count sketch's filter: keep the rows whose key's counter
                 // is kept (the tally's pack_key + hash_key), compacted in place
                 uint32_t m = 0;
