@@ -334,10 +334,11 @@ def gpu_arm(args, wl):
             e2e_times.append(dt)
     e2e_value = n / statistics.median(e2e_times)
     # the ceiling e2e is bounded by: the same bytes copied from the same
-    # pinned buffers by plain cudaMemcpyAsync, one per column
+    # pinned buffers by plain cudaMemcpyAsync, one per column; the fastest of
+    # six passes (the host link's rate varies between passes on a shared host)
     dev_bufs = [torch.empty(t.numel() * t.element_size(), dtype=torch.uint8, device="cuda") for _, _, t, _ in inputs]
     h2d_ms = []
-    for i in range(4):
+    for i in range(7):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
@@ -349,7 +350,8 @@ def gpu_arm(args, wl):
         if i:
             h2d_ms.append(e0.elapsed_time(e1))
     del dev_bufs
-    h2d_gbs = h2d_bytes / (statistics.median(h2d_ms) / 1e3) / 1e9
+    h2d_best = min(h2d_ms)
+    h2d_gbs = h2d_bytes / (h2d_best / 1e3) / 1e9
 
     peak, peak_kind = load_peak()
     scan_avg = statistics.mean(scan_ms)
@@ -402,8 +404,8 @@ def gpu_arm(args, wl):
                          "step_frac": alg_bytes / (ms_per_step / 1e3) / 1e9 / peak},
             "e2e": {"value": e2e_value, "unit": "rows/s", "h2d_bytes_per_step": h2d_bytes,
                     "d2h_bytes_per_step": d2h, "ms_per_step": statistics.median(e2e_times) * 1e3,
-                    "h2d_ceiling_gbs": h2d_gbs, "h2d_ceiling_ms": statistics.median(h2d_ms),
-                    "frac_of_h2d_ceiling": statistics.median(h2d_ms) / (statistics.median(e2e_times) * 1e3)},
+                    "h2d_ceiling_gbs": h2d_gbs, "h2d_ceiling_ms": h2d_best,
+                    "frac_of_h2d_ceiling": h2d_best / (statistics.median(e2e_times) * 1e3)},
             "parity": parity,
             "gpu_launches": launches,
             "clocks": clk,

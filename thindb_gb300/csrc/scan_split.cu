@@ -30,9 +30,11 @@ constexpr uint32_t SELECT_SPAN = 2048;  // rows a warp filters before it writes 
 // past the table's last row is read element by element.
 template <typename T>
 __device__ __forceinline__ uint32_t filter_vec(const DevQuery &q, uint64_t row0, uint64_t row_end, uint16_t *list) {
-    // U steps' loads in flight: 2 measured ahead of 4 and 8 (0.470 against
-    // 0.489 and 0.482 ms for 100M rows), the span's warps already keep
-    // enough bytes in flight and fewer registers leave room for more warps
+    // U steps' loads in flight.  The select kernel's occupancy matters more
+    // than the depth per warp: at two CTAs an SM (64 registers) U = 2 and 4
+    // measured within 1% of one another for 100M rows, at one CTA an SM (U = 4
+    // took 128 registers unbounded) 4% slower, at three (40 registers, with
+    // spills) 4% slower too
     constexpr int V = 16 / (int)sizeof(T), U = 2;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -144,7 +146,7 @@ __device__ __forceinline__ uint32_t keep_vec(const DevQuery &q, uint64_t row0, u
     return n;
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) select_rows_kernel(const __grid_constant__ DevQuery q, uint32_t *rows,
+__global__ void __launch_bounds__(SCAN_THREADS, 2) select_rows_kernel(const __grid_constant__ DevQuery q, uint32_t *rows,
                                                                    unsigned long long *n_rows) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
