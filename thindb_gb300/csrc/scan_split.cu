@@ -146,8 +146,8 @@ __device__ __forceinline__ uint32_t keep_vec(const DevQuery &q, uint64_t row0, u
     return n;
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS, 2) select_rows_kernel(const __grid_constant__ DevQuery q, uint32_t *rows,
-                                                                   unsigned long long *n_rows) {
+__global__ void __launch_bounds__(SCAN_THREADS, 2) select_rows_kernel(const __grid_constant__ DevQuery q,
+                                                                      uint32_t *rows, unsigned long long *n_rows) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint16_t *list = (uint16_t *)smem_raw + (size_t)warp * SELECT_SPAN;
