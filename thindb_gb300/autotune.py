@@ -17,7 +17,10 @@ knobs are
     flags           scan mode: the staged scan (column tiles through a
                     shared-memory ring of bulk copies), dense loads or survivor
                     gathers; the in-warp pre-combine on or off; which L2
-                    prefetches run (table slots, next chunks, distinct entries)
+                    prefetches run (table slots, next chunks, distinct entries);
+                    the split scan off; the radix-partitioned route (its
+                    partition bits follow the group estimate, so groups_shift
+                    moves them too)
 
 For each shape class (tgpu_shape: key width, fold signature, aggregate count,
 distinct, selectivity class, group-count class, batched or not) a coordinate
@@ -49,7 +52,7 @@ KNOBS = {
               abi.FLAG_NO_WARP_COMBINE,
               abi.FLAG_NO_PREFETCH, abi.FLAG_NO_CHUNK_PREFETCH, abi.FLAG_NO_PREFETCH | abi.FLAG_NO_CHUNK_PREFETCH,
               abi.FLAG_DISTINCT_PREFETCH, abi.FLAG_NO_DISTINCT_PARTITION,
-              abi.FLAG_NO_SPLIT | abi.FLAG_NO_PREFETCH | abi.FLAG_NO_CHUNK_PREFETCH],
+              abi.FLAG_NO_SPLIT | abi.FLAG_NO_PREFETCH | abi.FLAG_NO_CHUNK_PREFETCH, abi.FLAG_RADIX],
     "chunk_rows": [0, 512, 1024, 2048, 4096],
     "cache_slots": [0, -1, 256, 1024, 4096],
     "table_load_pct": [0, 25, 70],
