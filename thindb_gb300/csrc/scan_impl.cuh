@@ -266,6 +266,16 @@ __device__ __forceinline__ uint64_t global_slot(const DevQuery &q, uint64_t k0, 
     return global_slot(q, k0, k1, hash_key(k0, k1));
 }
 
+// The slot of a one-word key when `home`, the key its home slot held at some
+// earlier moment of this query, is the key itself (a claimed slot keeps its
+// key), with no load; otherwise the probe.  home = 0 (no such load) always
+// probes.
+__device__ __forceinline__ uint64_t global_slot_from(const DevQuery &q, uint64_t k0, uint64_t k1, uint64_t hk,
+                                                     uint64_t home) {
+    if (q.key_words == 1 && k0 != 0 && home == k0) return hk & (q.cap - 1);
+    return global_slot(q, k0, k1, hk);
+}
+
 // A hashed key's slot: probe by the digest (word 1); a slot holding the same
 // digest is the group only if its representative row (word 0 - 1) holds the
 // same key; claiming writes (row + 1, digest) in one 16-byte CAS.
@@ -949,9 +959,16 @@ struct FastFold {
         fold_body(q, sm, in, active);
     }
 
+    // ... one for a caller that loaded each row's home-slot key ahead (see
+    // global_slot_from) ...
+    __device__ __noinline__ static void fold_hinted(const DevQuery &q, const ScanSmem sm, const Row in,
+                                                    unsigned active, uint64_t home) {
+        fold_body(q, sm, in, active, home);
+    }
+
     // ... and the body itself, inlined where a loop has one call site.
     __device__ __forceinline__ static void fold_body(const DevQuery &q, const ScanSmem &sm, const Row &in,
-                                                     unsigned active) {
+                                                     unsigned active, uint64_t home = 0) {
         const int lane = threadIdx.x & 31;
         const bool me = (active >> lane) & 1u;
         uint64_t val[NV];
@@ -1036,7 +1053,7 @@ struct FastFold {
                 const int e = cache_find(q, sm, k0, hk, claimed);
                 if (e >= 0) {
                     if (claimed) {
-                        gid = (uint32_t)global_slot(q, k0, 0, hk);
+                        gid = (uint32_t)global_slot_from(q, k0, 0, hk, home);
                         sm.cgid[e] = gid;
                     } else if (DISTINCT) {
                         gid = *((volatile uint32_t *)sm.cgid + e);
@@ -1047,7 +1064,7 @@ struct FastFold {
                 }
             }
             if (!st) {
-                gid = (uint32_t)global_slot(q, k0, k1, hk);
+                gid = (uint32_t)global_slot_from(q, k0, k1, hk, home);
                 if (gid != NO_GID) st = q.table + (uint64_t)gid * q.slot_words + q.key_words;
             }
             if (st) {
