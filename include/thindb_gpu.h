@@ -643,6 +643,14 @@ uint32_t tgpu_tuning_get(tgpu_tuning *entries, uint32_t cap);
  * and that the next query on the same context is correct.  Process-wide. */
 tgpu_status tgpu_debug_set_wait_limit(uint64_t sm_cycles);
 
+/* Test hook for hashed group keys, after thinDB's THINDB_V2_KEY_DIGEST_BITS
+ * (tests/integration/exact_group_keys_test.zig): queries planned from now on
+ * keep only the low `bits` of a hashed key's 64-bit digest (0 = all), so
+ * distinct keys share digests and the exact check of the key's parts
+ * against each group's representative row decides every match.  Results do
+ * not change; probes get longer.  Process-wide. */
+tgpu_status tgpu_debug_set_digest_bits(uint32_t bits);
+
 /* ------------------------------------------------- allocation-free call -- */
 
 /* No counterpart in thinDB.  For callers that cannot let the library

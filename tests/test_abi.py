@@ -159,3 +159,16 @@ def test_aggregate_registry_names():
             engine.register_aggregate(bad)
     with pytest.raises(engine.EngineError):
         engine.unregister_aggregate("never_registered")
+
+
+def test_debug_hooks_validate_their_bounds():
+    """The test hooks take effect for queries planned later and refuse values
+    out of range (no device needed)."""
+    for bits in (8, 63, 0):
+        engine.set_digest_bits(bits)
+    with pytest.raises(engine.EngineError) as e:
+        engine.set_digest_bits(64)
+    assert e.value.status == abi.ERR_INVALID_ARGUMENT
+    engine.set_device_wait_limit(0)
+    with pytest.raises(engine.EngineError):
+        engine.set_device_wait_limit((1 << 40) + 1)

@@ -153,3 +153,4 @@ def test_hashed_declines(req):
     with pytest.raises(oracle.OracleDecline):
         oracle.run(oracle.HostTable(cols), req)
     t.close()
+

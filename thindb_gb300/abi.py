@@ -235,6 +235,7 @@ SIGNATURES += [
     ("tgpu_tuning_set", C.c_int, [C.POINTER(Tuning), C.c_uint32]),
     ("tgpu_tuning_get", C.c_uint32, [C.POINTER(Tuning), C.c_uint32]),
     ("tgpu_debug_set_wait_limit", C.c_int, [C.c_uint64]),
+    ("tgpu_debug_set_digest_bits", C.c_int, [C.c_uint32]),
 ]
 
 

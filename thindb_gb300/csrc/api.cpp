@@ -45,6 +45,8 @@ namespace {
 std::atomic<long long> g_wait_limit{0};
 }
 long long tgpu::device_wait_limit() { return g_wait_limit.load(std::memory_order_relaxed); }
+std::atomic<uint32_t> g_digest_bits{0};
+uint32_t tgpu::hashed_digest_bits() { return g_digest_bits.load(std::memory_order_relaxed); }
 
 namespace {
 
@@ -771,6 +773,7 @@ tgpu_status plan_query(tgpu_query *q, const tgpu_table *t, const tgpu_request *r
         q->key_cols.push_back(c);
     }
     dq.hashed = df.hashed = hashed ? 1 : 0;
+    dq.digest_bits = hashed ? hashed_digest_bits() : 0;
     dq.key_words = hashed || off > 64 ? 2 : 1;
     // a global aggregate's one group takes the packed key 1, not the empty
     // marker 0, so it lives in each CTA's shared-memory table
@@ -1698,6 +1701,12 @@ uint32_t tgpu_abi_version(void) { return TGPU_ABI_VERSION; }
 tgpu_status tgpu_debug_set_wait_limit(uint64_t sm_cycles) {
     if (sm_cycles > (uint64_t)1 << 40) return fail(TGPU_ERR_INVALID_ARGUMENT, "wait limit above 2^40 SM clocks");
     g_wait_limit.store((long long)sm_cycles, std::memory_order_relaxed);
+    return TGPU_OK;
+}
+
+tgpu_status tgpu_debug_set_digest_bits(uint32_t bits) {
+    if (bits > 63) return fail(TGPU_ERR_INVALID_ARGUMENT, "digest bits above 63 (0 keeps all 64)");
+    g_digest_bits.store(bits, std::memory_order_relaxed);
     return TGPU_OK;
 }
 

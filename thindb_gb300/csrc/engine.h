@@ -132,7 +132,7 @@ struct DevQuery {
     // the parts' digest, word 0 the representative row + 1; equal digests
     // are told apart by comparing the rows' key parts
     int32_t hashed;
-    int32_t pad_h;
+    uint32_t digest_bits;     // 0: the full 64-bit digest; else only its low bits (set for tests of the exact check)
     uint64_t key_or;          // OR'ed into every packed key: 1 for a global aggregate (its one group), else 0
     DevAgg aggs[MAX_AGGS];
     int32_t n_aggs;
@@ -402,6 +402,10 @@ cudaError_t launch_distinct_partitions(const DevQuery &q, int word, cudaStream_t
 // Bound of the device's bulk-copy waits for queries planned from now on, in
 // SM clocks (0 = the built-in ~2 s); set by tgpu_debug_set_wait_limit.
 long long device_wait_limit();
+
+// Low bits of a hashed key's digest that queries planned from now on keep
+// (0 = all 64); set by tgpu_debug_set_digest_bits.
+uint32_t hashed_digest_bits();
 
 // Message returned by tgpu_last_error_message() on this thread (api.cpp).
 void set_error(const char *msg);

@@ -145,7 +145,7 @@ __device__ uint64_t hashed_digest(const DevQuery &q, uint64_t r) {
             d = digest_step(d, int_part_hash(col_int(c, r)));
         }
     }
-    return d;
+    return q.digest_bits ? d & ((1ULL << q.digest_bits) - 1) : d;
 }
 
 // Whether rows a and b hold the same key (every part: NULL alike, equal

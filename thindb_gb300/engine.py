@@ -80,6 +80,13 @@ def set_device_wait_limit(sm_cycles: int) -> None:
     _check(lib().tgpu_debug_set_wait_limit(sm_cycles))
 
 
+def set_digest_bits(bits: int) -> None:
+    """Keep only the low `bits` of hashed keys' digests for queries planned
+    from now on (0 = all 64): a test hook that makes distinct keys share
+    digests, so the exact key check decides every match."""
+    _check(lib().tgpu_debug_set_digest_bits(bits))
+
+
 def register_aggregate(name: str) -> None:
     """Record a host user-defined aggregate's name (thinDB's registerAggregate):
     requests naming it decline to the caller's executor."""
