@@ -212,3 +212,70 @@ def test_replicated_image_repeats_the_rows():
     assert big[-4:] == b"tDBS"
     fsize = struct.unpack_from("<I", big, len(big) - 8)[0]
     assert struct.unpack_from("<I", big, len(big) - fsize)[0] == 9  # row groups: 3 x 3
+
+
+def _rows_equal(dec, values, validity):
+    for c, (vals, ok) in enumerate(dec):
+        want = np.asarray(values[c])
+        mask = np.ones(want.size, bool) if validity[c] is None else validity[c]
+        if validity[c] is None:
+            assert ok is None
+        else:
+            assert np.array_equal(ok, mask), c
+        assert np.array_equal(vals[mask], want[mask]), c
+
+
+def test_reference_for_table_round_trips():
+    """for_encoding_test.zig:8-48: 2,500 rows in 256-row groups; `k` (200
+    values above 1,000,000) and `neg` (a negative base, both bounds present)
+    narrow to FOR, `wide` cannot narrow and stays raw, `solo` is one value,
+    `maybe_null` is NULL every 4th row; every value decodes exactly."""
+    import oracle
+    i = np.arange(2500, dtype=np.int64)
+    neg = -30_000 + (i * 7) % 5_001
+    neg[0], neg[1] = -30_000, -25_000
+    types = [abi.BIGINT, abi.BIGINT, abi.BIGINT, abi.BIGINT, abi.INT]
+    values = [1_000_000 + i % 200, neg, (i * 2_400_000_000_007) % (2**63 - 1), np.full(2500, 12_345, np.int64),
+              (500 + i % 50).astype(np.int32)]
+    validity = [None, None, None, None, i % 4 != 0]
+    image, _ = write_segment(types, values, validity, row_group_rows=256)
+    _, _, encs = read_segment(image, types)
+    enc = np.array(encs).reshape(-1, len(types))
+    assert (enc[:, 0] == ENC_FOR).all() and (enc[:, 1] == ENC_FOR).all() and (enc[:, 2] == ENC_RAW).all()
+    assert (enc[:, 4] == ENC_FOR).all()
+    _rows_equal(oracle.decode_segment(image, types, [v is not None for v in validity]), values, validity)
+
+
+def test_reference_rle_table_known_answers():
+    """rle_encoding_test.zig:17-45, :128-166: 2,500 rows in 256-row groups;
+    the long-run columns take RLE (runs straddle row groups), the alternating
+    one does not; every value decodes exactly and the test's aggregates over
+    the decoded table hold."""
+    import oracle
+    from thindb_gb300.engine import AggSpec, Pred, Request
+    i = np.arange(2500, dtype=np.int64)
+    types = [abi.BIGINT, abi.TINYINT, abi.INT, abi.BIGINT]
+    values = [7_000_000_000 + i // 100, np.where(i % 250 == 249, 1, 0).astype(np.int8),
+              (100 + i % 2).astype(np.int32), 40_000 + i // 50]
+    validity = [None, None, None, i % 4 != 0]
+    image, _ = write_segment(types, values, validity, row_group_rows=256)
+    _, _, encs = read_segment(image, types)
+    enc = np.array(encs).reshape(-1, len(types))
+    assert (enc[:, 0] == ENC_RLE).all() and (enc[:, 1] == ENC_RLE).all() and (enc[:, 2] != ENC_RLE).all()
+    dec = oracle.decode_segment(image, types, [v is not None for v in validity])
+    _rows_equal(dec, values, validity)
+    cols = [Column("runs", abi.BIGINT, dec[0][0]), Column("flag", abi.TINYINT, dec[1][0]),
+            Column("alt", abi.INT, dec[2][0]), Column("runs_null", abi.BIGINT, dec[3][0], validity=dec[3][1])]
+    t = oracle.HostTable(cols)
+
+    def count(where):
+        return int(oracle.run(t, Request([], [AggSpec("count", None, "c")], where=[where]))["c"][0][0])
+
+    assert count(Pred("runs", "=", 7_000_000_003)) == 100
+    assert count(Pred("flag", "!=", 0)) == 10
+    assert count(Pred("flag", "=", 0)) == 2490
+    assert count(Pred("runs", ">", 7_000_000_010)) == 1400
+    assert count(Pred("runs", "<=", 7_000_000_010)) == 1100
+    sums = oracle.run(t, Request([], [AggSpec("sum", "flag", "f"), AggSpec("sum", "runs", "r")]))
+    assert int(sums["f"][0][0]) == 10
+    assert int(sums["r"][0][0]) == sum(7_000_000_000 + k // 100 for k in range(2500))
